@@ -1,0 +1,90 @@
+"""ctypes binding to the oracle (oracle/_build/libwqlref.so) for the tests."""
+import ctypes
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+_LIB = None
+
+STREAMS = ["Uface", "Vface", "S", "Uhat", "Vhat", "Svel", "trup", "state"]
+NCOMP = {"Uface": 9, "Vface": 9, "S": 4, "Uhat": 6, "Vhat": 6, "Svel": 3, "trup": 1, "state": 1}
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "libwqlref.so"))
+        L.wqlref_create.restype = ctypes.c_void_p
+        L.wqlref_create.argtypes = [ctypes.c_char_p]
+        L.wqlref_last_error.restype = ctypes.c_char_p
+        vp = ctypes.c_void_p
+        L.wqlref_destroy.argtypes = [vp]
+        L.wqlref_step.argtypes = [vp, ctypes.c_int]
+        L.wqlref_frame_count.argtypes = [vp]
+        L.wqlref_get_frames.argtypes = [vp, ctypes.c_int, vp]
+        L.wqlref_get_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_set_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_get_geom.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_get_iface.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_info.argtypes = [vp, vp, vp, vp, vp, vp]
+        _LIB = L
+    return _LIB
+
+
+class Oracle:
+    """One reference-semantics domain (two blocks, one fault) on the CPU."""
+
+    def __init__(self, in_path):
+        L = lib()
+        h = L.wqlref_create(str(in_path).encode())
+        if not h:
+            raise RuntimeError(L.wqlref_last_error().decode())
+        self.h = ctypes.c_void_p(h)
+        dims = (ctypes.c_int * 6)()
+        dt, t = ctypes.c_double(), ctypes.c_double()
+        nt, ns = ctypes.c_int(), ctypes.c_int()
+        L.wqlref_info(self.h, dims, ctypes.byref(dt), ctypes.byref(t), ctypes.byref(nt), ctypes.byref(ns))
+        self.dims = [tuple(dims[3 * b:3 * b + 3]) for b in range(2)]
+        self.dt = dt.value
+        self.nt = nt.value
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _LIB is not None:
+            _LIB.wqlref_destroy(self.h)
+            self.h = None
+
+    def step(self, n=1):
+        lib().wqlref_step(self.h, n)
+
+    def field(self, block, comp):
+        nq, nr, ns = self.dims[block]
+        out = np.empty(nq * nr * ns, np.float64)
+        lib().wqlref_get_field(self.h, block, comp, out.ctypes.data)
+        return out.reshape(ns, nr, nq)
+
+    def fields(self, block):
+        return np.stack([self.field(block, c) for c in range(9)])
+
+    def set_field(self, block, comp, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        lib().wqlref_set_field(self.h, block, comp, a.ctypes.data)
+
+    def geom(self, block, what):
+        nq, nr, ns = self.dims[block]
+        out = np.empty(nq * nr * ns, np.float64)
+        lib().wqlref_get_geom(self.h, block, what, out.ctypes.data)
+        return out.reshape(ns, nr, nq)
+
+    def iface(self, block, what):
+        nr, ns = self.dims[0][1], self.dims[0][2]
+        out = np.empty(nr * ns, np.float64)
+        lib().wqlref_get_iface(self.h, block, what, out.ctypes.data)
+        return out.reshape(ns, nr)
+
+    def frames(self, name):
+        nf = lib().wqlref_frame_count(self.h)
+        nr, ns = self.dims[0][1], self.dims[0][2]
+        out = np.empty(nf * NCOMP[name] * nr * ns, np.float32)
+        lib().wqlref_get_frames(self.h, STREAMS.index(name), out.ctypes.data)
+        return out.reshape(nf, NCOMP[name], ns, nr)
