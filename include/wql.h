@@ -1,0 +1,116 @@
+/*
+ * wql.h -- C ABI of the GB300 time-stepping library for WaveQLab3D inputs.
+ *
+ * The reference (aaimran/waveqlab3d-gh, Fortran 2008 + MPI) advances a
+ * two-block domain with
+ *     do n = 1, nt; call time_step_RK(D, D%dt, RK, n); end do
+ * (src/main.f90:83-85, src/time_step.f90:68-150).  This library owns the
+ * device state of that domain and replaces the body of time_step_RK: the
+ * five RK stages of scale_rates / set_rates / exchange_fields_interface /
+ * enforce_bound_iface_conditions / update_fields (src/domain.f90:586-994),
+ * the stage-1 fault output (src/domain.f90:715-806) and the plastic update
+ * on the last stage.  Setup reads the reference's `.in` namelist format.
+ *
+ * Conventions: every function returns WQL_OK (0) or a WQL_E_* code and never
+ * exits the process (the reference calls `stop`/MPI_Abort instead,
+ * src/mpi3dbasic.f90:287-325).  wql_last_error() gives the message of the
+ * last failure on the calling thread.  Host buffers are caller-owned;
+ * device memory is owned by the scenario.  Arrays use the reference's
+ * column-major point order (q fastest, then r, then s), without ghost layers.
+ * Calls on one scenario must not overlap; different scenarios are
+ * independent.
+ */
+#ifndef WQL_H
+#define WQL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WQL_OK 0
+#define WQL_E_INPUT 1   /* malformed input or unsupported option */
+#define WQL_E_OOM 2     /* device allocation failed */
+#define WQL_E_CUDA 3    /* CUDA runtime error */
+#define WQL_E_NAN 4     /* non-finite values detected */
+#define WQL_E_SOLVER 5  /* rate-and-state solve hit its iteration cap */
+#define WQL_E_STATE 6   /* call not valid in the current state */
+
+#define WQL_FP64 0  /* reference-matching FP64 everywhere */
+#define WQL_FP32C 1 /* FP32 fields with Kahan-compensated RK update, FP64 fault */
+
+typedef struct wql_ctx wql_ctx;
+typedef struct wql_scn wql_scn;
+
+typedef struct wql_info {
+  int nq[2], nr[2], ns[2]; /* block dimensions */
+  double dt;               /* time step (src/domain.f90:222-235) */
+  double t;                /* current time */
+  int nt;                  /* floor(t_final/dt) (src/domain.f90:494) */
+  int nstep;               /* steps taken */
+  int precision;           /* WQL_FP64 or WQL_FP32C */
+  int frames;              /* fault frames recorded so far */
+  long long device_bytes;  /* device memory held by the scenario */
+} wql_info;
+
+/* Copies the last error message of this thread into buf (NUL-terminated).
+ * Returns the message length. */
+int wql_last_error(char* buf, size_t n);
+
+/* Context bound to one CUDA device.  Replaces MPI start-up
+ * (src/main.f90:63, src/mpi3dbasic.f90:24-120). */
+int wql_ctx_create(int device, wql_ctx** out);
+int wql_ctx_destroy(wql_ctx* ctx);
+
+/* Build a scenario from a reference `.in` file: init_domain
+ * (src/domain.f90:31-564) -- namelists, grids, metrics, materials, normals,
+ * boundary codes, PML slabs, interface state (src/Interface_Condition.f90:
+ * 2722-2850).  precision is WQL_FP64 or WQL_FP32C. */
+int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision, wql_scn** out);
+
+/* Same, from the text of a `.in` file (relative paths resolve against
+ * base_dir, which may be NULL). */
+int wql_scenario_create_from_text(wql_ctx* ctx, const char* in_text, const char* base_dir,
+                                  int precision, wql_scn** out);
+int wql_scenario_destroy(wql_scn* scn);
+
+/* Advance nsteps steps = nsteps calls of time_step_RK (src/time_step.f90:68). */
+int wql_step(wql_scn* scn, int nsteps);
+
+/* Blocks until all queued work of the scenario finished; reports device
+ * faults and non-finite state (when check_nan is nonzero). */
+int wql_sync(wql_scn* scn, int check_nan);
+
+int wql_get_info(wql_scn* scn, wql_info* info);
+
+/* Field component comp (0..8 = vx,vy,vz,sxx,syy,szz,sxy,sxz,syz,
+ * src/JU_xJU_yJU_z6.f90:16304-16314) of block (0/1) to host, as double. */
+int wql_get_field(wql_scn* scn, int block, int comp, double* host_out);
+int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in);
+
+/* Interface state of block copy (0/1): what 0..3 = S(1..4), 4 = W, 5 = trup;
+ * nr*ns values (src/iface.f90:13-49). */
+int wql_get_iface(wql_scn* scn, int copy, int what, double* host_out);
+
+/* Fault output frames in the reference's file layout
+ * (src/fault_output.f90:13-122, src/mpi3dio.f90:327-364): frame-major, then
+ * component, then r fastest.  what: 0 Uface(9), 1 Vface(9), 2 S(4), 3 Uhat(6),
+ * 4 Vhat(6), 5 Svel(3), 6 trup(1), 7 state(1).  host_out holds
+ * frames*ncomp*nr*ns floats. */
+int wql_frame_count(wql_scn* scn, int* frames);
+int wql_get_frames(wql_scn* scn, int what, float* host_out);
+
+/* The CUDA stream the scenario's kernels run on (cudaStream_t as integer),
+ * for callers that time or order work around wql_step. */
+int wql_scenario_stream(wql_scn* scn, uintptr_t* stream);
+
+/* Number of kernel launches one step issues (for launch accounting). */
+int wql_launches_per_step(wql_scn* scn, int* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WQL_H */

@@ -1,0 +1,20 @@
+"""Shared helpers for the GPU parity tests (CUDA path vs the oracle)."""
+import numpy as np
+
+
+def rel_l2(a, b):
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def run_pair(wql, oracle_lib, ctx, path, steps, precision=0):
+    s = wql.Scenario(ctx, path, precision=precision)
+    o = oracle_lib.Oracle(path)
+    s.step(steps)
+    s.sync(check_nan=True)
+    o.step(steps)
+    return s, o
+
+
+def field_errors(s, o):
+    return [rel_l2(s.fields(b), o.fields(b)) for b in range(2)]

@@ -1,0 +1,241 @@
+// Block coordinates on the host (one-time FP64 setup); see wql_grid.h.
+#include "wql_grid.h"
+
+#include <cmath>
+
+namespace wql {
+namespace {
+
+const double kPi = 3.141592653589793;
+
+// 2D transfinite interpolation of one face from its four edge curves
+// (Gen_Surf_Mesh, src/grid.f90:2418-2455).  L/R run along the second index
+// (length nb), B/T along the first (length na).  Output index a + na*b.
+void face_tfi(int na, int nb, const std::vector<double>& L, const std::vector<double>& R,
+              const std::vector<double>& Bo, const std::vector<double>& T,
+              std::vector<double>& out) {
+  out.assign((size_t)na * nb, 0.0);
+  const double ha = 1.0 / (double)(na - 1), hb = 1.0 / (double)(nb - 1);
+  for (int b = 0; b < nb; ++b)
+    for (int a = 0; a < na; ++a) {
+      const double q = (double)a * ha, r = (double)b * hb;
+      out[(size_t)a + (size_t)na * b] = (1.0 - q) * L[b] + q * R[b] + (1.0 - r) * Bo[a] + r * T[a] -
+                                        (1.0 - q) * (1.0 - r) * L[0] - q * (1.0 - r) * R[0] -
+                                        r * (1.0 - q) * T[0] - (r * q) * T[na - 1];
+    }
+}
+
+struct Faces {  // one coordinate component on the six faces
+  std::vector<double> left, right;   // (j,k): j + nr*k
+  std::vector<double> top, bottom;   // (i,k): i + nq*k   (top = r-min face)
+  std::vector<double> front, back;   // (i,j): i + nq*j   (front = s-min face)
+};
+
+// 3D transfinite interpolation (Gen3_Curve_Mesh, src/grid.f90:2290-2416).
+void block_tfi(int nq, int nr, int ns, const Faces& f, std::vector<double>& x) {
+  x.assign((size_t)nq * nr * ns, 0.0);
+  const double hq = 1.0 / (double)(nq - 1), hr = 1.0 / (double)(nr - 1), hs = 1.0 / (double)(ns - 1);
+  auto LK = [&](const std::vector<double>& a, int j, int k) { return a[(size_t)j + (size_t)nr * k]; };
+  auto IK = [&](const std::vector<double>& a, int i, int k) { return a[(size_t)i + (size_t)nq * k]; };
+  auto IJ = [&](const std::vector<double>& a, int i, int j) { return a[(size_t)i + (size_t)nq * j]; };
+  for (int k = 0; k < ns; ++k)
+    for (int j = 0; j < nr; ++j)
+      for (int i = 0; i < nq; ++i) {
+        const double q = (double)i * hq, r = (double)j * hr, s = (double)k * hs;
+        const double U = (1.0 - q) * LK(f.left, j, k) + q * LK(f.right, j, k);
+        const double V = (1.0 - r) * IK(f.top, i, k) + r * IK(f.bottom, i, k);
+        const double W = (1.0 - s) * IJ(f.front, i, j) + s * IJ(f.back, i, j);
+        const double UW = (1.0 - q) * ((1.0 - r) * LK(f.left, 0, k) + r * LK(f.left, nr - 1, k)) +
+                          q * ((1.0 - r) * LK(f.right, 0, k) + r * LK(f.right, nr - 1, k));
+        const double UV = (1.0 - r) * ((1.0 - s) * IK(f.top, i, 0) + s * IK(f.top, i, ns - 1)) +
+                          r * ((1.0 - s) * IK(f.bottom, i, 0) + s * IK(f.bottom, i, ns - 1));
+        const double VW = (1.0 - s) * ((1.0 - q) * IJ(f.front, 0, j) + q * IJ(f.front, nq - 1, j)) +
+                          s * ((1.0 - q) * IJ(f.back, 0, j) + q * IJ(f.back, nq - 1, j));
+        const double C1 = (1.0 - q) * ((1.0 - r) * ((1.0 - s) * IK(f.top, 0, 0) + s * IK(f.top, 0, ns - 1)) +
+                                       r * ((1.0 - s) * IK(f.bottom, 0, 0) + s * IK(f.bottom, 0, ns - 1)));
+        const double C2 = q * ((1.0 - r) * ((1.0 - s) * IK(f.top, nq - 1, 0) + s * IK(f.top, nq - 1, ns - 1)) +
+                               r * ((1.0 - s) * IK(f.bottom, nq - 1, 0) + s * IK(f.bottom, nq - 1, ns - 1)));
+        x[(size_t)i + (size_t)nq * ((size_t)j + (size_t)nr * k)] = U + V + W - UV - UW - VW + C1 + C2;
+      }
+}
+
+int curvilinear(const BlockParams& bp, BlockGrid& G, std::string& err) {
+  const int mx = G.nq, my = G.nr, mz = G.ns;
+  const double ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1];
+  const double az = bp.aqrs[2], bz = bp.bqrs[2];
+  const std::string& pt = bp.profile_type;
+  const bool flat = pt.empty() || pt == "No-path" || pt == "no_path" || pt == "none";
+  if (!(flat || pt == "analytical_tpv28" || pt == "analytical_test_problem")) {
+    err = "profile_type '" + pt + "' is not supported";
+    return 1;
+  }
+  const size_t nx = (size_t)my * mz;
+  Faces X, Y, Z;
+  X.left.resize(nx); X.right.resize(nx);
+  Y.left.resize(nx); Y.right.resize(nx);
+  Z.left.resize(nx); Z.right.resize(nx);
+  const double hy = (by - ay) / (double)(my - 1), hz = (bz - az) / (double)(mz - 1);
+  // x-faces (src/grid.f90:593-620): uniform (y,z) with the fault profile on x
+  for (int k = 0; k < mz; ++k)
+    for (int j = 0; j < my; ++j) {
+      const size_t p = (size_t)j + (size_t)my * k;
+      const double y = ay + (double)j * hy, z = az + (double)k * hz;
+      Y.left[p] = Y.right[p] = y;
+      Z.left[p] = Z.right[p] = z;
+      X.left[p] = ax;
+      X.right[p] = bx;
+      if (pt == "analytical_tpv28") {  // two cosine bumps (src/grid.f90:664-681)
+        double f = 0.0;
+        const double r1 = std::sqrt((z + 10.5) * (z + 10.5) + (y - 7.5) * (y - 7.5));
+        const double r2 = std::sqrt((z - 10.5) * (z - 10.5) + (y - 7.5) * (y - 7.5));
+        if (r1 <= 3.0) f = -0.3 * (1.0 + std::cos(kPi * r1 / 3.0));
+        if (r2 <= 3.0) f = -0.3 * (1.0 + std::cos(kPi * r2 / 3.0));
+        X.left[p] += bp.rc * f;
+        X.right[p] += bp.lc * f;
+      }
+    }
+  if (pt == "analytical_test_problem") {
+    // (y,z) meshed by Gen_Surf_Mesh from straight edges, then a Gaussian bump
+    // plus a sine product on x (src/grid.f90:790-841)
+    std::vector<double> eyL(mz, ay), eyR(mz, by), eyB(my), eyT(my), ezL(mz), ezR(mz), ezB(my, az),
+        ezT(my, bz);
+    for (int j = 0; j < my; ++j) eyB[j] = eyT[j] = ay + (double)j * hy;
+    for (int k = 0; k < mz; ++k) ezL[k] = ezR[k] = az + (double)k * hz;
+    face_tfi(my, mz, eyL, eyR, eyB, eyT, Y.left);
+    face_tfi(my, mz, ezL, ezR, ezB, ezT, Z.left);
+    Y.right = Y.left;
+    Z.right = Z.left;
+    for (size_t p = 0; p < nx; ++p) {
+      auto bump = [&](double y, double z) {
+        const double dy = 1.0 * y - 0.5 * (ay + by), dz = z - 0.5 * (az + bz);
+        return 0.1 * std::exp(-(dy * dy + 1.0 * (dz * dz)) / 0.025) +
+               0.1 * std::sin(2.0 / (by - ay) * kPi * y) * std::sin(2.0 / (bz - az) * kPi * z);
+      };
+      X.left[p] = ax + bp.rc * bump(Y.left[p], Z.left[p]);
+      X.right[p] = bx + bp.lc * bump(Y.right[p], Z.right[p]);
+    }
+  }
+  auto L = [&](const std::vector<double>& a, int j, int k) { return a[(size_t)j + (size_t)my * k]; };
+  // s-faces (front k=0, back k=mz-1): edges from the x-faces, straight in q
+  auto s_face = [&](int k, const Faces& C, std::vector<double>& out, bool use_y_edges) {
+    std::vector<double> eL(my), eR(my), eB(mx), eT(mx);
+    for (int j = 0; j < my; ++j) {
+      eL[j] = L(C.left, j, k);
+      eR[j] = L(C.right, j, k);
+    }
+    for (int i = 0; i < mx; ++i) {
+      double h = (L(C.right, 0, k) - L(C.left, 0, k)) / (double)(mx - 1);
+      eB[i] = L(C.left, 0, k) + (double)i * h;
+      h = (L(C.right, my - 1, k) - L(C.left, my - 1, k)) / (double)(mx - 1);
+      eT[i] = L(C.left, my - 1, k) + (double)i * h;
+    }
+    (void)use_y_edges;
+    face_tfi(mx, my, eL, eR, eB, eT, out);
+  };
+  s_face(0, X, X.front, false);
+  s_face(0, Y, Y.front, true);
+  s_face(mz - 1, X, X.back, false);
+  s_face(mz - 1, Y, Y.back, true);
+  Z.front.assign((size_t)mx * my, az);
+  Z.back.assign((size_t)mx * my, bz);
+  // r-faces (top j=0, bottom j=my-1)
+  auto r_face = [&](int j, const Faces& C, std::vector<double>& out, double zb, double zt, bool zcomp) {
+    std::vector<double> eL(mz), eR(mz), eB(mx), eT(mx);
+    for (int k = 0; k < mz; ++k) {
+      eL[k] = L(C.left, j, k);
+      eR[k] = L(C.right, j, k);
+    }
+    for (int i = 0; i < mx; ++i) {
+      if (zcomp) {
+        eB[i] = zb;
+        eT[i] = zt;
+      } else {
+        double h = (L(C.right, j, 0) - L(C.left, j, 0)) / (double)(mx - 1);
+        eB[i] = L(C.left, j, 0) + (double)i * h;
+        h = (L(C.right, j, mz - 1) - L(C.left, j, mz - 1)) / (double)(mx - 1);
+        eT[i] = L(C.left, j, mz - 1) + (double)i * h;
+      }
+    }
+    face_tfi(mx, mz, eL, eR, eB, eT, out);
+  };
+  r_face(0, X, X.top, 0, 0, false);
+  r_face(0, Z, Z.top, az, bz, true);
+  r_face(my - 1, X, X.bottom, 0, 0, false);
+  r_face(my - 1, Z, Z.bottom, az, bz, true);
+  Y.top.assign((size_t)mx * mz, ay);
+  Y.bottom.assign((size_t)mx * mz, by);
+  block_tfi(mx, my, mz, X, G.x[0]);
+  block_tfi(mx, my, mz, Y, G.x[1]);
+  block_tfi(mx, my, mz, Z, G.x[2]);
+  return 0;
+}
+
+}  // namespace
+
+int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockGrid& G,
+                    std::string& err) {
+  const BlockParams& bp = P.btp[block];
+  G.nq = bp.nqrs[0];
+  G.nr = bp.nqrs[1];
+  G.ns = bp.nqrs[2];
+  const size_t np = (size_t)G.nq * G.nr * G.ns;
+  if (P.mesh_source != "compute") {
+    err = "mesh_source '" + P.mesh_source + "' is not supported (grids are computed)";
+    return 1;
+  }
+  if (P.type_of_mesh == "cartesian") {
+    const double bh[3] = {(bp.bqrs[0] - bp.aqrs[0]) / (double)(G.nq - 1),
+                          (bp.bqrs[1] - bp.aqrs[1]) / (double)(G.nr - 1),
+                          (bp.bqrs[2] - bp.aqrs[2]) / (double)(G.ns - 1)};
+    for (int c = 0; c < 3; ++c) G.x[c].resize(np);
+    for (int k = 0; k < G.ns; ++k)
+      for (int j = 0; j < G.nr; ++j)
+        for (int i = 0; i < G.nq; ++i) {
+          const size_t p = (size_t)i + (size_t)G.nq * ((size_t)j + (size_t)G.nr * k);
+          G.x[0][p] = bp.aqrs[0] + (double)i * bh[0];
+          G.x[1][p] = bp.aqrs[1] + (double)j * bh[1];
+          G.x[2][p] = bp.aqrs[2] + (double)k * bh[2];
+        }
+  } else if (P.type_of_mesh == "curvilinear") {
+    if (P.use_topography) {
+      err = "use_topography reads topography files; pass a seeded surface through the API instead";
+      return 1;
+    }
+    if (curvilinear(bp, G, err)) return 1;
+  } else {
+    err = "unknown type_of_mesh '" + P.type_of_mesh + "'";
+    return 1;
+  }
+  // Seeded surface displacements, blended linearly into the block so the
+  // opposite faces stay put.
+  if (!mods.fault_offset.empty()) {
+    if (mods.fault_offset.size() != (size_t)G.nr * G.ns) {
+      err = "fault_offset has the wrong size";
+      return 1;
+    }
+    for (int k = 0; k < G.ns; ++k)
+      for (int j = 0; j < G.nr; ++j)
+        for (int i = 0; i < G.nq; ++i) {
+          const double q = (double)i / (double)(G.nq - 1);
+          const double w = (block == 0) ? q : 1.0 - q;
+          G.x[0][(size_t)i + (size_t)G.nq * ((size_t)j + (size_t)G.nr * k)] +=
+              w * mods.fault_offset[(size_t)j + (size_t)G.nr * k];
+        }
+  }
+  if (!mods.topo_offset.empty()) {
+    if (mods.topo_offset.size() != (size_t)G.nq * G.ns) {
+      err = "topo_offset has the wrong size";
+      return 1;
+    }
+    for (int k = 0; k < G.ns; ++k)
+      for (int j = 0; j < G.nr; ++j)
+        for (int i = 0; i < G.nq; ++i) {
+          const double w = 1.0 - (double)j / (double)(G.nr - 1);
+          G.x[1][(size_t)i + (size_t)G.nq * ((size_t)j + (size_t)G.nr * k)] +=
+              w * mods.topo_offset[(size_t)i + (size_t)G.nq * k];
+        }
+  }
+  return 0;
+}
+
+}  // namespace wql

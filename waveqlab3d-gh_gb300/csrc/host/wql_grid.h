@@ -1,0 +1,36 @@
+// Host-side block geometry: grid point coordinates for one block.
+//
+// Cartesian blocks follow cartesian_grid_3d (src/grid.f90:213-240).
+// Curvilinear blocks follow the flat-topography branch of Curve_Grid_3D3
+// (src/grid.f90:471-1160, 1873-1875): six boundary surfaces, each face meshed
+// by 2D transfinite interpolation (Gen_Surf_Mesh, src/grid.f90:2418-2455),
+// then 3D transfinite interpolation (Gen3_Curve_Mesh, src/grid.f90:2290-2416).
+// Supported fault profiles: flat (default / 'No-path' / 'no_path'),
+// 'analytical_tpv28' (src/grid.f90:650-683) and 'analytical_test_problem'
+// (src/grid.f90:790-841).  Two extensions feed the seeded rough-fault and
+// topography generators: `fault_offset` displaces the interface face along x
+// and `topo_offset` displaces the r-min face along y (both given on the
+// face's own (r,s) / (q,s) grid, see wql_surfaces.h).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "wql_input.h"
+
+namespace wql {
+
+struct BlockGrid {
+  int nq = 0, nr = 0, ns = 0;
+  std::vector<double> x[3];  // index (i-1) + nq*((j-1) + nr*(k-1))
+};
+
+// Optional surface displacements (empty = none).
+struct SurfaceMods {
+  std::vector<double> fault_offset;  // nr*ns, x-offset of the interface face
+  std::vector<double> topo_offset;   // nq*ns, y-offset of the r=1 face
+};
+
+int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockGrid& G,
+                    std::string& err);
+
+}  // namespace wql

@@ -1,0 +1,719 @@
+// C ABI implementation: scenario setup (init_domain) and the RK step driver
+// (time_step_RK, src/time_step.f90:68-150) over the device kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/wql.h"
+#include "host/wql_grid.h"
+#include "host/wql_input.h"
+#include "wql_internal.h"
+
+using namespace wql;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) return fail(WQL_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Kennedy-Carpenter (5,4) 2N-storage coefficients (src/time_step.f90:53-62).
+struct RK {
+  double A[6], B[6], C[6];
+  RK() {
+    A[1] = 0.0;
+    A[2] = -567301805773.0 / 1357537059087.0;
+    A[3] = -2404267990393.0 / 2016746695238.0;
+    A[4] = -3550918686646.0 / 2091501179385.0;
+    A[5] = -1275806237668.0 / 842570457699.0;
+    B[1] = 1432997174477.0 / 9575080441755.0;
+    B[2] = 5161836677717.0 / 13612068292357.0;
+    B[3] = 1720146321549.0 / 2090206949498.0;
+    B[4] = 3134564353537.0 / 4481467310338.0;
+    B[5] = 2277821191437.0 / 14882151754819.0;
+    C[0] = 0.0;
+    C[1] = 1432997174477.0 / 9575080441755.0;
+    C[2] = 2526269341429.0 / 6820363962896.0;
+    C[3] = 2006345519317.0 / 3224310063776.0;
+    C[4] = 2802321613138.0 / 2924317926251.0;
+    C[5] = 1.0;
+  }
+};
+
+int preset_of(const std::string& pb) {
+  if (pb == "TPV5" || pb == "LOH1" || pb == "OKLAHOMA") return PRE_TPV5;
+  if (pb == "TPV26") return PRE_TPV26;
+  if (pb == "TPV27") return PRE_TPV27;
+  if (pb == "TPV28") return PRE_TPV28;
+  if (pb == "TPV29") return PRE_TPV29;
+  if (pb == "TPV30") return PRE_TPV30;
+  if (pb == "TPV10") return PRE_TPV10;
+  if (pb == "TPV101") return PRE_TPV101;
+  if (pb == "TPV102") return PRE_TPV102;
+  if (pb == "sw_param") return PRE_SW_PARAM;
+  if (pb == "rs_param") return PRE_RS_PARAM;
+  return PRE_NONE;
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct wql_ctx {
+  int device = 0;
+};
+
+struct wql_scn {
+  wql_ctx* ctx = nullptr;
+  Problem P;
+  int prec = WQL_FP64;
+  size_t esz = 8;
+  cudaStream_t stream = nullptr;
+  RK rk;
+  double dt = 0, t = 0;
+  int nt = 0, nstep = 0;
+  bool curv = false;
+  std::vector<DevBuf> allocs;
+  long long device_bytes = 0;
+  struct Block {
+    int nq = 0, nr = 0, ns = 0;
+    long long np = 0;
+    void* F[2] = {nullptr, nullptr};
+    void* DF = nullptr;
+    void* C = nullptr;
+    void* coef = nullptr;
+    double* face[6] = {};
+    int bc[6] = {};
+    int pml[6] = {};
+    int npml = 0;
+    void* Q[6] = {};
+    void* DQ[6] = {};
+    long long slab_np[6] = {};
+    void* y = nullptr;
+    double cart_metric[3] = {1, 1, 1};
+    double tau_h[3] = {};
+  } B[2];
+  int cur = 0;
+  // interface (two block copies)
+  double *S = nullptr, *DS = nullptr, *W = nullptr, *DW = nullptr, *trup = nullptr, *xij = nullptr;
+  void* sat = nullptr;
+  unsigned int* solver_fail = nullptr;
+  FaultParams fp{};
+  int bc_form = BC_CHARACTERISTIC;
+  bool plastic = false;
+  double pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
+  // fault frames
+  float* frame_dev = nullptr;
+  int frame_cap = 0, frame_fill = 0;
+  std::vector<float> frames_host;
+  int nframes = 0;
+
+  ~wql_scn() {
+    for (auto& a : allocs)
+      if (a.p) cudaFree(a.p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int alloc(void** p, size_t bytes, bool zero = true) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      *p = nullptr;
+      return fail(WQL_E_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                 cudaGetErrorString(e));
+    }
+    allocs.push_back({*p, bytes});
+    device_bytes += (long long)bytes;
+    if (zero) {
+      e = cudaMemsetAsync(*p, 0, bytes, stream);
+      if (e != cudaSuccess) return fail(WQL_E_CUDA, cudaGetErrorString(e));
+    }
+    return WQL_OK;
+  }
+  void release(void* p) {
+    for (auto& a : allocs)
+      if (a.p == p) {
+        cudaFree(a.p);
+        device_bytes -= (long long)a.bytes;
+        a.p = nullptr;
+      }
+  }
+};
+
+namespace {
+
+template <typename T>
+__global__ void fill_comp(T* F, long long np, int comp, T val) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p < np) F[comp * np + p] = val;
+}
+
+template <typename T>
+__global__ void to_double(const T* in, double* out, long long n) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p < n) out[p] = (double)in[p];
+}
+
+template <typename T>
+__global__ void from_double(const double* in, T* out, long long n) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p < n) out[p] = (T)in[p];
+}
+
+template <typename T>
+__global__ void count_nonfinite(const T* a, long long n, unsigned int* cnt) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p < n && !isfinite((double)a[p])) atomicAdd(cnt, 1u);
+}
+
+int setup_block(wql_scn* S, int b) {
+  const BlockParams& bp = S->P.btp[b];
+  auto& B = S->B[b];
+  BlockGrid G;
+  std::string err;
+  SurfaceMods mods;
+  if (make_block_grid(S->P, b, mods, G, err)) return fail(WQL_E_INPUT, err);
+  B.nq = G.nq;
+  B.nr = G.nr;
+  B.ns = G.ns;
+  B.np = (long long)G.nq * G.nr * G.ns;
+  const long long np = B.np;
+  // geometry on the device (FP64) for the one-time precompute
+  double *x = nullptr, *metric = nullptr, *J = nullptr, *mat = nullptr;
+  int rc;
+  if ((rc = S->alloc((void**)&x, 3 * np * sizeof(double), false))) return rc;
+  for (int c = 0; c < 3; ++c)
+    CK(cudaMemcpyAsync(x + c * np, G.x[c].data(), np * sizeof(double), cudaMemcpyHostToDevice, S->stream));
+  if ((rc = S->alloc((void**)&metric, 9 * np * sizeof(double), false))) return rc;
+  if ((rc = S->alloc((void**)&J, np * sizeof(double), false))) return rc;
+  launch_metrics(B.nq, B.nr, B.ns, x, metric, J, S->stream);
+  CK(cudaGetLastError());
+  // homogeneous material from rho_s_p (src/material.f90:180-187)
+  if (S->P.material_source != "hardcode")
+    return fail(WQL_E_INPUT, "material_source '" + S->P.material_source + "' is not supported");
+  if ((rc = S->alloc((void**)&mat, 3 * np * sizeof(double), false))) return rc;
+  {
+    const double rho = bp.rho_s_p[0], cs = bp.rho_s_p[1], cp = bp.rho_s_p[2];
+    const double lam = rho * (cp * cp - 2.0 * (cs * cs)), mu = rho * (cs * cs);
+    std::vector<double> h(np);
+    const double vals[3] = {lam, mu, rho};
+    for (int c = 0; c < 3; ++c) {
+      std::fill(h.begin(), h.end(), vals[c]);
+      CK(cudaMemcpyAsync(mat + c * np, h.data(), np * sizeof(double), cudaMemcpyHostToDevice, S->stream));
+      CK(cudaStreamSynchronize(S->stream));
+    }
+  }
+  // faces
+  for (int s = 0; s < 6; ++s) {
+    const int axis = s / 2;
+    const long long nf = axis == 0 ? (long long)B.nr * B.ns : (axis == 1 ? (long long)B.nq * B.ns : (long long)B.nq * B.nr);
+    if ((rc = S->alloc((void**)&B.face[s], kFaceWords * nf * sizeof(double), false))) return rc;
+  }
+  launch_faces(B.nq, B.nr, B.ns, metric, mat, mat + np, mat + 2 * np, B.face, S->stream);
+  CK(cudaGetLastError());
+  // coefficients
+  const int ncoef = S->curv ? kCurvCoef : kCartCoef;
+  if ((rc = S->alloc(&B.coef, ncoef * np * S->esz, false))) return rc;
+  if (S->prec == WQL_FP64)
+    launch_coef<double>(np, S->curv, metric, J, mat, mat + np, mat + 2 * np, (double*)B.coef, S->stream);
+  else
+    launch_coef<float>(np, S->curv, metric, J, mat, mat + np, mat + 2 * np, (float*)B.coef, S->stream);
+  CK(cudaGetLastError());
+  // Cartesian diagonal metric, taken at the block centre
+  {
+    const long long pc = (B.nq / 2) + (long long)B.nq * ((B.nr / 2) + (long long)B.nr * (B.ns / 2));
+    const int diag[3] = {0, 4, 8};  // metricx(1), metricy(2), metricz(3)
+    for (int d = 0; d < 3; ++d)
+      CK(cudaMemcpyAsync(&B.cart_metric[d], metric + diag[d] * np + pc, sizeof(double),
+                         cudaMemcpyDeviceToHost, S->stream));
+  }
+  // fields
+  for (int i = 0; i < 2; ++i)
+    if ((rc = S->alloc(&B.F[i], 9 * np * S->esz))) return rc;
+  if ((rc = S->alloc(&B.DF, 9 * np * S->esz))) return rc;
+  if (S->prec == WQL_FP32C)
+    if ((rc = S->alloc(&B.C, 9 * np * S->esz))) return rc;
+  // boundary codes (src/BoundaryConditions.f90:15-48) and PML slabs (src/block.f90:163-178)
+  B.bc[0] = bp.lqrs[0]; B.bc[1] = bp.rqrs[0];
+  B.bc[2] = bp.lqrs[1]; B.bc[3] = bp.rqrs[1];
+  B.bc[4] = bp.lqrs[2]; B.bc[5] = bp.rqrs[2];
+  B.npml = 0;
+  for (int s = 0; s < 6; ++s) {
+    B.pml[s] = (s % 2 == 0) ? bp.pml_lqrs[s / 2] : bp.pml_rqrs[s / 2];
+    if (B.pml[s]) B.npml = bp.npml;
+  }
+  if (B.npml > 0) {
+    const int dims[3] = {B.nq, B.nr, B.ns};
+    for (int s = 0; s < 6; ++s) {
+      if (!B.pml[s]) continue;
+      if (B.npml >= dims[s / 2]) return fail(WQL_E_INPUT, "npml exceeds the block size");
+      long long slab = np / dims[s / 2] * B.npml;
+      B.slab_np[s] = slab;
+      if ((rc = S->alloc(&B.Q[s], 9 * slab * S->esz))) return rc;
+      if ((rc = S->alloc(&B.DQ[s], 9 * slab * S->esz))) return rc;
+    }
+  }
+  const double tau0 = 1.0 / (0.315949074074074);  // src/block.f90:191
+  const int dims[3] = {B.nq, B.nr, B.ns};
+  for (int d = 0; d < 3; ++d) B.tau_h[d] = tau0 / (1.0 / (double)(dims[d] - 1));
+  // depth coordinate for the plastic update
+  if (S->plastic) {
+    if ((rc = S->alloc(&B.y, np * S->esz, false))) return rc;
+    if (S->prec == WQL_FP64)
+      CK(cudaMemcpyAsync(B.y, x + np, np * sizeof(double), cudaMemcpyDeviceToDevice, S->stream));
+    else
+      from_double<float><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(x + np, (float*)B.y, np);
+  }
+  // interface coordinates of this block's fault face
+  {
+    const long long nf = (long long)B.nr * B.ns;
+    std::vector<double> xi(3 * nf);
+    const int iq = (b == 0) ? B.nq - 1 : 0;
+    for (int k = 0; k < B.ns; ++k)
+      for (int j = 0; j < B.nr; ++j) {
+        const long long p = iq + (long long)B.nq * (j + (long long)B.nr * k);
+        for (int c = 0; c < 3; ++c) xi[c * nf + j + (long long)B.nr * k] = G.x[c][p];
+      }
+    CK(cudaMemcpyAsync(S->xij + (long long)b * 3 * nf, xi.data(), 3 * nf * sizeof(double),
+                       cudaMemcpyHostToDevice, S->stream));
+    CK(cudaStreamSynchronize(S->stream));
+  }
+  CK(cudaStreamSynchronize(S->stream));
+  S->release(x);
+  S->release(metric);
+  S->release(J);
+  S->release(mat);
+  return WQL_OK;
+}
+
+// Init_Vel_State (src/Interface_Condition.f90:2722-2850) for each block copy.
+int init_rate_state(wql_scn* S) {
+  const long long nf = (long long)S->B[0].nr * S->B[0].ns;
+  const double Vin = (S->fp.preset == PRE_RS_PARAM) ? S->fp.Vini : 1.0e-12;
+  std::vector<double> W(2 * nf);
+  for (int b = 0; b < 2; ++b) {
+    auto& B = S->B[b];
+    const int side = (b == 0) ? 1 : 0;
+    std::vector<double> face(kFaceWords * nf), xi(3 * nf);
+    CK(cudaMemcpy(face.data(), B.face[side], face.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(xi.data(), S->xij + (long long)b * 3 * nf, xi.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (long long f = 0; f < nf; ++f) {
+      double n[3], m[3], l[3], x[3];
+      for (int c = 0; c < 3; ++c) {
+        n[c] = face[(0 + c) * nf + f];
+        m[c] = face[(3 + c) * nf + f];
+        l[c] = face[(6 + c) * nf + f];
+        x[c] = xi[c * nf + f];
+      }
+      double Tn, Tm, Tl;
+      prestress(S->fp, x, 0.0, l, m, n, Tn, Tm, Tl);
+      const RSParams r = rs_params(S->fp, x);
+      const double sn = -Tn;
+      const double theta =
+          r.L0 / r.V0 * std::exp(((r.a * std::log(2.0 * std::sinh(Tl / (r.a * sn)))) - r.f0 - r.a * std::log(Vin / r.V0)) / r.b);
+      W[b * nf + f] = r.f0 + r.b * std::log(r.V0 / r.L0 * theta);
+    }
+    // uniform initial slip velocity split across the fault: -/+ Vin/2 in z
+    const double vz = (b == 0 ? -1.0 : 1.0) * std::fabs(0.5 * Vin);
+    const long long np = B.np;
+    for (int i = 0; i < 2; ++i) {
+      if (S->prec == WQL_FP64)
+        fill_comp<double><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>((double*)B.F[i], np, 2, vz);
+      else
+        fill_comp<float><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>((float*)B.F[i], np, 2, (float)vz);
+    }
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpy(S->W, W.data(), W.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return WQL_OK;
+}
+
+int create(wql_ctx* ctx, Problem&& P, int precision, wql_scn** out) {
+  if (!ctx || !out) return fail(WQL_E_INPUT, "null argument");
+  if (precision != WQL_FP64 && precision != WQL_FP32C) return fail(WQL_E_INPUT, "unknown precision");
+  std::unique_ptr<wql_scn> S(new wql_scn());
+  S->ctx = ctx;
+  S->P = std::move(P);
+  S->prec = precision;
+  S->esz = precision == WQL_FP64 ? 8 : 4;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+  const Problem& Pr = S->P;
+  if (Pr.fd_type != "traditional")
+    return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' is not supported (6th-order traditional SBP only)");
+  if (Pr.response == "anelastic") return fail(WQL_E_INPUT, "response='anelastic' is not supported");
+  if (Pr.use_moment_tensor) return fail(WQL_E_INPUT, "moment-tensor sources are not supported by this entry point");
+  S->curv = Pr.type_of_mesh == "curvilinear";
+  S->bc_form = Pr.bc_penalty == "weighted" ? BC_WEIGHTED : BC_CHARACTERISTIC;
+  S->plastic = Pr.response == "plastic";
+  if (S->plastic && Pr.plastic_model != "scec")
+    return fail(WQL_E_INPUT, "only plastic_model='scec' is supported");
+  if (Pr.plast.set) {
+    S->pl_c = Pr.plast.cohesion;
+    S->pl_nu = Pr.plast.friction;
+    S->pl_Tv = Pr.plast.Tv;
+  } else if (Pr.problem == "TPV30") {
+    S->pl_c = 1.18; S->pl_nu = 0.1680; S->pl_Tv = 0.05;  // src/plastic.f90:178-182
+  }
+  // coupling and friction preset
+  FaultParams& fp = S->fp;
+  std::memset(&fp, 0, sizeof(fp));
+  const std::string& cp = Pr.coupling;
+  if (cp == "locked") fp.coupling = CPL_LOCKED;
+  else if (cp == "linear_friction") fp.coupling = CPL_LINEAR;
+  else if (cp == "slip-weakening_friction") fp.coupling = CPL_SW;
+  else if (cp == "rate-and-state_friction") fp.coupling = CPL_RS;
+  else return fail(WQL_E_INPUT, "invalid coupling condition '" + cp + "'");
+  fp.preset = preset_of(Pr.problem);
+  const bool sw_ok = fp.preset == PRE_TPV5 || fp.preset == PRE_TPV26 || fp.preset == PRE_TPV27 ||
+                     fp.preset == PRE_TPV28 || fp.preset == PRE_TPV29 || fp.preset == PRE_TPV30 ||
+                     fp.preset == PRE_TPV10 || fp.preset == PRE_SW_PARAM;
+  const bool rs_ok = fp.preset == PRE_TPV101 || fp.preset == PRE_TPV102 || fp.preset == PRE_RS_PARAM;
+  if ((fp.coupling == CPL_SW && !sw_ok) || (fp.coupling == CPL_RS && !rs_ok))
+    return fail(WQL_E_INPUT, "problem '" + Pr.problem + "' has no preset for coupling '" + cp + "'");
+  if (S->plastic) {
+    double s0[6], x0[3] = {0, 0, 0};
+    if (!initial_stress(fp.preset, x0, s0))
+      return fail(WQL_E_INPUT, "problem '" + Pr.problem + "' has no initial stress tensor for plasticity");
+  }
+  const FrictionExt& fe = Pr.fric;
+  fp.fs = fe.fs; fp.fd = fe.fd; fp.Dc = fe.Dc; fp.barrier_y = fe.barrier_y; fp.barrier_z = fe.barrier_z;
+  fp.a = fe.a; fp.b = fe.b; fp.V0 = fe.V0; fp.f0 = fe.f0; fp.L = fe.L; fp.Vini = fe.Vini;
+  fp.Tn = fe.Tn; fp.Tm = fe.Tm; fp.Tl = fe.Tl; fp.nuc_amp = fe.nuc_amp; fp.nuc_radius = fe.nuc_radius;
+  fp.nuc_y = fe.nuc_y; fp.nuc_z = fe.nuc_z; fp.nuc_rise = fe.nuc_rise;
+  // the two blocks share the fault face (src/domain.f90:243-244, 518-530)
+  if (Pr.btp[0].nqrs[1] != Pr.btp[1].nqrs[1] || Pr.btp[0].nqrs[2] != Pr.btp[1].nqrs[2])
+    return fail(WQL_E_INPUT, "the two blocks must share the fault face (equal nr, ns)");
+  const long long nf = (long long)Pr.btp[0].nqrs[1] * Pr.btp[0].nqrs[2];
+  int rc;
+  if ((rc = S->alloc((void**)&S->xij, 2 * 3 * nf * sizeof(double)))) return rc;
+  for (int b = 0; b < 2; ++b)
+    if ((rc = setup_block(S.get(), b))) return rc;
+  if ((rc = S->alloc((void**)&S->S, 2 * 4 * nf * sizeof(double)))) return rc;
+  if ((rc = S->alloc((void**)&S->DS, 2 * 4 * nf * sizeof(double)))) return rc;
+  if ((rc = S->alloc((void**)&S->W, 2 * nf * sizeof(double)))) return rc;
+  if ((rc = S->alloc((void**)&S->DW, 2 * nf * sizeof(double)))) return rc;
+  if ((rc = S->alloc((void**)&S->trup, 2 * nf * sizeof(double), false))) return rc;
+  {
+    std::vector<double> t9(2 * nf, 1.0e9);  // src/iface.f90:41
+    CK(cudaMemcpy(S->trup, t9.data(), t9.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if ((rc = S->alloc(&S->sat, 2 * 9 * nf * S->esz))) return rc;
+  if ((rc = S->alloc((void**)&S->solver_fail, sizeof(unsigned int)))) return rc;
+  if (fp.coupling == CPL_RS)
+    if ((rc = init_rate_state(S.get()))) return rc;
+  if (Pr.w_fault) {
+    S->frame_cap = 64;
+    if ((rc = S->alloc((void**)&S->frame_dev, (size_t)S->frame_cap * kFrameWords * nf * sizeof(float)))) return rc;
+  }
+  // time step: src/domain.f90:222-235, src/block.f90:437-452
+  double dtmin = 1e300;
+  for (int b = 0; b < 2; ++b) {
+    const BlockParams& bp = Pr.btp[b];
+    double h = 1e300;
+    for (int d = 0; d < 3; ++d) h = std::fmin(h, (bp.bqrs[d] - bp.aqrs[d]) / (double)(bp.nqrs[d] - 1));
+    dtmin = std::fmin(dtmin, Pr.CFL * h / std::sqrt(bp.rho_s_p[1] * bp.rho_s_p[1] + bp.rho_s_p[2] * bp.rho_s_p[2]));
+  }
+  S->dt = dtmin;
+  S->nt = (int)std::floor(Pr.t_final / dtmin);
+  CK(cudaStreamSynchronize(S->stream));
+  CK(cudaGetLastError());
+  *out = S.release();
+  return WQL_OK;
+}
+
+int flush_frames(wql_scn* S) {
+  if (S->frame_fill == 0) return WQL_OK;
+  const long long nf = (long long)S->B[0].nr * S->B[0].ns;
+  const size_t words = (size_t)S->frame_fill * kFrameWords * nf;
+  const size_t old = S->frames_host.size();
+  S->frames_host.resize(old + words);
+  CK(cudaMemcpyAsync(S->frames_host.data() + old, S->frame_dev, words * sizeof(float),
+                     cudaMemcpyDeviceToHost, S->stream));
+  CK(cudaStreamSynchronize(S->stream));
+  S->frame_fill = 0;
+  return WQL_OK;
+}
+
+template <typename T>
+VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
+  auto& B = S->B[b];
+  VolumeArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.nq = B.nq; a.nr = B.nr; a.ns = B.ns; a.np = B.np; a.block = b;
+  a.rh[0] = (T)(B.nq - 1); a.rh[1] = (T)(B.nr - 1); a.rh[2] = (T)(B.ns - 1);
+  a.Fin = (const T*)B.F[S->cur];
+  a.Fout = (T*)B.F[S->cur ^ 1];
+  a.DF = (T*)B.DF;
+  a.C = (T*)B.C;
+  a.coef = (const T*)B.coef;
+  for (int d = 0; d < 3; ++d) {
+    a.cart_metric[d] = (T)B.cart_metric[d];
+    a.tau_h[d] = (T)B.tau_h[d];
+  }
+  for (int s = 0; s < 6; ++s) {
+    a.face[s] = B.face[s];
+    a.bc[s] = B.bc[s];
+    a.pml[s] = B.pml[s];
+    a.Q[s] = (T*)B.Q[s];
+    a.DQ[s] = (T*)B.DQ[s];
+    a.slab_np[s] = B.slab_np[s];
+  }
+  a.bc_form = S->bc_form;
+  a.fault_sat = (const T*)S->sat + (long long)b * 9 * B.nr * B.ns;
+  a.npml = B.npml;
+  a.A = (T)A;
+  a.Bdt = (T)Bdt;
+  a.plastic = (S->plastic && last) ? 1 : 0;
+  a.preset = S->fp.preset;
+  a.ycoord = (const T*)B.y;
+  a.pl_c = S->pl_c; a.pl_nu = S->pl_nu; a.pl_Tv = S->pl_Tv; a.dt = S->dt;
+  return a;
+}
+
+int run_step(wql_scn* S) {
+  const long long nf = (long long)S->B[0].nr * S->B[0].ns;
+  const bool want_frame = S->frame_dev && (S->nstep % std::max(S->P.w_stride, 1) == 0);
+  const double t0 = S->t;
+  for (int stage = 1; stage <= 5; ++stage) {
+    const double A = S->rk.A[stage], Bdt = S->rk.B[stage] * S->dt;
+    const double ts = t0 + S->rk.C[stage - 1] * S->dt;
+    InterfaceArgs ia;
+    std::memset(&ia, 0, sizeof(ia));
+    ia.nr = S->B[0].nr; ia.ns = S->B[0].ns;
+    ia.np0 = S->B[0].np; ia.np1 = S->B[1].np; ia.nq0 = S->B[0].nq;
+    ia.fp64 = S->prec == WQL_FP64;
+    ia.F0 = S->B[0].F[S->cur];
+    ia.F1 = S->B[1].F[S->cur];
+    ia.face0 = S->B[0].face[1];
+    ia.face1 = S->B[1].face[0];
+    ia.xij = S->xij;
+    ia.S = S->S; ia.DS = S->DS; ia.W = S->W; ia.DW = S->DW; ia.trup = S->trup;
+    ia.sat = S->sat;
+    ia.tau_h[0] = S->B[0].tau_h[0];
+    ia.tau_h[1] = S->B[1].tau_h[0];
+    ia.A = A; ia.Bdt = Bdt; ia.t = ts; ia.stage = stage;
+    ia.fp = S->fp;
+    ia.frame = (want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
+    ia.solver_fail = S->solver_fail;
+    launch_interface(ia, S->stream);
+    for (int b = 0; b < 2; ++b) {
+      if (S->prec == WQL_FP64) launch_volume<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+      else launch_volume<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+    }
+    S->cur ^= 1;
+  }
+  CK(cudaGetLastError());
+  S->t = t0 + S->rk.C[5] * S->dt;
+  S->nstep += 1;
+  if (want_frame) {
+    S->frame_fill += 1;
+    S->nframes += 1;
+    if (S->frame_fill == S->frame_cap) return flush_frames(S);
+  }
+  return WQL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wql_last_error(char* buf, size_t n) {
+  if (buf && n) {
+    std::snprintf(buf, n, "%s", g_err.c_str());
+  }
+  return (int)g_err.size();
+}
+
+int wql_ctx_create(int device, wql_ctx** out) {
+  if (!out) return fail(WQL_E_INPUT, "null argument");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(WQL_E_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= ndev) return fail(WQL_E_INPUT, "device index out of range");
+  CK(cudaSetDevice(device));
+  wql_ctx* c = new wql_ctx();
+  c->device = device;
+  *out = c;
+  return WQL_OK;
+}
+
+int wql_ctx_destroy(wql_ctx* ctx) {
+  delete ctx;
+  return WQL_OK;
+}
+
+int wql_scenario_create_from_text(wql_ctx* ctx, const char* in_text, const char* base_dir,
+                                  int precision, wql_scn** out) {
+  if (!in_text) return fail(WQL_E_INPUT, "null input text");
+  Problem P;
+  std::string err;
+  if (parse_in_text(in_text, base_dir ? base_dir : "", P, err)) return fail(WQL_E_INPUT, err);
+  return create(ctx, std::move(P), precision, out);
+}
+
+int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision, wql_scn** out) {
+  if (!in_path) return fail(WQL_E_INPUT, "null path");
+  Problem P;
+  std::string err;
+  if (parse_in_file(in_path, P, err)) return fail(WQL_E_INPUT, err);
+  return create(ctx, std::move(P), precision, out);
+}
+
+int wql_scenario_destroy(wql_scn* scn) {
+  delete scn;
+  return WQL_OK;
+}
+
+int wql_step(wql_scn* scn, int nsteps) {
+  if (!scn) return fail(WQL_E_INPUT, "null scenario");
+  if (nsteps < 0) return fail(WQL_E_INPUT, "negative step count");
+  CK(cudaSetDevice(scn->ctx->device));
+  for (int n = 0; n < nsteps; ++n) {
+    int rc = run_step(scn);
+    if (rc) return rc;
+  }
+  return flush_frames(scn);
+}
+
+int wql_sync(wql_scn* scn, int check_nan) {
+  if (!scn) return fail(WQL_E_INPUT, "null scenario");
+  CK(cudaStreamSynchronize(scn->stream));
+  CK(cudaGetLastError());
+  unsigned int fails = 0;
+  CK(cudaMemcpy(&fails, scn->solver_fail, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (check_nan) {
+    unsigned int* cnt = nullptr;
+    CK(cudaMalloc(&cnt, sizeof(unsigned)));
+    CK(cudaMemset(cnt, 0, sizeof(unsigned)));
+    for (int b = 0; b < 2; ++b) {
+      const long long n = 9 * scn->B[b].np;
+      if (scn->prec == WQL_FP64)
+        count_nonfinite<double><<<(unsigned)((n + 255) / 256), 256, 0, scn->stream>>>((const double*)scn->B[b].F[scn->cur], n, cnt);
+      else
+        count_nonfinite<float><<<(unsigned)((n + 255) / 256), 256, 0, scn->stream>>>((const float*)scn->B[b].F[scn->cur], n, cnt);
+    }
+    unsigned int h = 0;
+    CK(cudaStreamSynchronize(scn->stream));
+    CK(cudaMemcpy(&h, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    cudaFree(cnt);
+    if (h) return fail(WQL_E_NAN, std::to_string(h) + " non-finite field values");
+  }
+  if (fails) return fail(WQL_E_SOLVER, std::to_string(fails) + " rate-and-state solves hit the 5000-iteration cap");
+  return WQL_OK;
+}
+
+int wql_get_info(wql_scn* scn, wql_info* info) {
+  if (!scn || !info) return fail(WQL_E_INPUT, "null argument");
+  for (int b = 0; b < 2; ++b) {
+    info->nq[b] = scn->B[b].nq;
+    info->nr[b] = scn->B[b].nr;
+    info->ns[b] = scn->B[b].ns;
+  }
+  info->dt = scn->dt;
+  info->t = scn->t;
+  info->nt = scn->nt;
+  info->nstep = scn->nstep;
+  info->precision = scn->prec;
+  info->frames = scn->nframes;
+  info->device_bytes = scn->device_bytes;
+  return WQL_OK;
+}
+
+int wql_get_field(wql_scn* scn, int block, int comp, double* host_out) {
+  if (!scn || !host_out || block < 0 || block > 1 || comp < 0 || comp > 8)
+    return fail(WQL_E_INPUT, "bad argument");
+  auto& B = scn->B[block];
+  CK(cudaStreamSynchronize(scn->stream));
+  if (scn->prec == WQL_FP64) {
+    CK(cudaMemcpy(host_out, (const double*)B.F[scn->cur] + comp * B.np, B.np * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    double* tmp = nullptr;
+    CK(cudaMalloc(&tmp, B.np * sizeof(double)));
+    to_double<float><<<(unsigned)((B.np + 255) / 256), 256, 0, scn->stream>>>((const float*)B.F[scn->cur] + comp * B.np, tmp, B.np);
+    CK(cudaStreamSynchronize(scn->stream));
+    CK(cudaMemcpy(host_out, tmp, B.np * sizeof(double), cudaMemcpyDeviceToHost));
+    cudaFree(tmp);
+  }
+  return WQL_OK;
+}
+
+int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in) {
+  if (!scn || !host_in || block < 0 || block > 1 || comp < 0 || comp > 8)
+    return fail(WQL_E_INPUT, "bad argument");
+  auto& B = scn->B[block];
+  CK(cudaStreamSynchronize(scn->stream));
+  double* tmp = nullptr;
+  CK(cudaMalloc(&tmp, B.np * sizeof(double)));
+  CK(cudaMemcpy(tmp, host_in, B.np * sizeof(double), cudaMemcpyHostToDevice));
+  if (scn->prec == WQL_FP64)
+    CK(cudaMemcpy((double*)B.F[scn->cur] + comp * B.np, tmp, B.np * sizeof(double), cudaMemcpyDeviceToDevice));
+  else
+    from_double<float><<<(unsigned)((B.np + 255) / 256), 256, 0, scn->stream>>>(tmp, (float*)B.F[scn->cur] + comp * B.np, B.np);
+  CK(cudaStreamSynchronize(scn->stream));
+  cudaFree(tmp);
+  return WQL_OK;
+}
+
+int wql_get_iface(wql_scn* scn, int copy, int what, double* host_out) {
+  if (!scn || !host_out || copy < 0 || copy > 1 || what < 0 || what > 5) return fail(WQL_E_INPUT, "bad argument");
+  const long long nf = (long long)scn->B[0].nr * scn->B[0].ns;
+  const double* src;
+  if (what < 4) src = scn->S + ((long long)copy * 4 + what) * nf;
+  else if (what == 4) src = scn->W + (long long)copy * nf;
+  else src = scn->trup + (long long)copy * nf;
+  CK(cudaStreamSynchronize(scn->stream));
+  CK(cudaMemcpy(host_out, src, nf * sizeof(double), cudaMemcpyDeviceToHost));
+  return WQL_OK;
+}
+
+int wql_frame_count(wql_scn* scn, int* frames) {
+  if (!scn || !frames) return fail(WQL_E_INPUT, "null argument");
+  *frames = scn->nframes;
+  return WQL_OK;
+}
+
+int wql_get_frames(wql_scn* scn, int what, float* host_out) {
+  if (!scn || !host_out || what < 0 || what > 7) return fail(WQL_E_INPUT, "bad argument");
+  int rc = flush_frames(scn);
+  if (rc) return rc;
+  const long long nf = (long long)scn->B[0].nr * scn->B[0].ns;
+  const int off = kFrameOff[what], nc = kFrameOff[what + 1] - kFrameOff[what];
+  for (int fr = 0; fr < scn->nframes; ++fr) {
+    const float* src = scn->frames_host.data() + (size_t)fr * kFrameWords * nf + (size_t)off * nf;
+    std::memcpy(host_out + (size_t)fr * nc * nf, src, (size_t)nc * nf * sizeof(float));
+  }
+  return WQL_OK;
+}
+
+int wql_scenario_stream(wql_scn* scn, uintptr_t* stream) {
+  if (!scn || !stream) return fail(WQL_E_INPUT, "null argument");
+  *stream = (uintptr_t)scn->stream;
+  return WQL_OK;
+}
+
+int wql_launches_per_step(wql_scn* scn, int* launches) {
+  if (!scn || !launches) return fail(WQL_E_INPUT, "null argument");
+  *launches = 5 * 3;  // per stage: interface + one volume launch per block
+  return WQL_OK;
+}
+
+}  // extern "C"

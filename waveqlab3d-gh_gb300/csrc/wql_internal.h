@@ -1,0 +1,111 @@
+// Device-side data layout and kernel argument blocks (internal).
+//
+// HBM layout per block (nq x nr x ns points, q fastest, no ghost layers --
+// the reference's 3-deep MPI halos, src/mpi3dcomm.f90:722-746, do not exist
+// on one GPU):
+//   F[2]  : 9 x np field components, ping-pong buffers (stage reads one and
+//           writes the other, so neighbours never see a half-updated state)
+//   DF    : 9 x np rates (RK 2N-storage register), updated in place
+//   C     : 9 x np Kahan compensation of F (FP32-compensated mode only)
+//   coef  : curvilinear: 13 x np = J*metric (3 directions x 3 components),
+//           1/J, lambda, mu, 1/(rho*J); Cartesian: 3 x np = lambda, mu, 1/rho
+//   face  : per side 15 x nface (FP64): n(3), m(3), l(3), grad(3) of the
+//           face-normal coordinate, lambda, mu, rho
+//   Q/DQ  : PML auxiliary fields on slabs of npml layers per active side
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "wql_presets.cuh"
+
+namespace wql {
+
+constexpr int kFaceWords = 15;
+constexpr int kCurvCoef = 13;
+constexpr int kCartCoef = 3;
+
+// Boundary penalty selection for the outer faces.
+enum BcForm : int { BC_CHARACTERISTIC = 0, BC_WEIGHTED = 1 };
+
+template <typename T>
+struct VolumeArgs {
+  int nq, nr, ns;
+  long long np;
+  int block;          // 0: fault on the q = nq face; 1: fault on the q = 1 face
+  T rh[3];            // 1/h per axis, h = 1/(n-1)
+  const T* __restrict__ Fin;
+  T* __restrict__ Fout;
+  T* __restrict__ DF;
+  T* __restrict__ C;  // compensation (FP32C) or nullptr
+  const T* __restrict__ coef;
+  T cart_metric[3];   // q_x, r_y, s_z for Cartesian blocks
+  // outer faces (side 0..5 = -q,+q,-r,+r,-s,+s)
+  const double* face[6];
+  int bc[6];          // 1 absorbing, 2 free surface, 3 clamped, else none
+  int bc_form;
+  T tau_h[3];         // tau0 / h per axis
+  // fault SAT added on the fault face (9 x nr*ns), already scaled by tau0/h
+  const T* __restrict__ fault_sat;
+  // PML
+  int pml[6];
+  int npml;
+  T* Q[6];
+  T* DQ[6];
+  long long slab_np[6];
+  int interior_lo[3], interior_hi[3];  // 0-based inclusive interior box
+  // RK
+  T A, Bdt;
+  // plasticity on the last stage
+  int plastic;
+  int preset;
+  const T* __restrict__ ycoord;  // depth coordinate for the initial stress
+  double pl_c, pl_nu, pl_Tv, dt;
+};
+
+struct InterfaceArgs {
+  int nr, ns;
+  long long np0, np1;
+  int nq0;
+  int fp64;                 // fields are double (1) or float (0)
+  const void* F0;           // block 0 fields (9 x np0)
+  const void* F1;           // block 1 fields (9 x np1)
+  const double* face0;      // block 0, side +q (15 x nf)
+  const double* face1;      // block 1, side -q (15 x nf)
+  const double* xij;        // 2 x 3 x nf fault-point coordinates per block copy
+  double* S;                // 2 x 4 x nf
+  double* DS;               // 2 x 4 x nf
+  double* W;                // 2 x nf
+  double* DW;               // 2 x nf
+  double* trup;             // 2 x nf
+  void* sat;                // 2 x 9 x nf (T), scaled by tau0/h of the block
+  double tau_h[2];
+  double A, Bdt, t;
+  int stage;
+  FaultParams fp;
+  float* frame;             // 39 x nf or nullptr
+  unsigned int* solver_fail;  // count of non-converged rate-and-state solves
+};
+
+// Frame record layout (floats per fault point, component-major):
+// Uface 9, Vface 9, S 4, Uhat 6, Vhat 6, Svel 3, trup 1, state 1.
+constexpr int kFrameWords = 39;
+enum FrameOff : int {
+  FR_UFACE = 0, FR_VFACE = 9, FR_S = 18, FR_UHAT = 22, FR_VHAT = 28, FR_SVEL = 34,
+  FR_TRUP = 37, FR_STATE = 38, FR_END = 39
+};
+// offsets of streams 0..7 (+ end) in the order of wql_get_frames
+constexpr int kFrameOff[9] = {FR_UFACE, FR_VFACE, FR_S, FR_UHAT, FR_VHAT, FR_SVEL, FR_TRUP, FR_STATE, FR_END};
+
+// Kernel launchers (stream-ordered).
+template <typename T>
+void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream);
+void launch_interface(const InterfaceArgs& a, void* stream);
+void launch_metrics(int nq, int nr, int ns, const double* x, double* metric, double* J,
+                    void* stream);
+void launch_faces(int nq, int nr, int ns, const double* metric, const double* lam,
+                  const double* mu, const double* rho, double* const face[6], void* stream);
+template <typename T>
+void launch_coef(long long np, bool curv, const double* metric, const double* J,
+                 const double* lam, const double* mu, const double* rho, T* coef, void* stream);
+
+}  // namespace wql

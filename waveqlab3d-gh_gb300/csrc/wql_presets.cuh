@@ -1,0 +1,256 @@
+// Fault-physics presets evaluated per fault point on the device (and host).
+//
+// The reference selects prestress, strength, rate-and-state parameters and
+// initial stress by the `problem` string inside every per-point call
+// (src/Interface_Condition.f90:1268-2476, src/initial_stress_condition.f90).
+// Here the string is resolved once to an integer preset and the formulas are
+// evaluated branch-free of string compares.  `param` presets (sw_param,
+// rs_param) take their constants from the &fault_list extension group.
+#pragma once
+#include <math.h>
+
+#include "wql_sbp.cuh"
+
+namespace wql {
+
+enum Preset : int {
+  PRE_NONE = 0,
+  PRE_TPV5 = 1,   // also LOH1 / OKLAHOMA prestress
+  PRE_TPV26 = 2,
+  PRE_TPV27 = 3,
+  PRE_TPV28 = 4,
+  PRE_TPV29 = 5,
+  PRE_TPV30 = 6,
+  PRE_TPV10 = 7,
+  PRE_TPV101 = 8,
+  PRE_TPV102 = 9,
+  PRE_SW_PARAM = 10,
+  PRE_RS_PARAM = 11,
+};
+
+enum Coupling : int { CPL_LOCKED = 0, CPL_LINEAR = 1, CPL_SW = 2, CPL_RS = 3 };
+
+struct FaultParams {
+  int preset;
+  int coupling;
+  double fs, fd, Dc, barrier_y, barrier_z;
+  double a, b, V0, f0, L, Vini;
+  double Tn, Tm, Tl, nuc_amp, nuc_radius, nuc_y, nuc_z, nuc_rise;
+};
+
+// boxcar / smooth_boxcar: src/Interface_Condition.f90:2438-2476
+WQL_HD double boxcar(double x, double w) {
+  const double tol = 100.0 * 2.220446049250313e-16;
+  if (-w + tol < x && x < w - tol) return 1.0;
+  if (fabs(-w - x) <= tol || fabs(x - w) <= tol) return 0.5;
+  return 0.0;
+}
+
+WQL_HD double smooth_boxcar(double x, double w, double wr) {
+  if (-w <= x && x <= w) return 1.0;
+  const double ax = fabs(x);
+  if (ax > w && ax < w + wr) return 0.5 * (1.0 + tanh(wr / (ax - w - wr) + wr / (ax - w)));
+  return 0.0;
+}
+
+// initial_stress_tensor (src/initial_stress_condition.f90:8-254): s0 =
+// (sxx, syy, szz, sxy, sxz, syz).  Returns false for presets without one.
+WQL_HD bool initial_stress(int preset, const double x[3], double s0[6]) {
+  switch (preset) {
+    case PRE_TPV26:
+    case PRE_TPV27:
+    case PRE_TPV29:
+    case PRE_TPV30: {
+      const bool p29 = preset == PRE_TPV29 || preset == PRE_TPV30;
+      const double y1 = p29 ? 17.0 : 15.0, y2 = p29 ? 22.0 : 20.0;
+      double Om = 0.0;
+      if (x[1] <= y1) Om = 1.0;
+      else if (x[1] >= y1 && x[1] <= y2) Om = (y2 - x[1]) / 5.0;
+      const double b11 = p29 ? 1.025837 : 0.926793, b33 = p29 ? 0.974162 : 1.073206;
+      const double b13 = p29 ? -0.158649 : -0.169029;
+      const double Pf = 9.8 * x[1], s22 = -2.67 * 9.8 * x[1];
+      s0[0] = Om * (b33 * (s22 + Pf) - Pf) + (1.0 - Om) * s22 + Pf;
+      s0[1] = s22 + Pf;
+      s0[2] = Om * (b11 * (s22 + Pf) - Pf) + (1.0 - Om) * s22 + Pf;
+      s0[3] = 0.0;
+      s0[4] = Om * (b13 * (s22 + Pf));
+      s0[5] = 0.0;
+      return true;
+    }
+    case PRE_TPV28:
+      s0[0] = -60.0; s0[1] = 0.0; s0[2] = 60.0; s0[3] = 0.0; s0[4] = 29.38; s0[5] = 0.0;
+      return true;
+    case PRE_TPV101:
+    case PRE_TPV102:
+      s0[0] = -120.0; s0[1] = 0.0; s0[2] = -120.0; s0[3] = 0.0; s0[4] = 75.0; s0[5] = 0.0;
+      return true;
+    case PRE_TPV10:
+      s0[0] = -7.378 * x[1]; s0[1] = 0.0; s0[2] = -7.378 * x[1]; s0[3] = 0.0;
+      s0[4] = -0.55 * s0[0]; s0[5] = 0.0;
+      return true;
+    default:
+      return false;
+  }
+}
+
+WQL_HD void tensor_traction(const double s0[6], const double n[3], const double m[3],
+                            const double l[3], double& Tn, double& Tm, double& Tl) {
+  const double Tx = n[0] * s0[0] + n[1] * s0[3] + n[2] * s0[4];
+  const double Ty = n[0] * s0[3] + n[1] * s0[1] + n[2] * s0[5];
+  const double Tz = n[0] * s0[4] + n[1] * s0[5] + n[2] * s0[2];
+  Tn = n[0] * Tx + n[1] * Ty + n[2] * Tz;
+  Tm = m[0] * Tx + m[1] * Ty + m[2] * Tz;
+  Tl = l[0] * Tx + l[1] * Ty + l[2] * Tz;
+}
+
+// TPV101/102 nucleation time function G(t) (src/Interface_Condition.f90:2344-2351)
+WQL_HD double smooth_ramp(double t) {
+  double G = 0.0;
+  if (t > 0.0 && t < 1.0) G = exp((t - 1.0) * (t - 1.0) / (t * (t - 2.0)));
+  if (t >= 1.0) G = 1.0;
+  return G;
+}
+
+// prestress (src/Interface_Condition.f90:1802-2435)
+WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const double l[3],
+                      const double m[3], const double n[3], double& Tn, double& Tm, double& Tl) {
+  double s0[6];
+  switch (fp.preset) {
+    case PRE_TPV5:
+      Tn = -120.0;
+      Tm = 0.0;
+      Tl = 70.0;
+      Tl = Tl + 8.0 * boxcar(x[1] - 7.5, 1.5) * boxcar(x[2] + 7.5, 1.5);
+      Tl = Tl + 11.6 * boxcar(x[1] - 7.5, 1.5) * boxcar(x[2], 1.5);
+      Tl = Tl - 8.0 * boxcar(x[1] - 7.5, 1.5) * boxcar(x[2] - 7.5, 1.5);
+      return;
+    case PRE_TPV26:
+    case PRE_TPV27:
+    case PRE_TPV29:
+    case PRE_TPV30:
+      initial_stress(fp.preset, x, s0);
+      tensor_traction(s0, n, m, l, Tn, Tm, Tl);
+      return;
+    case PRE_TPV28: {
+      initial_stress(fp.preset, x, s0);
+      tensor_traction(s0, n, m, l, Tn, Tm, Tl);
+      const double r = sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
+      double nuke = 0.0;
+      if (r <= 1.4) nuke = 11.60;
+      else if (r >= 1.4 && r <= 2.0) nuke = 5.8 * (1.0 + cos(3.141592653589793 * (r - 1.4) / 0.6));
+      Tl = Tl + nuke;
+      return;
+    }
+    case PRE_TPV101:
+    case PRE_TPV102: {
+      initial_stress(fp.preset, x, s0);
+      tensor_traction(s0, n, m, l, Tn, Tm, Tl);
+      const double r = sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
+      double F = 0.0;
+      if (r < 3.0) F = exp(r * r / (r * r - 9.0));
+      Tl = Tl + 25.0 * F * smooth_ramp(t);
+      return;
+    }
+    case PRE_TPV10: {
+      const double g = 2.0 / sqrt(3.0);
+      Tn = -7.378 * x[1] * g;
+      Tm = -0.55 * Tn;
+      Tl = 0.0;
+      Tm = Tm + (-(0.760 + 0.0057) * Tn + 0.2 - Tm) * boxcar(x[1] * g - 12.0, 1.5) * boxcar(x[2], 1.5);
+      return;
+    }
+    case PRE_SW_PARAM:
+    case PRE_RS_PARAM: {
+      Tn = fp.Tn;
+      Tm = fp.Tm;
+      Tl = fp.Tl;
+      const double dy = x[1] - fp.nuc_y, dz = x[2] - fp.nuc_z;
+      const double F = exp(-(dy * dy + dz * dz) / (2.0 * fp.nuc_radius * fp.nuc_radius));
+      const double G = fp.nuc_rise > 0.0 ? smooth_ramp(t / fp.nuc_rise) : 1.0;
+      Tl = Tl + fp.nuc_amp * F * G;
+      return;
+    }
+    default:
+      Tn = Tm = Tl = 0.0;
+  }
+}
+
+WQL_HD double forced_rupture_time(double r, double Vs) {
+  const double rc = 4.0;
+  if (r < rc - 1.0e-9) return r / (0.7 * Vs) + 0.081 * rc / (0.7 * Vs) * (1.0 / (1.0 - (r / rc) * (r / rc)) - 1.0);
+  return 1.0e9;
+}
+
+// Tau_strength (src/Interface_Condition.f90:1268-1797)
+WQL_HD double tau_strength(const FaultParams& fp, double sigma_n, double D, const double x[3],
+                           double t) {
+  switch (fp.preset) {
+    case PRE_TPV5: {
+      double fs = 0.677 + 1.0e10 * (1.0 - boxcar(x[1], 15.0) * boxcar(x[2], 15.0));
+      const double fd = 0.525, Dc = 0.4;
+      return sigma_n * (fs - (fs - fd) * fmin(D, Dc) / Dc);
+    }
+    case PRE_TPV28: {
+      double fs = 0.677 + 1.0e10 * (1.0 - boxcar(x[1], 15.0) * boxcar(x[2], 18.0));
+      const double fd = 0.373, Dc = 0.4;
+      return sigma_n * (fs - (fs - fd) * fmin(D, Dc) / Dc);
+    }
+    case PRE_TPV26:
+    case PRE_TPV27:
+    case PRE_TPV29:
+    case PRE_TPV30: {
+      const bool p29 = fp.preset == PRE_TPV29 || fp.preset == PRE_TPV30;
+      double fs = 0.18;
+      const double fd = 0.12, Dc = 0.3, t0 = 0.5, Vs = 3.464;
+      const double r = sqrt((x[1] - 10.0) * (x[1] - 10.0) + (x[2] + 5.0) * (x[2] + 5.0));
+      const double depth = x[1];
+      double C0;
+      if (p29) C0 = depth <= 4.0 ? 0.4 + 0.2 * (4.0 - depth) : 0.4;
+      else C0 = depth <= 5.0 ? 0.4 + 0.72 * (5.0 - depth) : 0.4;
+      const double box = boxcar(x[1], 20.0) * boxcar(x[2], 20.0);
+      if (p29) C0 = C0 + 1.0e10 * (1.0 - box);
+      const double tf = forced_rupture_time(r, Vs);
+      const double f1 = fmin(D / Dc, 1.0);
+      double f2 = 0.0;
+      if (t < tf) f2 = 0.0;
+      else if (t >= tf && t < tf + t0) f2 = (t - tf) / t0;
+      else if (t >= tf + t0) f2 = 1.0;
+      if (!p29) fs = fs + 1.0e10 * (1.0 - box);
+      const double f = fs - (fs - fd) * fmax(f1, f2);
+      return C0 + f * sigma_n;
+    }
+    case PRE_TPV10: {
+      const double g = 2.0 / sqrt(3.0);
+      const double bb = boxcar(x[1] * g, 15.0) * boxcar(x[2], 15.0);
+      const double fs = 0.760 + (1.0e4 - 0.760) * (1.0 - bb);
+      const double fd = 0.448, Dc = 0.50;
+      const double f = fs - (fs - fd) * fmin(D, Dc) / Dc;
+      const double C0 = 0.2 + 1.0e3 * (1.0 - bb);
+      return C0 + fmax(sigma_n, 0.0) * f;
+    }
+    case PRE_SW_PARAM: {
+      double fs = fp.fs + 1.0e10 * (1.0 - boxcar(x[1], fp.barrier_y) * boxcar(x[2], fp.barrier_z));
+      return sigma_n * (fs - (fs - fp.fd) * fmin(D, fp.Dc) / fp.Dc);
+    }
+    default:
+      return 0.0;
+  }
+}
+
+struct RSParams {
+  double L0, f0, b, V0, a;
+};
+
+// rate-and-state constants per point (src/Interface_Condition.f90:384-417)
+WQL_HD RSParams rs_params(const FaultParams& fp, const double x[3]) {
+  RSParams r;
+  if (fp.preset == PRE_RS_PARAM) {
+    r.L0 = fp.L; r.f0 = fp.f0; r.b = fp.b; r.V0 = fp.V0; r.a = fp.a;
+  } else {
+    r.L0 = 0.02; r.f0 = 0.6; r.b = 0.012; r.V0 = 1.0e-6;
+    r.a = 0.008 + 0.008 * (1.0 - smooth_boxcar(x[1], 15.0, 3.0) * smooth_boxcar(x[2], 15.0, 3.0));
+  }
+  return r;
+}
+
+}  // namespace wql

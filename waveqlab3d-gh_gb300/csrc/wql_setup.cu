@@ -1,0 +1,183 @@
+// One-time FP64 precompute on the device: metric terms, Jacobian, face
+// frames and the per-point stencil coefficients.
+//
+//   metrics + J ....... derivatives (src/grid.f90:396-469) with the SBP-6
+//                       operator (src/metrics.f90:16-488)
+//   face frames ....... local_orth_vectors_{q,r,s} + gen_orth_vectors
+//                       (src/unit_normals.f90:8-282)
+//   coefficients ...... J*metric, 1/J, lambda, mu, 1/(rho*J), the terms the
+//                       stencils of src/JU_xJU_yJU_z6.f90 multiply by
+#include <cuda_runtime.h>
+
+#include "wql_internal.h"
+#include "wql_sbp.cuh"
+
+namespace wql {
+namespace {
+
+__constant__ double c_sbp_setup[6][9] = WQL_SBP_TABLE;
+
+// D(u)/h along one axis at 0-based index i (stride between neighbours `st`).
+__device__ double deriv_fp64(const double* __restrict__ u, long long p, int i, int n,
+                             long long st, double rh) {
+  const int kind = sbp_kind(i, n);
+  double s;
+  if (kind == 0) {
+    s = kC1 * (u[p + st] - u[p - st]) + kC2 * (u[p + 2 * st] - u[p - 2 * st]) +
+        kC3 * (u[p + 3 * st] - u[p - 3 * st]);
+  } else if (kind < 0) {
+    const int row = -kind - 1;
+    const long long p0 = p - (long long)i * st;
+    s = 0.0;
+    for (int c = 0; c < 9; ++c) s += c_sbp_setup[row][c] * u[p0 + c * st];
+  } else {
+    const int row = kind - 1;
+    const long long pn = p + (long long)(n - 1 - i) * st;
+    s = 0.0;
+    for (int c = 0; c < 9; ++c) s += c_sbp_setup[row][c] * u[pn - c * st];
+    s = -s;
+  }
+  return rh * s;
+}
+
+__global__ void metrics_kernel(int nq, int nr, int ns, const double* __restrict__ x,
+                               double* __restrict__ metric, double* __restrict__ J) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nq || j >= nr || k >= ns) return;
+  const long long np = (long long)nq * nr * ns;
+  const long long p = i + (long long)nq * (j + (long long)nr * k);
+  const long long st[3] = {1, nq, (long long)nq * nr};
+  const int idx[3] = {i, j, k};
+  const int n[3] = {nq, nr, ns};
+  double Xd[3][3];  // Xd[d][c] = d x_c / d xi_d
+  for (int d = 0; d < 3; ++d)
+    for (int c = 0; c < 3; ++c)
+      Xd[d][c] = deriv_fp64(x + c * np, p, idx[d], n[d], st[d], (double)(n[d] - 1));
+  const double* Xq = Xd[0];
+  const double* Xr = Xd[1];
+  const double* Xs = Xd[2];
+  const double Jp = Xq[0] * (Xr[1] * Xs[2] - Xr[2] * Xs[1]) - Xq[1] * (Xr[0] * Xs[2] - Xr[2] * Xs[0]) +
+                    Xq[2] * (Xr[0] * Xs[1] - Xr[1] * Xs[0]);
+  const double iJ = 1.0 / Jp;
+  J[p] = Jp;
+  // metric[3*j + d]: j = x,y,z component, d = q,r,s
+  metric[0 * np + p] = iJ * (Xr[1] * Xs[2] - Xr[2] * Xs[1]);
+  metric[1 * np + p] = iJ * (Xq[2] * Xs[1] - Xq[1] * Xs[2]);
+  metric[2 * np + p] = iJ * (Xq[1] * Xr[2] - Xq[2] * Xr[1]);
+  metric[3 * np + p] = iJ * (Xr[2] * Xs[0] - Xr[0] * Xs[2]);
+  metric[4 * np + p] = iJ * (Xq[0] * Xs[2] - Xq[2] * Xs[0]);
+  metric[5 * np + p] = iJ * (Xq[2] * Xr[0] - Xq[0] * Xr[2]);
+  metric[6 * np + p] = iJ * (Xr[0] * Xs[1] - Xr[1] * Xs[0]);
+  metric[7 * np + p] = iJ * (Xq[1] * Xs[0] - Xq[0] * Xs[1]);
+  metric[8 * np + p] = iJ * (Xq[0] * Xr[1] - Xq[1] * Xr[0]);
+}
+
+struct FacePtrs {
+  double* f[6];
+};
+
+__global__ void faces_kernel(int nq, int nr, int ns, const double* __restrict__ metric,
+                             const double* __restrict__ lam, const double* __restrict__ mu,
+                             const double* __restrict__ rho, FacePtrs out) {
+  const int side = blockIdx.z;
+  const int axis = side / 2;
+  const bool hi = side & 1;
+  const int na = axis == 0 ? nr : nq;
+  const int nb = axis == 2 ? nr : ns;
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= na || b >= nb) return;
+  int i, j, k;
+  if (axis == 0) { i = hi ? nq - 1 : 0; j = a; k = b; }
+  else if (axis == 1) { i = a; j = hi ? nr - 1 : 0; k = b; }
+  else { i = a; j = b; k = hi ? ns - 1 : 0; }
+  const long long np = (long long)nq * nr * ns;
+  const long long p = i + (long long)nq * (j + (long long)nr * k);
+  const double gx = metric[(0 * 3 + axis) * np + p];
+  const double gy = metric[(1 * 3 + axis) * np + p];
+  const double gz = metric[(2 * 3 + axis) * np + p];
+  const double norm = sqrt(gx * gx + gy * gy + gz * gz);
+  const double n[3] = {gx / norm, gy / norm, gz / norm};
+  // gen_orth_vectors: m seeded with y, Gram-Schmidt; z if n is parallel to y
+  double m[3] = {0.0, 1.0, 0.0};
+  const double d1 = sqrt((n[0] - m[0]) * (n[0] - m[0]) + (n[1] - m[1]) * (n[1] - m[1]) + (n[2] - m[2]) * (n[2] - m[2]));
+  const double d2 = sqrt((n[0] + m[0]) * (n[0] + m[0]) + (n[1] + m[1]) * (n[1] + m[1]) + (n[2] + m[2]) * (n[2] + m[2]));
+  if (!(d1 >= 1.0e-12 && d2 >= 1.0e-12)) { m[1] = 0.0; m[2] = 1.0; }
+  const double an = n[0] * m[0] + n[1] * m[1] + n[2] * m[2];
+  for (int c = 0; c < 3; ++c) m[c] -= an * n[c];
+  const double inv = 1.0 / sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+  for (int c = 0; c < 3; ++c) m[c] *= inv;
+  const double l[3] = {n[1] * m[2] - n[2] * m[1], n[2] * m[0] - n[0] * m[2], n[0] * m[1] - n[1] * m[0]};
+  const long long nf = (long long)na * nb;
+  const long long f = a + (long long)na * b;
+  double* o = out.f[side];
+  for (int c = 0; c < 3; ++c) {
+    o[(0 + c) * nf + f] = n[c];
+    o[(3 + c) * nf + f] = m[c];
+    o[(6 + c) * nf + f] = l[c];
+  }
+  o[9 * nf + f] = gx;
+  o[10 * nf + f] = gy;
+  o[11 * nf + f] = gz;
+  o[12 * nf + f] = lam[p];
+  o[13 * nf + f] = mu[p];
+  o[14 * nf + f] = rho[p];
+}
+
+template <typename T>
+__global__ void coef_kernel(long long np, int curv, const double* __restrict__ metric,
+                            const double* __restrict__ J, const double* __restrict__ lam,
+                            const double* __restrict__ mu, const double* __restrict__ rho,
+                            T* __restrict__ coef) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  if (curv) {
+    const double Jp = J[p];
+    for (int d = 0; d < 3; ++d)
+      for (int c = 0; c < 3; ++c) coef[(d * 3 + c) * np + p] = (T)(Jp * metric[(c * 3 + d) * np + p]);
+    coef[9 * np + p] = (T)(1.0 / Jp);
+    coef[10 * np + p] = (T)lam[p];
+    coef[11 * np + p] = (T)mu[p];
+    coef[12 * np + p] = (T)(1.0 / (rho[p] * Jp));
+  } else {
+    coef[0 * np + p] = (T)lam[p];
+    coef[1 * np + p] = (T)mu[p];
+    coef[2 * np + p] = (T)(1.0 / rho[p]);
+  }
+}
+
+}  // namespace
+
+void launch_metrics(int nq, int nr, int ns, const double* x, double* metric, double* J,
+                    void* stream) {
+  dim3 blk(32, 4, 1), grd((nq + 31) / 32, (nr + 3) / 4, ns);
+  metrics_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(nq, nr, ns, x, metric, J);
+}
+
+void launch_faces(int nq, int nr, int ns, const double* metric, const double* lam,
+                  const double* mu, const double* rho, double* const face[6], void* stream) {
+  FacePtrs fp;
+  for (int s = 0; s < 6; ++s) fp.f[s] = face[s];
+  const int mx = nq > nr ? nq : nr;
+  const int my = nr > ns ? nr : ns;
+  dim3 blk(32, 4, 1), grd((mx + 31) / 32, (my + 3) / 4, 6);
+  faces_kernel<<<grd, blk, 0, (cudaStream_t)stream>>>(nq, nr, ns, metric, lam, mu, rho, fp);
+}
+
+template <typename T>
+void launch_coef(long long np, bool curv, const double* metric, const double* J,
+                 const double* lam, const double* mu, const double* rho, T* coef, void* stream) {
+  const int blk = 256;
+  const long long grd = (np + blk - 1) / blk;
+  coef_kernel<T><<<(unsigned)grd, blk, 0, (cudaStream_t)stream>>>(np, curv ? 1 : 0, metric, J, lam,
+                                                                   mu, rho, coef);
+}
+
+template void launch_coef<double>(long long, bool, const double*, const double*, const double*,
+                                  const double*, const double*, double*, void*);
+template void launch_coef<float>(long long, bool, const double*, const double*, const double*,
+                                 const double*, const double*, float*, void*);
+
+}  // namespace wql

@@ -1,0 +1,176 @@
+"""Python binding of the C ABI in include/wql.h (ctypes).
+
+Mirrors the reference's driver loop (src/main.f90:63-129): build a domain
+from a `.in` file, advance it step by step, read fields and the fault output
+streams.  The library must have been built (wql_build.build()); there is no
+fallback path -- without the CUDA library every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libwql.so")
+
+FP64 = 0
+FP32C = 1
+STREAMS = ["Uface", "Vface", "S", "Uhat", "Vhat", "Svel", "trup", "state"]
+NCOMP = {"Uface": 9, "Vface": 9, "S": 4, "Uhat": 6, "Vhat": 6, "Svel": 3, "trup": 1, "state": 1}
+ERRORS = {1: "WQL_E_INPUT", 2: "WQL_E_OOM", 3: "WQL_E_CUDA", 4: "WQL_E_NAN", 5: "WQL_E_SOLVER",
+          6: "WQL_E_STATE"}
+EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_create_from_in",
+           "wql_scenario_create_from_text", "wql_scenario_destroy", "wql_step", "wql_sync",
+           "wql_get_info", "wql_get_field", "wql_set_field", "wql_get_iface", "wql_frame_count",
+           "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step"]
+
+
+class WqlError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("nq", ctypes.c_int * 2), ("nr", ctypes.c_int * 2), ("ns", ctypes.c_int * 2),
+                ("dt", ctypes.c_double), ("t", ctypes.c_double), ("nt", ctypes.c_int),
+                ("nstep", ctypes.c_int), ("precision", ctypes.c_int), ("frames", ctypes.c_int),
+                ("device_bytes", ctypes.c_longlong)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise WqlError(3, f"{LIB_PATH} is missing; build it with wql_build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ci = ctypes.c_void_p, ctypes.c_int
+        L.wql_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+        L.wql_ctx_create.argtypes = [ci, ctypes.POINTER(vp)]
+        L.wql_ctx_destroy.argtypes = [vp]
+        L.wql_scenario_create_from_in.argtypes = [vp, ctypes.c_char_p, ci, ctypes.POINTER(vp)]
+        L.wql_scenario_create_from_text.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ci, ctypes.POINTER(vp)]
+        L.wql_scenario_destroy.argtypes = [vp]
+        L.wql_step.argtypes = [vp, ci]
+        L.wql_sync.argtypes = [vp, ci]
+        L.wql_get_info.argtypes = [vp, ctypes.POINTER(Info)]
+        L.wql_get_field.argtypes = [vp, ci, ci, vp]
+        L.wql_set_field.argtypes = [vp, ci, ci, vp]
+        L.wql_get_iface.argtypes = [vp, ci, ci, vp]
+        L.wql_frame_count.argtypes = [vp, ctypes.POINTER(ci)]
+        L.wql_get_frames.argtypes = [vp, ci, vp]
+        L.wql_scenario_stream.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+        L.wql_launches_per_step.argtypes = [vp, ctypes.POINTER(ci)]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(1024)
+        lib().wql_last_error(buf, 1024)
+        raise WqlError(rc, buf.value.decode())
+
+
+class Context:
+    def __init__(self, device=0):
+        self.h = ctypes.c_void_p()
+        _check(lib().wql_ctx_create(device, ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            lib().wql_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scenario:
+    """One two-block domain on the GPU (the reference's `domain_type`)."""
+
+    def __init__(self, ctx, in_path=None, text=None, precision=FP64, base_dir=None):
+        self.ctx = ctx
+        self.h = ctypes.c_void_p()
+        if text is not None:
+            _check(lib().wql_scenario_create_from_text(
+                ctx.h, text.encode(), base_dir.encode() if base_dir else None, precision,
+                ctypes.byref(self.h)))
+        else:
+            _check(lib().wql_scenario_create_from_in(ctx.h, str(in_path).encode(), precision,
+                                                     ctypes.byref(self.h)))
+        self.precision = precision
+
+    def close(self):
+        if self.h:
+            lib().wql_scenario_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        i = Info()
+        _check(lib().wql_get_info(self.h, ctypes.byref(i)))
+        return i
+
+    @property
+    def dims(self):
+        i = self.info()
+        return [(i.nq[b], i.nr[b], i.ns[b]) for b in range(2)]
+
+    def step(self, n=1):
+        _check(lib().wql_step(self.h, n))
+
+    def sync(self, check_nan=False):
+        _check(lib().wql_sync(self.h, 1 if check_nan else 0))
+
+    def field(self, block, comp):
+        nq, nr, ns = self.dims[block]
+        out = np.empty(nq * nr * ns, np.float64)
+        _check(lib().wql_get_field(self.h, block, comp, out.ctypes.data))
+        return out.reshape(ns, nr, nq)
+
+    def fields(self, block):
+        return np.stack([self.field(block, c) for c in range(9)])
+
+    def set_field(self, block, comp, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        _check(lib().wql_set_field(self.h, block, comp, a.ctypes.data))
+
+    def iface(self, copy, what):
+        nr, ns = self.dims[0][1], self.dims[0][2]
+        out = np.empty(nr * ns, np.float64)
+        _check(lib().wql_get_iface(self.h, copy, what, out.ctypes.data))
+        return out.reshape(ns, nr)
+
+    def frame_count(self):
+        n = ctypes.c_int()
+        _check(lib().wql_frame_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def frames(self, name):
+        nf = self.frame_count()
+        nr, ns = self.dims[0][1], self.dims[0][2]
+        out = np.empty(nf * NCOMP[name] * nr * ns, np.float32)
+        _check(lib().wql_get_frames(self.h, STREAMS.index(name), out.ctypes.data))
+        return out.reshape(nf, NCOMP[name], ns, nr)
+
+    def stream(self):
+        s = ctypes.c_size_t()
+        _check(lib().wql_scenario_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def launches_per_step(self):
+        n = ctypes.c_int()
+        _check(lib().wql_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value
