@@ -1,0 +1,339 @@
+"""Throughput benchmark: grid-point RK-stage updates/s on one GB300.
+
+Workload (default): config 1 -- two 201^3 curvilinear blocks with seeded
+topography and a self-similar rough fault, aging-law rate-and-state friction,
+run in the FP32-compensated mode (the production path) with the FP64 mode
+timed side by side.  One "step" is one time step = 5 RK stages over both
+blocks (src/time_step.f90:68-150).  updates = sum(nq*nr*ns) * 5 * steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the reference's CPU algorithm (the FP64 restatement in
+oracle/, all host threads) is timed on the same workload; each step is one
+full time step of config 1.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "waveqlab3d-gh_gb300"))
+
+METRIC = "grid-pt RK-stage updates/s + HBM %peak; served solves/s, p50/p99 @FP32 vs FP64"
+UNIT = "grid-point RK-stage updates/s"
+# Algorithmic bytes per grid-point RK stage of the fused volume kernel:
+# F read 9 + F write 9 + DF read 9 + DF write 9 (+ Kahan compensation read 9 +
+# write 9 in FP32C) + coefficients (J*metric 9, 1/J, lambda, mu, 1/(rho J)).
+BYTES_PER_UPDATE = {("curv", "fp32c"): (54 + 13) * 4, ("curv", "fp64"): (36 + 13) * 8,
+                    ("cart", "fp32c"): (54 + 3) * 4, ("cart", "fp64"): (36 + 3) * 8}
+L2_BYTES = 129 * 1024 * 1024
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def workload(args):
+    import wql_configs
+    text, media = wql_configs.config1(n=args.n, steps=10 ** 6, seed=args.seed)
+    return text, media, wql_configs.updates_per_step(text)
+
+
+def time_gpu(wql, ctx, text, media, prec, steps, warmup, world):
+    import torch
+    s = wql.Scenario(ctx, text=text, precision=prec, media=media)
+    st = torch.cuda.ExternalStream(s.stream())
+    s.step(warmup)
+    s.sync(check_nan=True)
+    s.profile(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0.record(st)
+    s.step(steps)
+    e1.record(st)
+    s.sync()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    kt = s.kernel_times()
+    s.profile(False)
+    s.sync(check_nan=True)
+    info = s.info()
+    launches = steps * s.launches_per_step()
+    s.close()
+    return ms, kt, info, launches
+
+
+def time_e2e(wql, ctx, text, media, prec, steps):
+    """Whole job through the public API with host buffers: scenario creation
+    (grid/surface upload), `steps` calls of wql_step(1) with the fault frame
+    returned to the host after every step (the reference writes its fault
+    output every step), and the final velocity fields read back."""
+    import numpy as np
+    text_f = text.replace("w_fault = F", "w_fault = T")
+    t0 = time.perf_counter()
+    s = wql.Scenario(ctx, text=text_f, precision=prec, media=media)
+    for _ in range(steps):
+        s.step(1)
+    frames = s.frames("Svel")
+    v = [s.field(b, c) for b in range(2) for c in range(3)]
+    s.sync()
+    t1 = time.perf_counter()
+    info = s.info()
+    np_pts = sum(info.nq[b] * info.nr[b] * info.ns[b] for b in range(2))
+    nf = info.nr[0] * info.ns[0]
+    h2d = 3 * np_pts * 8 + sum(a.nbytes for k, a in _media_arrays(media))
+    d2h = steps * 39 * nf * 4 + sum(x.nbytes for x in v)
+    s.close()
+    del frames
+    return t1 - t0, h2d, d2h
+
+
+def _media_arrays(media):
+    if not media:
+        return []
+    out = []
+    for k, v in media.items():
+        if isinstance(v, (list, tuple)):
+            out += [(k, a) for a in v if a is not None]
+        elif v is not None:
+            out.append((k, v))
+    return out
+
+
+def cpu_sample(text, media, steps):
+    """The oracle (FP64 CPU restatement of the reference) on the same workload,
+    all host threads; returns (seconds for `steps` steps, threads)."""
+    import ctypes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_oracle
+    build_oracle.build()
+    L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "libwqlref.so"))
+    L.wqlref_create_ex.restype = ctypes.c_void_p
+    L.wqlref_create_ex.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 9
+    L.wqlref_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.wqlref_destroy.argtypes = [ctypes.c_void_p]
+    L.wqlref_last_error.restype = ctypes.c_char_p
+    m = media or {}
+
+    def ptr(a):
+        return None if a is None else a.ctypes.data
+
+    topo = m.get("topo_offset") or (None, None)
+    lam = m.get("lam") or (None, None)
+    mu = m.get("mu") or (None, None)
+    rho = m.get("rho") or (None, None)
+    h = L.wqlref_create_ex(text.encode(), ptr(m.get("fault_offset")), ptr(topo[0]), ptr(topo[1]),
+                           ptr(lam[0]), ptr(mu[0]), ptr(rho[0]), ptr(lam[1]), ptr(mu[1]), ptr(rho[1]))
+    if not h:
+        raise RuntimeError(L.wqlref_last_error().decode())
+    t0 = time.perf_counter()
+    L.wqlref_step(h, steps)
+    t1 = time.perf_counter()
+    L.wqlref_destroy(h)
+    return t1 - t0, os.cpu_count()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=201)
+    ap.add_argument("--seed", type=int, default=2239)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    text, media, ups = workload(args)
+    wl = (f"config1: 2 x {args.n}^3 curvilinear blocks, seeded topography + self-similar rough fault, "
+          f"aging-law rate-and-state, {ups // 5} grid points")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        secs, cores = cpu_sample(text, media, args.warmup + args.steps)
+        # warm-up steps are part of the timed CPU sample's steady state; report per step
+        v = ups * (args.warmup + args.steps) / secs
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * secs / (args.warmup + args.steps), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": wl, "precision": "fp64"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{args.warmup + args.steps} full time steps of the workload, "
+                                           "oracle/wql_ref.cpp (FP64 restatement), OpenMP on all host threads"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    import wql_build
+    wql_build.build()
+    import wql
+    ctx = wql.Context(local)
+    res = {}
+    with Clocks(local) as clk:
+        for name, prec, steps in (("fp32c", wql.FP32C, args.steps), ("fp64", wql.FP64, max(3, args.steps // 4))):
+            ms, kt, info, launches = time_gpu(wql, ctx, text, media, prec, steps, args.warmup, world)
+            ms = allmax(world, ms)
+            res[name] = dict(ms=ms, steps=steps, kt=kt, launches=launches, info=info)
+    clocks = clk.summary()
+    total_ups = allsum(world, ups)
+    out = {}
+    for name, r in res.items():
+        per_step = r["ms"] / r["steps"]
+        out[name] = {"value": total_ups / (per_step * 1e-3), "ms_per_step": per_step}
+    main_r = res["fp32c"]
+    peak, peak_kind = peaks()
+    vol_ms, vol_n = main_r["kt"]["volume"]
+    pts_per_launch = (args.n ** 3)
+    algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
+    achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_volume_fp32c_curv.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            t = json.load(f)
+        traffic = t.get("bytes_per_point", 0) * pts_per_launch or None
+    e2e = None
+    if not args.no_e2e:
+        secs, h2d, d2h = time_e2e(wql, ctx, text, media, wql.FP32C, args.steps)
+        e2e = {"value": total_ups * args.steps / allmax(world, secs), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
+               "includes": "scenario setup upload, per-step fault frame D2H, final velocity D2H"}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        secs, cores = cpu_sample(text, media, args.cpu_steps)
+        cpu = {"value": ups * args.cpu_steps / secs, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_steps} full time step(s) of the same workload, oracle/wql_ref.cpp "
+                         "(FP64 restatement), OpenMP on all host threads"}
+    if rank != 0:
+        return
+    ws_bytes = main_r["info"].device_bytes
+    line = {
+        "metric": METRIC, "value": out["fp32c"]["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["fp32c"]["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields, Kahan-compensated RK update, f64 fault solve",
+        "data": "synthetic (seeded topography, fault roughness)",
+        "config": {"workload": wl, "precision": "fp32c", "steps_timed": args.steps,
+                   "l2": f"inputs larger than L2: {ws_bytes / 2**20:.0f} MiB resident per GPU vs 129 MiB L2",
+                   "parallelism": f"{world} independent replica(s), no collective"},
+        "fp64": {"value": out["fp64"]["value"], "ms_per_step": out["fp64"]["ms_per_step"],
+                 "steps_timed": res["fp64"]["steps"]},
+        "fp32c_over_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "peak_kind": peak_kind, "kernel": "volume_kernel<float,curv,kahan>",
+                     "bytes_per_update": BYTES_PER_UPDATE[("curv", "fp32c")],
+                     "avg_launch_ms": vol_ms / vol_n if vol_n else None,
+                     "interface_avg_launch_ms": (main_r["kt"]["interface"][0] / main_r["kt"]["interface"][1])
+                     if main_r["kt"]["interface"][1] else None},
+        "clocks": clocks,
+        "gpu_launches": main_r["launches"] + res["fp64"]["launches"],
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

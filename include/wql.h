@@ -74,6 +74,22 @@ int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision
  * base_dir, which may be NULL). */
 int wql_scenario_create_from_text(wql_ctx* ctx, const char* in_text, const char* base_dir,
                                   int precision, wql_scn** out);
+/* Seeded geometry and media supplied by the caller instead of files.  The
+ * reference reads fault surfaces and topography from text files
+ * (src/grid.f90:832-1160 'read_from_memomry_fractal', :1394-1450
+ * 'read_topo_from_memory') and heterogeneous media from binary files
+ * (src/material.f90:706-747); here the arrays are passed in directly.  Any
+ * pointer may be NULL.  Layouts are column-major without ghosts. */
+typedef struct wql_media {
+  const double* fault_offset;   /* nr*ns: x-displacement of the fault surface (km) */
+  const double* topo_offset[2]; /* per block nq*ns: y-displacement of the r = 1 surface */
+  const double* lam[2];         /* per block nq*nr*ns: Lame lambda (GPa) */
+  const double* mu[2];          /* per block: shear modulus (GPa) */
+  const double* rho[2];         /* per block: density (g/cm^3) */
+} wql_media;
+
+int wql_scenario_create_ex(wql_ctx* ctx, const char* in_text, const char* base_dir, int precision,
+                           const wql_media* media, wql_scn** out);
 int wql_scenario_destroy(wql_scn* scn);
 
 /* Advance nsteps steps = nsteps calls of time_step_RK (src/time_step.f90:68). */
@@ -105,6 +121,13 @@ int wql_get_frames(wql_scn* scn, int what, float* host_out);
 /* The CUDA stream the scenario's kernels run on (cudaStream_t as integer),
  * for callers that time or order work around wql_step. */
 int wql_scenario_stream(wql_scn* scn, uintptr_t* stream);
+
+/* Per-launch timing with CUDA events on the scenario stream: enable resets
+ * the record; wql_kernel_times returns the summed device time and launch
+ * count of the fused volume kernel and of the interface kernel since then. */
+int wql_profile(wql_scn* scn, int enable);
+int wql_kernel_times(wql_scn* scn, double* volume_ms, int* volume_launches, double* interface_ms,
+                     int* interface_launches);
 
 /* Number of kernel launches one step issues (for launch accounting). */
 int wql_launches_per_step(wql_scn* scn, int* launches);

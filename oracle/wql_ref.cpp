@@ -208,9 +208,10 @@ void prestress(wp& T0n, wp& T0m, wp& T0l, const wp x[3], wp t, const Presets& P,
     // parametric presets (extension &fault_list): uniform background traction
     // plus a Gaussian overstress ramped in time like TPV101's G(t)
     const wql::FrictionExt& f = *P.fx;
-    T0n = f.Tn;
-    T0m = f.Tm;
-    T0l = f.Tl;
+    if (!f.stress_profile.empty() && initial_stress_tensor(s0, x, f.stress_profile))
+      traction_nml(s0, n, m, l, T0n, T0m, T0l);
+    else
+      traction_nml(f.s0, n, m, l, T0n, T0m, T0l);
     wp dy = x[1] - f.nuc_y, dz = x[2] - f.nuc_z;
     wp F = std::exp(-(dy * dy + dz * dz) / (2.0 * f.nuc_radius * f.nuc_radius));
     wp G = 1.0;
@@ -437,6 +438,7 @@ void metrics(RBlock& B) {
     B.mz[c].assign(B.np, 0);
   }
   B.J.assign(B.np, 0);
+#pragma omp parallel for schedule(static)
   for (int s = 1; s <= B.ns; ++s)
     for (int r = 1; r <= B.nr; ++r)
       for (int q = 1; q <= B.nq; ++q) {
@@ -729,7 +731,15 @@ struct Domain {
   std::string err;
 };
 
-int init_block(Domain& D, int b) {
+// Seeded surfaces and media handed in by the caller (the product's
+// wql_scenario_create_ex extension); all pointers may be null.
+struct Media {
+  const double* fault_offset = nullptr;
+  const double* topo_offset[2] = {nullptr, nullptr};
+  const double* mat[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+};
+
+int init_block(Domain& D, int b, const Media& md) {
   RBlock& B = D.Bk[b];
   const wql::BlockParams& bp = D.P.btp[b];
   B.nq = bp.nqrs[0];
@@ -763,15 +773,33 @@ int init_block(Domain& D, int b) {
     D.err = "unknown type_of_mesh " + D.P.type_of_mesh;
     return 1;
   }
+  // seeded surface displacements, blended linearly across the block (the
+  // extension's generator; the reference reads such surfaces from files)
+  if (md.fault_offset)
+    for (int k = 1; k <= B.ns; ++k)
+      for (int j = 1; j <= B.nr; ++j)
+        for (int i = 1; i <= B.nq; ++i) {
+          wp q = (wp)(i - 1) / (wp)(B.nq - 1);
+          wp w = (b == 0) ? q : 1.0 - q;
+          B.X[0][B.id(i, j, k)] += w * md.fault_offset[(size_t)(j - 1) + (size_t)B.nr * (k - 1)];
+        }
+  if (md.topo_offset[b])
+    for (int k = 1; k <= B.ns; ++k)
+      for (int j = 1; j <= B.nr; ++j)
+        for (int i = 1; i <= B.nq; ++i) {
+          wp w = 1.0 - (wp)(j - 1) / (wp)(B.nr - 1);
+          B.X[1][B.id(i, j, k)] += w * md.topo_offset[b][(size_t)(i - 1) + (size_t)B.nq * (k - 1)];
+        }
   metrics(B);
-  // init_material default branch: src/material.f90:180-187
+  // init_material default branch: src/material.f90:180-187, or per-point
+  // media (src/material.f90:706-747 reads them from files)
   for (int c = 0; c < 3; ++c) B.M[c].assign(B.np, 0);
   wp lam = bp.rho_s_p[0] * (bp.rho_s_p[2] * bp.rho_s_p[2] - 2.0 * (bp.rho_s_p[1] * bp.rho_s_p[1]));
   wp mu = bp.rho_s_p[0] * (bp.rho_s_p[1] * bp.rho_s_p[1]);
   for (size_t p = 0; p < B.np; ++p) {
-    B.M[0][p] = lam;
-    B.M[1][p] = mu;
-    B.M[2][p] = bp.rho_s_p[0];
+    B.M[0][p] = md.mat[b][0] ? md.mat[b][0][p] : lam;
+    B.M[1][p] = md.mat[b][1] ? md.mat[b][1][p] : mu;
+    B.M[2][p] = md.mat[b][2] ? md.mat[b][2][p] : bp.rho_s_p[0];
   }
   for (int c = 0; c < 9; ++c) {
     B.F[c].assign(B.np, 0.0);
@@ -1493,13 +1521,16 @@ void plasticity(Domain& D, RBlock& B) {
   if (D.P.problem == "TPV30" && !D.P.plast.set) {
     c = 1.18; nu = 0.1680; Tv = 0.05;
   }
+#pragma omp parallel for schedule(static)
   for (int k = iz; k <= fz; ++k)
     for (int j = iy; j <= fy; ++j)
       for (int i = ix; i <= fx; ++i) {
         size_t p = B.id(i, j, k);
         wp x[3] = {B.X[0][p], B.X[1][p], B.X[2][p]}, s0[6];
-        if (!initial_stress_tensor(s0, x, D.P.problem)) {
-          for (int t = 0; t < 6; ++t) s0[t] = 0.0;
+        const bool param = D.P.problem == "sw_param" || D.P.problem == "rs_param";
+        const std::string& prof = param ? D.P.fric.stress_profile : D.P.problem;
+        if (!initial_stress_tensor(s0, x, prof)) {
+          for (int t = 0; t < 6; ++t) s0[t] = param ? D.P.fric.s0[t] : 0.0;
         }
         wp s[6], sa[6];
         for (int t = 0; t < 6; ++t) s[t] = B.F[3 + t][p];
@@ -1566,8 +1597,12 @@ void time_step(Domain& D) {
     // scale_rates
     for (int b = 0; b < 2; ++b) {
       RBlock& B = D.Bk[b];
-      for (int c = 0; c < 9; ++c)
-        for (auto& v : B.DF[c]) v = A * v;
+      const long long np = (long long)B.np;
+      for (int c = 0; c < 9; ++c) {
+        wp* a = B.DF[c].data();
+#pragma omp parallel for schedule(static)
+        for (long long p = 0; p < np; ++p) a[p] = A * a[p];
+      }
       for (int s = 1; s <= 6; ++s)
         if (B.pml[s])
           for (int c = 0; c < 9; ++c)
@@ -1597,8 +1632,13 @@ void time_step(Domain& D) {
     // update_fields
     for (int b = 0; b < 2; ++b) {
       RBlock& B = D.Bk[b];
-      for (int c = 0; c < 9; ++c)
-        for (size_t p = 0; p < B.np; ++p) B.F[c][p] = B.F[c][p] + Bdt * B.DF[c][p];
+      const long long np = (long long)B.np;
+      for (int c = 0; c < 9; ++c) {
+        wp* f = B.F[c].data();
+        const wp* df = B.DF[c].data();
+#pragma omp parallel for schedule(static)
+        for (long long p = 0; p < np; ++p) f[p] = f[p] + Bdt * df[p];
+      }
       for (int s = 1; s <= 6; ++s)
         if (B.pml[s])
           for (int c = 0; c < 9; ++c)
@@ -1657,6 +1697,8 @@ static char g_err[512];
 
 const char* wqlref_last_error() { return g_err; }
 
+static void* create_domain(Domain* D, const Media& md);
+
 void* wqlref_create(const char* in_path) {
   Domain* D = new Domain();
   std::string err;
@@ -1665,6 +1707,33 @@ void* wqlref_create(const char* in_path) {
     delete D;
     return nullptr;
   }
+  return create_domain(D, Media());
+}
+
+// Same as wqlref_create, from input text plus seeded surfaces and media
+// (any pointer may be null): fault x-offset (nr*ns), per-block r=1 surface
+// y-offsets (nq*ns), per-block lambda, mu, rho (np each).
+void* wqlref_create_ex(const char* in_text, const double* fault_offset, const double* topo0,
+                       const double* topo1, const double* lam0, const double* mu0,
+                       const double* rho0, const double* lam1, const double* mu1,
+                       const double* rho1) {
+  Domain* D = new Domain();
+  std::string err;
+  if (wql::parse_in_text(in_text, "", D->P, err) != 0) {
+    std::snprintf(g_err, sizeof(g_err), "%s", err.c_str());
+    delete D;
+    return nullptr;
+  }
+  Media md;
+  md.fault_offset = fault_offset;
+  md.topo_offset[0] = topo0;
+  md.topo_offset[1] = topo1;
+  md.mat[0][0] = lam0; md.mat[0][1] = mu0; md.mat[0][2] = rho0;
+  md.mat[1][0] = lam1; md.mat[1][1] = mu1; md.mat[1][2] = rho1;
+  return create_domain(D, md);
+}
+
+static void* create_domain(Domain* D, const Media& md) {
   D->pre.problem = D->P.problem;
   D->pre.fx = &D->P.fric;
   D->rk = rk54();
@@ -1705,7 +1774,7 @@ void* wqlref_create(const char* in_path) {
     D->pl_Tv = D->P.plast.Tv;
   }
   for (int b = 0; b < 2; ++b)
-    if (init_block(*D, b) != 0) {
+    if (init_block(*D, b, md) != 0) {
       std::snprintf(g_err, sizeof(g_err), "%s", D->err.c_str());
       delete D;
       return nullptr;

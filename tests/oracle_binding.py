@@ -28,6 +28,8 @@ def lib():
         L.wqlref_get_geom.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_get_iface.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_info.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.wqlref_create_ex.restype = ctypes.c_void_p
+        L.wqlref_create_ex.argtypes = [ctypes.c_char_p] + [vp] * 9
         _LIB = L
     return _LIB
 
@@ -35,9 +37,26 @@ def lib():
 class Oracle:
     """One reference-semantics domain (two blocks, one fault) on the CPU."""
 
-    def __init__(self, in_path):
+    def __init__(self, in_path=None, text=None, media=None):
         L = lib()
-        h = L.wqlref_create(str(in_path).encode())
+        if text is None:
+            h = L.wqlref_create(str(in_path).encode())
+        else:
+            m = media or {}
+            self._keep = []
+
+            def ptr(a):
+                if a is None:
+                    return None
+                a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+                self._keep.append(a)
+                return a.ctypes.data
+
+            pair = lambda k: m.get(k) or (None, None)  # noqa: E731
+            h = L.wqlref_create_ex(text.encode(), ptr(m.get("fault_offset")), ptr(pair("topo_offset")[0]),
+                                   ptr(pair("topo_offset")[1]), ptr(pair("lam")[0]), ptr(pair("mu")[0]),
+                                   ptr(pair("rho")[0]), ptr(pair("lam")[1]), ptr(pair("mu")[1]),
+                                   ptr(pair("rho")[1]))
         if not h:
             raise RuntimeError(L.wqlref_last_error().decode())
         self.h = ctypes.c_void_p(h)

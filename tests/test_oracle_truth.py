@@ -77,3 +77,29 @@ def test_compiled_bc_form_differs_from_fixture(oracle_lib, tmp_path, truth_cart)
     uf = o.frames("Uface").astype(np.float64)
     assert np.abs(uf[0] - truth_cart["Uface"][0]).max() == 0.0
     assert np.abs(uf - truth_cart["Uface"]).max() > 1e-2
+
+
+def test_seeded_generators_statistics():
+    """Seeded generators: reproducible, with the requested rms/std."""
+    import wql_configs
+    a = wql_configs.gaussian_surface((101, 81), (0.075, 0.075), 1.0, 0.15, 7)
+    b = wql_configs.gaussian_surface((101, 81), (0.075, 0.075), 1.0, 0.15, 7)
+    assert np.array_equal(a, b) and abs(a.std() - 0.15) < 1e-12
+    f = wql_configs.self_similar_surface((81, 81), (0.075, 0.075), 0.01, 0.2, 3)
+    assert abs(f.std() - 0.01 * 80 * 0.075) < 1e-12
+    v = wql_configs.von_karman((33, 17, 17), (0.05, 0.05, 0.05), 2.0, 0.2, 0.05, 11)
+    assert abs(v.std() - 0.05) < 1e-12 and abs(v.mean()) < 1e-3
+    rho = wql_configs.nafe_drake_rho(6.0)
+    assert 2.6 < rho < 2.8
+
+
+def test_config_texts_parse_with_oracle(oracle_lib):
+    import wql_configs
+    t0, _ = wql_configs.config0()
+    o = oracle_lib.Oracle(text=t0)
+    assert o.dims[0] == (41, 41, 41) and o.nt == 200
+    t1, m1 = wql_configs.config1(n=21, steps=5)
+    o1 = oracle_lib.Oracle(text=t1, media=m1)
+    assert o1.nt == 5
+    o1.step(2)
+    assert np.isfinite(o1.fields(0)).all()

@@ -328,6 +328,8 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
   }
   if (groups.count("fault_list")) {
     P.fric.set = true;
+    for (auto& it : items_of("fault_list"))
+      if (it.key == "stress_profile" && !it.values.empty()) P.fric.stress_profile = it.values[0];
     for (auto& it : items_of("fault_list")) {
       double v = it.values.empty() ? 0.0 : to_double(it.values[0]);
       const auto& k = it.key;
@@ -342,9 +344,8 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
       else if (k == "f0") P.fric.f0 = v;
       else if (k == "l") P.fric.L = v;
       else if (k == "vini") P.fric.Vini = v;
-      else if (k == "tn") P.fric.Tn = v;
-      else if (k == "tm") P.fric.Tm = v;
-      else if (k == "tl") P.fric.Tl = v;
+      else if (k == "s0")
+        for (int c = 0; c < 6 && c < (int)it.values.size(); ++c) P.fric.s0[c] = to_double(it.values[c]);
       else if (k == "nuc_amp") P.fric.nuc_amp = v;
       else if (k == "nuc_radius") P.fric.nuc_radius = v;
       else if (k == "nuc_y") P.fric.nuc_y = v;

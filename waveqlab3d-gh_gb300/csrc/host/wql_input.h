@@ -42,8 +42,13 @@ struct FrictionExt {
   double barrier_y = 15.0, barrier_z = 15.0;
   // rate and state, aging law (IC:386-393, IC:433)
   double a = 0.008, b = 0.012, V0 = 1.0e-6, f0 = 0.6, L = 0.02, Vini = 1.0e-12;
-  // background traction and Gaussian overstress nucleation
-  double Tn = -120.0, Tm = 0.0, Tl = 75.0;
+  // uniform background stress tensor (sxx, syy, szz, sxy, sxz, syz), projected
+  // on each fault point's (n, m, l) frame like the TPV101 preset
+  // (src/Interface_Condition.f90:2324-2342), plus a Gaussian overstress
+  double s0[6] = {-120.0, 0.0, -120.0, 0.0, 75.0, 0.0};
+  // optional depth-dependent tensor instead of s0: the name of a preset
+  // with an initial_stress_tensor (e.g. 'TPV26', src/initial_stress_condition.f90:26-50)
+  std::string stress_profile;
   double nuc_amp = 0.0, nuc_radius = 1.5, nuc_y = 7.5, nuc_z = 0.0, nuc_rise = 1.0;
 };
 

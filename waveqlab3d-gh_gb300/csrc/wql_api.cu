@@ -83,6 +83,7 @@ struct wql_ctx {
 struct wql_scn {
   wql_ctx* ctx = nullptr;
   Problem P;
+  wql_media media{};
   int prec = WQL_FP64;
   size_t esz = 8;
   cudaStream_t stream = nullptr;
@@ -124,8 +125,22 @@ struct wql_scn {
   int frame_cap = 0, frame_fill = 0;
   std::vector<float> frames_host;
   int nframes = 0;
+  // optional per-launch timing (CUDA events on the scenario stream)
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<size_t, int>> ev_marks;  // (index of start event, kind 0 interface / 1 volume)
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
 
   ~wql_scn() {
+    for (auto e : ev_pool) cudaEventDestroy(e);
     for (auto& a : allocs)
       if (a.p) cudaFree(a.p);
     if (stream) cudaStreamDestroy(stream);
@@ -189,6 +204,11 @@ int setup_block(wql_scn* S, int b) {
   BlockGrid G;
   std::string err;
   SurfaceMods mods;
+  {
+    const long long nr = bp.nqrs[1], ns = bp.nqrs[2], nq = bp.nqrs[0];
+    if (S->media.fault_offset) mods.fault_offset.assign(S->media.fault_offset, S->media.fault_offset + nr * ns);
+    if (S->media.topo_offset[b]) mods.topo_offset.assign(S->media.topo_offset[b], S->media.topo_offset[b] + nq * ns);
+  }
   if (make_block_grid(S->P, b, mods, G, err)) return fail(WQL_E_INPUT, err);
   B.nq = G.nq;
   B.nr = G.nr;
@@ -205,11 +225,18 @@ int setup_block(wql_scn* S, int b) {
   if ((rc = S->alloc((void**)&J, np * sizeof(double), false))) return rc;
   launch_metrics(B.nq, B.nr, B.ns, x, metric, J, S->stream);
   CK(cudaGetLastError());
-  // homogeneous material from rho_s_p (src/material.f90:180-187)
-  if (S->P.material_source != "hardcode")
-    return fail(WQL_E_INPUT, "material_source '" + S->P.material_source + "' is not supported");
+  // material: caller arrays (the reference's file media, src/material.f90:706-747)
+  // or homogeneous from rho_s_p (src/material.f90:180-187)
   if ((rc = S->alloc((void**)&mat, 3 * np * sizeof(double), false))) return rc;
-  {
+  const double* user[3] = {S->media.lam[b], S->media.mu[b], S->media.rho[b]};
+  if (user[0] || user[1] || user[2]) {
+    if (!(user[0] && user[1] && user[2])) return fail(WQL_E_INPUT, "lam, mu and rho must be given together");
+    for (int c = 0; c < 3; ++c)
+      CK(cudaMemcpyAsync(mat + c * np, user[c], np * sizeof(double), cudaMemcpyHostToDevice, S->stream));
+    CK(cudaStreamSynchronize(S->stream));
+  } else if (S->P.material_source != "hardcode") {
+    return fail(WQL_E_INPUT, "material_source '" + S->P.material_source + "' needs the media arrays");
+  } else {
     const double rho = bp.rho_s_p[0], cs = bp.rho_s_p[1], cp = bp.rho_s_p[2];
     const double lam = rho * (cp * cp - 2.0 * (cs * cs)), mu = rho * (cs * cs);
     std::vector<double> h(np);
@@ -345,12 +372,13 @@ int init_rate_state(wql_scn* S) {
   return WQL_OK;
 }
 
-int create(wql_ctx* ctx, Problem&& P, int precision, wql_scn** out) {
+int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql_scn** out) {
   if (!ctx || !out) return fail(WQL_E_INPUT, "null argument");
   if (precision != WQL_FP64 && precision != WQL_FP32C) return fail(WQL_E_INPUT, "unknown precision");
   std::unique_ptr<wql_scn> S(new wql_scn());
   S->ctx = ctx;
   S->P = std::move(P);
+  if (media) S->media = *media;
   S->prec = precision;
   S->esz = precision == WQL_FP64 ? 8 : 4;
   CK(cudaSetDevice(ctx->device));
@@ -388,16 +416,20 @@ int create(wql_ctx* ctx, Problem&& P, int precision, wql_scn** out) {
   const bool rs_ok = fp.preset == PRE_TPV101 || fp.preset == PRE_TPV102 || fp.preset == PRE_RS_PARAM;
   if ((fp.coupling == CPL_SW && !sw_ok) || (fp.coupling == CPL_RS && !rs_ok))
     return fail(WQL_E_INPUT, "problem '" + Pr.problem + "' has no preset for coupling '" + cp + "'");
-  if (S->plastic) {
+  const FrictionExt& fe = Pr.fric;
+  fp.fs = fe.fs; fp.fd = fe.fd; fp.Dc = fe.Dc; fp.barrier_y = fe.barrier_y; fp.barrier_z = fe.barrier_z;
+  fp.a = fe.a; fp.b = fe.b; fp.V0 = fe.V0; fp.f0 = fe.f0; fp.L = fe.L; fp.Vini = fe.Vini;
+  for (int c = 0; c < 6; ++c) fp.s0[c] = fe.s0[c];
+  fp.s0_profile = fe.stress_profile.empty() ? PRE_NONE : preset_of(fe.stress_profile);
+  if (!fe.stress_profile.empty() && fp.s0_profile == PRE_NONE)
+    return fail(WQL_E_INPUT, "unknown stress_profile '" + fe.stress_profile + "'");
+  fp.nuc_amp = fe.nuc_amp; fp.nuc_radius = fe.nuc_radius;
+  fp.nuc_y = fe.nuc_y; fp.nuc_z = fe.nuc_z; fp.nuc_rise = fe.nuc_rise;
+  if (S->plastic && fp.preset != PRE_SW_PARAM && fp.preset != PRE_RS_PARAM) {
     double s0[6], x0[3] = {0, 0, 0};
     if (!initial_stress(fp.preset, x0, s0))
       return fail(WQL_E_INPUT, "problem '" + Pr.problem + "' has no initial stress tensor for plasticity");
   }
-  const FrictionExt& fe = Pr.fric;
-  fp.fs = fe.fs; fp.fd = fe.fd; fp.Dc = fe.Dc; fp.barrier_y = fe.barrier_y; fp.barrier_z = fe.barrier_z;
-  fp.a = fe.a; fp.b = fe.b; fp.V0 = fe.V0; fp.f0 = fe.f0; fp.L = fe.L; fp.Vini = fe.Vini;
-  fp.Tn = fe.Tn; fp.Tm = fe.Tm; fp.Tl = fe.Tl; fp.nuc_amp = fe.nuc_amp; fp.nuc_radius = fe.nuc_radius;
-  fp.nuc_y = fe.nuc_y; fp.nuc_z = fe.nuc_z; fp.nuc_rise = fe.nuc_rise;
   // the two blocks share the fault face (src/domain.f90:243-244, 518-530)
   if (Pr.btp[0].nqrs[1] != Pr.btp[1].nqrs[1] || Pr.btp[0].nqrs[2] != Pr.btp[1].nqrs[2])
     return fail(WQL_E_INPUT, "the two blocks must share the fault face (equal nr, ns)");
@@ -483,6 +515,8 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.Bdt = (T)Bdt;
   a.plastic = (S->plastic && last) ? 1 : 0;
   a.preset = S->fp.preset;
+  if (S->fp.preset == PRE_SW_PARAM || S->fp.preset == PRE_RS_PARAM) a.preset = S->fp.s0_profile;
+  for (int c = 0; c < 6; ++c) a.s0u[c] = S->fp.s0[c];
   a.ycoord = (const T*)B.y;
   a.pl_c = S->pl_c; a.pl_nu = S->pl_nu; a.pl_Tv = S->pl_Tv; a.dt = S->dt;
   return a;
@@ -513,10 +547,19 @@ int run_step(wql_scn* S) {
     ia.fp = S->fp;
     ia.frame = (want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
     ia.solver_fail = S->solver_fail;
+    auto mark = [&](int kind) {
+      S->ev_marks.push_back({S->ev_used, kind});
+      cudaEventRecord(S->next_event(), S->stream);
+    };
+    auto mark_end = [&]() { cudaEventRecord(S->next_event(), S->stream); };
+    if (S->profiling) mark(0);
     launch_interface(ia, S->stream);
+    if (S->profiling) mark_end();
     for (int b = 0; b < 2; ++b) {
+      if (S->profiling) mark(1);
       if (S->prec == WQL_FP64) launch_volume<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       else launch_volume<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+      if (S->profiling) mark_end();
     }
     S->cur ^= 1;
   }
@@ -567,7 +610,16 @@ int wql_scenario_create_from_text(wql_ctx* ctx, const char* in_text, const char*
   Problem P;
   std::string err;
   if (parse_in_text(in_text, base_dir ? base_dir : "", P, err)) return fail(WQL_E_INPUT, err);
-  return create(ctx, std::move(P), precision, out);
+  return create(ctx, std::move(P), precision, nullptr, out);
+}
+
+int wql_scenario_create_ex(wql_ctx* ctx, const char* in_text, const char* base_dir, int precision,
+                           const wql_media* media, wql_scn** out) {
+  if (!in_text) return fail(WQL_E_INPUT, "null input text");
+  Problem P;
+  std::string err;
+  if (parse_in_text(in_text, base_dir ? base_dir : "", P, err)) return fail(WQL_E_INPUT, err);
+  return create(ctx, std::move(P), precision, media, out);
 }
 
 int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision, wql_scn** out) {
@@ -575,7 +627,7 @@ int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision
   Problem P;
   std::string err;
   if (parse_in_file(in_path, P, err)) return fail(WQL_E_INPUT, err);
-  return create(ctx, std::move(P), precision, out);
+  return create(ctx, std::move(P), precision, nullptr, out);
 }
 
 int wql_scenario_destroy(wql_scn* scn) {
@@ -707,6 +759,35 @@ int wql_get_frames(wql_scn* scn, int what, float* host_out) {
 int wql_scenario_stream(wql_scn* scn, uintptr_t* stream) {
   if (!scn || !stream) return fail(WQL_E_INPUT, "null argument");
   *stream = (uintptr_t)scn->stream;
+  return WQL_OK;
+}
+
+int wql_profile(wql_scn* scn, int enable) {
+  if (!scn) return fail(WQL_E_INPUT, "null scenario");
+  CK(cudaStreamSynchronize(scn->stream));
+  scn->profiling = enable != 0;
+  scn->ev_used = 0;
+  scn->ev_marks.clear();
+  return WQL_OK;
+}
+
+int wql_kernel_times(wql_scn* scn, double* volume_ms, int* volume_launches, double* interface_ms,
+                     int* interface_launches) {
+  if (!scn || !volume_ms || !volume_launches || !interface_ms || !interface_launches)
+    return fail(WQL_E_INPUT, "null argument");
+  CK(cudaStreamSynchronize(scn->stream));
+  double t[2] = {0.0, 0.0};
+  int n[2] = {0, 0};
+  for (auto& m : scn->ev_marks) {
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, scn->ev_pool[m.first], scn->ev_pool[m.first + 1]));
+    t[m.second] += ms;
+    n[m.second] += 1;
+  }
+  *interface_ms = t[0];
+  *interface_launches = n[0];
+  *volume_ms = t[1];
+  *volume_launches = n[1];
   return WQL_OK;
 }
 

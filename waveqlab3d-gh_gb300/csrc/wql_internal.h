@@ -57,7 +57,8 @@ struct VolumeArgs {
   T A, Bdt;
   // plasticity on the last stage
   int plastic;
-  int preset;
+  int preset;          // initial-stress preset for the plastic update (PRE_NONE: s0u)
+  double s0u[6];       // uniform initial stress
   const T* __restrict__ ycoord;  // depth coordinate for the initial stress
   double pl_c, pl_nu, pl_Tv, dt;
 };

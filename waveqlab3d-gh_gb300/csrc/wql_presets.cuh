@@ -35,7 +35,8 @@ struct FaultParams {
   int coupling;
   double fs, fd, Dc, barrier_y, barrier_z;
   double a, b, V0, f0, L, Vini;
-  double Tn, Tm, Tl, nuc_amp, nuc_radius, nuc_y, nuc_z, nuc_rise;
+  double s0[6], nuc_amp, nuc_radius, nuc_y, nuc_z, nuc_rise;
+  int s0_profile;  // preset whose initial stress replaces s0 (PRE_NONE: uniform s0)
 };
 
 // boxcar / smooth_boxcar: src/Interface_Condition.f90:2438-2476
@@ -88,6 +89,9 @@ WQL_HD bool initial_stress(int preset, const double x[3], double s0[6]) {
       s0[0] = -7.378 * x[1]; s0[1] = 0.0; s0[2] = -7.378 * x[1]; s0[3] = 0.0;
       s0[4] = -0.55 * s0[0]; s0[5] = 0.0;
       return true;
+    case PRE_SW_PARAM:
+    case PRE_RS_PARAM:
+      return false;  // uniform tensor: supplied by the caller (FaultParams::s0)
     default:
       return false;
   }
@@ -161,9 +165,10 @@ WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const 
     }
     case PRE_SW_PARAM:
     case PRE_RS_PARAM: {
-      Tn = fp.Tn;
-      Tm = fp.Tm;
-      Tl = fp.Tl;
+      if (fp.s0_profile != PRE_NONE && initial_stress(fp.s0_profile, x, s0))
+        tensor_traction(s0, n, m, l, Tn, Tm, Tl);
+      else
+        tensor_traction(fp.s0, n, m, l, Tn, Tm, Tl);
       const double dy = x[1] - fp.nuc_y, dz = x[2] - fp.nuc_z;
       const double F = exp(-(dy * dy + dz * dz) / (2.0 * fp.nuc_radius * fp.nuc_radius));
       const double G = fp.nuc_rise > 0.0 ? smooth_ramp(t / fp.nuc_rise) : 1.0;

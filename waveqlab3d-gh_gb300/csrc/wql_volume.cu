@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(256) volume_kernel(const VolumeArgs<T> a) {
     if (inside) {
       double xs[3] = {0.0, (double)a.ycoord[p], 0.0}, s0[6];
       if (!initial_stress(a.preset, xs, s0))
-        for (int c = 0; c < 6; ++c) s0[c] = 0.0;
+        for (int c = 0; c < 6; ++c) s0[c] = a.s0u[c];
       T sa[6];
 #pragma unroll
       for (int c = 0; c < 6; ++c) sa[c] = fo[3 + c] + (T)s0[c];

@@ -20,9 +20,15 @@ NCOMP = {"Uface": 9, "Vface": 9, "S": 4, "Uhat": 6, "Vhat": 6, "Svel": 3, "trup"
 ERRORS = {1: "WQL_E_INPUT", 2: "WQL_E_OOM", 3: "WQL_E_CUDA", 4: "WQL_E_NAN", 5: "WQL_E_SOLVER",
           6: "WQL_E_STATE"}
 EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_create_from_in",
-           "wql_scenario_create_from_text", "wql_scenario_destroy", "wql_step", "wql_sync",
+           "wql_scenario_create_from_text", "wql_scenario_create_ex", "wql_scenario_destroy", "wql_step", "wql_sync",
            "wql_get_info", "wql_get_field", "wql_set_field", "wql_get_iface", "wql_frame_count",
-           "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step"]
+           "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step", "wql_profile",
+           "wql_kernel_times"]
+
+
+class Media(ctypes.Structure):
+    _fields_ = [("fault_offset", ctypes.c_void_p), ("topo_offset", ctypes.c_void_p * 2),
+                ("lam", ctypes.c_void_p * 2), ("mu", ctypes.c_void_p * 2), ("rho", ctypes.c_void_p * 2)]
 
 
 class WqlError(RuntimeError):
@@ -53,6 +59,8 @@ def lib():
         L.wql_ctx_destroy.argtypes = [vp]
         L.wql_scenario_create_from_in.argtypes = [vp, ctypes.c_char_p, ci, ctypes.POINTER(vp)]
         L.wql_scenario_create_from_text.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ci, ctypes.POINTER(vp)]
+        L.wql_scenario_create_ex.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ci, ctypes.POINTER(Media),
+                                             ctypes.POINTER(vp)]
         L.wql_scenario_destroy.argtypes = [vp]
         L.wql_step.argtypes = [vp, ci]
         L.wql_sync.argtypes = [vp, ci]
@@ -64,6 +72,9 @@ def lib():
         L.wql_get_frames.argtypes = [vp, ci, vp]
         L.wql_scenario_stream.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
         L.wql_launches_per_step.argtypes = [vp, ctypes.POINTER(ci)]
+        L.wql_profile.argtypes = [vp, ci]
+        cd = ctypes.POINTER(ctypes.c_double)
+        L.wql_kernel_times.argtypes = [vp, cd, ctypes.POINTER(ci), cd, ctypes.POINTER(ci)]
         _lib = L
     return _lib
 
@@ -95,10 +106,35 @@ class Context:
 class Scenario:
     """One two-block domain on the GPU (the reference's `domain_type`)."""
 
-    def __init__(self, ctx, in_path=None, text=None, precision=FP64, base_dir=None):
+    def __init__(self, ctx, in_path=None, text=None, precision=FP64, base_dir=None, media=None):
+        """media: optional dict with 'fault_offset' (nr*ns), 'topo_offset'
+        (pair of nq*ns), 'lam'/'mu'/'rho' (pairs of per-point arrays)."""
         self.ctx = ctx
         self.h = ctypes.c_void_p()
-        if text is not None:
+        if media is not None:
+            if text is None:
+                with open(in_path) as f:
+                    text = f.read()
+            keep = []
+
+            def ptr(a):
+                if a is None:
+                    return None
+                a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+                keep.append(a)
+                return a.ctypes.data
+
+            m = Media()
+            m.fault_offset = ptr(media.get("fault_offset"))
+            for key in ("topo_offset", "lam", "mu", "rho"):
+                pair = media.get(key) or (None, None)
+                arr = getattr(m, key)
+                for b in range(2):
+                    arr[b] = ptr(pair[b])
+            _check(lib().wql_scenario_create_ex(ctx.h, text.encode(),
+                                                base_dir.encode() if base_dir else None, precision,
+                                                ctypes.byref(m), ctypes.byref(self.h)))
+        elif text is not None:
             _check(lib().wql_scenario_create_from_text(
                 ctx.h, text.encode(), base_dir.encode() if base_dir else None, precision,
                 ctypes.byref(self.h)))
@@ -174,3 +210,14 @@ class Scenario:
         n = ctypes.c_int()
         _check(lib().wql_launches_per_step(self.h, ctypes.byref(n)))
         return n.value
+
+    def profile(self, enable=True):
+        _check(lib().wql_profile(self.h, 1 if enable else 0))
+
+    def kernel_times(self):
+        """{'volume': (ms_total, launches), 'interface': (ms_total, launches)}"""
+        vm, im = ctypes.c_double(), ctypes.c_double()
+        vn, inn = ctypes.c_int(), ctypes.c_int()
+        _check(lib().wql_kernel_times(self.h, ctypes.byref(vm), ctypes.byref(vn), ctypes.byref(im),
+                                      ctypes.byref(inn)))
+        return {"volume": (vm.value, vn.value), "interface": (im.value, inn.value)}

@@ -1,0 +1,182 @@
+"""Seeded synthetic workloads in the reference's `.in` format.
+
+The reference ships fixed input files and offline generators (Matlab
+inputfile/*.m for fault and topography surfaces, python/vonKarman_3D.py for
+random media) whose outputs it reads from disk.  This module generates the
+same kinds of inputs from a seed, in memory, and returns `.in` text plus the
+arrays for wql_scenario_create_ex:
+
+  config 0  2 x 41^3 Cartesian, TPV5 slip-weakening, 200 steps (CPU-runnable)
+  config 1  2 x 201^3 curvilinear, Gaussian-correlated topography, self-similar
+            rough fault, aging-law rate and state, Gaussian overstress, 2000 steps
+  config 2  2 x 401x201x201, 20-point PML on 5 sides, von Karman medium,
+            Drucker-Prager viscoplasticity, depth-dependent stress, slip weakening
+"""
+import math
+
+import numpy as np
+
+RHO, CS, CP = 2.67, 3.464, 6.0
+
+
+def _problem(name, problem, coupling, mesh, t_final, extra=""):
+    return (f"&problem_list\n name = '{name}',\n problem = '{problem}',\n nblocks = 2,\n"
+            f" t_final = {t_final!r},\n CFL = 0.5d0,\n coupling = '{coupling}',\n"
+            f" type_of_mesh = '{mesh}',\n w_stride = 1,\n w_fault = F{extra} /\n")
+
+
+def _block(b, n, a, bb, lqrs, rqrs, pml_l=None, pml_r=None, npml=0):
+    s = (f"btp({b})%nqrs = {n[0]}, {n[1]}, {n[2]},\n"
+         f"btp({b})%aqrs = {a[0]!r}, {a[1]!r}, {a[2]!r},\n"
+         f"btp({b})%bqrs = {bb[0]!r}, {bb[1]!r}, {bb[2]!r},\n"
+         f"btp({b})%rho_s_p = {RHO!r}, {CS!r}, {CP!r},\n"
+         f"btp({b})%lqrs = {lqrs[0]}, {lqrs[1]}, {lqrs[2]},\n"
+         f"btp({b})%rqrs = {rqrs[0]}, {rqrs[1]}, {rqrs[2]},\n")
+    if pml_l is not None:
+        tf = lambda v: "T" if v else "F"  # noqa: E731
+        s += (f"btp({b})%pml_lqrs = {', '.join(tf(v) for v in pml_l)},\n"
+              f"btp({b})%pml_rqrs = {', '.join(tf(v) for v in pml_r)},\n"
+              f"btp({b})%npml = {npml},\n")
+    return s
+
+
+def dt_of(n, extent):
+    """Time step of src/block.f90:437-452 (CFL 0.5)."""
+    h = min(e / (k - 1) for e, k in zip(extent, n))
+    return 0.5 * h / math.sqrt(CS * CS + CP * CP)
+
+
+# ----------------------------------------------------------------- fields ----
+
+def gaussian_surface(shape, spacing, corr_len, rms, seed):
+    """Gaussian-correlated random surface (autocorrelation exp(-r^2/l^2)):
+    white noise filtered in Fourier space by exp(-k^2 l^2 / 8), scaled to rms."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape)
+    k = [2 * np.pi * np.fft.fftfreq(n, d) for n, d in zip(shape, spacing)]
+    K2 = sum(np.meshgrid(*[kk * kk for kk in k], indexing="ij"))
+    f = np.real(np.fft.ifftn(np.fft.fftn(w) * np.exp(-K2 * corr_len ** 2 / 8.0)))
+    f -= f.mean()
+    return f * (rms / f.std())
+
+
+def self_similar_surface(shape, spacing, alpha, lam_min, seed):
+    """Self-similar (Hurst 1) rough surface: 2D power spectrum ~ k^-4, cut at
+    k_max = 2 pi / lam_min, rms height = alpha * (longest side)."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape)
+    k = [2 * np.pi * np.fft.fftfreq(n, d) for n, d in zip(shape, spacing)]
+    K = np.sqrt(sum(np.meshgrid(*[kk * kk for kk in k], indexing="ij")))
+    kmin = 2 * np.pi / max(n * d for n, d in zip(shape, spacing))
+    amp = np.where((K > 0) & (K <= 2 * np.pi / lam_min), np.maximum(K, kmin) ** -2.0, 0.0)
+    f = np.real(np.fft.ifftn(np.fft.fftn(w) * amp))
+    f -= f.mean()
+    L = max((n - 1) * d for n, d in zip(shape, spacing))
+    return f * (alpha * L / f.std())
+
+
+def von_karman(shape, spacing, corr_len, hurst, std, seed, kmax=None):
+    """3D von Karman random field with PSD ~ (1 + k^2 a^2)^-(H + 3/2), unit
+    variance scaled to `std`, cut at kmax (the method of
+    python/vonKarman_3D.py, seeded)."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape).astype(np.float64)
+    k = [2 * np.pi * np.fft.fftfreq(n, d) for n, d in zip(shape, spacing)]
+    K2 = sum(np.meshgrid(*[kk * kk for kk in k], indexing="ij", sparse=True))
+    psd = (1.0 + K2 * corr_len ** 2) ** (-(hurst + 1.5))
+    if kmax is not None:
+        psd = np.where(K2 <= kmax * kmax, psd, 0.0)
+    spec = np.fft.fftn(w) * np.sqrt(psd)
+    spec.flat[0] = 0.0
+    f = np.real(np.fft.ifftn(spec))
+    return f * (std / f.std())
+
+
+def nafe_drake_rho(cp):
+    """Density from P velocity (the polynomial used by python/vonKarman_3D.py)."""
+    return 1.6612 * cp - 0.4721 * cp ** 2 + 0.0671 * cp ** 3 - 0.0043 * cp ** 4 + 0.000106 * cp ** 5
+
+
+# ---------------------------------------------------------------- configs ----
+
+def config0(steps=200):
+    """2 x 41^3 Cartesian blocks over 20 x 10 x 10 km, planar fault at x = 10 km,
+    TPV5 slip weakening (IC:1283-1299, 1822-1831), CFL 0.5."""
+    n = (41, 41, 41)
+    dt = dt_of(n, (10.0, 10.0, 10.0))
+    text = _problem("config0", "TPV5", "slip-weakening_friction", "cartesian", (steps + 0.5) * dt)
+    text += "&block_list\n" + _block(1, n, (0.0, 0.0, -5.0), (10.0, 10.0, 5.0), (1, 2, 1), (0, 1, 1))
+    text += _block(2, n, (10.0, 0.0, -5.0), (20.0, 10.0, 5.0), (0, 2, 1), (1, 1, 1)) + " /\n"
+    return text, None
+
+
+def config1(n=201, steps=2000, seed=2239):
+    """2 x n^3 curvilinear blocks, (-15,0,-7.5)-(0,15,7.5) and (0,0,-7.5)-(15,15,7.5) km;
+    seeded topography (l = 1 km, rms 150 m) on the y = 0 free surface, self-similar
+    fault (alpha = 0.01, lambda_min = 200 m), aging-law rate and state with uniform
+    a = 0.008, b = 0.012, V0 = 1e-6, f0 = 0.6, L = 0.02, Vini = 1e-12, stress
+    (-120, 0, -120, 0, 75, 0) MPa and a 25 MPa Gaussian overstress (R = 1.5 km)
+    at (y, z) = (7.5, 0) ramped over 1 s."""
+    ext = 15.0
+    h = ext / (n - 1)
+    dt = dt_of((n, n, n), (ext, ext, ext))
+    text = _problem("config1", "rs_param", "rate-and-state_friction", "curvilinear", (steps + 0.5) * dt)
+    text += "&block_list\n" + _block(1, (n, n, n), (-ext, 0.0, -ext / 2), (0.0, ext, ext / 2), (1, 2, 1), (0, 1, 1))
+    text += _block(2, (n, n, n), (0.0, 0.0, -ext / 2), (ext, ext, ext / 2), (0, 2, 1), (1, 1, 1)) + " /\n"
+    text += ("&fault_list\n a = 0.008d0, b = 0.012d0, V0 = 1d-6, f0 = 0.6d0, L = 0.02d0, Vini = 1d-12,\n"
+             " s0 = -120d0, 0d0, -120d0, 0d0, 75d0, 0d0,\n"
+             " nuc_amp = 25d0, nuc_radius = 1.5d0, nuc_y = 7.5d0, nuc_z = 0d0, nuc_rise = 1d0 /\n")
+    # topography over the whole x range (2n-1 points), split at the fault
+    topo = gaussian_surface((2 * n - 1, n), (h, h), 1.0, 0.15, seed)
+    topo0 = np.asfortranarray(topo[:n, :])       # (q, s) for block 1
+    topo1 = np.asfortranarray(topo[n - 1:, :])   # block 2 shares the fault column
+    # fault surface on (r, s); zero it near the free surface edge so the
+    # interface and the topography meet consistently
+    fault = self_similar_surface((n, n), (h, h), 0.01, 0.2, seed + 1)
+    media = {
+        "fault_offset": np.asfortranarray(fault).ravel(order="F"),
+        "topo_offset": (topo0.ravel(order="F"), topo1.ravel(order="F")),
+    }
+    return text, media
+
+
+def config2(nq=401, nrs=201, steps=3000, seed=2239, npml=20):
+    """2 x nq x nrs x nrs blocks, (-20,0,-5)-(0,10,5) and (0,0,-5)-(20,10,5) km,
+    20-point PML on the 5 non-free-surface outer sides, von Karman medium (a = 2 km,
+    H = 0.2, 5 % on cp and cs, rho from cp), scec viscoplasticity (c = 1 MPa,
+    friction 0.75, Tv = 0.03 s), TPV26 depth-dependent stress, slip weakening as
+    config 0."""
+    ext = (20.0, 10.0, 10.0)
+    h = ext[0] / (nq - 1)
+    dt = dt_of((nq, nrs, nrs), ext)
+    extra = ",\n response = 'plastic',\n plastic_model = 'scec'"
+    text = _problem("config2", "sw_param", "slip-weakening_friction", "curvilinear", (steps + 0.5) * dt, extra)
+    text += "&block_list\n" + _block(1, (nq, nrs, nrs), (-20.0, 0.0, -5.0), (0.0, 10.0, 5.0), (1, 2, 1), (0, 1, 1),
+                                     (True, False, True), (False, True, True), npml)
+    text += _block(2, (nq, nrs, nrs), (0.0, 0.0, -5.0), (20.0, 10.0, 5.0), (0, 2, 1), (1, 1, 1),
+                   (False, False, True), (True, True, True), npml) + " /\n"
+    text += ("&fault_list\n fs = 0.677d0, fd = 0.525d0, Dc = 0.4d0, stress_profile = 'TPV26',\n"
+             " nuc_amp = 20d0, nuc_radius = 1.5d0, nuc_y = 7.5d0, nuc_z = 0d0, nuc_rise = 0d0 /\n"
+             "&plastic_list\n cohesion = 1d0, friction = 0.75d0, Tv = 0.03d0 /\n")
+    r = von_karman((2 * nq - 1, nrs, nrs), (h, h, h), 2.0, 0.2, 0.05, seed, kmax=np.pi / h)
+    media = {"lam": [], "mu": [], "rho": []}
+    for b in range(2):
+        sl = r[:nq] if b == 0 else r[nq - 1:]
+        cp = CP * (1.0 + sl)
+        cs = CS * (1.0 + sl)
+        rho = nafe_drake_rho(cp)
+        mu = rho * cs * cs
+        lam = rho * cp * cp - 2.0 * mu
+        for key, val in (("lam", lam), ("mu", mu), ("rho", rho)):
+            media[key].append(np.asfortranarray(val).ravel(order="F"))
+    media = {k: tuple(v) for k, v in media.items()}
+    return text, media
+
+
+def updates_per_step(text):
+    """Grid-point RK-stage updates per time step: sum of nq*nr*ns x 5 stages."""
+    import re
+    tot = 0
+    for m in re.finditer(r"btp\(\d\)%nqrs\s*=\s*(\d+),\s*(\d+),\s*(\d+)", text):
+        tot += int(m.group(1)) * int(m.group(2)) * int(m.group(3))
+    return 5 * tot
