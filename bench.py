@@ -283,7 +283,8 @@ def main():
         out[name] = {"value": total_ups / (per_step * 1e-3), "ms_per_step": per_step}
     main_r = res["fp32c"]
     peak, peak_kind = peaks()
-    vol_ms, vol_n = main_r["kt"]["volume"]
+    vol_ms, vol_n = main_r["kt"]["stencil"]
+    kernel_name = "stencil_kernel_tiled<float,curv,kahan>"
     pts_per_launch = (args.n ** 3)
     algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
@@ -292,7 +293,8 @@ def main():
     if os.path.exists(tpath):
         with open(tpath) as f:
             t = json.load(f)
-        traffic = t.get("bytes_per_point", 0) * pts_per_launch or None
+        if t.get("kernel") == kernel_name:
+            traffic = t.get("bytes_per_point", 0) * pts_per_launch or None
     e2e = None
     if not args.no_e2e:
         secs, h2d, d2h = time_e2e(wql, ctx, text, media, wql.FP32C, args.steps)
@@ -322,11 +324,13 @@ def main():
         "fp32c_over_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "peak_kind": peak_kind, "kernel": "volume_kernel<float,curv,kahan>",
+                     "peak_kind": peak_kind, "kernel": kernel_name,
                      "bytes_per_update": BYTES_PER_UPDATE[("curv", "fp32c")],
                      "avg_launch_ms": vol_ms / vol_n if vol_n else None,
                      "interface_avg_launch_ms": (main_r["kt"]["interface"][0] / main_r["kt"]["interface"][1])
-                     if main_r["kt"]["interface"][1] else None},
+                     if main_r["kt"]["interface"][1] else None,
+                     "corrections_avg_launch_ms": (main_r["kt"]["corrections"][0] / main_r["kt"]["corrections"][1])
+                     if main_r["kt"]["corrections"][1] else None},
         "clocks": clocks,
         "gpu_launches": main_r["launches"] + res["fp64"]["launches"],
         "e2e": e2e,

@@ -124,12 +124,22 @@ int wql_scenario_stream(wql_scn* scn, uintptr_t* stream);
 
 /* Per-launch timing with CUDA events on the scenario stream: enable resets
  * the record; wql_kernel_times returns the summed device time and launch
- * count of the fused volume kernel and of the interface kernel since then. */
+ * count since then of one kernel kind: 0 the interface (fault) kernel, 1 the
+ * volume stencil kernel, 2 the correction kernels (PML, boundary and fault
+ * penalties, plasticity) timed together per block and stage. */
 int wql_profile(wql_scn* scn, int enable);
-int wql_kernel_times(wql_scn* scn, double* volume_ms, int* volume_launches, double* interface_ms,
-                     int* interface_launches);
+int wql_kernel_times(wql_scn* scn, int kind, double* ms, int* launches);
 
-/* Number of kernel launches one step issues (for launch accounting). */
+/* Volume-stencil tuning: kernel_variant 0 = default (the per-point kernel in
+ * WQL_FP32C, tiled 32x8 in WQL_FP64), 1 = per-point form (every neighbour
+ * read through the caches), 2 = tiled shared-memory kernel with 32x8 tiles,
+ * 3 = the same at three blocks per SM (FP32), 4 = 64x8 tiles (WQL_FP32C
+ * only); schunk = planes per thread block along s for the tiled kernels
+ * (0 = 16). */
+int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk);
+
+/* Number of kernel launches the last wql_step issued per time step (for
+ * launch accounting); WQL_E_STATE before the first step. */
 int wql_launches_per_step(wql_scn* scn, int* launches);
 
 #ifdef __cplusplus

@@ -79,3 +79,23 @@ def test_curvilinear_path_flat_grid_truth1(ctx, wqlmod, oracle_lib, tmp_path):
         assert np.abs(got - truth[name]).max() <= 1e-7 * max(np.abs(truth[name]).max(), 1.0), name
     for e in field_errors(s, o):
         assert e < TOL
+
+
+@pytest.mark.parametrize("variant,prec", [(0, "fp64"), (2, "fp64"), (3, "fp64"),
+                                          (2, "fp32c"), (3, "fp32c"), (4, "fp32c")])
+def test_tiled_matches_pointwise(ctx, wqlmod, tmp_path, variant, prec):
+    """The tiled stencil variants compute the same stencil as the per-point
+    form (curvilinear bumpy fault, closures in all three axes, small s chunks
+    so chunk edges fall on closure rows).  FP64 agrees to rounding; FP32C to
+    float rounding of the differently contracted sums."""
+    p = write(tmp_path, "curv.in", golden_in("test_rup_curv_fric"))
+    pr = wqlmod.FP64 if prec == "fp64" else wqlmod.FP32C
+    a = wqlmod.Scenario(ctx, p, precision=pr)
+    b = wqlmod.Scenario(ctx, p, precision=pr)
+    a.set_tuning(1, 0)
+    b.set_tuning(variant, 5)
+    a.step(10)
+    b.step(10)
+    tol = 1e-13 if prec == "fp64" else 2e-6
+    for blk in range(2):
+        assert rel_l2(b.fields(blk), a.fields(blk)) < tol

@@ -118,6 +118,8 @@ struct wql_scn {
   unsigned int* solver_fail = nullptr;
   FaultParams fp{};
   int bc_form = BC_CHARACTERISTIC;
+  int kernel_variant = 0;  // stencil variant (0 default per precision)
+  int schunk = 0;          // planes per CTA along s (0: default)
   bool plastic = false;
   double pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
   // fault frames
@@ -129,7 +131,8 @@ struct wql_scn {
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
-  std::vector<std::pair<size_t, int>> ev_marks;  // (index of start event, kind 0 interface / 1 volume)
+  std::vector<std::pair<size_t, int>> ev_marks;  // (start event, kind 0 interface / 1 stencil / 2 corrections)
+  int launches_last_step = 0;
   cudaEvent_t next_event() {
     if (ev_used == ev_pool.size()) {
       cudaEvent_t e;
@@ -509,6 +512,8 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
     a.slab_np[s] = B.slab_np[s];
   }
   a.bc_form = S->bc_form;
+  a.kernel = S->kernel_variant;
+  a.schunk = S->schunk;
   a.fault_sat = (const T*)S->sat + (long long)b * 9 * B.nr * B.ns;
   a.npml = B.npml;
   a.A = (T)A;
@@ -526,6 +531,7 @@ int run_step(wql_scn* S) {
   const long long nf = (long long)S->B[0].nr * S->B[0].ns;
   const bool want_frame = S->frame_dev && (S->nstep % std::max(S->P.w_stride, 1) == 0);
   const double t0 = S->t;
+  int launches = 0;
   for (int stage = 1; stage <= 5; ++stage) {
     const double A = S->rk.A[stage], Bdt = S->rk.B[stage] * S->dt;
     const double ts = t0 + S->rk.C[stage - 1] * S->dt;
@@ -554,16 +560,23 @@ int run_step(wql_scn* S) {
     auto mark_end = [&]() { cudaEventRecord(S->next_event(), S->stream); };
     if (S->profiling) mark(0);
     launch_interface(ia, S->stream);
+    launches += 1;
     if (S->profiling) mark_end();
     for (int b = 0; b < 2; ++b) {
       if (S->profiling) mark(1);
       if (S->prec == WQL_FP64) launch_volume<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       else launch_volume<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       if (S->profiling) mark_end();
+      if (S->profiling) mark(2);
+      if (S->prec == WQL_FP64) launches += launch_corrections<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+      else launches += launch_corrections<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+      if (S->profiling) mark_end();
+      launches += 1;
     }
     S->cur ^= 1;
   }
   CK(cudaGetLastError());
+  S->launches_last_step = launches;
   S->t = t0 + S->rk.C[5] * S->dt;
   S->nstep += 1;
   if (want_frame) {
@@ -771,29 +784,38 @@ int wql_profile(wql_scn* scn, int enable) {
   return WQL_OK;
 }
 
-int wql_kernel_times(wql_scn* scn, double* volume_ms, int* volume_launches, double* interface_ms,
-                     int* interface_launches) {
-  if (!scn || !volume_ms || !volume_launches || !interface_ms || !interface_launches)
-    return fail(WQL_E_INPUT, "null argument");
+int wql_kernel_times(wql_scn* scn, int kind, double* ms, int* launches) {
+  if (!scn || !ms || !launches) return fail(WQL_E_INPUT, "null argument");
+  if (kind < 0 || kind > 2) return fail(WQL_E_INPUT, "kernel kind must be 0 (interface), 1 (stencil) or 2 (corrections)");
   CK(cudaStreamSynchronize(scn->stream));
-  double t[2] = {0.0, 0.0};
-  int n[2] = {0, 0};
+  double t = 0.0;
+  int n = 0;
   for (auto& m : scn->ev_marks) {
-    float ms = 0.0f;
-    CK(cudaEventElapsedTime(&ms, scn->ev_pool[m.first], scn->ev_pool[m.first + 1]));
-    t[m.second] += ms;
-    n[m.second] += 1;
+    if (m.second != kind) continue;
+    float e = 0.0f;
+    CK(cudaEventElapsedTime(&e, scn->ev_pool[m.first], scn->ev_pool[m.first + 1]));
+    t += e;
+    n += 1;
   }
-  *interface_ms = t[0];
-  *interface_launches = n[0];
-  *volume_ms = t[1];
-  *volume_launches = n[1];
+  *ms = t;
+  *launches = n;
+  return WQL_OK;
+}
+
+int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk) {
+  if (!scn || kernel_variant < 0 || kernel_variant > 4 || schunk < 0) return fail(WQL_E_INPUT, "bad tuning");
+  // 64x8 tiles of FP64 need 273 KiB of shared memory, more than a block may hold.
+  if (kernel_variant == 4 && scn->prec == WQL_FP64)
+    return fail(WQL_E_INPUT, "stencil variant 4 (64x8 tiles) is FP32-only");
+  scn->kernel_variant = kernel_variant;
+  scn->schunk = schunk;
   return WQL_OK;
 }
 
 int wql_launches_per_step(wql_scn* scn, int* launches) {
   if (!scn || !launches) return fail(WQL_E_INPUT, "null argument");
-  *launches = 5 * 3;  // per stage: interface + one volume launch per block
+  if (scn->launches_last_step == 0) return fail(WQL_E_STATE, "no step taken yet");
+  *launches = scn->launches_last_step;
   return WQL_OK;
 }
 

@@ -52,7 +52,8 @@ struct VolumeArgs {
   T* Q[6];
   T* DQ[6];
   long long slab_np[6];
-  int interior_lo[3], interior_hi[3];  // 0-based inclusive interior box
+  int kernel;         // stencil variant: 0 default, 1 per-point, 2..4 tiled
+  int schunk;         // planes per CTA along s for the tiled kernel (0: default)
   // RK
   T A, Bdt;
   // plasticity on the last stage
@@ -98,8 +99,13 @@ enum FrameOff : int {
 constexpr int kFrameOff[9] = {FR_UFACE, FR_VFACE, FR_S, FR_UHAT, FR_VHAT, FR_SVEL, FR_TRUP, FR_STATE, FR_END};
 
 // Kernel launchers (stream-ordered).
+// One stage on one block: launch_volume runs the stencil kernel (DF and the
+// updated fields for every point); launch_corrections then adds the PML,
+// boundary/fault penalty and plastic kernels and returns how many it issued.
 template <typename T>
 void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream);
+template <typename T>
+int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream);
 void launch_interface(const InterfaceArgs& a, void* stream);
 void launch_metrics(int nq, int nr, int ns, const double* x, double* metric, double* J,
                     void* stream);

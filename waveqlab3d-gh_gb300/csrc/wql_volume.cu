@@ -1,5 +1,6 @@
-// Fused volume kernel: one RK stage of the elastic velocity-stress system on
-// one block, per grid point:
+// Volume kernels: one RK stage of the elastic velocity-stress system on one
+// block.  The stencil kernel does the bulk per grid point; small correction
+// kernels add the PML, boundary/fault penalties and the plastic map:
 //
 //   DF <- A*DF + L(F)                 (scale_rates + set_rates,
 //                                      src/fields.f90:49-108,
@@ -40,10 +41,9 @@ template <>
 __device__ __forceinline__ float sbp_w<float>(int row, int col) { return c_sbp_f[row][col]; }
 
 // sigma_{c,j} component index in F: rows x,y,z of the symmetric stress.
-__device__ __forceinline__ int sig(int c, int j) {
+__host__ __device__ constexpr int sig(int c, int j) {
   // sxx=3 syy=4 szz=5 sxy=6 sxz=7 syz=8
-  const int t[3][3] = {{3, 6, 7}, {6, 4, 8}, {7, 8, 5}};
-  return t[c][j];
+  return c == j ? 3 + c : 5 + c + j;
 }
 
 // Load the six differenced quantities at point q for axis d: velocities
@@ -228,60 +228,313 @@ __device__ void boundary_sat(const double u[9], const double* __restrict__ face,
   sat[8] = mu * ubc[8];
 }
 
+
+// ---------------------------------------------------------------------------
+// SBP row lookup shared by every stencil: for a point at 0-based index i of
+// n, entry t (0..8) of its row is weight w at offset off from i.  Central
+// rows use entries 0..5, closure rows all nine (src/JU_xJU_yJU_z6.f90:55-164).
+template <typename T>
+__device__ __forceinline__ void row_entry(int kind, int t, T& w, int& off) {
+  if (kind == 0) {
+    const int k = t < 3 ? 3 - t : t - 2;  // 3,2,1 then 1,2,3
+    const T c = k == 1 ? T(kC1) : (k == 2 ? T(kC2) : T(kC3));
+    w = t < 3 ? -c : c;
+    off = t < 3 ? -k : k;
+    if (t > 5) { w = T(0); off = 0; }
+  } else if (kind < 0) {  // left closure row i = -kind-1, columns are points 0..8
+    const int i = -kind - 1;
+    w = sbp_w<T>(i, t);
+    off = t - i;
+  } else {  // right closure row k = n-1-i, columns are points n-1..n-9
+    const int k = kind - 1;
+    w = -sbp_w<T>(k, t);
+    off = k - t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Main stencil kernel (2.5-D tiled).  Computes, for every point of the block,
+//   DF <- A*DF + L(F)      and      F_out <- F + B*dt*DF
+// (scale_rates + set_rates + update_fields, src/fields.f90:49-171,
+// src/JU_xJU_yJU_z6.f90:12-812 and 16141-16449, src/RHS_Interior.f90:133-274),
+// with the Kahan-compensated update in FP32C mode.  Boundary penalties, PML
+// terms and the plastic return map are applied afterwards by the correction
+// kernels below (they are linear in DF, so the order of the sums changes only
+// rounding).
+//
+// A CTA of TQ x TR threads owns a (q,r) tile and marches along s through a
+// chunk of planes.  Per plane the tile plus a 3-point halo in q and r is
+// staged into shared memory as the differenced quantities -- velocities and
+// the q- and r-face momentum fluxes J*metric*sigma -- so each is formed once
+// and read by up to 7 neighbours from shared memory.  Along s every thread
+// keeps (v, s-face flux) of a 9-plane window in private shared-memory slots,
+// enough for the 7-point central rows and for the one-sided closure rows,
+// which read planes 0..8 (or n-9..n-1).  The last tile along q and r is
+// shifted to end on the last point and owns its whole width, so every
+// closure row lies inside one tile plus halo (needs TQ, TR >= 8).
+template <typename T, int TQ, int TR>
+struct Tile {
+  static constexpr int HQ = TQ + 6, HR = TR + 6, NRING = 9;
+  static constexpr int sgq_off = 3 * HR * HQ, sgr_off = sgq_off + 3 * TR * HQ, ring_off = sgr_off + 3 * HR * TQ;
+  static constexpr size_t words = ring_off + NRING * 6 * TR * TQ;
+  __device__ static T& sv(T* b, int c, int lr, int lq) { return b[(c * HR + lr) * HQ + lq]; }
+  __device__ static T& sgq(T* b, int c, int ty, int lq) { return b[sgq_off + (c * TR + ty) * HQ + lq]; }
+  __device__ static T& sgr(T* b, int c, int lr, int tx) { return b[sgr_off + (c * HR + lr) * TQ + tx]; }
+  __device__ static T& ring(T* b, int slot, int c, int ty, int tx) {
+    return b[ring_off + ((slot * 6 + c) * TR + ty) * TQ + tx];
+  }
+};
+
+struct TileSpan {
+  int origin, own_lo, own_hi;
+};
+__device__ __forceinline__ TileSpan tile_span(int t, int n, int T_) {
+  const int ntiles = (n + T_ - 1) / T_;
+  TileSpan sp;
+  if (n <= T_) {
+    sp.origin = 0; sp.own_lo = 0; sp.own_hi = n;
+  } else if (t == ntiles - 1) {
+    sp.origin = n - T_; sp.own_lo = n - T_; sp.own_hi = n;
+  } else {
+    sp.origin = t * T_; sp.own_lo = t * T_; sp.own_hi = min((t + 1) * T_, n - T_);
+  }
+  return sp;
+}
+
+template <typename T, bool CURV, bool KAHAN, int TQ, int TR, int MINB>
+__global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __grid_constant__ VolumeArgs<T> a,
+                                                                       int schunk) {
+  using TL = Tile<T, TQ, TR>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nq = a.nq, nr = a.nr, ns = a.ns;
+  const long long np = a.np;
+  const long long sts = (long long)nq * nr;
+  const TileSpan spq = tile_span(blockIdx.x, nq, TQ), spr = tile_span(blockIdx.y, nr, TR);
+  const int q0 = spq.origin, r0 = spr.origin;
+  const int q = q0 + tx, r = r0 + ty;
+  const bool valid = q < nq && r < nr;
+  const bool own = valid && q >= spq.own_lo && q < spq.own_hi && r >= spr.own_lo && r < spr.own_hi;
+  const int s_begin = blockIdx.z * schunk;
+  const int s_end = min(ns, s_begin + schunk);
+  const T* __restrict__ F = a.Fin;
+  const T* __restrict__ coef = a.coef;
+  const int lq = tx + 3, lr = ty + 3;
+  const int kq = sbp_kind(q, nq), kr = sbp_kind(r, nr);
+  const long long col = q + (long long)nq * r;
+  int lo = 0, hi = -1;  // planes held by the ring (uniform across the CTA)
+
+  for (int s = s_begin; s < s_end; ++s) {
+    const long long p = col + sts * s;
+    // ---- ring: make planes [need_lo, need_hi] resident (private slots)
+    const int ks = sbp_kind(s, ns);
+    const int need_lo = ks < 0 ? 0 : (ks > 0 ? ns - 9 : s - 3);
+    const int need_hi = ks < 0 ? 8 : (ks > 0 ? ns - 1 : s + 3);
+    if (need_lo < lo || need_lo > hi + 1) {
+      lo = need_lo;
+      hi = need_lo - 1;
+    }
+    for (int pl = hi + 1; pl <= need_hi; ++pl) {
+      if (valid) {
+        T t6[6];
+        load6<T, CURV>(F, coef, np, col + sts * pl, 2, t6);
+        const int slot = pl % 9;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) TL::ring(sm, slot, c, ty, tx) = t6[c];
+      }
+    }
+    hi = need_hi;
+    lo = max(lo, hi - 8);
+    // ---- stage the plane's cross region into shared memory
+    __syncthreads();
+    auto stage = [&](int gq, int gr, int lq_, int lr_, bool wq, bool wr) {
+      const long long pp = gq + (long long)nq * gr + sts * s;
+      T f[9];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) f[c] = F[c * np + pp];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) TL::sv(sm, c, lr_, lq_) = f[c];
+      if (wq) {
+        if (CURV) {
+          const T a0 = coef[0 * np + pp], a1 = coef[1 * np + pp], a2 = coef[2 * np + pp];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            TL::sgq(sm, c, lr_ - 3, lq_) = a0 * f[sig(c, 0)] + a1 * f[sig(c, 1)] + a2 * f[sig(c, 2)];
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) TL::sgq(sm, c, lr_ - 3, lq_) = f[sig(c, 0)];
+        }
+      }
+      if (wr) {
+        if (CURV) {
+          const T a0 = coef[3 * np + pp], a1 = coef[4 * np + pp], a2 = coef[5 * np + pp];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            TL::sgr(sm, c, lr_, lq_ - 3) = a0 * f[sig(c, 0)] + a1 * f[sig(c, 1)] + a2 * f[sig(c, 2)];
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) TL::sgr(sm, c, lr_, lq_ - 3) = f[sig(c, 1)];
+        }
+      }
+    };
+    if (valid) stage(q, r, lq, lr, true, true);
+    if (r < nr) {
+      if (tx < 3 && q0 - 3 + tx >= 0) stage(q0 - 3 + tx, r, tx, lr, true, false);
+      if (tx >= TQ - 3 && q0 + TQ + (tx - (TQ - 3)) < nq)
+        stage(q0 + TQ + (tx - (TQ - 3)), r, TQ + 3 + (tx - (TQ - 3)), lr, true, false);
+    }
+    if (q < nq) {
+      if (ty < 3 && r0 - 3 + ty >= 0) stage(q, r0 - 3 + ty, lq, ty, false, true);
+      if (ty >= TR - 3 && r0 + TR + (ty - (TR - 3)) < nr)
+        stage(q, r0 + TR + (ty - (TR - 3)), lq, TR + 3 + (ty - (TR - 3)), false, true);
+    }
+    __syncthreads();
+    if (!own) continue;
+
+    // ---- derivatives, consumed axis by axis
+    T g[3][3], dv[3];
+    const T Jinv = CURV ? coef[9 * np + p] : T(1);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      T o[6];
+      const int kind = d == 0 ? kq : (d == 1 ? kr : ks);
+      if (kind == 0) {
+        const T c1 = T(kC1), c2 = T(kC2), c3 = T(kC3);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+          T xp1, xm1, xp2, xm2, xp3, xm3;
+          if (d == 0) {
+            auto X = [&](int l) -> T { return c < 3 ? TL::sv(sm, c, lr, l) : TL::sgq(sm, c - 3, ty, l); };
+            xp1 = X(lq + 1); xm1 = X(lq - 1); xp2 = X(lq + 2); xm2 = X(lq - 2); xp3 = X(lq + 3); xm3 = X(lq - 3);
+          } else if (d == 1) {
+            auto X = [&](int l) -> T { return c < 3 ? TL::sv(sm, c, l, lq) : TL::sgr(sm, c - 3, l, tx); };
+            xp1 = X(lr + 1); xm1 = X(lr - 1); xp2 = X(lr + 2); xm2 = X(lr - 2); xp3 = X(lr + 3); xm3 = X(lr - 3);
+          } else {
+            xp1 = TL::ring(sm, (s + 1) % 9, c, ty, tx); xm1 = TL::ring(sm, (s + 8) % 9, c, ty, tx);
+            xp2 = TL::ring(sm, (s + 2) % 9, c, ty, tx); xm2 = TL::ring(sm, (s + 7) % 9, c, ty, tx);
+            xp3 = TL::ring(sm, (s + 3) % 9, c, ty, tx); xm3 = TL::ring(sm, (s + 6) % 9, c, ty, tx);
+          }
+          o[c] = c1 * (xp1 - xm1) + c2 * (xp2 - xm2) + c3 * (xp3 - xm3);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) o[c] = T(0);
+#pragma unroll 1
+        for (int t = 0; t < 9; ++t) {
+          T w;
+          int off;
+          row_entry<T>(kind, t, w, off);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            T x;
+            if (d == 0) x = c < 3 ? TL::sv(sm, c, lr, lq + off) : TL::sgq(sm, c - 3, ty, lq + off);
+            else if (d == 1) x = c < 3 ? TL::sv(sm, c, lr + off, lq) : TL::sgr(sm, c - 3, lr + off, tx);
+            else x = TL::ring(sm, (s + off + 18) % 9, c, ty, tx);
+            o[c] += w * x;
+          }
+        }
+      }
+      const T rh = a.rh[d];
+      if (CURV) {
+        T m[3];
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) m[jj] = coef[(d * 3 + jj) * np + p] * Jinv;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          dv[c] = d == 0 ? rh * o[3 + c] : dv[c] + rh * o[3 + c];
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) g[c][jj] = d == 0 ? m[jj] * (rh * o[c]) : g[c][jj] + m[jj] * (rh * o[c]);
+        }
+      } else {
+        const T sc = a.cart_metric[d] * rh;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          dv[c] = d == 0 ? sc * o[3 + c] : dv[c] + sc * o[3 + c];
+          g[c][d] = sc * o[c];
+        }
+      }
+    }
+    T lam, mu, rinv;
+    if (CURV) {
+      lam = coef[10 * np + p];
+      mu = coef[11 * np + p];
+      rinv = coef[12 * np + p];
+    } else {
+      lam = coef[0 * np + p];
+      mu = coef[1 * np + p];
+      rinv = coef[2 * np + p];
+    }
+    const T l2m = lam + T(2) * mu;
+    T du[9];
+    du[0] = rinv * dv[0];
+    du[1] = rinv * dv[1];
+    du[2] = rinv * dv[2];
+    du[3] = l2m * g[0][0] + lam * (g[1][1] + g[2][2]);
+    du[4] = l2m * g[1][1] + lam * (g[0][0] + g[2][2]);
+    du[5] = l2m * g[2][2] + lam * (g[0][0] + g[1][1]);
+    du[6] = mu * (g[0][1] + g[1][0]);
+    du[7] = mu * (g[0][2] + g[2][0]);
+    du[8] = mu * (g[1][2] + g[2][1]);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+      const T f0 = F[c * np + p];
+      const T df = a.A * a.DF[c * np + p] + du[c];
+      a.DF[c * np + p] = df;
+      if (KAHAN) {
+        const T y = a.Bdt * df - a.C[c * np + p];
+        const T t = f0 + y;
+        a.C[c * np + p] = (t - f0) - y;
+        a.Fout[c * np + p] = t;
+      } else {
+        a.Fout[c * np + p] = f0 + a.Bdt * df;
+      }
+    }
+  }
+}
+
+// Per-point form of the same stencil kernel: every neighbour value is read
+// through L1/L2 (kept for cross-checks of the tiled kernel).
 template <typename T, bool CURV, bool KAHAN>
-__global__ void __launch_bounds__(256) volume_kernel(const VolumeArgs<T> a) {
+__global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_constant__ VolumeArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= a.nq || j >= a.nr) return;
-  const int nq = a.nq, nr = a.nr, ns = a.ns;
   const long long np = a.np;
-  const long long p = i + (long long)nq * (j + (long long)nr * k);
-  const long long st[3] = {1, nq, (long long)nq * nr};
-  const int idx[3] = {i, j, k};
-  const int nn[3] = {nq, nr, ns};
-  const T* __restrict__ F = a.Fin;
-  const T* __restrict__ coef = a.coef;
-
-  T res[3][6];
+  const long long p = i + (long long)a.nq * (j + (long long)a.nr * k);
+  T g[3][3], dv[3];
+  const T Jinv = CURV ? a.coef[9 * np + p] : T(1);
+  const int idx[3] = {i, j, k}, nn[3] = {a.nq, a.nr, a.ns};
+  const long long st[3] = {1, a.nq, (long long)a.nq * a.nr};
 #pragma unroll
-  for (int d = 0; d < 3; ++d) diff6<T, CURV>(F, coef, np, p, idx[d], nn[d], st[d], d, res[d]);
-
-  T lam, mu, rinv, Jinv = T(1);
-  T g[3][3];  // g[c][j] = d v_c / d x_j
-  T dv[3];    // momentum: divergence of stress
-  if (CURV) {
-    Jinv = coef[9 * np + p];
-    lam = coef[10 * np + p];
-    mu = coef[11 * np + p];
-    rinv = coef[12 * np + p];  // 1/(rho J)
-    T met[3][3];               // met[j][d] = metric_j(d) at the centre
+  for (int d = 0; d < 3; ++d) {
+    T o[6];
+    diff6<T, CURV>(a.Fin, a.coef, np, p, idx[d], nn[d], st[d], d, o);
+    const T rh = a.rh[d];
+    if (CURV) {
+      T m[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
+      for (int jj = 0; jj < 3; ++jj) m[jj] = a.coef[(d * 3 + jj) * np + p] * Jinv;
 #pragma unroll
-      for (int jj = 0; jj < 3; ++jj) met[jj][d] = coef[(d * 3 + jj) * np + p] * Jinv;
+      for (int c = 0; c < 3; ++c) {
+        dv[c] = d == 0 ? rh * o[3 + c] : dv[c] + rh * o[3 + c];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      dv[c] = a.rh[0] * res[0][3 + c] + a.rh[1] * res[1][3 + c] + a.rh[2] * res[2][3 + c];
+        for (int jj = 0; jj < 3; ++jj) g[c][jj] = d == 0 ? m[jj] * (rh * o[c]) : g[c][jj] + m[jj] * (rh * o[c]);
+      }
+    } else {
+      const T sc = a.cart_metric[d] * rh;
 #pragma unroll
-      for (int jj = 0; jj < 3; ++jj)
-        g[c][jj] = met[jj][0] * (a.rh[0] * res[0][c]) + met[jj][1] * (a.rh[1] * res[1][c]) +
-                   met[jj][2] * (a.rh[2] * res[2][c]);
-    }
-  } else {
-    lam = coef[0 * np + p];
-    mu = coef[1 * np + p];
-    rinv = coef[2 * np + p];  // 1/rho
-    T sc[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) sc[d] = a.cart_metric[d] * a.rh[d];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      dv[c] = sc[0] * res[0][3 + c] + sc[1] * res[1][3 + c] + sc[2] * res[2][3 + c];
-#pragma unroll
-      for (int jj = 0; jj < 3; ++jj) g[c][jj] = sc[jj] * res[jj][c];
+      for (int c = 0; c < 3; ++c) {
+        dv[c] = d == 0 ? sc * o[3 + c] : dv[c] + sc * o[3 + c];
+        g[c][d] = sc * o[c];
+      }
     }
   }
+  const T* coef = a.coef;
+  const T lam = CURV ? coef[10 * np + p] : coef[0 * np + p];
+  const T mu = CURV ? coef[11 * np + p] : coef[1 * np + p];
+  const T rinv = CURV ? coef[12 * np + p] : coef[2 * np + p];
   const T l2m = lam + T(2) * mu;
   T du[9];
   du[0] = rinv * dv[0];
@@ -293,215 +546,345 @@ __global__ void __launch_bounds__(256) volume_kernel(const VolumeArgs<T> a) {
   du[6] = mu * (g[0][1] + g[1][0]);
   du[7] = mu * (g[0][2] + g[2][0]);
   du[8] = mu * (g[1][2] + g[2][1]);
-
-  // ---------------- PML (slabs of npml layers on the active sides) -------
-  if (a.npml > 0) {
-    const double d0 = 6.0 / (2.0 * 1.0) * log(1.0 / 1.0e-3);
-    const T cfs = T(1);
-    // reference order of the layers: s-low, s-high, r-low, r-high, q-low, q-high
-    const int order[6] = {4, 5, 2, 3, 0, 1};
-    for (int oi = 0; oi < 6; ++oi) {
-      const int side = order[oi];
-      if (!a.pml[side]) continue;
-      const int axis = side >> 1;
-      const bool hi = side & 1;
-      const int ii = idx[axis], n = nn[axis], npml = a.npml;
-      const bool in = hi ? (ii >= n - npml) : (ii < npml);
-      if (!in) continue;
-      // damping profile in grid-index units (src/RHS_Interior.f90:1855,1973,2092)
-      double dd;
-      if (axis == 2) dd = hi ? fabs((double)(ii + 1 - (n - npml)) / npml) : fabs((double)(ii + 1 - npml) / npml);
-      else dd = hi ? fabs((double)(ii + 1 - (n - npml)) / npml) : fabs((double)(ii - npml) / npml);
-      const T damp = (T)(d0 * dd);
-      // slab index
-      long long sp;
-      if (axis == 0) sp = (hi ? ii - (n - npml) : ii) + (long long)npml * (j + (long long)nr * k);
-      else if (axis == 1) sp = i + (long long)nq * ((hi ? ii - (n - npml) : ii) + (long long)npml * k);
-      else sp = i + (long long)nq * (j + (long long)nr * (hi ? ii - (n - npml) : ii));
-      const long long snp = a.slab_np[side];
-      T* Q = a.Q[side];
-      T* DQ = a.DQ[side];
-      T q[9];
-#pragma unroll
-      for (int c = 0; c < 9; ++c) q[c] = Q[c * snp + sp];
-      // per-axis stress derivative for the auxiliary sources
-      T sd[3];
-      const int jx = axis;  // physical axis paired with this side
-      if (CURV) {
-        T acc3[3] = {T(0), T(0), T(0)};
-        for (int d = 0; d < 3; ++d) {
-          T r3[3];
-          diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, jx, r3);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) acc3[c] += a.rh[d] * r3[c];
-        }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) sd[c] = acc3[c] * Jinv;
-      } else {
-        const T sc = a.cart_metric[jx] * a.rh[jx];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) sd[c] = sc * res[jx][3 + c];
-      }
-      const T rhoinv = CURV ? (rinv / Jinv) : rinv;  // J/(rho J) = 1/rho
-      du[0] -= damp * q[0] * rhoinv;
-      du[1] -= damp * q[1] * rhoinv;
-      du[2] -= damp * q[2] * rhoinv;
-      du[3] -= damp * (l2m * q[3] + lam * q[4] + lam * q[5]);
-      du[4] -= damp * (lam * q[3] + l2m * q[4] + lam * q[5]);
-      du[5] -= damp * (lam * q[3] + lam * q[4] + l2m * q[5]);
-      du[6] -= mu * damp * q[6];
-      du[7] -= mu * damp * q[7];
-      du[8] -= mu * damp * q[8];
-      T src[9];
-#pragma unroll
-      for (int c = 0; c < 9; ++c) src[c] = T(0);
-      src[0] = sd[0];
-      src[1] = sd[1];
-      src[2] = sd[2];
-      // velocity-gradient sources (src/RHS_Interior.f90:1890-1907, 2008-2025, 2125-2142)
-      if (jx == 0) { src[3] = g[0][0]; src[6] = g[1][0]; src[7] = g[2][0]; }
-      else if (jx == 1) { src[4] = g[1][1]; src[6] = g[0][1]; src[8] = g[2][1]; }
-      else { src[5] = g[2][2]; src[7] = g[0][2]; src[8] = g[1][2]; }
-      T dq[9];
-#pragma unroll
-      for (int c = 0; c < 9; ++c) dq[c] = a.A * DQ[c * snp + sp] + src[c] - (damp + cfs) * q[c];
-      // boundary SAT on this side's own face also drives DQ
-      const bool on_face = hi ? (ii == n - 1) : (ii == 0);
-      if (on_face && a.bc[side] >= 1 && a.bc[side] <= 3) {
-        double u[9], sat[9], ubc[9];
-#pragma unroll
-        for (int c = 0; c < 9; ++c) u[c] = (double)F[c * np + p];
-        const int na = axis == 0 ? nr : nq;
-        const long long f = axis == 0 ? (j + (long long)nr * k) : (axis == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
-        const long long nf = (long long)na * (axis == 2 ? nr : ns);
-        boundary_sat(u, a.face[side], nf, f, a.bc[side], hi, a.bc_form, sat, ubc);
-#pragma unroll
-        for (int c = 0; c < 9; ++c) dq[c] -= a.tau_h[axis] * (T)ubc[c];
-      }
-#pragma unroll
-      for (int c = 0; c < 9; ++c) {
-        DQ[c * snp + sp] = dq[c];
-        Q[c * snp + sp] = q[c] + a.Bdt * dq[c];
-      }
-    }
-  }
-
-  // ---------------- RK register: DF <- A*DF + L(F) -------------------------
-  T df[9];
-#pragma unroll
-  for (int c = 0; c < 9; ++c) df[c] = a.A * a.DF[c * np + p] + du[c];
-
-  // ---------------- outer-boundary SAT --------------------------------------
-  const bool on_boundary = (i == 0) | (i == nq - 1) | (j == 0) | (j == nr - 1) | (k == 0) | (k == ns - 1);
-  if (on_boundary) {
-    double u[9];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) u[c] = (double)F[c * np + p];
-    for (int side = 0; side < 6; ++side) {
-      const int code = a.bc[side];
-      if (code < 1 || code > 3) continue;
-      const int axis = side >> 1;
-      const bool hi = side & 1;
-      if (idx[axis] != (hi ? nn[axis] - 1 : 0)) continue;
-      const int na = axis == 0 ? nr : nq;
-      const long long nf = (long long)na * (axis == 2 ? nr : ns);
-      const long long f = axis == 0 ? (j + (long long)nr * k) : (axis == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
-      double sat[9], ubc[9];
-      boundary_sat(u, a.face[side], nf, f, code, hi, a.bc_form, sat, ubc);
-#pragma unroll
-      for (int c = 0; c < 9; ++c) df[c] -= a.tau_h[axis] * (T)sat[c];
-    }
-    // fault SAT on the interface face
-    if (a.fault_sat && ((a.block == 0 && i == nq - 1) || (a.block == 1 && i == 0))) {
-      const long long nf = (long long)nr * ns;
-      const long long f = j + (long long)nr * k;
-#pragma unroll
-      for (int c = 0; c < 9; ++c) df[c] -= a.fault_sat[c * nf + f];
-    }
-  }
-
-  // ---------------- update ---------------------------------------------------
-  T fo[9];
-  if (KAHAN) {
-    T cc[9];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) {
-      const T f0 = F[c * np + p];
-      const T y = a.Bdt * df[c] - a.C[c * np + p];
-      const T t = f0 + y;
-      cc[c] = (t - f0) - y;
-      fo[c] = t;
-    }
-    if (a.plastic) {
-      // fall through to the plastic update below with the compensation kept
-    }
-#pragma unroll
-    for (int c = 0; c < 9; ++c) a.C[c * np + p] = cc[c];
-  } else {
-#pragma unroll
-    for (int c = 0; c < 9; ++c) fo[c] = F[c * np + p] + a.Bdt * df[c];
-  }
-
-  // ---------------- plasticity (last stage, non-PML points) ----------------
-  if (a.plastic) {
-    bool inside = true;
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      if (a.pml[2 * ax] && idx[ax] < a.npml) inside = false;
-      if (a.pml[2 * ax + 1] && idx[ax] >= nn[ax] - a.npml) inside = false;
-    }
-    if (inside) {
-      double xs[3] = {0.0, (double)a.ycoord[p], 0.0}, s0[6];
-      if (!initial_stress(a.preset, xs, s0))
-        for (int c = 0; c < 6; ++c) s0[c] = a.s0u[c];
-      T sa[6];
-#pragma unroll
-      for (int c = 0; c < 6; ++c) sa[c] = fo[3 + c] + (T)s0[c];
-      const T sigma = (sa[0] + sa[1] + sa[2]) / T(3);
-      const T J2 = ((sa[0] - sa[1]) * (sa[0] - sa[1]) + (sa[1] - sa[2]) * (sa[1] - sa[2]) +
-                    (sa[2] - sa[0]) * (sa[2] - sa[0])) / T(6) +
-                   sa[3] * sa[3] + sa[4] * sa[4] + sa[5] * sa[5];
-      const T tau = sqrt(J2);
-      const T Ys = fmax(T(0), (T)(a.pl_c * cos(atan(a.pl_nu))) - sigma * (T)sin(atan(a.pl_nu)));
-      if (tau - Ys > T(0)) {
-        const T e = (T)exp(-a.dt / a.pl_Tv);
-        const T r = e + (T(1) - e) * Ys / tau;
-        const T delta[6] = {T(1), T(1), T(1), T(0), T(0), T(0)};
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-          const T sd = sa[c] - sigma * delta[c];
-          fo[3 + c] = (sigma * delta[c] + r * sd) - (T)s0[c];
-        }
-        if (KAHAN)
-#pragma unroll
-          for (int c = 3; c < 9; ++c) a.C[c * np + p] = T(0);
-      }
-    }
-  }
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
-    a.DF[c * np + p] = df[c];
-    a.Fout[c * np + p] = fo[c];
+    const T f0 = a.Fin[c * np + p];
+    const T df = a.A * a.DF[c * np + p] + du[c];
+    a.DF[c * np + p] = df;
+    if (KAHAN) {
+      const T y = a.Bdt * df - a.C[c * np + p];
+      const T t = f0 + y;
+      a.C[c * np + p] = (t - f0) - y;
+      a.Fout[c * np + p] = t;
+    } else {
+      a.Fout[c * np + p] = f0 + a.Bdt * df;
+    }
+  }
+}
+
+// Adds corr to DF and B*dt*corr to the updated field of one point
+// (compensated in FP32C).
+template <typename T, bool KAHAN>
+__device__ __forceinline__ void add_correction(const VolumeArgs<T>& a, long long p, const T (&corr)[9]) {
+  const long long np = a.np;
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    if (corr[c] == T(0)) continue;
+    a.DF[c * np + p] += corr[c];
+    const T f0 = a.Fout[c * np + p];
+    if (KAHAN) {
+      const T y = a.Bdt * corr[c] - a.C[c * np + p];
+      const T t = f0 + y;
+      a.C[c * np + p] = (t - f0) - y;
+      a.Fout[c * np + p] = t;
+    } else {
+      a.Fout[c * np + p] = f0 + a.Bdt * corr[c];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// PML kernel (src/RHS_Interior.f90:1782-2201, src/fields.f90:70-105,131-166):
+// for every point inside one or more active slabs, the damping terms of the
+// rates, DQ <- A*DQ + sources - (d+cfs)*Q (plus the face penalty on the
+// slab's own boundary, src/RHS_Interior.f90:1560-1700) and Q <- Q + B*dt*DQ.
+// One thread per point of the block; points outside every slab exit.
+template <typename T, bool CURV, bool KAHAN>
+__global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  const int nq = a.nq, nr = a.nr, ns = a.ns, npml = a.npml;
+  if (i >= nq || j >= nr) return;
+  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
+  bool any = false;
+#pragma unroll
+  for (int side = 0; side < 6; ++side) {
+    const int ax = side >> 1;
+    if (a.pml[side] && ((side & 1) ? idx[ax] >= nn[ax] - npml : idx[ax] < npml)) any = true;
+  }
+  if (!any) return;
+  const long long np = a.np;
+  const long long p = i + (long long)nq * (j + (long long)nr * k);
+  const long long st[3] = {1, nq, (long long)nq * nr};
+  const T* __restrict__ F = a.Fin;
+  const T* __restrict__ coef = a.coef;
+  // velocity gradient at the point
+  T g[3][3];
+  const T Jinv = CURV ? coef[9 * np + p] : T(1);
+  for (int d = 0; d < 3; ++d) {
+    T o[6];
+    diff6<T, CURV>(F, coef, np, p, idx[d], nn[d], st[d], d, o);
+    const T rh = a.rh[d];
+    for (int c = 0; c < 3; ++c) {
+      if (CURV) {
+        for (int jj = 0; jj < 3; ++jj) {
+          const T m = coef[(d * 3 + jj) * np + p] * Jinv;
+          g[c][jj] = d == 0 ? m * (rh * o[c]) : g[c][jj] + m * (rh * o[c]);
+        }
+      } else {
+        g[c][d] = a.cart_metric[d] * rh * o[c];
+      }
+    }
+    // Cartesian: the per-axis stress derivatives are the flux derivatives
+  }
+  const T lam = CURV ? coef[10 * np + p] : coef[0 * np + p];
+  const T mu = CURV ? coef[11 * np + p] : coef[1 * np + p];
+  const T rinv = CURV ? coef[12 * np + p] : coef[2 * np + p];
+  const T rhoinv = CURV ? rinv / Jinv : rinv;
+  const T l2m = lam + T(2) * mu;
+  const double d0 = 6.0 / (2.0 * 1.0) * log(1.0 / 1.0e-3);
+  const T cfs = T(1);
+  T corr[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) corr[c] = T(0);
+  // reference order of the layers: s-low, s-high, r-low, r-high, q-low, q-high
+  for (int oi = 0; oi < 6; ++oi) {
+    const int side = oi < 2 ? 4 + oi : (oi < 4 ? oi : oi - 4);
+    if (!a.pml[side]) continue;
+    const int axis = side >> 1;
+    const bool hi = side & 1;
+    const int ii = idx[axis], n = nn[axis];
+    if (!(hi ? (ii >= n - npml) : (ii < npml))) continue;
+    double dd;  // damping profile in grid-index units (src/RHS_Interior.f90:1855,1973,2092)
+    if (axis == 2) dd = hi ? fabs((double)(ii + 1 - (n - npml)) / npml) : fabs((double)(ii + 1 - npml) / npml);
+    else dd = hi ? fabs((double)(ii + 1 - (n - npml)) / npml) : fabs((double)(ii - npml) / npml);
+    const T damp = (T)(d0 * dd);
+    long long sp;
+    if (axis == 0) sp = (hi ? ii - (n - npml) : ii) + (long long)npml * (j + (long long)nr * k);
+    else if (axis == 1) sp = i + (long long)nq * ((hi ? ii - (n - npml) : ii) + (long long)npml * k);
+    else sp = i + (long long)nq * (j + (long long)nr * (hi ? ii - (n - npml) : ii));
+    const long long snp = a.slab_np[side];
+    T* Q = a.Q[side];
+    T* DQ = a.DQ[side];
+    T qv[9];
+    for (int c = 0; c < 9; ++c) qv[c] = Q[c * snp + sp];
+    // per-axis split of the stress divergence along physical axis `axis`
+    T sd[3];
+    if (CURV) {
+      T acc3[3] = {T(0), T(0), T(0)};
+      for (int d = 0; d < 3; ++d) {
+        T r3[3];
+        diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
+        for (int c = 0; c < 3; ++c) acc3[c] += a.rh[d] * r3[c];
+      }
+      for (int c = 0; c < 3; ++c) sd[c] = acc3[c] * Jinv;
+    } else {
+      T o[6];
+      diff6<T, false>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, o);
+      for (int c = 0; c < 3; ++c) sd[c] = a.cart_metric[axis] * a.rh[axis] * o[3 + c];
+    }
+    corr[0] -= damp * qv[0] * rhoinv;
+    corr[1] -= damp * qv[1] * rhoinv;
+    corr[2] -= damp * qv[2] * rhoinv;
+    corr[3] -= damp * (l2m * qv[3] + lam * qv[4] + lam * qv[5]);
+    corr[4] -= damp * (lam * qv[3] + l2m * qv[4] + lam * qv[5]);
+    corr[5] -= damp * (lam * qv[3] + lam * qv[4] + l2m * qv[5]);
+    corr[6] -= mu * damp * qv[6];
+    corr[7] -= mu * damp * qv[7];
+    corr[8] -= mu * damp * qv[8];
+    T src[9];
+    for (int c = 0; c < 9; ++c) src[c] = T(0);
+    src[0] = sd[0];
+    src[1] = sd[1];
+    src[2] = sd[2];
+    // velocity-gradient sources (src/RHS_Interior.f90:1890-1907, 2008-2025, 2125-2142)
+    if (axis == 0) { src[3] = g[0][0]; src[6] = g[1][0]; src[7] = g[2][0]; }
+    else if (axis == 1) { src[4] = g[1][1]; src[6] = g[0][1]; src[8] = g[2][1]; }
+    else { src[5] = g[2][2]; src[7] = g[0][2]; src[8] = g[1][2]; }
+    T dq[9];
+    for (int c = 0; c < 9; ++c) dq[c] = a.A * DQ[c * snp + sp] + src[c] - (damp + cfs) * qv[c];
+    const bool on_face = hi ? (ii == n - 1) : (ii == 0);
+    if (on_face && a.bc[side] >= 1 && a.bc[side] <= 3) {
+      double u[9], sat[9], ubc[9];
+      for (int c = 0; c < 9; ++c) u[c] = (double)F[c * np + p];
+      const int na = axis == 0 ? nr : nq;
+      const long long f = axis == 0 ? (j + (long long)nr * k) : (axis == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
+      const long long nf = (long long)na * (axis == 2 ? nr : ns);
+      boundary_sat(u, a.face[side], nf, f, a.bc[side], hi, a.bc_form, sat, ubc);
+      for (int c = 0; c < 9; ++c) dq[c] -= a.tau_h[axis] * (T)ubc[c];
+    }
+    for (int c = 0; c < 9; ++c) {
+      DQ[c * snp + sp] = dq[c];
+      Q[c * snp + sp] = qv[c] + a.Bdt * dq[c];
+    }
+  }
+  add_correction<T, KAHAN>(a, p, corr);
+}
+
+// ---------------------------------------------------------------------------
+// Face kernel: outer-boundary SAT (src/RHS_Interior.f90:1516-1703 with
+// src/BoundaryConditions.f90:777-918 + structure(), or the weighted form of
+// src/BoundaryConditions3.f90:777-903) and the fault SAT computed by the
+// interface kernel (src/RHS_Interior.f90:1757-1772).  One thread per face
+// point; a point on several faces is handled once, by its lowest side.
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(256) face_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  const int nq = a.nq, nr = a.nr, ns = a.ns;
+  const long long nfs[6] = {(long long)nr * ns, (long long)nr * ns, (long long)nq * ns, (long long)nq * ns,
+                            (long long)nq * nr, (long long)nq * nr};
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int side = 0;
+  while (side < 6 && t >= nfs[side]) {
+    t -= nfs[side];
+    ++side;
+  }
+  if (side >= 6) return;
+  const int axis = side >> 1;
+  int i, j, k;
+  if (axis == 0) { i = (side & 1) ? nq - 1 : 0; j = (int)(t % nr); k = (int)(t / nr); }
+  else if (axis == 1) { i = (int)(t % nq); j = (side & 1) ? nr - 1 : 0; k = (int)(t / nq); }
+  else { i = (int)(t % nq); j = (int)(t / nq); k = (side & 1) ? ns - 1 : 0; }
+  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
+  // owner: the lowest side containing the point
+  for (int s2 = 0; s2 < side; ++s2) {
+    const int ax2 = s2 >> 1;
+    if (idx[ax2] == ((s2 & 1) ? nn[ax2] - 1 : 0)) return;
+  }
+  const long long np = a.np;
+  const long long p = i + (long long)nq * (j + (long long)nr * k);
+  double tot[9];
+  for (int c = 0; c < 9; ++c) tot[c] = 0.0;
+  bool any = false;
+  double u[9];
+  for (int c = 0; c < 9; ++c) u[c] = (double)a.Fin[c * np + p];
+  for (int s2 = 0; s2 < 6; ++s2) {
+    const int code = a.bc[s2];
+    if (code < 1 || code > 3) continue;
+    const int ax2 = s2 >> 1;
+    const bool hi = s2 & 1;
+    if (idx[ax2] != (hi ? nn[ax2] - 1 : 0)) continue;
+    const int na = ax2 == 0 ? nr : nq;
+    const long long nf = (long long)na * (ax2 == 2 ? nr : ns);
+    const long long f = ax2 == 0 ? (j + (long long)nr * k) : (ax2 == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
+    double sat[9], ubc[9];
+    boundary_sat(u, a.face[s2], nf, f, code, hi, a.bc_form, sat, ubc);
+    for (int c = 0; c < 9; ++c) tot[c] += (double)a.tau_h[ax2] * sat[c];
+    any = true;
+  }
+  T corr[9];
+  for (int c = 0; c < 9; ++c) corr[c] = (T)(-tot[c]);
+  if (a.fault_sat && ((a.block == 0 && i == nq - 1) || (a.block == 1 && i == 0))) {
+    const long long nf = (long long)nr * ns;
+    const long long f = j + (long long)nr * k;
+    for (int c = 0; c < 9; ++c) corr[c] -= a.fault_sat[c * nf + f];
+    any = true;
+  }
+  if (any) add_correction<T, KAHAN>(a, p, corr);
+}
+
+// ---------------------------------------------------------------------------
+// Plastic return map after the last stage (update_fields_plastic,
+// src/plastic.f90:11-151, plastic_flow2 :153-217), on points outside the PML
+// slabs, applied to the updated stresses.
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= a.nq || j >= a.nr) return;
+  const int idx[3] = {i, j, k}, nn[3] = {a.nq, a.nr, a.ns};
+  for (int ax = 0; ax < 3; ++ax) {
+    if (a.pml[2 * ax] && idx[ax] < a.npml) return;
+    if (a.pml[2 * ax + 1] && idx[ax] >= nn[ax] - a.npml) return;
+  }
+  const long long np = a.np;
+  const long long p = i + (long long)a.nq * (j + (long long)a.nr * k);
+  double xs[3] = {0.0, (double)a.ycoord[p], 0.0}, s0[6];
+  if (!initial_stress(a.preset, xs, s0))
+    for (int c = 0; c < 6; ++c) s0[c] = a.s0u[c];
+  T sa[6];
+  for (int c = 0; c < 6; ++c) sa[c] = a.Fout[(3 + c) * np + p] + (T)s0[c];
+  const T sigma = (sa[0] + sa[1] + sa[2]) / T(3);
+  const T J2 = ((sa[0] - sa[1]) * (sa[0] - sa[1]) + (sa[1] - sa[2]) * (sa[1] - sa[2]) +
+                (sa[2] - sa[0]) * (sa[2] - sa[0])) / T(6) +
+               sa[3] * sa[3] + sa[4] * sa[4] + sa[5] * sa[5];
+  const T tau = sqrt(J2);
+  const T Ys = fmax(T(0), (T)(a.pl_c * cos(atan(a.pl_nu))) - sigma * (T)sin(atan(a.pl_nu)));
+  if (!(tau - Ys > T(0))) return;
+  const T e = (T)exp(-a.dt / a.pl_Tv);
+  const T rr = e + (T(1) - e) * Ys / tau;
+  for (int c = 0; c < 6; ++c) {
+    const T dlt = c < 3 ? T(1) : T(0);
+    const T sd = sa[c] - sigma * dlt;
+    a.Fout[(3 + c) * np + p] = (sigma * dlt + rr * sd) - (T)s0[c];
+    if (KAHAN) a.C[(3 + c) * np + p] = T(0);
   }
 }
 
 }  // namespace
 
+template <typename T, bool CURV, bool KAHAN, int TQ, int TR, int MINB>
+void launch_tiled(const VolumeArgs<T>& a, cudaStream_t s) {
+  const size_t smem = sizeof(T) * Tile<T, TQ, TR>::words;
+  auto kern = stencil_kernel_tiled<T, CURV, KAHAN, TQ, TR, MINB>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr_done = true;
+  }
+  const int schunk = a.schunk > 0 ? a.schunk : 16;
+  dim3 blk(TQ, TR, 1), grd((a.nq + TQ - 1) / TQ, (a.nr + TR - 1) / TR, (a.ns + schunk - 1) / schunk);
+  kern<<<grd, blk, smem, s>>>(a, schunk);
+}
+
+// Stencil-kernel variants (the tuning table): 1 per-point, 2 tiled 32x8 at
+// 1 CTA/SM, 3 tiled 32x8 at 3 CTAs/SM in FP32, 4 tiled 64x8 at 1 CTA/SM;
+// 0 picks the fastest measured on a 2 x 201^3 curvilinear block pair
+// (per-point in FP32, tiled 32x8 in FP64).
+template <typename T, bool CURV, bool KAHAN>
+void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
+  constexpr bool f32 = sizeof(T) == 4;
+  const int v = a.kernel != 0 ? a.kernel : (f32 ? 1 : 2);
+  switch (v) {
+    case 1: {
+      dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
+      stencil_kernel_pointwise<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a);
+      return;
+    }
+    case 3: launch_tiled<T, CURV, KAHAN, 32, 8, f32 ? 3 : 1>(a, s); return;
+    case 4: launch_tiled<T, CURV, KAHAN, 64, 8, 1>(a, s); return;
+    default: launch_tiled<T, CURV, KAHAN, 32, 8, 1>(a, s); return;
+  }
+}
+
+template <typename T, bool CURV, bool KAHAN>
+int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
+  int n = 0;
+  dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
+  if (a.npml > 0) {
+    pml_kernel<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a);
+    ++n;
+  }
+  const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
+  face_kernel<T, KAHAN><<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(a);
+  ++n;
+  if (a.plastic) {
+    plastic_kernel<T, KAHAN><<<grd, blk, 0, s>>>(a);
+    ++n;
+  }
+  return n;
+}
+
 template <typename T>
 void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream) {
-  dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
   cudaStream_t s = (cudaStream_t)stream;
   const bool kahan = a.C != nullptr;
-  if (curv) {
-    if (kahan) volume_kernel<T, true, true><<<grd, blk, 0, s>>>(a);
-    else volume_kernel<T, true, false><<<grd, blk, 0, s>>>(a);
-  } else {
-    if (kahan) volume_kernel<T, false, true><<<grd, blk, 0, s>>>(a);
-    else volume_kernel<T, false, false><<<grd, blk, 0, s>>>(a);
-  }
+  if (curv) kahan ? launch_stencil<T, true, true>(a, s) : launch_stencil<T, true, false>(a, s);
+  else kahan ? launch_stencil<T, false, true>(a, s) : launch_stencil<T, false, false>(a, s);
+}
+
+template <typename T>
+int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool kahan = a.C != nullptr;
+  if (curv) return kahan ? launch_corr<T, true, true>(a, s) : launch_corr<T, true, false>(a, s);
+  return kahan ? launch_corr<T, false, true>(a, s) : launch_corr<T, false, false>(a, s);
 }
 
 template void launch_volume<double>(const VolumeArgs<double>&, bool, void*);
 template void launch_volume<float>(const VolumeArgs<float>&, bool, void*);
+template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
+template int launch_corrections<float>(const VolumeArgs<float>&, bool, void*);
 
 }  // namespace wql

@@ -23,7 +23,7 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_scenario_create_from_text", "wql_scenario_create_ex", "wql_scenario_destroy", "wql_step", "wql_sync",
            "wql_get_info", "wql_get_field", "wql_set_field", "wql_get_iface", "wql_frame_count",
            "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step", "wql_profile",
-           "wql_kernel_times"]
+           "wql_kernel_times", "wql_set_tuning"]
 
 
 class Media(ctypes.Structure):
@@ -73,8 +73,9 @@ def lib():
         L.wql_scenario_stream.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
         L.wql_launches_per_step.argtypes = [vp, ctypes.POINTER(ci)]
         L.wql_profile.argtypes = [vp, ci]
+        L.wql_set_tuning.argtypes = [vp, ci, ci]
         cd = ctypes.POINTER(ctypes.c_double)
-        L.wql_kernel_times.argtypes = [vp, cd, ctypes.POINTER(ci), cd, ctypes.POINTER(ci)]
+        L.wql_kernel_times.argtypes = [vp, ci, cd, ctypes.POINTER(ci)]
         _lib = L
     return _lib
 
@@ -215,9 +216,13 @@ class Scenario:
         _check(lib().wql_profile(self.h, 1 if enable else 0))
 
     def kernel_times(self):
-        """{'volume': (ms_total, launches), 'interface': (ms_total, launches)}"""
-        vm, im = ctypes.c_double(), ctypes.c_double()
-        vn, inn = ctypes.c_int(), ctypes.c_int()
-        _check(lib().wql_kernel_times(self.h, ctypes.byref(vm), ctypes.byref(vn), ctypes.byref(im),
-                                      ctypes.byref(inn)))
-        return {"volume": (vm.value, vn.value), "interface": (im.value, inn.value)}
+        """{'interface' | 'stencil' | 'corrections': (ms_total, launches)} since profile(True)."""
+        out = {}
+        for kind, name in enumerate(("interface", "stencil", "corrections")):
+            ms, n = ctypes.c_double(), ctypes.c_int()
+            _check(lib().wql_kernel_times(self.h, kind, ctypes.byref(ms), ctypes.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def set_tuning(self, kernel=0, schunk=0):
+        _check(lib().wql_set_tuning(self.h, kernel, schunk))
