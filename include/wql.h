@@ -130,12 +130,13 @@ int wql_scenario_stream(wql_scn* scn, uintptr_t* stream);
 int wql_profile(wql_scn* scn, int enable);
 int wql_kernel_times(wql_scn* scn, int kind, double* ms, int* launches);
 
-/* Volume-stencil tuning: kernel_variant 0 = default (the per-point kernel in
- * WQL_FP32C, tiled 32x8 in WQL_FP64), 1 = per-point form (every neighbour
- * read through the caches), 2 = tiled shared-memory kernel with 32x8 tiles,
- * 3 = the same at three blocks per SM (FP32), 4 = 64x8 tiles (WQL_FP32C
- * only); schunk = planes per thread block along s for the tiled kernels
- * (0 = 16). */
+/* Volume-stencil tuning: kernel_variant 0 = default (the TMA-pipelined kernel
+ * in WQL_FP32C, tiled 32x8 in WQL_FP64), 1 = per-point form (every
+ * neighbour read through the caches), 2 = tiled shared-memory kernel with
+ * 32x8 tiles, 3 = the same at three blocks per SM (FP32), 4 = 64x8 tiles
+ * (WQL_FP32C only), 5 = TMA-pipelined kernel with a 3-deep stage ring
+ * (WQL_FP32C only), 6 = the same with 2 stages; schunk = planes per thread
+ * block along s (0 = automatic). */
 int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk);
 
 /* Number of kernel launches the last wql_step issued per time step (for

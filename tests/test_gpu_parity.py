@@ -82,7 +82,8 @@ def test_curvilinear_path_flat_grid_truth1(ctx, wqlmod, oracle_lib, tmp_path):
 
 
 @pytest.mark.parametrize("variant,prec", [(0, "fp64"), (2, "fp64"), (3, "fp64"),
-                                          (2, "fp32c"), (3, "fp32c"), (4, "fp32c")])
+                                          (2, "fp32c"), (3, "fp32c"), (4, "fp32c"), (5, "fp32c"),
+                                          (6, "fp32c")])
 def test_tiled_matches_pointwise(ctx, wqlmod, tmp_path, variant, prec):
     """The tiled stencil variants compute the same stencil as the per-point
     form (curvilinear bumpy fault, closures in all three axes, small s chunks
@@ -99,3 +100,23 @@ def test_tiled_matches_pointwise(ctx, wqlmod, tmp_path, variant, prec):
     tol = 1e-13 if prec == "fp64" else 2e-6
     for blk in range(2):
         assert rel_l2(b.fields(blk), a.fields(blk)) < tol
+
+
+@pytest.mark.parametrize("cfg,schunk", [("config0", 0), ("config0", 7), ("config1", 0), ("config1", 5)])
+def test_tma_matches_pointwise(ctx, wqlmod, cfg, schunk):
+    """The TMA-pipelined FP32 stencil against the per-point form on the
+    seeded workloads at 41^3 (Cartesian) and 45^3 (curvilinear): two q
+    tiles, a shifted last r tile, several s chunks (automatic and 7 or 5
+    planes) next to the per-point s-boundary planes."""
+    import wql_configs
+    text, media = (wql_configs.config0(steps=10) if cfg == "config0"
+                   else wql_configs.config1(n=45, steps=10))
+    a = wqlmod.Scenario(ctx, text=text, precision=wqlmod.FP32C, media=media)
+    b = wqlmod.Scenario(ctx, text=text, precision=wqlmod.FP32C, media=media)
+    a.set_tuning(1, 0)
+    b.set_tuning(5, schunk)
+    a.step(6)
+    b.step(6)
+    b.sync(check_nan=True)
+    for blk in range(2):
+        assert rel_l2(b.fields(blk), a.fields(blk)) < 2e-6

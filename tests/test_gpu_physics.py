@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from gpu_helpers import field_errors, rel_l2, rs_close, run_pair
-from inputs import case_text, golden_in, write
+from inputs import block_list, case_text, golden_in, problem, write
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-11
@@ -53,14 +53,21 @@ def test_plasticity_is_active(ctx, wqlmod, tmp_path):
     assert rel_l2(a.fields(0), b.fields(0)) > 1e-6
 
 
-def test_fp32c_error_vs_fp64(ctx, wqlmod, tmp_path):
-    """FP32 + Kahan RK vs FP64 on the truth/1 problem: velocity fields, slip,
+@pytest.mark.parametrize("case", ["slip_weakening", "rate_state"])
+def test_fp32c_error_vs_fp64(ctx, wqlmod, tmp_path, case):
+    """FP32 + Kahan RK vs FP64 on the truth/1 problem (slip weakening) and on
+    its rate-and-state variant (FP32C solves the friction law by Newton's
+    method, FP64 by the reference's regula falsi): velocity fields, slip,
     peak slip rate and rupture time (at most one time step)."""
-    p = write(tmp_path, "cart.in", golden_in("test_rup_cart_fric"))
+    if case == "slip_weakening":
+        text, steps = golden_in("test_rup_cart_fric"), 46
+    else:  # ruptures from about step 60
+        text, steps = problem("TPV101", "rate-and-state_friction", t_final="3.0d0") + block_list(), 100
+    p = write(tmp_path, "cart.in", text)
     d = wqlmod.Scenario(ctx, p, precision=wqlmod.FP64)
     f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
-    d.step(46)
-    f.step(46)
+    d.step(steps)
+    f.step(steps)
     f.sync(check_nan=True)
     dt = d.info().dt
     vel = max(rel_l2(f.fields(b)[:3], d.fields(b)[:3]) for b in range(2))
@@ -69,8 +76,9 @@ def test_fp32c_error_vs_fp64(ctx, wqlmod, tmp_path):
     tr_d, tr_f = d.iface(0, 5), f.iface(0, 5)
     ruptured = (tr_d < 1e8) & (tr_f < 1e8)
     assert ((tr_d < 1e8) == (tr_f < 1e8)).all()
+    assert ruptured.any()
     terr = np.abs(tr_f[ruptured] - tr_d[ruptured]).max() / dt
-    print(f"FP32C vs FP64: vel relL2 {vel:.2e} slip relL2 {slip:.2e} peak-rate {peak:.2e} trup {terr:.2f} dt")
+    print(f"{case} FP32C vs FP64: vel relL2 {vel:.2e} slip relL2 {slip:.2e} peak-rate {peak:.2e} trup {terr:.2f} dt")
     assert vel < 1e-4 and slip < 1e-4 and peak < 1e-4
     assert terr <= 1.0
 

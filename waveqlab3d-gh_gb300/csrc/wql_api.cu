@@ -95,6 +95,8 @@ struct wql_scn {
   long long device_bytes = 0;
   struct Block {
     int nq = 0, nr = 0, ns = 0;
+    int pq = 0;         // row pitch along q: nq rounded up to a multiple of 16 bytes
+    long long npd = 0;  // nq * nr * ns (dense, the precompute arrays)
     long long np = 0;
     void* F[2] = {nullptr, nullptr};
     void* DF = nullptr;
@@ -110,12 +112,15 @@ struct wql_scn {
     void* y = nullptr;
     double cart_metric[3] = {1, 1, 1};
     double tau_h[3] = {};
+    StencilMaps maps{};  // TMA tensor maps (FP32 fields)
   } B[2];
   int cur = 0;
   // interface (two block copies)
   double *S = nullptr, *DS = nullptr, *W = nullptr, *DW = nullptr, *trup = nullptr, *xij = nullptr;
+  double* pre = nullptr;  // 2 x 5 x nf time-independent interface data
   void* sat = nullptr;
   unsigned int* solver_fail = nullptr;
+  int* err_dev = nullptr;  // kernel error word (bounded pipeline waits that ran out)
   FaultParams fp{};
   int bc_form = BC_CHARACTERISTIC;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
@@ -195,6 +200,13 @@ __global__ void from_double(const double* in, T* out, long long n) {
   if (p < n) out[p] = (T)in[p];
 }
 
+// Dense (nq-pitched) FP64 array to a pq-pitched array of T.
+template <typename T>
+__global__ void pad_rows(const double* in, T* out, int nq, int pq, long long npd) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p < npd) out[p % nq + (long long)pq * (p / nq)] = (T)in[p];
+}
+
 template <typename T>
 __global__ void count_nonfinite(const T* a, long long n, unsigned int* cnt) {
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -216,8 +228,13 @@ int setup_block(wql_scn* S, int b) {
   B.nq = G.nq;
   B.nr = G.nr;
   B.ns = G.ns;
-  B.np = (long long)G.nq * G.nr * G.ns;
-  const long long np = B.np;
+  // resident arrays (fields, rates, coefficients) use a row pitch of a
+  // multiple of 16 bytes so that every row starts on a TMA-legal address
+  const int per16 = 16 / S->esz;
+  B.pq = (G.nq + per16 - 1) / per16 * per16;
+  B.npd = (long long)G.nq * G.nr * G.ns;
+  B.np = (long long)B.pq * G.nr * G.ns;
+  const long long np = B.npd;  // dense count for the one-time precompute below
   // geometry on the device (FP64) for the one-time precompute
   double *x = nullptr, *metric = nullptr, *J = nullptr, *mat = nullptr;
   int rc;
@@ -260,11 +277,13 @@ int setup_block(wql_scn* S, int b) {
   CK(cudaGetLastError());
   // coefficients
   const int ncoef = S->curv ? kCurvCoef : kCartCoef;
-  if ((rc = S->alloc(&B.coef, ncoef * np * S->esz, false))) return rc;
+  if ((rc = S->alloc(&B.coef, ncoef * B.np * S->esz))) return rc;
   if (S->prec == WQL_FP64)
-    launch_coef<double>(np, S->curv, metric, J, mat, mat + np, mat + 2 * np, (double*)B.coef, S->stream);
+    launch_coef<double>(B.nq, B.nr, B.ns, B.pq, S->curv, metric, J, mat, mat + np, mat + 2 * np, (double*)B.coef,
+                        S->stream);
   else
-    launch_coef<float>(np, S->curv, metric, J, mat, mat + np, mat + 2 * np, (float*)B.coef, S->stream);
+    launch_coef<float>(B.nq, B.nr, B.ns, B.pq, S->curv, metric, J, mat, mat + np, mat + 2 * np, (float*)B.coef,
+                       S->stream);
   CK(cudaGetLastError());
   // Cartesian diagonal metric, taken at the block centre
   {
@@ -276,10 +295,13 @@ int setup_block(wql_scn* S, int b) {
   }
   // fields
   for (int i = 0; i < 2; ++i)
-    if ((rc = S->alloc(&B.F[i], 9 * np * S->esz))) return rc;
-  if ((rc = S->alloc(&B.DF, 9 * np * S->esz))) return rc;
-  if (S->prec == WQL_FP32C)
-    if ((rc = S->alloc(&B.C, 9 * np * S->esz))) return rc;
+    if ((rc = S->alloc(&B.F[i], 9 * B.np * S->esz))) return rc;
+  if ((rc = S->alloc(&B.DF, 9 * B.np * S->esz))) return rc;
+  if (S->prec == WQL_FP32C) {
+    if ((rc = S->alloc(&B.C, 9 * B.np * S->esz))) return rc;
+    const int erc = make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, S->curv);
+    if (erc) return fail(WQL_E_CUDA, "cuTensorMapEncodeTiled failed for the stencil maps (error " + std::to_string(erc) + ")");
+  }
   // boundary codes (src/BoundaryConditions.f90:15-48) and PML slabs (src/block.f90:163-178)
   B.bc[0] = bp.lqrs[0]; B.bc[1] = bp.rqrs[0];
   B.bc[2] = bp.lqrs[1]; B.bc[3] = bp.rqrs[1];
@@ -305,11 +327,11 @@ int setup_block(wql_scn* S, int b) {
   for (int d = 0; d < 3; ++d) B.tau_h[d] = tau0 / (1.0 / (double)(dims[d] - 1));
   // depth coordinate for the plastic update
   if (S->plastic) {
-    if ((rc = S->alloc(&B.y, np * S->esz, false))) return rc;
+    if ((rc = S->alloc(&B.y, B.np * S->esz))) return rc;
     if (S->prec == WQL_FP64)
-      CK(cudaMemcpyAsync(B.y, x + np, np * sizeof(double), cudaMemcpyDeviceToDevice, S->stream));
+      pad_rows<double><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(x + np, (double*)B.y, B.nq, B.pq, np);
     else
-      from_double<float><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(x + np, (float*)B.y, np);
+      pad_rows<float><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(x + np, (float*)B.y, B.nq, B.pq, np);
   }
   // interface coordinates of this block's fault face
   {
@@ -330,6 +352,39 @@ int setup_block(wql_scn* S, int b) {
   S->release(metric);
   S->release(J);
   S->release(mat);
+  return WQL_OK;
+}
+
+// Per fault point and block copy, the parts of the interface condition that
+// do not change in time: the static prestress in the copy's (n, m, l) frame,
+// the nucleation weight (prestress(t) = static + weight * ramp(t)) and the
+// rate-and-state direct-effect parameter a(x).
+int precompute_fault(wql_scn* S) {
+  const long long nf = (long long)S->B[0].nr * S->B[0].ns;
+  std::vector<double> pre(2 * 5 * nf, 0.0);
+  for (int b = 0; b < 2; ++b) {
+    auto& B = S->B[b];
+    const int side = (b == 0) ? 1 : 0;
+    std::vector<double> face(kFaceWords * nf), xi(3 * nf);
+    CK(cudaMemcpy(face.data(), B.face[side], face.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(xi.data(), S->xij + (long long)b * 3 * nf, xi.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double* P = pre.data() + (long long)b * 5 * nf;
+    for (long long f = 0; f < nf; ++f) {
+      double n[3], m[3], l[3], x[3];
+      for (int c = 0; c < 3; ++c) {
+        n[c] = face[(0 + c) * nf + f];
+        m[c] = face[(3 + c) * nf + f];
+        l[c] = face[(6 + c) * nf + f];
+        x[c] = xi[c * nf + f];
+      }
+      prestress_static(S->fp, x, l, m, n, P[f], P[nf + f], P[2 * nf + f]);
+      P[3 * nf + f] = nucleation_weight(S->fp, x);
+      P[4 * nf + f] = S->fp.coupling == CPL_RS ? rs_direct_a(S->fp, x) : 0.0;
+    }
+  }
+  int rc;
+  if ((rc = S->alloc((void**)&S->pre, pre.size() * sizeof(double), false))) return rc;
+  CK(cudaMemcpy(S->pre, pre.data(), pre.size() * sizeof(double), cudaMemcpyHostToDevice));
   return WQL_OK;
 }
 
@@ -452,6 +507,9 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   }
   if ((rc = S->alloc(&S->sat, 2 * 9 * nf * S->esz))) return rc;
   if ((rc = S->alloc((void**)&S->solver_fail, sizeof(unsigned int)))) return rc;
+  if ((rc = S->alloc((void**)&S->err_dev, sizeof(int)))) return rc;
+  if (fp.coupling == CPL_SW || fp.coupling == CPL_RS)
+    if ((rc = precompute_fault(S.get()))) return rc;
   if (fp.coupling == CPL_RS)
     if ((rc = init_rate_state(S.get()))) return rc;
   if (Pr.w_fault) {
@@ -492,7 +550,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   auto& B = S->B[b];
   VolumeArgs<T> a;
   std::memset(&a, 0, sizeof(a));
-  a.nq = B.nq; a.nr = B.nr; a.ns = B.ns; a.np = B.np; a.block = b;
+  a.nq = B.nq; a.nr = B.nr; a.ns = B.ns; a.pq = B.pq; a.np = B.np; a.block = b;
   a.rh[0] = (T)(B.nq - 1); a.rh[1] = (T)(B.nr - 1); a.rh[2] = (T)(B.ns - 1);
   a.Fin = (const T*)B.F[S->cur];
   a.Fout = (T*)B.F[S->cur ^ 1];
@@ -524,6 +582,9 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   for (int c = 0; c < 6; ++c) a.s0u[c] = S->fp.s0[c];
   a.ycoord = (const T*)B.y;
   a.pl_c = S->pl_c; a.pl_nu = S->pl_nu; a.pl_Tv = S->pl_Tv; a.dt = S->dt;
+  a.err = S->err_dev;
+  B.maps.cur = S->cur;
+  a.tma = &B.maps;
   return a;
 }
 
@@ -539,6 +600,7 @@ int run_step(wql_scn* S) {
     std::memset(&ia, 0, sizeof(ia));
     ia.nr = S->B[0].nr; ia.ns = S->B[0].ns;
     ia.np0 = S->B[0].np; ia.np1 = S->B[1].np; ia.nq0 = S->B[0].nq;
+    ia.pq0 = S->B[0].pq; ia.pq1 = S->B[1].pq;
     ia.fp64 = S->prec == WQL_FP64;
     ia.F0 = S->B[0].F[S->cur];
     ia.F1 = S->B[1].F[S->cur];
@@ -550,6 +612,8 @@ int run_step(wql_scn* S) {
     ia.tau_h[0] = S->B[0].tau_h[0];
     ia.tau_h[1] = S->B[1].tau_h[0];
     ia.A = A; ia.Bdt = Bdt; ia.t = ts; ia.stage = stage;
+    ia.pre = S->pre;
+    ia.ramp = nucleation_ramp(S->fp, ts);
     ia.fp = S->fp;
     ia.frame = (want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
     ia.solver_fail = S->solver_fail;
@@ -665,6 +729,9 @@ int wql_sync(wql_scn* scn, int check_nan) {
   CK(cudaGetLastError());
   unsigned int fails = 0;
   CK(cudaMemcpy(&fails, scn->solver_fail, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  int kerr = 0;
+  CK(cudaMemcpy(&kerr, scn->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+  if (kerr) return fail(WQL_E_CUDA, "stencil pipeline wait ran out of its iteration limit (code " + std::to_string(kerr) + ")");
   if (check_nan) {
     unsigned int* cnt = nullptr;
     CK(cudaMalloc(&cnt, sizeof(unsigned)));
@@ -708,14 +775,17 @@ int wql_get_field(wql_scn* scn, int block, int comp, double* host_out) {
     return fail(WQL_E_INPUT, "bad argument");
   auto& B = scn->B[block];
   CK(cudaStreamSynchronize(scn->stream));
+  const size_t rows = (size_t)B.nr * B.ns;
   if (scn->prec == WQL_FP64) {
-    CK(cudaMemcpy(host_out, (const double*)B.F[scn->cur] + comp * B.np, B.np * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy2D(host_out, B.nq * sizeof(double), (const double*)B.F[scn->cur] + comp * B.np,
+                    B.pq * sizeof(double), B.nq * sizeof(double), rows, cudaMemcpyDeviceToHost));
   } else {
     double* tmp = nullptr;
     CK(cudaMalloc(&tmp, B.np * sizeof(double)));
     to_double<float><<<(unsigned)((B.np + 255) / 256), 256, 0, scn->stream>>>((const float*)B.F[scn->cur] + comp * B.np, tmp, B.np);
     CK(cudaStreamSynchronize(scn->stream));
-    CK(cudaMemcpy(host_out, tmp, B.np * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy2D(host_out, B.nq * sizeof(double), tmp, B.pq * sizeof(double), B.nq * sizeof(double), rows,
+                    cudaMemcpyDeviceToHost));
     cudaFree(tmp);
   }
   return WQL_OK;
@@ -726,9 +796,12 @@ int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in) {
     return fail(WQL_E_INPUT, "bad argument");
   auto& B = scn->B[block];
   CK(cudaStreamSynchronize(scn->stream));
+  const size_t rows = (size_t)B.nr * B.ns;
   double* tmp = nullptr;
   CK(cudaMalloc(&tmp, B.np * sizeof(double)));
-  CK(cudaMemcpy(tmp, host_in, B.np * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(tmp, 0, B.np * sizeof(double)));
+  CK(cudaMemcpy2D(tmp, B.pq * sizeof(double), host_in, B.nq * sizeof(double), B.nq * sizeof(double), rows,
+                  cudaMemcpyHostToDevice));
   if (scn->prec == WQL_FP64)
     CK(cudaMemcpy((double*)B.F[scn->cur] + comp * B.np, tmp, B.np * sizeof(double), cudaMemcpyDeviceToDevice));
   else
@@ -803,7 +876,9 @@ int wql_kernel_times(wql_scn* scn, int kind, double* ms, int* launches) {
 }
 
 int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk) {
-  if (!scn || kernel_variant < 0 || kernel_variant > 4 || schunk < 0) return fail(WQL_E_INPUT, "bad tuning");
+  if (!scn || kernel_variant < 0 || kernel_variant > 6 || schunk < 0) return fail(WQL_E_INPUT, "bad tuning");
+  if ((kernel_variant == 5 || kernel_variant == 6) && scn->prec == WQL_FP64)
+    return fail(WQL_E_INPUT, "stencil variants 5 and 6 (TMA pipeline) are FP32-only");
   // 64x8 tiles of FP64 need 273 KiB of shared memory, more than a block may hold.
   if (kernel_variant == 4 && scn->prec == WQL_FP64)
     return fail(WQL_E_INPUT, "stencil variant 4 (64x8 tiles) is FP32-only");

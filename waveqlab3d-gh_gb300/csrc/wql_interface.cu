@@ -25,10 +25,12 @@ namespace {
 // Regula falsi for V + a*sigma_n/eta*asinh(V/(2V0)*exp(psi/a)) = Phi/eta on
 // [0, Phi/eta] (src/Interface_Condition.f90:1170-1265), including the
 // reference's acceptance test `fv*fl > tol`.  Returns false when the
-// iteration budget (5000) is exhausted.
+// iteration budget (5000) is exhausted.  exp(psi/a) is evaluated once; the
+// residual is otherwise formed exactly as the reference forms it.
 __device__ bool regula_falsi(double& V, double Phi, double eta, double sn, double psi, double V0,
                              double a) {
-  auto f = [&](double v) { return v + a * sn / eta * asinh(0.5 * v / V0 * exp(psi / a)) - Phi / eta; };
+  const double ek = exp(psi / a);
+  auto f = [&](double v) { return v + a * sn / eta * asinh(0.5 * v / V0 * ek) - Phi / eta; };
   const double tol = 1.0e-12;
   double Vl = 0.0, Vr = Phi / eta;
   double fv = f(V), fl = f(Vl), fr = f(Vr);
@@ -55,56 +57,117 @@ __device__ bool regula_falsi(double& V, double Phi, double eta, double sn, doubl
   return !(k >= 5000);
 }
 
-template <typename T>
-__device__ __forceinline__ void load_face(const void* F, long long np, long long p, double out[9]) {
-  const T* f = (const T*)F;
-#pragma unroll
-  for (int c = 0; c < 9; ++c) out[c] = (double)f[c * np + p];
+// The same equation for FP32 fields, by Newton's method in u = ln V.  With
+// s = V/(2V0)*exp(psi/a), g(u) = e^u + c*asinh(s) - Phi/eta is increasing and
+// convex in u (d asinh(s)/du = s/sqrt(1+s^2) grows with u), so Newton iterates
+// clamped to u <= ln(Phi/eta) (where g >= 0) decrease monotonically to the
+// root after at most one step from the left.  The iteration runs in FP32 on
+// w = ln s (asinh(e^w) = w + ln 2 for large w, e^w for very negative w, so
+// nothing overflows although exp(psi/a) exceeds the FP32 range) until the
+// step is at the FP32 resolution of u, then in FP64 until the step is below
+// 1e-9 (quadratic convergence: V is then accurate far below the regula
+// falsi's 1e-12 tolerance).  Returns false if it does not converge.
+__device__ bool newton_mixed(double& V, double Phi, double eta, double sn, double psi, double V0, double a) {
+  const double target = Phi / eta;
+  if (!(target > 0.0)) {
+    V = 0.0;
+    return true;
+  }
+  const double c = a * sn / eta;
+  const float tf = (float)target, cf = (float)c;
+  const float lek = (float)(psi / a) + logf(0.5f / (float)V0);
+  const float uhi = logf(tf);
+  const float vf = (float)V;
+  float u = vf > 0.0f ? fminf(logf(vf), uhi) : uhi;
+  for (int it = 0; it < 40; ++it) {
+    const float w = u + lek;
+    const float v = expf(u);
+    float A, dA;
+    if (w > 20.0f) {
+      A = w + 0.6931471806f;
+      dA = 1.0f;
+    } else if (w < -20.0f) {
+      A = expf(w);
+      dA = A;
+    } else {
+      const float sw = expf(w);
+      A = asinhf(sw);
+      dA = sw / sqrtf(1.0f + sw * sw);
+    }
+    const float un = fminf(u - (v + cf * A - tf) / (v + cf * dA), uhi);
+    const float du = un - u;
+    u = un;
+    if (fabsf(du) <= 4.0e-7f * fmaxf(1.0f, fabsf(u))) break;
+  }
+  const double ek = 0.5 / V0 * exp(psi / a);
+  double ud = (double)u;
+  for (int it = 0; it < 8; ++it) {
+    const double v = exp(ud);
+    const double sd = ek * v;
+    const double g = v + c * asinh(sd) - target;
+    const double ds = sd > 1.0 ? 1.0 / sqrt(1.0 + 1.0 / (sd * sd)) : sd / sqrt(1.0 + sd * sd);
+    const double du = -g / (v + c * ds);
+    ud += du;
+    if (fabs(du) <= 1.0e-9) {
+      V = exp(ud);
+      return true;
+    }
+  }
+  V = exp(ud);
+  return false;
 }
 
 template <typename T>
-__global__ void interface_kernel(const InterfaceArgs a) {
+__device__ __forceinline__ void load_face(const void* F, long long np, long long p, T out[9]) {
+  const T* f = (const T*)F;
+#pragma unroll
+  for (int c = 0; c < 9; ++c) out[c] = f[c * np + p];
+}
+
+// R is the arithmetic type of the characteristic algebra: the field type
+// (FP64 fields keep every operation of the FP64 restatement; FP32 fields do
+// the algebra in FP32 with the slip, state and their rates kept in FP64).
+template <typename T>
+__global__ void interface_kernel(const __grid_constant__ InterfaceArgs a) {
+  using R = T;
+  constexpr bool F64 = sizeof(T) == 8;
   const long long nf = (long long)a.nr * a.ns;
   const long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
   if (f >= nf) return;
   const int j = (int)(f % a.nr), k = (int)(f / a.nr);
   // fields on both faces: block 0 at q = nq0-1, block 1 at q = 0
-  double u[9], v[9];
-  load_face<T>(a.F0, a.np0, (a.nq0 - 1) + (long long)a.nq0 * (j + (long long)a.nr * k), u);
-  {
-    // block 1 has the same (nr, ns) face; its q stride is its own nq
-    const long long nq1 = a.np1 / nf;
-    load_face<T>(a.F1, a.np1, (long long)nq1 * (j + (long long)a.nr * k), v);
-  }
+  R u[9], v[9];
+  load_face<T>(a.F0, a.np0, (a.nq0 - 1) + (long long)a.pq0 * (j + (long long)a.nr * k), u);
+  load_face<T>(a.F1, a.np1, (long long)a.pq1 * (j + (long long)a.nr * k), v);
   const double* face = b == 0 ? a.face0 : a.face1;
-  double n[3], m[3], l[3];
+  R n[3], m[3], l[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    n[c] = face[(0 + c) * nf + f];
-    m[c] = face[(3 + c) * nf + f];
-    l[c] = face[(6 + c) * nf + f];
+    n[c] = (R)face[(0 + c) * nf + f];
+    m[c] = (R)face[(3 + c) * nf + f];
+    l[c] = (R)face[(6 + c) * nf + f];
   }
-  const double gx = face[9 * nf + f], gy = face[10 * nf + f], gz = face[11 * nf + f];
+  const R gx = (R)face[9 * nf + f], gy = (R)face[10 * nf + f], gz = (R)face[11 * nf + f];
   // material on each side (block 0 / block 1 face)
-  const double lam1 = a.face0[12 * nf + f], mu1 = a.face0[13 * nf + f], rho1 = a.face0[14 * nf + f];
-  const double lam2 = a.face1[12 * nf + f], mu2 = a.face1[13 * nf + f], rho2 = a.face1[14 * nf + f];
-  const double c1p = sqrt((2.0 * mu1 + lam1) / rho1), c1s = sqrt(mu1 / rho1);
-  const double c2p = sqrt((2.0 * mu2 + lam2) / rho2), c2s = sqrt(mu2 / rho2);
-  const double Z1p = rho1 * c1p, Z1s = rho1 * c1s, Z2p = rho2 * c2p, Z2s = rho2 * c2s;
+  const R lam1 = (R)a.face0[12 * nf + f], mu1 = (R)a.face0[13 * nf + f], rho1 = (R)a.face0[14 * nf + f];
+  const R lam2 = (R)a.face1[12 * nf + f], mu2 = (R)a.face1[13 * nf + f], rho2 = (R)a.face1[14 * nf + f];
+  const R c1p = sqrt((R(2) * mu1 + lam1) / rho1), c1s = sqrt(mu1 / rho1);
+  const R c2p = sqrt((R(2) * mu2 + lam2) / rho2), c2s = sqrt(mu2 / rho2);
+  const R Z1p = rho1 * c1p, Z1s = rho1 * c1s, Z2p = rho2 * c2p, Z2s = rho2 * c2s;
   double x[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) x[c] = a.xij[(b * 3 + c) * nf + f];
 
   // tractions on the face, then rotate velocities and tractions to (n,m,l)
-  double ur[6], vr[6];
+  R ur[6], vr[6];
   {
-    const double Tu0 = n[0] * u[3] + n[1] * u[6] + n[2] * u[7];
-    const double Tu1 = n[0] * u[6] + n[1] * u[4] + n[2] * u[8];
-    const double Tu2 = n[0] * u[7] + n[1] * u[8] + n[2] * u[5];
-    const double Tv0 = n[0] * v[3] + n[1] * v[6] + n[2] * v[7];
-    const double Tv1 = n[0] * v[6] + n[1] * v[4] + n[2] * v[8];
-    const double Tv2 = n[0] * v[7] + n[1] * v[8] + n[2] * v[5];
+    const R Tu0 = n[0] * u[3] + n[1] * u[6] + n[2] * u[7];
+    const R Tu1 = n[0] * u[6] + n[1] * u[4] + n[2] * u[8];
+    const R Tu2 = n[0] * u[7] + n[1] * u[8] + n[2] * u[5];
+    const R Tv0 = n[0] * v[3] + n[1] * v[6] + n[2] * v[7];
+    const R Tv1 = n[0] * v[6] + n[1] * v[4] + n[2] * v[8];
+    const R Tv2 = n[0] * v[7] + n[1] * v[8] + n[2] * v[5];
     ur[0] = n[0] * u[0] + n[1] * u[1] + n[2] * u[2];
     ur[1] = m[0] * u[0] + m[1] * u[1] + m[2] * u[2];
     ur[2] = l[0] * u[0] + l[1] * u[1] + l[2] * u[2];
@@ -120,13 +183,13 @@ __global__ void interface_kernel(const InterfaceArgs a) {
   }
 
   // characteristics (src/Interface_Condition.f90:809-828)
-  const double p_n = Z1p * ur[0] - ur[3], p_m = Z1s * ur[1] - ur[4], p_l = Z1s * ur[2] - ur[5];
-  const double q_n = Z2p * vr[0] + vr[3], q_m = Z2s * vr[1] + vr[4], q_l = Z2s * vr[2] + vr[5];
-  const double eta_s = 1.0 / (1.0 / Z1s + 1.0 / Z2s);
-  const double eta_p = 1.0 / (1.0 / Z1p + 1.0 / Z2p);
-  const double phi_n = eta_p * (q_n / Z2p - p_n / Z1p);
-  const double phi_m = eta_s * (q_m / Z2s - p_m / Z1s);
-  const double phi_l = eta_s * (q_l / Z2s - p_l / Z1s);
+  const R p_n = Z1p * ur[0] - ur[3], p_m = Z1s * ur[1] - ur[4], p_l = Z1s * ur[2] - ur[5];
+  const R q_n = Z2p * vr[0] + vr[3], q_m = Z2s * vr[1] + vr[4], q_l = Z2s * vr[2] + vr[5];
+  const R eta_s = R(1) / (R(1) / Z1s + R(1) / Z2s);
+  const R eta_p = R(1) / (R(1) / Z1p + R(1) / Z2p);
+  const R phi_n = eta_p * (q_n / Z2p - p_n / Z1p);
+  const R phi_m = eta_s * (q_m / Z2s - p_m / Z1s);
+  const R phi_l = eta_s * (q_l / Z2s - p_l / Z1s);
 
   double* S = a.S + (long long)b * 4 * nf;
   double* DS = a.DS + (long long)b * 4 * nf;
@@ -134,7 +197,7 @@ __global__ void interface_kernel(const InterfaceArgs a) {
   double* DW = a.DW + (long long)b * nf;
   double* trup = a.trup + (long long)b * nf;
 
-  double P[6], Q[6], Vel = 0.0;
+  R P[6], Q[6];
   double T0n = 0.0, T0m = 0.0, T0l = 0.0;
   const int cpl = a.fp.coupling;
   if (cpl == CPL_LOCKED) {
@@ -144,73 +207,89 @@ __global__ void interface_kernel(const InterfaceArgs a) {
     P[3] = Q[3] = phi_n; P[4] = Q[4] = phi_m; P[5] = Q[5] = phi_l;
   } else if (cpl == CPL_LINEAR) {
     // Linear_Friction with alpha = 1e14 (src/Interface_Condition.f90:639-742)
-    const double al = 1.0e14;
-    const double tm = al / (al + eta_s) * phi_m, tl = al / (al + eta_s) * phi_l;
+    const R al = R(1.0e14);
+    const R tm = al / (al + eta_s) * phi_m, tl = al / (al + eta_s) * phi_l;
     P[0] = (q_n - phi_n) / Z2p; Q[0] = (p_n + phi_n) / Z1p;
-    Q[1] = (p_m + tm) / Z1s + 1.0 / (al + eta_s) * phi_m;
-    Q[2] = (p_l + tl) / Z1s + 1.0 / (al + eta_s) * phi_l;
-    P[1] = 0.0;
-    P[2] = (q_l - tl) / Z2s - 1.0 / (al + eta_s) * phi_l;
+    Q[1] = (p_m + tm) / Z1s + R(1) / (al + eta_s) * phi_m;
+    Q[2] = (p_l + tl) / Z1s + R(1) / (al + eta_s) * phi_l;
+    P[1] = R(0);
+    P[2] = (q_l - tl) / Z2s - R(1) / (al + eta_s) * phi_l;
     P[3] = Q[3] = phi_n; P[4] = Q[4] = tm; P[5] = Q[5] = tl;
   } else {
-    prestress(a.fp, x, a.t, l, m, n, T0n, T0m, T0l);
+    // prestress: static part + nucleation weight x the stage's uniform ramp
+    const double* pre = a.pre + (long long)b * 5 * nf;
+    T0n = pre[f];
+    T0m = pre[nf + f];
+    T0l = pre[2 * nf + f];
+    const double wn = pre[3 * nf + f];
+    if (wn != 0.0) T0l = T0l + wn * a.ramp;
+    // the friction law in FP64 for both field types
+    const double phm = phi_m, phl = phi_l, phn = phi_n, es = eta_s;
     double tau_m_hat, tau_l_hat, vv_m, vv_l;
-    const double phi_1 = T0m + phi_m, phi_2 = T0l + phi_l;
+    const double phi_1 = T0m + phm, phi_2 = T0l + phl;
     if (cpl == CPL_SW) {
       // Slip_Weakening_Friction + solve (src/Interface_Condition.f90:745-916, 1147-1166)
-      const double tau_lock = sqrt((T0l + phi_l) * (T0l + phi_l) + (T0m + phi_m) * (T0m + phi_m));
-      const double sn = fmax(0.0, -(T0n + phi_n));
+      const double tau_lock = sqrt((T0l + phl) * (T0l + phl) + (T0m + phm) * (T0m + phm));
+      const double sn = fmax(0.0, -(T0n + phn));
       const double tau_str = tau_strength(a.fp, sn, S[3 * nf + f], x, a.t);
       if (tau_lock > tau_str) {
         const double Phi = sqrt(phi_1 * phi_1 + phi_2 * phi_2);
-        const double V = (Phi - tau_str) / eta_s;
-        Vel = V;
-        vv_m = phi_1 / (eta_s + tau_str / V);
-        vv_l = phi_2 / (eta_s + tau_str / V);
-        tau_m_hat = (phi_1 - eta_s * vv_m) - T0m;
-        tau_l_hat = (phi_2 - eta_s * vv_l) - T0l;
+        const double V = (Phi - tau_str) / es;
+        vv_m = phi_1 / (es + tau_str / V);
+        vv_l = phi_2 / (es + tau_str / V);
+        tau_m_hat = (phi_1 - es * vv_m) - T0m;
+        tau_l_hat = (phi_2 - es * vv_l) - T0l;
       } else {
-        tau_m_hat = phi_m;
-        tau_l_hat = phi_l;
+        tau_m_hat = phm;
+        tau_l_hat = phl;
         vv_m = vv_l = 0.0;
-        Vel = 0.0;
       }
     } else {
       // rate_state_friction + solve + Regula_Falsi (src/Interface_Condition.f90:918-1146)
-      const RSParams rs = rs_params(a.fp, x);
+      const double ra = pre[4 * nf + f];  // direct-effect parameter a(x)
+      const RSParams rs = rs_params(a.fp, x, ra);
       const double psi = W[f];
-      const double sn = fmax(0.0, -(T0n + phi_n));
+      const double sn = fmax(0.0, -(T0n + phn));
       const double Phi = sqrt(phi_1 * phi_1 + phi_2 * phi_2);
-      double V = sqrt((vr[1] - ur[1]) * (vr[1] - ur[1]) + (vr[2] - ur[2]) * (vr[2] - ur[2]));
-      if (V > Phi) V = 0.5 * Phi / eta_s;
-      if (!regula_falsi(V, Phi, eta_s, sn, psi, rs.V0, rs.a) && a.solver_fail)
-        atomicAdd(a.solver_fail, 1u);
-      Vel = V;
-      const double fv = sn * rs.a * asinh(0.5 * V / rs.V0 * exp(psi / rs.a));
-      vv_m = phi_1 / (eta_s + fv / V);
-      vv_l = phi_2 / (eta_s + fv / V);
-      tau_m_hat = (phi_1 - eta_s * vv_m) - T0m;
-      tau_l_hat = (phi_2 - eta_s * vv_l) - T0l;
+      const double d1 = (double)vr[1] - (double)ur[1], d2 = (double)vr[2] - (double)ur[2];
+      double V = sqrt(d1 * d1 + d2 * d2);
+      if (V > Phi) V = 0.5 * Phi / es;
+      const bool ok = F64 ? regula_falsi(V, Phi, es, sn, psi, rs.V0, rs.a)
+                          : newton_mixed(V, Phi, es, sn, psi, rs.V0, rs.a);
+      if (!ok && a.solver_fail) atomicAdd(a.solver_fail, 1u);
+      if (F64) {
+        const double fv = sn * rs.a * asinh(0.5 * V / rs.V0 * exp(psi / rs.a));
+        vv_m = phi_1 / (es + fv / V);
+        vv_l = phi_2 / (es + fv / V);
+      } else {
+        // at the root the friction stress is Phi - eta*V, so
+        // phi/(eta + fv/V) = phi*V/Phi
+        const double ratio = Phi > 0.0 ? V / Phi : 0.0;
+        vv_m = phi_1 * ratio;
+        vv_l = phi_2 * ratio;
+      }
+      tau_m_hat = (phi_1 - es * vv_m) - T0m;
+      tau_l_hat = (phi_2 - es * vv_l) - T0l;
       // aging law (src/Interface_Condition.f90:431-436)
-      DW[f] = a.A * DW[f] + (rs.b * rs.V0 / rs.L0 * exp(-(psi - rs.f0) / rs.b) - Vel * rs.b / rs.L0);
+      DW[f] = a.A * DW[f] + (rs.b * rs.V0 / rs.L0 * exp(-(psi - rs.f0) / rs.b) - V * rs.b / rs.L0);
     }
+    const R tmh = (R)tau_m_hat, tlh = (R)tau_l_hat, vm = (R)vv_m, vl = (R)vv_l;
     P[0] = (q_n - phi_n) / Z2p;
     Q[0] = (p_n + phi_n) / Z1p;
     P[3] = Q[3] = phi_n;
-    P[4] = Q[4] = tau_m_hat;
-    P[5] = Q[5] = tau_l_hat;
-    Q[1] = (tau_m_hat + p_m) / Z1s + vv_m;
-    Q[2] = (tau_l_hat + p_l) / Z1s + vv_l;
-    P[1] = (q_m - tau_m_hat) / Z2s - vv_m;
-    P[2] = (q_l - tau_l_hat) / Z2s - vv_l;
+    P[4] = Q[4] = tmh;
+    P[5] = Q[5] = tlh;
+    Q[1] = (tmh + p_m) / Z1s + vm;
+    Q[2] = (tlh + p_l) / Z1s + vl;
+    P[1] = (q_m - tmh) / Z2s - vm;
+    P[2] = (q_l - tlh) / Z2s - vl;
   }
-  (void)Vel;
-  const double srate = sqrt((Q[1] - P[1]) * (Q[1] - P[1]) + (Q[2] - P[2]) * (Q[2] - P[2]));
+  const R srate = sqrt((Q[1] - P[1]) * (Q[1] - P[1]) + (Q[2] - P[2]) * (Q[2] - P[2]));
 
   // stage-1 outputs: rupture front and the fault frame (block 1's copy)
   if (a.stage == 1) {
-    const double sv1 = Q[1] - P[1], sv2 = Q[2] - P[2];
-    if (sqrt(sv1 * sv1 + sv2 * sv2) > 1.0e-3) trup[f] = fmin(trup[f], a.t);
+    const R sv1 = Q[1] - P[1], sv2 = Q[2] - P[2];
+    if (sqrt(sv1 * sv1 + sv2 * sv2) > R(1.0e-3)) trup[f] = fmin(trup[f], a.t);
     if (b == 0 && a.frame) {
       float* fr = a.frame;
 #pragma unroll
@@ -237,15 +316,15 @@ __global__ void interface_kernel(const InterfaceArgs a) {
 
   // slip and state: DS <- A*DS + rates, then the RK update of S and W
 #pragma unroll
-  for (int c = 0; c < 3; ++c) DS[c * nf + f] = a.A * DS[c * nf + f] + (Q[c] - P[c]);
-  DS[3 * nf + f] = a.A * DS[3 * nf + f] + srate;
+  for (int c = 0; c < 3; ++c) DS[c * nf + f] = a.A * DS[c * nf + f] + (double)(Q[c] - P[c]);
+  DS[3 * nf + f] = a.A * DS[3 * nf + f] + (double)srate;
 #pragma unroll
   for (int c = 0; c < 4; ++c) S[c * nf + f] += a.Bdt * DS[c * nf + f];
   if (cpl == CPL_RS) W[f] += a.Bdt * DW[f];
 
   // hat variables back to (x,y,z); grid values rotate back to themselves
-  double uh[6], vh[6];
-  auto back = [&](const double h[6], double o[6]) {
+  R uh[6], vh[6];
+  auto back = [&](const R h[6], R o[6]) {
     o[0] = n[0] * h[0] + m[0] * h[1] + l[0] * h[2];
     o[1] = n[1] * h[0] + m[1] * h[1] + l[1] * h[2];
     o[2] = n[2] * h[0] + m[2] * h[1] + l[2] * h[2];
@@ -255,46 +334,46 @@ __global__ void interface_kernel(const InterfaceArgs a) {
   };
   back(P, uh);
   back(Q, vh);
-  double ug[6], vg[6];
+  R ug[6], vg[6];
   back(ur, ug);
   back(vr, vg);
 
   // SAT vector for this copy's block (src/CouplingForcing.f90:238-466)
-  const double norm = sqrt(gx * gx + gy * gy + gz * gz);
-  const double Zp = b == 0 ? Z1p : Z2p, Zs = b == 0 ? Z1s : Z2s;
-  double Mm[3][3], Pm[3][3];
-  const double* e[3] = {n, m, l};
+  const R norm = sqrt(gx * gx + gy * gy + gz * gz);
+  const R Zp = b == 0 ? Z1p : Z2p, Zs = b == 0 ? Z1s : Z2s;
+  R Mm[3][3], Pm[3][3];
+  const R* e[3] = {n, m, l};
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       // M = sum_k e_r[k] e_c[k] Z_k with Z = (Zp, Zs, Zs) by component index
       Mm[r][c] = e[r][0] * e[c][0] * Zp + e[r][1] * e[c][1] * Zs + e[r][2] * e[c][2] * Zs;
-      Pm[r][c] = e[r][0] * e[c][0] * 1.0 / Zp + e[r][1] * e[c][1] * 1.0 / Zs + e[r][2] * e[c][2] * 1.0 / Zs;
+      Pm[r][c] = e[r][0] * e[c][0] * R(1) / Zp + e[r][1] * e[c][1] * R(1) / Zs + e[r][2] * e[c][2] * R(1) / Zs;
     }
-  double dch[3];
+  R dch[3];
   if (b == 0) {
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      const double ph = 0.5 * (Mm[r][0] * uh[0] + Mm[r][1] * uh[1] + Mm[r][2] * uh[2] + uh[3 + r]);
-      const double pg = 0.5 * (Mm[r][0] * ug[0] + Mm[r][1] * ug[1] + Mm[r][2] * ug[2] + ug[3 + r]);
+      const R ph = R(0.5) * (Mm[r][0] * uh[0] + Mm[r][1] * uh[1] + Mm[r][2] * uh[2] + uh[3 + r]);
+      const R pg = R(0.5) * (Mm[r][0] * ug[0] + Mm[r][1] * ug[1] + Mm[r][2] * ug[2] + ug[3 + r]);
       dch[r] = pg - ph;
     }
   } else {
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      const double qh = 0.5 * (Mm[r][0] * vh[0] + Mm[r][1] * vh[1] + Mm[r][2] * vh[2] - vh[3 + r]);
-      const double qg = 0.5 * (Mm[r][0] * vg[0] + Mm[r][1] * vg[1] + Mm[r][2] * vg[2] - vg[3 + r]);
+      const R qh = R(0.5) * (Mm[r][0] * vh[0] + Mm[r][1] * vh[1] + Mm[r][2] * vh[2] - vh[3 + r]);
+      const R qg = R(0.5) * (Mm[r][0] * vg[0] + Mm[r][1] * vg[1] + Mm[r][2] * vg[2] - vg[3 + r]);
       dch[r] = qg - qh;
     }
   }
-  double rr[3];
+  R rr[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) rr[r] = Pm[r][0] * dch[0] + Pm[r][1] * dch[1] + Pm[r][2] * dch[2];
-  const double lam = b == 0 ? lam1 : lam2, mu = b == 0 ? mu1 : mu2, rho = b == 0 ? rho1 : rho2;
-  const double sgn = b == 0 ? 1.0 : -1.0;
-  const double l2m = 2.0 * mu + lam;
-  double sat[9];
+  const R lam = b == 0 ? lam1 : lam2, mu = b == 0 ? mu1 : mu2, rho = b == 0 ? rho1 : rho2;
+  const R sgn = b == 0 ? R(1) : R(-1);
+  const R l2m = R(2) * mu + lam;
+  R sat[9];
   sat[0] = norm / rho * dch[0];
   sat[1] = norm / rho * dch[1];
   sat[2] = norm / rho * dch[2];
@@ -305,8 +384,9 @@ __global__ void interface_kernel(const InterfaceArgs a) {
   sat[7] = sgn * (mu * (gz * rr[0] + gx * rr[2]));
   sat[8] = sgn * (mu * (gz * rr[1] + gy * rr[2]));
   T* out = (T*)a.sat + (long long)b * 9 * nf;
+  const R th = (R)a.tau_h[b];
 #pragma unroll
-  for (int c = 0; c < 9; ++c) out[c * nf + f] = (T)(a.tau_h[b] * sat[c]);
+  for (int c = 0; c < 9; ++c) out[c * nf + f] = th * sat[c];
 }
 
 }  // namespace

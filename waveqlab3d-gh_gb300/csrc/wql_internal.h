@@ -2,7 +2,8 @@
 //
 // HBM layout per block (nq x nr x ns points, q fastest, no ghost layers --
 // the reference's 3-deep MPI halos, src/mpi3dcomm.f90:722-746, do not exist
-// on one GPU):
+// on one GPU).  Rows along q are padded to a pitch pq (a multiple of 16
+// bytes) so every row starts on a TMA-legal address; np = pq*nr*ns:
 //   F[2]  : 9 x np field components, ping-pong buffers (stage reads one and
 //           writes the other, so neighbours never see a half-updated state)
 //   DF    : 9 x np rates (RK 2N-storage register), updated in place
@@ -13,6 +14,8 @@
 //           face-normal coordinate, lambda, mu, rho
 //   Q/DQ  : PML auxiliary fields on slabs of npml layers per active side
 #pragma once
+#include <cuda.h>
+
 #include <cstddef>
 #include <cstdint>
 
@@ -30,7 +33,8 @@ enum BcForm : int { BC_CHARACTERISTIC = 0, BC_WEIGHTED = 1 };
 template <typename T>
 struct VolumeArgs {
   int nq, nr, ns;
-  long long np;
+  int pq;             // row pitch along q (nq rounded up to 16 bytes)
+  long long np;       // pq * nr * ns, the component stride of F, DF, C, coef
   int block;          // 0: fault on the q = nq face; 1: fault on the q = 1 face
   T rh[3];            // 1/h per axis, h = 1/(n-1)
   const T* __restrict__ Fin;
@@ -62,12 +66,15 @@ struct VolumeArgs {
   double s0u[6];       // uniform initial stress
   const T* __restrict__ ycoord;  // depth coordinate for the initial stress
   double pl_c, pl_nu, pl_Tv, dt;
+  int* err;                      // device error word (pipeline wait timeouts)
+  const void* tma;               // host pointer to the block's StencilMaps (FP32 only)
 };
 
 struct InterfaceArgs {
   int nr, ns;
-  long long np0, np1;
+  long long np0, np1;       // component strides (pitched) of the two blocks
   int nq0;
+  int pq0, pq1;             // row pitches along q
   int fp64;                 // fields are double (1) or float (0)
   const void* F0;           // block 0 fields (9 x np0)
   const void* F1;           // block 1 fields (9 x np1)
@@ -80,6 +87,8 @@ struct InterfaceArgs {
   double* DW;               // 2 x nf
   double* trup;             // 2 x nf
   void* sat;                // 2 x 9 x nf (T), scaled by tau0/h of the block
+  const double* pre;        // 2 x 5 x nf: static Tn, Tm, Tl, nucleation weight, rate-state a
+  double ramp;              // nucleation ramp at this stage's time
   double tau_h[2];
   double A, Bdt, t;
   int stage;
@@ -99,6 +108,24 @@ enum FrameOff : int {
 constexpr int kFrameOff[9] = {FR_UFACE, FR_VFACE, FR_S, FR_UHAT, FR_VHAT, FR_SVEL, FR_TRUP, FR_STATE, FR_END};
 
 // Kernel launchers (stream-ordered).
+// Tensor maps of one block for the TMA stencil kernel (FP32 fields): the
+// field box with halo and the lead-plane tile for each of the two field
+// buffers, and the coefficient boxes.  Built once at set-up.
+constexpr int kTmaTQ = 32, kTmaTR = 8;
+struct StencilMaps {
+  CUtensorMap fbox[2], flead[2];  // per field buffer
+  CUtensorMap ca, cb, cc, cl;     // coefficients: q-halo rows, r-halo columns, tile, lead plane
+  CUtensorMap df, ck;             // rates and compensation on the tile
+  int cur;                        // which field buffer is the stage input
+  int ok;
+};
+// Fills m for a block; returns 0 or a CUDA driver error code.
+int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
+                      bool curv);
+// Launches the TMA stencil kernel (every plane of the block) with a 2- or
+// 3-deep ring of shared-memory stages.
+void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int stages, void* stream);
+
 // One stage on one block: launch_volume runs the stencil kernel (DF and the
 // updated fields for every point); launch_corrections then adds the PML,
 // boundary/fault penalty and plastic kernels and returns how many it issued.
@@ -112,7 +139,7 @@ void launch_metrics(int nq, int nr, int ns, const double* x, double* metric, dou
 void launch_faces(int nq, int nr, int ns, const double* metric, const double* lam,
                   const double* mu, const double* rho, double* const face[6], void* stream);
 template <typename T>
-void launch_coef(long long np, bool curv, const double* metric, const double* J,
+void launch_coef(int nq, int nr, int ns, int pq, bool curv, const double* metric, const double* J,
                  const double* lam, const double* mu, const double* rho, T* coef, void* stream);
 
 }  // namespace wql

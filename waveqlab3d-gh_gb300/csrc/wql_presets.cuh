@@ -115,9 +115,14 @@ WQL_HD double smooth_ramp(double t) {
   return G;
 }
 
-// prestress (src/Interface_Condition.f90:1802-2435)
-WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const double l[3],
-                      const double m[3], const double n[3], double& Tn, double& Tm, double& Tl) {
+// prestress (src/Interface_Condition.f90:1802-2435), split as
+//   (Tn, Tm, Tl) = static(x) + (0, 0, nucleation_weight(x) * nucleation_ramp(t))
+// because the only time dependence of every preset is a fault-uniform ramp
+// of a nucleation patch; the static part and the weight are evaluated once
+// per fault point, the ramp once per stage.  prestress() recombines them
+// with the reference's arithmetic order (Tl + (weight * ramp)).
+WQL_HD void prestress_static(const FaultParams& fp, const double x[3], const double l[3], const double m[3],
+                             const double n[3], double& Tn, double& Tm, double& Tl) {
   double s0[6];
   switch (fp.preset) {
     case PRE_TPV5:
@@ -132,6 +137,8 @@ WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const 
     case PRE_TPV27:
     case PRE_TPV29:
     case PRE_TPV30:
+    case PRE_TPV101:
+    case PRE_TPV102:
       initial_stress(fp.preset, x, s0);
       tensor_traction(s0, n, m, l, Tn, Tm, Tl);
       return;
@@ -145,16 +152,6 @@ WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const 
       Tl = Tl + nuke;
       return;
     }
-    case PRE_TPV101:
-    case PRE_TPV102: {
-      initial_stress(fp.preset, x, s0);
-      tensor_traction(s0, n, m, l, Tn, Tm, Tl);
-      const double r = sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
-      double F = 0.0;
-      if (r < 3.0) F = exp(r * r / (r * r - 9.0));
-      Tl = Tl + 25.0 * F * smooth_ramp(t);
-      return;
-    }
     case PRE_TPV10: {
       const double g = 2.0 / sqrt(3.0);
       Tn = -7.378 * x[1] * g;
@@ -164,20 +161,57 @@ WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const 
       return;
     }
     case PRE_SW_PARAM:
-    case PRE_RS_PARAM: {
+    case PRE_RS_PARAM:
       if (fp.s0_profile != PRE_NONE && initial_stress(fp.s0_profile, x, s0))
         tensor_traction(s0, n, m, l, Tn, Tm, Tl);
       else
         tensor_traction(fp.s0, n, m, l, Tn, Tm, Tl);
-      const double dy = x[1] - fp.nuc_y, dz = x[2] - fp.nuc_z;
-      const double F = exp(-(dy * dy + dz * dz) / (2.0 * fp.nuc_radius * fp.nuc_radius));
-      const double G = fp.nuc_rise > 0.0 ? smooth_ramp(t / fp.nuc_rise) : 1.0;
-      Tl = Tl + fp.nuc_amp * F * G;
       return;
-    }
     default:
       Tn = Tm = Tl = 0.0;
   }
+}
+
+// Amplitude of the time-ramped nucleation traction at x (MPa).
+WQL_HD double nucleation_weight(const FaultParams& fp, const double x[3]) {
+  switch (fp.preset) {
+    case PRE_TPV101:
+    case PRE_TPV102: {
+      const double r = sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
+      double F = 0.0;
+      if (r < 3.0) F = exp(r * r / (r * r - 9.0));
+      return 25.0 * F;
+    }
+    case PRE_SW_PARAM:
+    case PRE_RS_PARAM: {
+      const double dy = x[1] - fp.nuc_y, dz = x[2] - fp.nuc_z;
+      const double F = exp(-(dy * dy + dz * dz) / (2.0 * fp.nuc_radius * fp.nuc_radius));
+      return fp.nuc_amp * F;
+    }
+    default:
+      return 0.0;
+  }
+}
+
+// The fault-uniform ramp of the nucleation traction at time t.
+WQL_HD double nucleation_ramp(const FaultParams& fp, double t) {
+  switch (fp.preset) {
+    case PRE_TPV101:
+    case PRE_TPV102:
+      return smooth_ramp(t);
+    case PRE_SW_PARAM:
+    case PRE_RS_PARAM:
+      return fp.nuc_rise > 0.0 ? smooth_ramp(t / fp.nuc_rise) : 1.0;
+    default:
+      return 0.0;
+  }
+}
+
+WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const double l[3],
+                      const double m[3], const double n[3], double& Tn, double& Tm, double& Tl) {
+  prestress_static(fp, x, l, m, n, Tn, Tm, Tl);
+  const double w = nucleation_weight(fp, x);
+  if (w != 0.0) Tl = Tl + w * nucleation_ramp(fp, t);
 }
 
 WQL_HD double forced_rupture_time(double r, double Vs) {
@@ -246,16 +280,25 @@ struct RSParams {
   double L0, f0, b, V0, a;
 };
 
-// rate-and-state constants per point (src/Interface_Condition.f90:384-417)
-WQL_HD RSParams rs_params(const FaultParams& fp, const double x[3]) {
+// rate-and-state constants per point (src/Interface_Condition.f90:384-417);
+// only the direct-effect parameter a varies along the fault
+WQL_HD double rs_direct_a(const FaultParams& fp, const double x[3]) {
+  if (fp.preset == PRE_RS_PARAM) return fp.a;
+  return 0.008 + 0.008 * (1.0 - smooth_boxcar(x[1], 15.0, 3.0) * smooth_boxcar(x[2], 15.0, 3.0));
+}
+
+WQL_HD RSParams rs_params(const FaultParams& fp, const double x[3], double a) {
+  (void)x;
   RSParams r;
   if (fp.preset == PRE_RS_PARAM) {
-    r.L0 = fp.L; r.f0 = fp.f0; r.b = fp.b; r.V0 = fp.V0; r.a = fp.a;
+    r.L0 = fp.L; r.f0 = fp.f0; r.b = fp.b; r.V0 = fp.V0;
   } else {
     r.L0 = 0.02; r.f0 = 0.6; r.b = 0.012; r.V0 = 1.0e-6;
-    r.a = 0.008 + 0.008 * (1.0 - smooth_boxcar(x[1], 15.0, 3.0) * smooth_boxcar(x[2], 15.0, 3.0));
   }
+  r.a = a;
   return r;
 }
+
+WQL_HD RSParams rs_params(const FaultParams& fp, const double x[3]) { return rs_params(fp, x, rs_direct_a(fp, x)); }
 
 }  // namespace wql

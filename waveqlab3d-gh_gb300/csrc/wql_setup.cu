@@ -127,24 +127,26 @@ __global__ void faces_kernel(int nq, int nr, int ns, const double* __restrict__ 
 }
 
 template <typename T>
-__global__ void coef_kernel(long long np, int curv, const double* __restrict__ metric,
+__global__ void coef_kernel(int nq, long long npd, int pq, long long np, int curv, const double* __restrict__ metric,
                             const double* __restrict__ J, const double* __restrict__ lam,
                             const double* __restrict__ mu, const double* __restrict__ rho,
                             T* __restrict__ coef) {
+  // p: dense index of the precompute arrays; o: pitched index of coef
   const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p >= np) return;
+  if (p >= npd) return;
+  const long long o = p % nq + (long long)pq * (p / nq);
   if (curv) {
     const double Jp = J[p];
     for (int d = 0; d < 3; ++d)
-      for (int c = 0; c < 3; ++c) coef[(d * 3 + c) * np + p] = (T)(Jp * metric[(c * 3 + d) * np + p]);
-    coef[9 * np + p] = (T)(1.0 / Jp);
-    coef[10 * np + p] = (T)lam[p];
-    coef[11 * np + p] = (T)mu[p];
-    coef[12 * np + p] = (T)(1.0 / (rho[p] * Jp));
+      for (int c = 0; c < 3; ++c) coef[(d * 3 + c) * np + o] = (T)(Jp * metric[(c * 3 + d) * npd + p]);
+    coef[9 * np + o] = (T)(1.0 / Jp);
+    coef[10 * np + o] = (T)lam[p];
+    coef[11 * np + o] = (T)mu[p];
+    coef[12 * np + o] = (T)(1.0 / (rho[p] * Jp));
   } else {
-    coef[0 * np + p] = (T)lam[p];
-    coef[1 * np + p] = (T)mu[p];
-    coef[2 * np + p] = (T)(1.0 / rho[p]);
+    coef[0 * np + o] = (T)lam[p];
+    coef[1 * np + o] = (T)mu[p];
+    coef[2 * np + o] = (T)(1.0 / rho[p]);
   }
 }
 
@@ -167,17 +169,18 @@ void launch_faces(int nq, int nr, int ns, const double* metric, const double* la
 }
 
 template <typename T>
-void launch_coef(long long np, bool curv, const double* metric, const double* J,
+void launch_coef(int nq, int nr, int ns, int pq, bool curv, const double* metric, const double* J,
                  const double* lam, const double* mu, const double* rho, T* coef, void* stream) {
   const int blk = 256;
-  const long long grd = (np + blk - 1) / blk;
-  coef_kernel<T><<<(unsigned)grd, blk, 0, (cudaStream_t)stream>>>(np, curv ? 1 : 0, metric, J, lam,
-                                                                   mu, rho, coef);
+  const long long npd = (long long)nq * nr * ns, np = (long long)pq * nr * ns;
+  const long long grd = (npd + blk - 1) / blk;
+  coef_kernel<T><<<(unsigned)grd, blk, 0, (cudaStream_t)stream>>>(nq, npd, pq, np, curv ? 1 : 0, metric, J,
+                                                                   lam, mu, rho, coef);
 }
 
-template void launch_coef<double>(long long, bool, const double*, const double*, const double*,
+template void launch_coef<double>(int, int, int, int, bool, const double*, const double*, const double*,
                                   const double*, const double*, double*, void*);
-template void launch_coef<float>(long long, bool, const double*, const double*, const double*,
+template void launch_coef<float>(int, int, int, int, bool, const double*, const double*, const double*,
                                  const double*, const double*, float*, void*);
 
 }  // namespace wql

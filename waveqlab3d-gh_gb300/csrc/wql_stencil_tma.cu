@@ -1,0 +1,587 @@
+// TMA-pipelined stencil kernel for FP32 fields (the FP32-compensated mode):
+// the same per-point update as the other stencil kernels,
+//   DF <- A*DF + L(F),   F_out <- F + B*dt*DF   (Kahan-compensated),
+// (scale_rates + set_rates + update_fields, src/fields.f90:49-171,
+// src/JU_xJU_yJU_z6.f90:12-812 and 16141-16449, src/RHS_Interior.f90:133-274)
+// on every plane of the block.
+//
+// A CTA owns a 32 x 8 (q, r) tile and marches along a chunk of s planes.  One
+// producer thread streams each plane into shared memory with
+// cp.async.bulk.tensor (TMA) through an NS-deep ring of stages guarded by
+// mbarriers ("full" completes on the transaction bytes, "empty" when all
+// consumer warps have read the stage):
+//   main (plane s)   : the 9 field components on the tile plus a q halo of
+//                      8 points each side (so every box starts on a 16-byte
+//                      boundary and every q closure row of a tile is inside
+//                      the box) and an r halo of 3 rows; J*metric_q on the
+//                      q-extended rows, J*metric_r on the r-extended columns,
+//                      the remaining 7 coefficients, the rates DF and the
+//                      compensation C on the tile;
+//   lead (plane s+3) : the 9 field components and J*metric_s on the tile.
+// Each consumer thread keeps the velocities and the s-face momentum flux of
+// planes s-3..s+3 of its point in registers (the first six read directly at
+// the start of a chunk, then one pushed per step from the lead tile), so
+// the s derivative of a central row needs no shared memory (lead planes
+// outside 0..ns-1 load as zeros and are never used: the 12 s closure rows
+// read their 9 planes from global memory); the q and r derivatives read the
+// main box, the curvilinear q and r fluxes formed once per box point into
+// the stage (one mbarrier phase among the consumer threads per step).  The r
+// tiles follow the ownership rule of tile_span (the last
+// tile is shifted to end on the last point), which keeps every r closure row
+// inside tile + halo.  DF, F_out and C are stored directly from registers.
+//
+// Every mbarrier wait is bounded; a wait that runs out sets *err and the
+// thread leaves its loop (the producer first waits, again bounded, for the
+// copies it issued).
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "wql_internal.h"
+#include "wql_stencil.cuh"
+
+namespace wql {
+namespace {
+
+template <bool CURV, bool KAHAN>
+struct TmaTile {
+  static constexpr int TQ = kTmaTQ, TR = kTmaTR, NC = TQ * TR;
+  static constexpr int BQ = TQ + 16, BR = TR + 6;  // field box: q from q0-8, r from r0-3
+  static constexpr int NCC = CURV ? 7 : 3;         // tile coefficients: 6..12 or lambda, mu, 1/rho
+  static constexpr int F_W = 9 * BR * BQ;
+  static constexpr int CA_W = CURV ? 3 * TR * BQ : 0;
+  static constexpr int CB_W = CURV ? 3 * BR * TQ : 0;
+  static constexpr int CC_W = NCC * NC;
+  static constexpr int LF_W = 9 * NC;
+  static constexpr int LC_W = CURV ? 3 * NC : 0;
+  static constexpr int DF_W = 9 * NC;            // rates of the main plane
+  static constexpr int CK_W = KAHAN ? 9 * NC : 0;  // compensation of the main plane
+  static constexpr int OFF_F = 0;
+  static constexpr int OFF_CA = OFF_F + F_W;
+  static constexpr int OFF_CB = OFF_CA + CA_W;
+  static constexpr int OFF_CC = OFF_CB + CB_W;
+  static constexpr int OFF_LF = OFF_CC + CC_W;
+  static constexpr int OFF_LC = OFF_LF + LF_W;
+  static constexpr int OFF_DF = OFF_LC + LC_W;
+  static constexpr int OFF_CK = OFF_DF + DF_W;
+  static constexpr int STAGE_W = OFF_CK + CK_W;
+  static constexpr unsigned MAIN_BYTES = 4u * (F_W + CA_W + CB_W + CC_W + DF_W + CK_W);
+  static constexpr unsigned LEAD_BYTES = 4u * (LF_W + LC_W);
+  // every sub-buffer starts on a 128-byte boundary
+  static_assert(F_W % 32 == 0 && CA_W % 32 == 0 && CB_W % 32 == 0 && CC_W % 32 == 0 && LF_W % 32 == 0 &&
+                    LC_W % 32 == 0 && DF_W % 32 == 0 && CK_W % 32 == 0,
+                "stage sub-buffers must be multiples of 128 bytes");
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
+// One potentially blocking test of the phase with parity `parity`; the
+// thread sleeps in hardware for at most about 0.5 ms before it returns false.
+__device__ __forceinline__ bool mbar_try(uint64_t* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity), "r"(500000u)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase of parity `parity` to complete: at most 8192
+// blocking tests (a few seconds).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+  for (unsigned i = 0; i < 8192u; ++i)
+    if (mbar_try(b, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                            int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// s derivative of the six differenced quantities on a closure row (planes
+// 0..5 and ns-6..ns-1), read from global memory: the s window in registers
+// holds only the 7 planes of a central row.
+template <bool CURV>
+__device__ __noinline__ void s_closure(const VolumeArgs<float>& a, long long p, int s, int ks, float o[6]) {
+  const long long np = a.np, st = (long long)a.pq * a.nr;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) o[c] = 0.0f;
+  for (int e = 0; e < 9; ++e) {
+    float w;
+    int off;
+    row_entry<float>(ks, e, w, off);
+    const long long pp = p + off * st;
+    float x[6];
+    const float* F = a.Fin;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) x[c] = F[c * np + pp];
+    if (CURV) {
+      const float a0 = a.coef[6 * np + pp], a1 = a.coef[7 * np + pp], a2 = a.coef[8 * np + pp];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        x[3 + c] = a0 * F[sig(c, 0) * np + pp] + a1 * F[sig(c, 1) * np + pp] + a2 * F[sig(c, 2) * np + pp];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[3 + c] = F[sig(c, 2) * np + pp];
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) o[c] += w * x[c];
+  }
+}
+
+struct MapArgs {
+  CUtensorMap fbox, flead, ca, cb, cc, cl, df, ck;
+};
+
+template <bool CURV, bool KAHAN, int NS>
+__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
+    stencil_kernel_tma(const __grid_constant__ VolumeArgs<float> a, const __grid_constant__ MapArgs m, int schunk) {
+  using TL = TmaTile<CURV, KAHAN>;
+  constexpr int TQ = TL::TQ, TR = TL::TR, NC = TL::NC, BQ = TL::BQ, BR = TL::BR;
+  constexpr int NCW = NC / 32;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // 128-byte aligned start, derived from the shared array itself so the
+  // compiler keeps every access in the shared address space
+  float* sm = reinterpret_cast<float*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + NS * TL::STAGE_W);
+  uint64_t* empty = full + NS;
+  uint64_t* fluxbar = empty + NS;  // consumer-only: fluxes of the step written
+
+  const int tid = threadIdx.x;
+  const int nq = a.nq, nr = a.nr, ns = a.ns;
+  const int q0 = blockIdx.x * TQ;
+  const TileSpan spr = tile_span(blockIdx.y, nr, TR);
+  const int r0 = spr.origin;
+  const int s_begin = blockIdx.z * schunk;
+  const int s_end = min(ns, s_begin + schunk);
+  const int nstep = s_end - s_begin;
+
+  if (tid == 0) {
+    for (int i = 0; i < NS; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], NCW);
+    }
+    mbar_init(fluxbar, NC);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  if (tid >= NC) {  // producer warp: one thread issues every copy
+    if (tid == NC) {
+      int issued = 0;
+      bool ok = true;
+      for (int t = 0; t < nstep; ++t) {
+        const int st = t % NS;
+        if (t >= NS && !mbar_wait(&empty[st], ((t / NS) & 1) ^ 1)) {
+          ok = false;
+          break;
+        }
+        const int sp = s_begin + t;  // main plane
+        mbar_expect_tx(&full[st], TL::LEAD_BYTES + TL::MAIN_BYTES);
+        float* S = sm + st * TL::STAGE_W;
+        tma_load_4d(S + TL::OFF_LF, &m.flead, &full[st], q0, r0, sp + 3, 0);
+        if (CURV) tma_load_4d(S + TL::OFF_LC, &m.cl, &full[st], q0, r0, sp + 3, 6);
+        tma_load_4d(S + TL::OFF_F, &m.fbox, &full[st], q0 - 8, r0 - 3, sp, 0);
+        tma_load_4d(S + TL::OFF_DF, &m.df, &full[st], q0, r0, sp, 0);
+        if (KAHAN) tma_load_4d(S + TL::OFF_CK, &m.ck, &full[st], q0, r0, sp, 0);
+        if (CURV) {
+          tma_load_4d(S + TL::OFF_CA, &m.ca, &full[st], q0 - 8, r0, sp, 0);
+          tma_load_4d(S + TL::OFF_CB, &m.cb, &full[st], q0, r0 - 3, sp, 3);
+          tma_load_4d(S + TL::OFF_CC, &m.cc, &full[st], q0, r0, sp, 6);
+        } else {
+          tma_load_4d(S + TL::OFF_CC, &m.cc, &full[st], q0, r0, sp, 0);
+        }
+        issued = t + 1;
+      }
+      if (!ok) atomicExch(a.err, 1);
+      // the copies this thread issued land before the CTA may leave
+      for (int t = max(0, issued - NS); t < issued; ++t) mbar_wait(&full[t % NS], (t / NS) & 1);
+    }
+    return;
+  }
+
+  // ---- consumers: one thread per (q, r) point of the tile
+  const int tx = tid % TQ, ty = tid / TQ;
+  const int q = q0 + tx, r = r0 + ty;
+  const bool own = q < nq && r >= spr.own_lo && r < spr.own_hi;
+  const int kq = sbp_kind(q, nq), kr = sbp_kind(r, nr);
+  const long long np = a.np;
+  const long long sts = (long long)a.pq * nr;
+  const long long col = q + (long long)a.pq * r;
+  const int lq = tx + 8, lr = ty + 3;
+  const float c1 = float(kC1), c2 = float(kC2), c3 = float(kC3);
+
+  float qv[7][6];  // velocities and s-face flux, planes s-3..s+3
+  // the window's first six planes (s_begin-3 .. s_begin+2) straight from
+  // global memory, all loads in flight at once; planes outside the block
+  // stay zero (only central rows read the window)
+#pragma unroll
+  for (int i = 0; i < 7; ++i) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) qv[i][c] = 0.0f;
+    const int pl = s_begin - 3 + i;
+    if (i < 6 && pl >= 0 && pl < ns && q < nq && r < nr) {
+      const long long pp = col + sts * pl;
+      const float* F = a.Fin;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) qv[i][c] = F[c * np + pp];
+      if (CURV) {
+        const float a0 = a.coef[6 * np + pp], a1 = a.coef[7 * np + pp], a2 = a.coef[8 * np + pp];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          qv[i][3 + c] = a0 * F[sig(c, 0) * np + pp] + a1 * F[sig(c, 1) * np + pp] + a2 * F[sig(c, 2) * np + pp];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) qv[i][3 + c] = F[sig(c, 2) * np + pp];
+      }
+    }
+  }
+
+  for (int t = 0; t < nstep; ++t) {
+    const int st = t % NS;
+    const int s = s_begin + t;  // output plane
+    const bool work = own;
+    const int ks = sbp_kind(s, ns);
+    const long long p = col + sts * s;
+    if (!mbar_wait(&full[st], (t / NS) & 1)) {
+      atomicExch(a.err, 2);
+      return;
+    }
+    const float* S = sm + st * TL::STAGE_W;
+    // push the lead plane s+3 into the s window
+    {
+      const float* LF = S + TL::OFF_LF;
+      const int li = ty * TQ + tx;
+      float f[9];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) f[c] = LF[c * NC + li];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) qv[6][c] = f[c];
+      if (CURV) {
+        const float* LC = S + TL::OFF_LC;
+        const float a0 = LC[li], a1 = LC[NC + li], a2 = LC[2 * NC + li];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) qv[6][3 + c] = a0 * f[sig(c, 0)] + a1 * f[sig(c, 1)] + a2 * f[sig(c, 2)];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) qv[6][3 + c] = f[sig(c, 2)];
+      }
+    }
+
+    // curvilinear: the q- and r-face momentum fluxes J*metric*sigma of the
+    // main plane, formed once per box point and written over the
+    // coefficients they come from (CA becomes the q flux on the q-extended
+    // rows, CB the r flux on the r-extended columns); each position is
+    // handled by one thread, which reads its coefficients first
+    float* FB = const_cast<float*>(S) + TL::OFF_F;
+    float* CA = const_cast<float*>(S) + TL::OFF_CA;
+    float* CB = const_cast<float*>(S) + TL::OFF_CB;
+    const float* CC = S + TL::OFF_CC;
+    auto fb = [&](int c, int rr, int qq) -> float { return FB[(c * BR + rr) * BQ + qq]; };
+    float mq[3] = {0.0f, 0.0f, 0.0f}, mr[3] = {0.0f, 0.0f, 0.0f};  // own J*metric_q, J*metric_r
+    if (CURV) {
+      auto qflux = [&](int row, int l, float m[3]) {
+        float sg[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sg[c] = fb(3 + c, row + 3, l);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) m[j] = CA[(j * TR + row) * BQ + l];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          CA[(c * TR + row) * BQ + l] = m[0] * sg[sig(c, 0) - 3] + m[1] * sg[sig(c, 1) - 3] + m[2] * sg[sig(c, 2) - 3];
+      };
+      auto rflux = [&](int l, int col_, float m[3]) {
+        float sg[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sg[c] = fb(3 + c, l, col_ + 8);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) m[j] = CB[(j * BR + l) * TQ + col_];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          CB[(c * BR + l) * TQ + col_] = m[0] * sg[sig(c, 0) - 3] + m[1] * sg[sig(c, 1) - 3] + m[2] * sg[sig(c, 2) - 3];
+      };
+      qflux(ty, lq, mq);
+      rflux(lr, tx, mr);
+      float tmp[3];
+      if (tx < 16) qflux(ty, tx < 8 ? tx : tx + TQ, tmp);     // q halo: 8 columns each side
+      if (ty < 6) rflux(ty < 3 ? ty : ty + TR, tx, tmp);      // r halo: 3 rows each side
+      // every consumer thread arrives; the bounded wait makes the fluxes of
+      // all of them visible (arrive releases, the wait acquires)
+      mbar_arrive(fluxbar);
+      if (!mbar_wait(fluxbar, t & 1)) {
+        atomicExch(a.err, 3);
+        return;
+      }
+    }
+
+    if (work) {
+      // differenced quantities along q at box column l (row lr) and along r at box row l (column lq)
+      auto qvals = [&](int l, float o[6]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[c] = fb(c, lr, l);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[3 + c] = CURV ? CA[(c * TR + ty) * BQ + l] : fb(sig(c, 0), lr, l);
+      };
+      auto rvals = [&](int l, float o[6]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[c] = fb(c, l, lq);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[3 + c] = CURV ? CB[(c * BR + l) * TQ + tx] : fb(sig(c, 1), l, lq);
+      };
+      float g[3][3], dv[3];
+      const float Jinv = CURV ? CC[3 * NC + ty * TQ + tx] : 1.0f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float o[6];
+        if (d == 2) {
+          if (ks == 0) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+              o[c] = c1 * (qv[4][c] - qv[2][c]) + c2 * (qv[5][c] - qv[1][c]) + c3 * (qv[6][c] - qv[0][c]);
+          } else {
+            s_closure<CURV>(a, p, s, ks, o);
+          }
+        } else {
+          const int kind = d == 0 ? kq : kr;
+          const int l0 = d == 0 ? lq : lr;
+          if (kind == 0) {
+            float xp[6], xm[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) o[c] = 0.0f;
+#pragma unroll
+            for (int k = 1; k <= 3; ++k) {
+              if (d == 0) {
+                qvals(l0 + k, xp);
+                qvals(l0 - k, xm);
+              } else {
+                rvals(l0 + k, xp);
+                rvals(l0 - k, xm);
+              }
+              const float ck = k == 1 ? c1 : (k == 2 ? c2 : c3);
+#pragma unroll
+              for (int c = 0; c < 6; ++c) o[c] += ck * (xp[c] - xm[c]);
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) o[c] = 0.0f;
+#pragma unroll 1
+            for (int e = 0; e < 9; ++e) {
+              float w;
+              int off;
+              row_entry<float>(kind, e, w, off);
+              float x[6];
+              if (d == 0) qvals(l0 + off, x);
+              else rvals(l0 + off, x);
+#pragma unroll
+              for (int c = 0; c < 6; ++c) o[c] += w * x[c];
+            }
+          }
+        }
+        const float rh = a.rh[d];
+        if (CURV) {
+          float mt[3];
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            const float cj = d == 0 ? mq[jj] : (d == 1 ? mr[jj] : CC[jj * NC + ty * TQ + tx]);
+            mt[jj] = cj * Jinv;
+          }
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            dv[c] = d == 0 ? rh * o[3 + c] : dv[c] + rh * o[3 + c];
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj) g[c][jj] = d == 0 ? mt[jj] * (rh * o[c]) : g[c][jj] + mt[jj] * (rh * o[c]);
+          }
+        } else {
+          const float sc = a.cart_metric[d] * rh;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            dv[c] = d == 0 ? sc * o[3 + c] : dv[c] + sc * o[3 + c];
+            g[c][d] = sc * o[c];
+          }
+        }
+      }
+      const int ci = ty * TQ + tx;
+      const float lam = CURV ? CC[4 * NC + ci] : CC[0 * NC + ci];
+      const float mu = CURV ? CC[5 * NC + ci] : CC[1 * NC + ci];
+      const float rinv = CURV ? CC[6 * NC + ci] : CC[2 * NC + ci];
+      const float l2m = lam + 2.0f * mu;
+      float du[9];
+      du[0] = rinv * dv[0];
+      du[1] = rinv * dv[1];
+      du[2] = rinv * dv[2];
+      du[3] = l2m * g[0][0] + lam * (g[1][1] + g[2][2]);
+      du[4] = l2m * g[1][1] + lam * (g[0][0] + g[2][2]);
+      du[5] = l2m * g[2][2] + lam * (g[0][0] + g[1][1]);
+      du[6] = mu * (g[0][1] + g[1][0]);
+      du[7] = mu * (g[0][2] + g[2][0]);
+      du[8] = mu * (g[1][2] + g[2][1]);
+#pragma unroll
+      for (int c = 0; c < 9; ++c) {
+        const float f0 = fb(c, lr, lq);
+        const float df = a.A * S[TL::OFF_DF + c * NC + ty * TQ + tx] + du[c];
+        a.DF[c * np + p] = df;
+        if (KAHAN) {
+          const float y = a.Bdt * df - S[TL::OFF_CK + c * NC + ty * TQ + tx];
+          const float tt = f0 + y;
+          a.C[c * np + p] = (tt - f0) - y;
+          a.Fout[c * np + p] = tt;
+        } else {
+          a.Fout[c * np + p] = f0 + a.Bdt * df;
+        }
+      }
+    }
+    // order this thread's shared-memory writes (the fluxes) before the
+    // producer's next bulk copy into the stage
+    if (CURV) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&empty[st]);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) qv[i][c] = qv[i + 1][c];
+  }
+}
+
+template <bool CURV, bool KAHAN, int NS>
+void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t s) {
+  using TL = TmaTile<CURV, KAHAN>;
+  const int ncen = a.ns;
+  const size_t smem = sizeof(float) * (size_t)NS * TL::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
+  auto kern = stencil_kernel_tma<CURV, KAHAN, NS>;
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr_done = true;
+  }
+  const int tq = (a.nq + TL::TQ - 1) / TL::TQ, tr = (a.nr + TL::TR - 1) / TL::TR;
+  int schunk = a.schunk;
+  if (schunk <= 0) {
+    // choose the number of s chunks (2..24) that wastes the least of the
+    // last wave of CTAs (one CTA per SM)
+    static int nsm = 0;
+    if (!nsm) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (nsm <= 0) nsm = 1;
+    }
+    double best = 1e30;
+    schunk = ncen;
+    for (int nc = 2; nc <= 24; ++nc) {
+      const int sc = (ncen + nc - 1) / nc;
+      const int nchunk = (ncen + sc - 1) / sc;
+      const long long ctas = (long long)tq * tr * nchunk;
+      const long long waves = (ctas + nsm - 1) / nsm;
+      // time ~ waves x (planes per chunk + about one step of prologue)
+      const double cost = (double)waves * (sc + 1);
+      if (cost < best) {
+        best = cost;
+        schunk = sc;
+      }
+    }
+  }
+  MapArgs m;
+  m.fbox = sm.fbox[sm.cur];
+  m.flead = sm.flead[sm.cur];
+  m.ca = sm.ca;
+  m.cb = sm.cb;
+  m.cc = sm.cc;
+  m.cl = sm.cl;
+  m.df = sm.df;
+  m.ck = sm.ck;
+  dim3 grd(tq, tr, (ncen + schunk - 1) / schunk);
+  kern<<<grd, TL::NC + 32, smem, s>>>(a, m, schunk);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// 4-D map over (q, r, s, component) of an FP32 array with row pitch pq.
+int encode4(CUtensorMap* map, void* base, int nq, int nr, int ns, int ncomp, int pq, int bq, int br, int bc) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return 1;
+  const long long np = (long long)pq * nr * ns;
+  cuuint64_t dims[4] = {(cuuint64_t)nq, (cuuint64_t)nr, (cuuint64_t)ns, (cuuint64_t)ncomp};
+  cuuint64_t strides[3] = {(cuuint64_t)pq * 4, (cuuint64_t)pq * nr * 4, (cuuint64_t)np * 4};
+  cuuint32_t box[4] = {(cuuint32_t)bq, (cuuint32_t)br, 1, (cuuint32_t)bc};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return (int)r;
+}
+
+}  // namespace
+
+int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
+                      bool curv) {
+  constexpr int TQ = kTmaTQ, TR = kTmaTR;
+  int rc = 0;
+  m.ok = 0;
+  m.cur = 0;
+  for (int i = 0; i < 2 && !rc; ++i) {
+    rc = encode4(&m.fbox[i], F[i], nq, nr, ns, 9, pq, TQ + 16, TR + 6, 9);
+    if (!rc) rc = encode4(&m.flead[i], F[i], nq, nr, ns, 9, pq, TQ, TR, 9);
+  }
+  if (!rc) rc = encode4(&m.df, DF, nq, nr, ns, 9, pq, TQ, TR, 9);
+  if (!rc) rc = encode4(&m.ck, C ? C : DF, nq, nr, ns, 9, pq, TQ, TR, 9);
+  if (curv) {
+    if (!rc) rc = encode4(&m.ca, coef, nq, nr, ns, kCurvCoef, pq, TQ + 16, TR, 3);
+    if (!rc) rc = encode4(&m.cb, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR + 6, 3);
+    if (!rc) rc = encode4(&m.cc, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR, 7);
+    if (!rc) rc = encode4(&m.cl, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR, 3);
+  } else {
+    if (!rc) rc = encode4(&m.cc, coef, nq, nr, ns, kCartCoef, pq, TQ, TR, 3);
+    m.ca = m.cb = m.cl = m.cc;
+  }
+  m.ok = rc == 0;
+  return rc;
+}
+
+void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int stages, void* stream) {
+  const StencilMaps& sm = *static_cast<const StencilMaps*>(a.tma);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (stages == 2) {
+    if (curv) kahan ? launch_tma<true, true, 2>(a, sm, s) : launch_tma<true, false, 2>(a, sm, s);
+    else kahan ? launch_tma<false, true, 2>(a, sm, s) : launch_tma<false, false, 2>(a, sm, s);
+  } else {
+    if (curv) kahan ? launch_tma<true, true, 3>(a, sm, s) : launch_tma<true, false, 3>(a, sm, s);
+    else kahan ? launch_tma<false, true, 3>(a, sm, s) : launch_tma<false, false, 3>(a, sm, s);
+  }
+}
+
+}  // namespace wql

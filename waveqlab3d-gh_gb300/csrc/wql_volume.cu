@@ -25,26 +25,10 @@
 #include <cuda_runtime.h>
 
 #include "wql_internal.h"
-#include "wql_sbp.cuh"
+#include "wql_stencil.cuh"
 
 namespace wql {
 namespace {
-
-__constant__ double c_sbp_d[6][9] = WQL_SBP_TABLE;
-__constant__ float c_sbp_f[6][9] = WQL_SBP_TABLE;
-
-template <typename T>
-__device__ __forceinline__ T sbp_w(int row, int col);
-template <>
-__device__ __forceinline__ double sbp_w<double>(int row, int col) { return c_sbp_d[row][col]; }
-template <>
-__device__ __forceinline__ float sbp_w<float>(int row, int col) { return c_sbp_f[row][col]; }
-
-// sigma_{c,j} component index in F: rows x,y,z of the symmetric stress.
-__host__ __device__ constexpr int sig(int c, int j) {
-  // sxx=3 syy=4 szz=5 sxy=6 sxz=7 syz=8
-  return c == j ? 3 + c : 5 + c + j;
-}
 
 // Load the six differenced quantities at point q for axis d: velocities
 // and the momentum fluxes through the d-faces.
@@ -152,49 +136,49 @@ __device__ void diff_pml_flux(const T* __restrict__ F, const T* __restrict__ coe
 // followed by structure() (src/RHS_Interior.f90:2203-2223); or the weighted
 // alpha/theta form of src/BoundaryConditions3.f90:777-903 added directly.
 // Returns sat (added to DF with -tau/h) and ubc (added to DQ in a PML).
-__device__ void boundary_sat(const double u[9], const double* __restrict__ face, long long nf,
-                             long long f, int code, bool plus, int form, double sat[9],
-                             double ubc[9]) {
-  double n[3], m[3], l[3];
+template <typename R>
+__device__ void boundary_sat(const R u[9], const double* __restrict__ face, long long nf, long long f, int code,
+                             bool plus, int form, R sat[9], R ubc[9]) {
+  R n[3], m[3], l[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    n[c] = face[(0 + c) * nf + f];
-    m[c] = face[(3 + c) * nf + f];
-    l[c] = face[(6 + c) * nf + f];
+    n[c] = (R)face[(0 + c) * nf + f];
+    m[c] = (R)face[(3 + c) * nf + f];
+    l[c] = (R)face[(6 + c) * nf + f];
   }
-  const double gx = face[9 * nf + f], gy = face[10 * nf + f], gz = face[11 * nf + f];
-  const double lam = face[12 * nf + f], mu = face[13 * nf + f], rho = face[14 * nf + f];
-  const double norm = sqrt(gx * gx + gy * gy + gz * gz);
-  const double cp = sqrt((2.0 * mu + lam) / rho), cs = sqrt(mu / rho);
-  const double Zp = rho * cp, Zs = rho * cs;
-  double r, alpha, theta;
-  if (code == 1) { r = 0.0; alpha = 2.0; theta = 0.0; }
-  else if (code == 2) { r = 1.0; alpha = 1.0; theta = 0.0; }
-  else { r = -1.0; alpha = 0.0; theta = plus ? 1.0 : -1.0; }
-  const double T0 = n[0] * u[3] + n[1] * u[6] + n[2] * u[7];
-  const double T1 = n[0] * u[6] + n[1] * u[4] + n[2] * u[8];
-  const double T2 = n[0] * u[7] + n[1] * u[8] + n[2] * u[5];
-  const double vl = l[0] * u[0] + l[1] * u[1] + l[2] * u[2];
-  const double vm = m[0] * u[0] + m[1] * u[1] + m[2] * u[2];
-  const double vn = n[0] * u[0] + n[1] * u[1] + n[2] * u[2];
-  const double Tl = l[0] * T0 + l[1] * T1 + l[2] * T2;
-  const double Tm = m[0] * T0 + m[1] * T1 + m[2] * T2;
-  const double Tn = n[0] * T0 + n[1] * T1 + n[2] * T2;
-  const double sg = plus ? 1.0 : -1.0;
-  const double pl = 0.5 * ((1.0 - r) * Zs * vl + sg * (1.0 + r) * Tl);
-  const double pm = 0.5 * ((1.0 - r) * Zs * vm + sg * (1.0 + r) * Tm);
-  const double pn = 0.5 * ((1.0 - r) * Zp * vn + sg * (1.0 + r) * Tn);
-  const double ql = 0.5 * ((1.0 - r) * vl + sg * (1.0 + r) / Zs * Tl);
-  const double qm = 0.5 * ((1.0 - r) * vm + sg * (1.0 + r) / Zs * Tm);
-  const double qn = 0.5 * ((1.0 - r) * vn + sg * (1.0 + r) / Zp * Tn);
-  const double Fx = l[0] * pl + m[0] * pm + n[0] * pn;
-  const double Fy = l[1] * pl + m[1] * pm + n[1] * pn;
-  const double Fz = l[2] * pl + m[2] * pm + n[2] * pn;
-  const double F_x = l[0] * ql + m[0] * qm + n[0] * qn;
-  const double F_y = l[1] * ql + m[1] * qm + n[1] * qn;
-  const double F_z = l[2] * ql + m[2] * qm + n[2] * qn;
+  const R gx = (R)face[9 * nf + f], gy = (R)face[10 * nf + f], gz = (R)face[11 * nf + f];
+  const R lam = (R)face[12 * nf + f], mu = (R)face[13 * nf + f], rho = (R)face[14 * nf + f];
+  const R norm = sqrt(gx * gx + gy * gy + gz * gz);
+  const R cp = sqrt((R(2.0) * mu + lam) / rho), cs = sqrt(mu / rho);
+  const R Zp = rho * cp, Zs = rho * cs;
+  R r, alpha, theta;
+  if (code == 1) { r = R(0.0); alpha = R(2.0); theta = R(0.0); }
+  else if (code == 2) { r = R(1.0); alpha = R(1.0); theta = R(0.0); }
+  else { r = -R(1.0); alpha = R(0.0); theta = plus ? R(1.0) : -R(1.0); }
+  const R T0 = n[0] * u[3] + n[1] * u[6] + n[2] * u[7];
+  const R T1 = n[0] * u[6] + n[1] * u[4] + n[2] * u[8];
+  const R T2 = n[0] * u[7] + n[1] * u[8] + n[2] * u[5];
+  const R vl = l[0] * u[0] + l[1] * u[1] + l[2] * u[2];
+  const R vm = m[0] * u[0] + m[1] * u[1] + m[2] * u[2];
+  const R vn = n[0] * u[0] + n[1] * u[1] + n[2] * u[2];
+  const R Tl = l[0] * T0 + l[1] * T1 + l[2] * T2;
+  const R Tm = m[0] * T0 + m[1] * T1 + m[2] * T2;
+  const R Tn = n[0] * T0 + n[1] * T1 + n[2] * T2;
+  const R sg = plus ? R(1.0) : -R(1.0);
+  const R pl = R(0.5) * ((R(1.0) - r) * Zs * vl + sg * (R(1.0) + r) * Tl);
+  const R pm = R(0.5) * ((R(1.0) - r) * Zs * vm + sg * (R(1.0) + r) * Tm);
+  const R pn = R(0.5) * ((R(1.0) - r) * Zp * vn + sg * (R(1.0) + r) * Tn);
+  const R ql = R(0.5) * ((R(1.0) - r) * vl + sg * (R(1.0) + r) / Zs * Tl);
+  const R qm = R(0.5) * ((R(1.0) - r) * vm + sg * (R(1.0) + r) / Zs * Tm);
+  const R qn = R(0.5) * ((R(1.0) - r) * vn + sg * (R(1.0) + r) / Zp * Tn);
+  const R Fx = l[0] * pl + m[0] * pm + n[0] * pn;
+  const R Fy = l[1] * pl + m[1] * pm + n[1] * pn;
+  const R Fz = l[2] * pl + m[2] * pm + n[2] * pn;
+  const R F_x = l[0] * ql + m[0] * qm + n[0] * qn;
+  const R F_y = l[1] * ql + m[1] * qm + n[1] * qn;
+  const R F_z = l[2] * ql + m[2] * qm + n[2] * qn;
   if (form == BC_WEIGHTED) {
-    const double l2m = lam + 2.0 * mu;
+    const R l2m = lam + R(2.0) * mu;
     ubc[0] = alpha * norm / rho * Fx;
     ubc[1] = alpha * norm / rho * Fy;
     ubc[2] = alpha * norm / rho * Fz;
@@ -217,40 +201,17 @@ __device__ void boundary_sat(const double u[9], const double* __restrict__ face,
   ubc[6] = sg * (norm * (n[1] * F_x + n[0] * F_y));
   ubc[7] = sg * (norm * (n[2] * F_x + n[0] * F_z));
   ubc[8] = sg * (norm * (n[2] * F_y + n[1] * F_z));
-  sat[0] = 1.0 / rho * ubc[0];
-  sat[1] = 1.0 / rho * ubc[1];
-  sat[2] = 1.0 / rho * ubc[2];
-  sat[3] = (2.0 * mu + lam) * ubc[3] + lam * (ubc[4] + ubc[5]);
-  sat[4] = (2.0 * mu + lam) * ubc[4] + lam * (ubc[3] + ubc[5]);
-  sat[5] = (2.0 * mu + lam) * ubc[5] + lam * (ubc[3] + ubc[4]);
+  sat[0] = R(1.0) / rho * ubc[0];
+  sat[1] = R(1.0) / rho * ubc[1];
+  sat[2] = R(1.0) / rho * ubc[2];
+  sat[3] = (R(2.0) * mu + lam) * ubc[3] + lam * (ubc[4] + ubc[5]);
+  sat[4] = (R(2.0) * mu + lam) * ubc[4] + lam * (ubc[3] + ubc[5]);
+  sat[5] = (R(2.0) * mu + lam) * ubc[5] + lam * (ubc[3] + ubc[4]);
   sat[6] = mu * ubc[6];
   sat[7] = mu * ubc[7];
   sat[8] = mu * ubc[8];
 }
 
-
-// ---------------------------------------------------------------------------
-// SBP row lookup shared by every stencil: for a point at 0-based index i of
-// n, entry t (0..8) of its row is weight w at offset off from i.  Central
-// rows use entries 0..5, closure rows all nine (src/JU_xJU_yJU_z6.f90:55-164).
-template <typename T>
-__device__ __forceinline__ void row_entry(int kind, int t, T& w, int& off) {
-  if (kind == 0) {
-    const int k = t < 3 ? 3 - t : t - 2;  // 3,2,1 then 1,2,3
-    const T c = k == 1 ? T(kC1) : (k == 2 ? T(kC2) : T(kC3));
-    w = t < 3 ? -c : c;
-    off = t < 3 ? -k : k;
-    if (t > 5) { w = T(0); off = 0; }
-  } else if (kind < 0) {  // left closure row i = -kind-1, columns are points 0..8
-    const int i = -kind - 1;
-    w = sbp_w<T>(i, t);
-    off = t - i;
-  } else {  // right closure row k = n-1-i, columns are points n-1..n-9
-    const int k = kind - 1;
-    w = -sbp_w<T>(k, t);
-    off = k - t;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Main stencil kernel (2.5-D tiled).  Computes, for every point of the block,
@@ -285,22 +246,6 @@ struct Tile {
   }
 };
 
-struct TileSpan {
-  int origin, own_lo, own_hi;
-};
-__device__ __forceinline__ TileSpan tile_span(int t, int n, int T_) {
-  const int ntiles = (n + T_ - 1) / T_;
-  TileSpan sp;
-  if (n <= T_) {
-    sp.origin = 0; sp.own_lo = 0; sp.own_hi = n;
-  } else if (t == ntiles - 1) {
-    sp.origin = n - T_; sp.own_lo = n - T_; sp.own_hi = n;
-  } else {
-    sp.origin = t * T_; sp.own_lo = t * T_; sp.own_hi = min((t + 1) * T_, n - T_);
-  }
-  return sp;
-}
-
 template <typename T, bool CURV, bool KAHAN, int TQ, int TR, int MINB>
 __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __grid_constant__ VolumeArgs<T> a,
                                                                        int schunk) {
@@ -310,7 +255,7 @@ __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __gr
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int nq = a.nq, nr = a.nr, ns = a.ns;
   const long long np = a.np;
-  const long long sts = (long long)nq * nr;
+  const long long sts = (long long)a.pq * nr;
   const TileSpan spq = tile_span(blockIdx.x, nq, TQ), spr = tile_span(blockIdx.y, nr, TR);
   const int q0 = spq.origin, r0 = spr.origin;
   const int q = q0 + tx, r = r0 + ty;
@@ -322,7 +267,7 @@ __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __gr
   const T* __restrict__ coef = a.coef;
   const int lq = tx + 3, lr = ty + 3;
   const int kq = sbp_kind(q, nq), kr = sbp_kind(r, nr);
-  const long long col = q + (long long)nq * r;
+  const long long col = q + (long long)a.pq * r;
   int lo = 0, hi = -1;  // planes held by the ring (uniform across the CTA)
 
   for (int s = s_begin; s < s_end; ++s) {
@@ -349,7 +294,7 @@ __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __gr
     // ---- stage the plane's cross region into shared memory
     __syncthreads();
     auto stage = [&](int gq, int gr, int lq_, int lr_, bool wq, bool wr) {
-      const long long pp = gq + (long long)nq * gr + sts * s;
+      const long long pp = gq + (long long)a.pq * gr + sts * s;
       T f[9];
 #pragma unroll
       for (int c = 0; c < 9; ++c) f[c] = F[c * np + pp];
@@ -495,18 +440,20 @@ __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __gr
 
 // Per-point form of the same stencil kernel: every neighbour value is read
 // through L1/L2 (kept for cross-checks of the tiled kernel).
+// smode 1 restricts it to the 12 s-boundary planes (grid z = 12), the part
+// the TMA kernel leaves out.
 template <typename T, bool CURV, bool KAHAN>
-__global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_constant__ VolumeArgs<T> a) {
+__global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_constant__ VolumeArgs<T> a, int smode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int k = smode ? (blockIdx.z < 6 ? (int)blockIdx.z : a.ns - 12 + (int)blockIdx.z) : (int)blockIdx.z;
   if (i >= a.nq || j >= a.nr) return;
   const long long np = a.np;
-  const long long p = i + (long long)a.nq * (j + (long long)a.nr * k);
+  const long long p = i + (long long)a.pq * (j + (long long)a.nr * k);
   T g[3][3], dv[3];
   const T Jinv = CURV ? a.coef[9 * np + p] : T(1);
   const int idx[3] = {i, j, k}, nn[3] = {a.nq, a.nr, a.ns};
-  const long long st[3] = {1, a.nq, (long long)a.nq * a.nr};
+  const long long st[3] = {1, a.pq, (long long)a.pq * a.nr};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     T o[6];
@@ -605,8 +552,8 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
   }
   if (!any) return;
   const long long np = a.np;
-  const long long p = i + (long long)nq * (j + (long long)nr * k);
-  const long long st[3] = {1, nq, (long long)nq * nr};
+  const long long p = i + (long long)a.pq * (j + (long long)nr * k);
+  const long long st[3] = {1, a.pq, (long long)a.pq * nr};
   const T* __restrict__ F = a.Fin;
   const T* __restrict__ coef = a.coef;
   // velocity gradient at the point
@@ -696,8 +643,8 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
     for (int c = 0; c < 9; ++c) dq[c] = a.A * DQ[c * snp + sp] + src[c] - (damp + cfs) * qv[c];
     const bool on_face = hi ? (ii == n - 1) : (ii == 0);
     if (on_face && a.bc[side] >= 1 && a.bc[side] <= 3) {
-      double u[9], sat[9], ubc[9];
-      for (int c = 0; c < 9; ++c) u[c] = (double)F[c * np + p];
+      T u[9], sat[9], ubc[9];
+      for (int c = 0; c < 9; ++c) u[c] = F[c * np + p];
       const int na = axis == 0 ? nr : nq;
       const long long f = axis == 0 ? (j + (long long)nr * k) : (axis == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
       const long long nf = (long long)na * (axis == 2 ? nr : ns);
@@ -742,12 +689,12 @@ __global__ void __launch_bounds__(256) face_kernel(const __grid_constant__ Volum
     if (idx[ax2] == ((s2 & 1) ? nn[ax2] - 1 : 0)) return;
   }
   const long long np = a.np;
-  const long long p = i + (long long)nq * (j + (long long)nr * k);
-  double tot[9];
-  for (int c = 0; c < 9; ++c) tot[c] = 0.0;
+  const long long p = i + (long long)a.pq * (j + (long long)nr * k);
+  T tot[9];
+  for (int c = 0; c < 9; ++c) tot[c] = T(0);
   bool any = false;
-  double u[9];
-  for (int c = 0; c < 9; ++c) u[c] = (double)a.Fin[c * np + p];
+  T u[9];
+  for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
   for (int s2 = 0; s2 < 6; ++s2) {
     const int code = a.bc[s2];
     if (code < 1 || code > 3) continue;
@@ -757,13 +704,13 @@ __global__ void __launch_bounds__(256) face_kernel(const __grid_constant__ Volum
     const int na = ax2 == 0 ? nr : nq;
     const long long nf = (long long)na * (ax2 == 2 ? nr : ns);
     const long long f = ax2 == 0 ? (j + (long long)nr * k) : (ax2 == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
-    double sat[9], ubc[9];
+    T sat[9], ubc[9];
     boundary_sat(u, a.face[s2], nf, f, code, hi, a.bc_form, sat, ubc);
-    for (int c = 0; c < 9; ++c) tot[c] += (double)a.tau_h[ax2] * sat[c];
+    for (int c = 0; c < 9; ++c) tot[c] += a.tau_h[ax2] * sat[c];
     any = true;
   }
   T corr[9];
-  for (int c = 0; c < 9; ++c) corr[c] = (T)(-tot[c]);
+  for (int c = 0; c < 9; ++c) corr[c] = -tot[c];
   if (a.fault_sat && ((a.block == 0 && i == nq - 1) || (a.block == 1 && i == 0))) {
     const long long nf = (long long)nr * ns;
     const long long f = j + (long long)nr * k;
@@ -789,7 +736,7 @@ __global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ Vo
     if (a.pml[2 * ax + 1] && idx[ax] >= nn[ax] - a.npml) return;
   }
   const long long np = a.np;
-  const long long p = i + (long long)a.nq * (j + (long long)a.nr * k);
+  const long long p = i + (long long)a.pq * (j + (long long)a.nr * k);
   double xs[3] = {0.0, (double)a.ycoord[p], 0.0}, s0[6];
   if (!initial_stress(a.preset, xs, s0))
     for (int c = 0; c < 6; ++c) s0[c] = a.s0u[c];
@@ -829,21 +776,39 @@ void launch_tiled(const VolumeArgs<T>& a, cudaStream_t s) {
 }
 
 // Stencil-kernel variants (the tuning table): 1 per-point, 2 tiled 32x8 at
-// 1 CTA/SM, 3 tiled 32x8 at 3 CTAs/SM in FP32, 4 tiled 64x8 at 1 CTA/SM;
-// 0 picks the fastest measured on a 2 x 201^3 curvilinear block pair
-// (per-point in FP32, tiled 32x8 in FP64).
+// 1 CTA/SM, 3 tiled 32x8 at 3 CTAs/SM in FP32, 4 tiled 64x8 at 1 CTA/SM,
+// 5 TMA-pipelined (FP32) with 3 stages, 6 the same with 2; 0 picks the
+// fastest measured on a 2 x 201^3 curvilinear block pair (TMA in FP32,
+// tiled 32x8 in FP64).
+//
+// A tiled axis of n points with tiles of T keeps every closure row inside
+// the tile that owns it plus a 3-point halo unless the shifted last tile
+// starts at 4 or 5 (then it would own left closure rows whose stencil
+// reaches point 0 from outside the halo); such sizes run per point.
+inline bool tiles_ok(int n, int T) { return n <= T + 3 || n >= T + 6; }
+
 template <typename T, bool CURV, bool KAHAN>
 void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
   constexpr bool f32 = sizeof(T) == 4;
-  const int v = a.kernel != 0 ? a.kernel : (f32 ? 1 : 2);
+  int v = a.kernel != 0 ? a.kernel : (f32 ? 5 : 2);
+  if ((v == 5 || v == 6) && !tiles_ok(a.nr, kTmaTR)) v = 1;
+  if ((v == 2 || v == 3) && !(tiles_ok(a.nq, 32) && tiles_ok(a.nr, 8))) v = 1;
+  if (v == 4 && !(tiles_ok(a.nq, 64) && tiles_ok(a.nr, 8))) v = 1;
   switch (v) {
     case 1: {
       dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
-      stencil_kernel_pointwise<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a);
+      stencil_kernel_pointwise<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a, 0);
       return;
     }
     case 3: launch_tiled<T, CURV, KAHAN, 32, 8, f32 ? 3 : 1>(a, s); return;
     case 4: launch_tiled<T, CURV, KAHAN, 64, 8, 1>(a, s); return;
+    case 5:
+    case 6:
+      if constexpr (f32) {
+        launch_stencil_tma(a, CURV, KAHAN, v == 6 ? 2 : 3, s);
+        return;
+      }
+      [[fallthrough]];
     default: launch_tiled<T, CURV, KAHAN, 32, 8, 1>(a, s); return;
   }
 }

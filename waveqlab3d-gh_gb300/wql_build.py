@@ -15,7 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwql.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["wql_api.cu", "wql_setup.cu", "wql_volume.cu", "wql_interface.cu"]
+CU = ["wql_api.cu", "wql_setup.cu", "wql_volume.cu", "wql_stencil_tma.cu", "wql_interface.cu"]
 CPP = ["host/wql_input.cpp", "host/wql_grid.cpp"]
 HEADERS = ["wql_internal.h", "wql_sbp.cuh", "wql_presets.cuh", "host/wql_input.h",
            "host/wql_grid.h", os.path.join("..", "..", "include", "wql.h")]
