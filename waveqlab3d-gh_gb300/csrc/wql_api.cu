@@ -614,6 +614,10 @@ int run_step(wql_scn* S) {
     ia.A = A; ia.Bdt = Bdt; ia.t = ts; ia.stage = stage;
     ia.pre = S->pre;
     ia.ramp = nucleation_ramp(S->fp, ts);
+    {
+      const double x0[3] = {0.0, 0.0, 0.0};  // V0 does not vary along the fault
+      ia.lnV0h = std::log(0.5 / rs_params(S->fp, x0, 0.0).V0);
+    }
     ia.fp = S->fp;
     ia.frame = (want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
     ia.solver_fail = S->solver_fail;
@@ -627,6 +631,10 @@ int run_step(wql_scn* S) {
     launches += 1;
     if (S->profiling) mark_end();
     for (int b = 0; b < 2; ++b) {
+      if (S->profiling) mark(2);
+      if (S->prec == WQL_FP64) launches += launch_pre<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->stream);
+      else launches += launch_pre<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->stream);
+      if (S->profiling) mark_end();
       if (S->profiling) mark(1);
       if (S->prec == WQL_FP64) launch_volume<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       else launch_volume<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);

@@ -58,29 +58,46 @@ __device__ bool regula_falsi(double& V, double Phi, double eta, double sn, doubl
 }
 
 // The same equation for FP32 fields, by Newton's method in u = ln V.  With
-// s = V/(2V0)*exp(psi/a), g(u) = e^u + c*asinh(s) - Phi/eta is increasing and
-// convex in u (d asinh(s)/du = s/sqrt(1+s^2) grows with u), so Newton iterates
-// clamped to u <= ln(Phi/eta) (where g >= 0) decrease monotonically to the
-// root after at most one step from the left.  The iteration runs in FP32 on
-// w = ln s (asinh(e^w) = w + ln 2 for large w, e^w for very negative w, so
-// nothing overflows although exp(psi/a) exceeds the FP32 range) until the
-// step is at the FP32 resolution of u, then in FP64 until the step is below
-// 1e-9 (quadratic convergence: V is then accurate far below the regula
-// falsi's 1e-12 tolerance).  Returns false if it does not converge.
-__device__ bool newton_mixed(double& V, double Phi, double eta, double sn, double psi, double V0, double a) {
+// s = V/(2V0)*exp(psi/a) = exp(w), w = u + ln(exp(psi/a)/(2V0)), the function
+// g(u) = e^u + c*asinh(s) - Phi/eta is increasing and convex in u
+// (d asinh(s)/du = s/sqrt(1+s^2) grows with u), so Newton iterates clamped to
+// u <= ln(Phi/eta) (where g >= 0) decrease monotonically to the root after at
+// most one step from the left.  asinh(e^w) is evaluated as w + ln 2 for
+// w > 20 and as e^w for w < -20 (relative error below 1e-17 in both), so
+// nothing overflows although exp(psi/a) exceeds the FP32 range.  The
+// iteration runs in FP32 until the step is below 1e-4 (relative to u; the
+// FP32 residual cannot resolve much less), then two FP64 Newton steps square
+// the remaining error twice (1e-4 -> 1e-8 -> 1e-16).  Returns false when the
+// second FP64 step is still above 1e-9.
+__device__ __forceinline__ void asinh_exp(double w, double& A, double& dA) {
+  if (w > 20.0) {
+    A = w + 0.69314718055994531;
+    dA = 1.0;
+  } else if (w < -20.0) {
+    A = exp(w);
+    dA = A;
+  } else {
+    const double sw = exp(w);
+    A = asinh(sw);
+    dA = sw / sqrt(1.0 + sw * sw);
+  }
+}
+
+__device__ bool newton_mixed(double& V, double Phi, double eta, double sn, double psi, double V0, double a,
+                             double lnV0h) {
   const double target = Phi / eta;
   if (!(target > 0.0)) {
     V = 0.0;
     return true;
   }
   const double c = a * sn / eta;
-  const float tf = (float)target, cf = (float)c;
-  const float lek = (float)(psi / a) + logf(0.5f / (float)V0);
+  const double L = psi / a + lnV0h;  // ln(exp(psi/a)/(2 V0))
+  const float tf = (float)target, cf = (float)c, Lf = (float)L;
   const float uhi = logf(tf);
   const float vf = (float)V;
   float u = vf > 0.0f ? fminf(logf(vf), uhi) : uhi;
   for (int it = 0; it < 40; ++it) {
-    const float w = u + lek;
+    const float w = u + Lf;
     const float v = expf(u);
     float A, dA;
     if (w > 20.0f) {
@@ -97,24 +114,18 @@ __device__ bool newton_mixed(double& V, double Phi, double eta, double sn, doubl
     const float un = fminf(u - (v + cf * A - tf) / (v + cf * dA), uhi);
     const float du = un - u;
     u = un;
-    if (fabsf(du) <= 4.0e-7f * fmaxf(1.0f, fabsf(u))) break;
+    if (fabsf(du) <= 1.0e-4f * fmaxf(1.0f, fabsf(u))) break;
   }
-  const double ek = 0.5 / V0 * exp(psi / a);
-  double ud = (double)u;
-  for (int it = 0; it < 8; ++it) {
+  double ud = (double)u, du = 0.0;
+  for (int it = 0; it < 2; ++it) {
     const double v = exp(ud);
-    const double sd = ek * v;
-    const double g = v + c * asinh(sd) - target;
-    const double ds = sd > 1.0 ? 1.0 / sqrt(1.0 + 1.0 / (sd * sd)) : sd / sqrt(1.0 + sd * sd);
-    const double du = -g / (v + c * ds);
+    double A, dA;
+    asinh_exp(ud + L, A, dA);
+    du = -(v + c * A - target) / (v + c * dA);
     ud += du;
-    if (fabs(du) <= 1.0e-9) {
-      V = exp(ud);
-      return true;
-    }
   }
   V = exp(ud);
-  return false;
+  return fabs(du) <= 1.0e-9 * fmax(1.0, fabs(ud));
 }
 
 template <typename T>
@@ -255,7 +266,7 @@ __global__ void interface_kernel(const __grid_constant__ InterfaceArgs a) {
       double V = sqrt(d1 * d1 + d2 * d2);
       if (V > Phi) V = 0.5 * Phi / es;
       const bool ok = F64 ? regula_falsi(V, Phi, es, sn, psi, rs.V0, rs.a)
-                          : newton_mixed(V, Phi, es, sn, psi, rs.V0, rs.a);
+                          : newton_mixed(V, Phi, es, sn, psi, rs.V0, rs.a, a.lnV0h);
       if (!ok && a.solver_fail) atomicAdd(a.solver_fail, 1u);
       if (F64) {
         const double fv = sn * rs.a * asinh(0.5 * V / rs.V0 * exp(psi / rs.a));

@@ -89,6 +89,7 @@ struct InterfaceArgs {
   void* sat;                // 2 x 9 x nf (T), scaled by tau0/h of the block
   const double* pre;        // 2 x 5 x nf: static Tn, Tm, Tl, nucleation weight, rate-state a
   double ramp;              // nucleation ramp at this stage's time
+  double lnV0h;             // ln(1/(2 V0)) of the rate-and-state law
   double tau_h[2];
   double A, Bdt, t;
   int stage;
@@ -131,6 +132,11 @@ void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int s
 // boundary/fault penalty and plastic kernels and returns how many it issued.
 template <typename T>
 void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream);
+// Before the stencil kernel of a variant without its own face pass: the
+// boundary and fault penalties folded into DF of the face points.  Returns
+// the number of launches.
+template <typename T>
+int launch_pre(const VolumeArgs<T>& a, void* stream);
 template <typename T>
 int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream);
 void launch_interface(const InterfaceArgs& a, void* stream);

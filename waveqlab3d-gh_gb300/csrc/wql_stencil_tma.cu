@@ -5,6 +5,10 @@
 // src/JU_xJU_yJU_z6.f90:12-812 and 16141-16449, src/RHS_Interior.f90:133-274)
 // on every plane of the block.
 //
+// The boundary and fault penalties of the face points (src/RHS_Interior.f90:
+// 1516-1703, 1757-1772) are folded into DF beforehand by the face
+// pre-kernel, so this kernel has no face-dependent work.
+//
 // A CTA owns a 32 x 8 (q, r) tile and marches along a chunk of s planes.  One
 // producer thread streams each plane into shared memory with
 // cp.async.bulk.tensor (TMA) through an NS-deep ring of stages guarded by
@@ -35,6 +39,8 @@
 // copies it issued).
 #include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "wql_internal.h"
 #include "wql_stencil.cuh"
@@ -182,6 +188,7 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
       mbar_init(&empty[i], NCW);
     }
     mbar_init(fluxbar, NC);
+
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -435,10 +442,15 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
       du[6] = mu * (g[0][1] + g[1][0]);
       du[7] = mu * (g[0][2] + g[2][0]);
       du[8] = mu * (g[1][2] + g[2][1]);
+      // the face pre-kernel has folded the boundary and fault penalties
+      // into DF of the face points: DF - tot/A, or -tot on the first stage
+      // (A = 0, where DF holds nothing else)
+      const bool face = q == 0 || q == nq - 1 || r == 0 || r == nr - 1 || s == 0 || s == ns - 1;
 #pragma unroll
       for (int c = 0; c < 9; ++c) {
         const float f0 = fb(c, lr, lq);
-        const float df = a.A * S[TL::OFF_DF + c * NC + ty * TQ + tx] + du[c];
+        const float dfs = S[TL::OFF_DF + c * NC + ty * TQ + tx];
+        const float df = a.A != 0.0f ? a.A * dfs + du[c] : (face ? dfs : 0.0f) + du[c];
         a.DF[c * np + p] = df;
         if (KAHAN) {
           const float y = a.Bdt * df - S[TL::OFF_CK + c * NC + ty * TQ + tx];
@@ -460,6 +472,7 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
 #pragma unroll
       for (int c = 0; c < 6; ++c) qv[i][c] = qv[i + 1][c];
   }
+
 }
 
 template <bool CURV, bool KAHAN, int NS>
@@ -476,29 +489,12 @@ void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t 
   const int tq = (a.nq + TL::TQ - 1) / TL::TQ, tr = (a.nr + TL::TR - 1) / TL::TR;
   int schunk = a.schunk;
   if (schunk <= 0) {
-    // choose the number of s chunks (2..24) that wastes the least of the
-    // last wave of CTAs (one CTA per SM)
-    static int nsm = 0;
-    if (!nsm) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      if (nsm <= 0) nsm = 1;
-    }
-    double best = 1e30;
-    schunk = ncen;
-    for (int nc = 2; nc <= 24; ++nc) {
-      const int sc = (ncen + nc - 1) / nc;
-      const int nchunk = (ncen + sc - 1) / sc;
-      const long long ctas = (long long)tq * tr * nchunk;
-      const long long waves = (ctas + nsm - 1) / nsm;
-      // time ~ waves x (planes per chunk + about one step of prologue)
-      const double cost = (double)waves * (sc + 1);
-      if (cost < best) {
-        best = cost;
-        schunk = sc;
-      }
-    }
+    // about 24 planes per chunk, equal chunks: measured on 2 x 201^3 blocks,
+    // shorter chunks balance the SMs better than fewer waves do, down to
+    // where the per-chunk start (the first six planes of the s window)
+    // shows
+    const int nc = std::max(1, (ncen + 12) / 24);
+    schunk = (ncen + nc - 1) / nc;
   }
   MapArgs m;
   m.fbox = sm.fbox[sm.cur];

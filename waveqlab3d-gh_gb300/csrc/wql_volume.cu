@@ -132,85 +132,6 @@ __device__ void diff_pml_flux(const T* __restrict__ F, const T* __restrict__ coe
   }
 }
 
-// Characteristic boundary forcing (BCm / BCp), src/BoundaryConditions.f90:777-918,
-// followed by structure() (src/RHS_Interior.f90:2203-2223); or the weighted
-// alpha/theta form of src/BoundaryConditions3.f90:777-903 added directly.
-// Returns sat (added to DF with -tau/h) and ubc (added to DQ in a PML).
-template <typename R>
-__device__ void boundary_sat(const R u[9], const double* __restrict__ face, long long nf, long long f, int code,
-                             bool plus, int form, R sat[9], R ubc[9]) {
-  R n[3], m[3], l[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    n[c] = (R)face[(0 + c) * nf + f];
-    m[c] = (R)face[(3 + c) * nf + f];
-    l[c] = (R)face[(6 + c) * nf + f];
-  }
-  const R gx = (R)face[9 * nf + f], gy = (R)face[10 * nf + f], gz = (R)face[11 * nf + f];
-  const R lam = (R)face[12 * nf + f], mu = (R)face[13 * nf + f], rho = (R)face[14 * nf + f];
-  const R norm = sqrt(gx * gx + gy * gy + gz * gz);
-  const R cp = sqrt((R(2.0) * mu + lam) / rho), cs = sqrt(mu / rho);
-  const R Zp = rho * cp, Zs = rho * cs;
-  R r, alpha, theta;
-  if (code == 1) { r = R(0.0); alpha = R(2.0); theta = R(0.0); }
-  else if (code == 2) { r = R(1.0); alpha = R(1.0); theta = R(0.0); }
-  else { r = -R(1.0); alpha = R(0.0); theta = plus ? R(1.0) : -R(1.0); }
-  const R T0 = n[0] * u[3] + n[1] * u[6] + n[2] * u[7];
-  const R T1 = n[0] * u[6] + n[1] * u[4] + n[2] * u[8];
-  const R T2 = n[0] * u[7] + n[1] * u[8] + n[2] * u[5];
-  const R vl = l[0] * u[0] + l[1] * u[1] + l[2] * u[2];
-  const R vm = m[0] * u[0] + m[1] * u[1] + m[2] * u[2];
-  const R vn = n[0] * u[0] + n[1] * u[1] + n[2] * u[2];
-  const R Tl = l[0] * T0 + l[1] * T1 + l[2] * T2;
-  const R Tm = m[0] * T0 + m[1] * T1 + m[2] * T2;
-  const R Tn = n[0] * T0 + n[1] * T1 + n[2] * T2;
-  const R sg = plus ? R(1.0) : -R(1.0);
-  const R pl = R(0.5) * ((R(1.0) - r) * Zs * vl + sg * (R(1.0) + r) * Tl);
-  const R pm = R(0.5) * ((R(1.0) - r) * Zs * vm + sg * (R(1.0) + r) * Tm);
-  const R pn = R(0.5) * ((R(1.0) - r) * Zp * vn + sg * (R(1.0) + r) * Tn);
-  const R ql = R(0.5) * ((R(1.0) - r) * vl + sg * (R(1.0) + r) / Zs * Tl);
-  const R qm = R(0.5) * ((R(1.0) - r) * vm + sg * (R(1.0) + r) / Zs * Tm);
-  const R qn = R(0.5) * ((R(1.0) - r) * vn + sg * (R(1.0) + r) / Zp * Tn);
-  const R Fx = l[0] * pl + m[0] * pm + n[0] * pn;
-  const R Fy = l[1] * pl + m[1] * pm + n[1] * pn;
-  const R Fz = l[2] * pl + m[2] * pm + n[2] * pn;
-  const R F_x = l[0] * ql + m[0] * qm + n[0] * qn;
-  const R F_y = l[1] * ql + m[1] * qm + n[1] * qn;
-  const R F_z = l[2] * ql + m[2] * qm + n[2] * qn;
-  if (form == BC_WEIGHTED) {
-    const R l2m = lam + R(2.0) * mu;
-    ubc[0] = alpha * norm / rho * Fx;
-    ubc[1] = alpha * norm / rho * Fy;
-    ubc[2] = alpha * norm / rho * Fz;
-    ubc[3] = theta * norm * (l2m * n[0] * F_x + lam * (n[1] * F_y + n[2] * F_z));
-    ubc[4] = theta * norm * (l2m * n[1] * F_y + lam * (n[0] * F_x + n[2] * F_z));
-    ubc[5] = theta * norm * (l2m * n[2] * F_z + lam * (n[0] * F_x + n[1] * F_y));
-    ubc[6] = theta * mu * norm * (n[1] * F_x + n[0] * F_y);
-    ubc[7] = theta * mu * norm * (n[2] * F_x + n[0] * F_z);
-    ubc[8] = theta * mu * norm * (n[2] * F_y + n[1] * F_z);
-#pragma unroll
-    for (int c = 0; c < 9; ++c) sat[c] = ubc[c];
-    return;
-  }
-  ubc[0] = norm * Fx;
-  ubc[1] = norm * Fy;
-  ubc[2] = norm * Fz;
-  ubc[3] = sg * (norm * n[0] * F_x);
-  ubc[4] = sg * (norm * n[1] * F_y);
-  ubc[5] = sg * (norm * n[2] * F_z);
-  ubc[6] = sg * (norm * (n[1] * F_x + n[0] * F_y));
-  ubc[7] = sg * (norm * (n[2] * F_x + n[0] * F_z));
-  ubc[8] = sg * (norm * (n[2] * F_y + n[1] * F_z));
-  sat[0] = R(1.0) / rho * ubc[0];
-  sat[1] = R(1.0) / rho * ubc[1];
-  sat[2] = R(1.0) / rho * ubc[2];
-  sat[3] = (R(2.0) * mu + lam) * ubc[3] + lam * (ubc[4] + ubc[5]);
-  sat[4] = (R(2.0) * mu + lam) * ubc[4] + lam * (ubc[3] + ubc[5]);
-  sat[5] = (R(2.0) * mu + lam) * ubc[5] + lam * (ubc[3] + ubc[4]);
-  sat[6] = mu * ubc[6];
-  sat[7] = mu * ubc[7];
-  sat[8] = mu * ubc[8];
-}
 
 
 // ---------------------------------------------------------------------------
@@ -509,27 +430,6 @@ __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_con
   }
 }
 
-// Adds corr to DF and B*dt*corr to the updated field of one point
-// (compensated in FP32C).
-template <typename T, bool KAHAN>
-__device__ __forceinline__ void add_correction(const VolumeArgs<T>& a, long long p, const T (&corr)[9]) {
-  const long long np = a.np;
-#pragma unroll
-  for (int c = 0; c < 9; ++c) {
-    if (corr[c] == T(0)) continue;
-    a.DF[c * np + p] += corr[c];
-    const T f0 = a.Fout[c * np + p];
-    if (KAHAN) {
-      const T y = a.Bdt * corr[c] - a.C[c * np + p];
-      const T t = f0 + y;
-      a.C[c * np + p] = (t - f0) - y;
-      a.Fout[c * np + p] = t;
-    } else {
-      a.Fout[c * np + p] = f0 + a.Bdt * corr[c];
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // PML kernel (src/RHS_Interior.f90:1782-2201, src/fields.f90:70-105,131-166):
 // for every point inside one or more active slabs, the damping terms of the
@@ -690,34 +590,56 @@ __global__ void __launch_bounds__(256) face_kernel(const __grid_constant__ Volum
   }
   const long long np = a.np;
   const long long p = i + (long long)a.pq * (j + (long long)nr * k);
-  T tot[9];
-  for (int c = 0; c < 9; ++c) tot[c] = T(0);
-  bool any = false;
-  T u[9];
+  T u[9], tot[9], corr[9];
   for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
-  for (int s2 = 0; s2 < 6; ++s2) {
-    const int code = a.bc[s2];
-    if (code < 1 || code > 3) continue;
-    const int ax2 = s2 >> 1;
-    const bool hi = s2 & 1;
-    if (idx[ax2] != (hi ? nn[ax2] - 1 : 0)) continue;
-    const int na = ax2 == 0 ? nr : nq;
-    const long long nf = (long long)na * (ax2 == 2 ? nr : ns);
-    const long long f = ax2 == 0 ? (j + (long long)nr * k) : (ax2 == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));
-    T sat[9], ubc[9];
-    boundary_sat(u, a.face[s2], nf, f, code, hi, a.bc_form, sat, ubc);
-    for (int c = 0; c < 9; ++c) tot[c] += a.tau_h[ax2] * sat[c];
-    any = true;
-  }
-  T corr[9];
+  const bool any = face_penalty(a, i, j, k, u, tot);
   for (int c = 0; c < 9; ++c) corr[c] = -tot[c];
-  if (a.fault_sat && ((a.block == 0 && i == nq - 1) || (a.block == 1 && i == 0))) {
-    const long long nf = (long long)nr * ns;
-    const long long f = j + (long long)nr * k;
-    for (int c = 0; c < 9; ++c) corr[c] -= a.fault_sat[c * nf + f];
-    any = true;
-  }
   if (any) add_correction<T, KAHAN>(a, p, corr);
+}
+
+// ---------------------------------------------------------------------------
+// Face pre-kernel (for the stencil variant without a face pass): the
+// boundary and fault penalty tot of each face point (face_penalty, as in the
+// face kernel) folded into the rates before the stencil kernel runs,
+// DF <- DF - tot/A, or DF <- -tot on a stage with A = 0, so that the
+// stencil's A*DF + du (or DF + du on face points when A = 0) carries it.
+// One thread per face point, a point on several faces taken by its lowest
+// side.
+template <typename T>
+__global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  const int nq = a.nq, nr = a.nr, ns = a.ns;
+  const long long nfs[6] = {(long long)nr * ns, (long long)nr * ns, (long long)nq * ns, (long long)nq * ns,
+                            (long long)nq * nr, (long long)nq * nr};
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int side = 0;
+  while (side < 6 && t >= nfs[side]) {
+    t -= nfs[side];
+    ++side;
+  }
+  if (side >= 6) return;
+  const int axis = side >> 1;
+  const int w = axis == 0 ? nr : nq;
+  const int c1 = (int)(t % w), c2 = (int)(t / w);
+  int i, j, k;
+  if (axis == 0) { i = (side & 1) ? nq - 1 : 0; j = c1; k = c2; }
+  else if (axis == 1) { i = c1; j = (side & 1) ? nr - 1 : 0; k = c2; }
+  else { i = c1; j = c2; k = (side & 1) ? ns - 1 : 0; }
+  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
+  for (int s2 = 0; s2 < side; ++s2) {
+    const int ax2 = s2 >> 1;
+    if (idx[ax2] == ((s2 & 1) ? nn[ax2] - 1 : 0)) return;
+  }
+  const long long np = a.np;
+  const long long p = i + (long long)a.pq * (j + (long long)nr * k);
+  T u[9], tot[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
+  if (!face_penalty(a, i, j, k, u, tot)) return;
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    T* df = a.DF + c * np + p;
+    *df = a.A != T(0) ? *df - tot[c] / a.A : -tot[c];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -787,13 +709,28 @@ void launch_tiled(const VolumeArgs<T>& a, cudaStream_t s) {
 // reaches point 0 from outside the halo); such sizes run per point.
 inline bool tiles_ok(int n, int T) { return n <= T + 3 || n >= T + 6; }
 
-template <typename T, bool CURV, bool KAHAN>
-void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
+template <typename T>
+int effective_variant(const VolumeArgs<T>& a) {
   constexpr bool f32 = sizeof(T) == 4;
   int v = a.kernel != 0 ? a.kernel : (f32 ? 5 : 2);
+  if ((v == 5 || v == 6) && !f32) v = 2;
   if ((v == 5 || v == 6) && !tiles_ok(a.nr, kTmaTR)) v = 1;
   if ((v == 2 || v == 3) && !(tiles_ok(a.nq, 32) && tiles_ok(a.nr, 8))) v = 1;
   if (v == 4 && !(tiles_ok(a.nq, 64) && tiles_ok(a.nr, 8))) v = 1;
+  return v;
+}
+
+// The TMA kernel applies the boundary and fault penalties itself.
+template <typename T>
+bool stencil_has_faces(const VolumeArgs<T>& a) {
+  const int v = effective_variant(a);
+  return v == 5 || v == 6;
+}
+
+template <typename T, bool CURV, bool KAHAN>
+void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
+  constexpr bool f32 = sizeof(T) == 4;
+  const int v = effective_variant(a);
   switch (v) {
     case 1: {
       dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
@@ -821,9 +758,11 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
     pml_kernel<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a);
     ++n;
   }
-  const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
-  face_kernel<T, KAHAN><<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(a);
-  ++n;
+  if (!stencil_has_faces(a)) {
+    const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
+    face_kernel<T, KAHAN><<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(a);
+    ++n;
+  }
   if (a.plastic) {
     plastic_kernel<T, KAHAN><<<grd, blk, 0, s>>>(a);
     ++n;
@@ -840,6 +779,14 @@ void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream) {
 }
 
 template <typename T>
+int launch_pre(const VolumeArgs<T>& a, void* stream) {
+  if (!stencil_has_faces(a)) return 0;
+  const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
+  face_pre_kernel<T><<<(unsigned)((nface + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a);
+  return 1;
+}
+
+template <typename T>
 int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   const bool kahan = a.C != nullptr;
@@ -850,6 +797,8 @@ int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream) {
 template void launch_volume<double>(const VolumeArgs<double>&, bool, void*);
 template void launch_volume<float>(const VolumeArgs<float>&, bool, void*);
 template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
+template int launch_pre<double>(const VolumeArgs<double>&, void*);
+template int launch_pre<float>(const VolumeArgs<float>&, void*);
 template int launch_corrections<float>(const VolumeArgs<float>&, bool, void*);
 
 }  // namespace wql
