@@ -106,6 +106,18 @@ int wql_get_info(wql_scn* scn, wql_info* info);
 int wql_get_field(wql_scn* scn, int block, int comp, double* host_out);
 int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in);
 
+/* wql_get_field without any device allocation, for callers that must not
+ * allocate device memory (cudaMalloc/cudaFree synchronise the whole device,
+ * so a monitoring thread reading a scenario would stall other threads'
+ * streams; a memory-capped host may have no room left).  FP32 fields are
+ * widened one s plane at a time through a fixed 8 MiB device array; a block
+ * whose pitched plane (pq*nr, pq = nq rounded up to a multiple of 4)
+ * exceeds 1048576 points returns WQL_E_INPUT.  The first call on a device
+ * resolves the array's address and must not happen during stream capture.
+ * The array is shared by all calls on a device: calls that overlap in time
+ * race.  No counterpart in the reference. */
+int wql_get_field_noalloc(wql_scn* scn, int block, int comp, double* host_out);
+
 /* Interface state of block copy (0/1): what 0..3 = S(1..4), 4 = W, 5 = trup;
  * nr*ns values (src/iface.f90:13-49). */
 int wql_get_iface(wql_scn* scn, int copy, int what, double* host_out);

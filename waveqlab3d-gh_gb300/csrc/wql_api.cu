@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -796,6 +797,74 @@ int wql_get_field(wql_scn* scn, int block, int comp, double* host_out) {
                     cudaMemcpyDeviceToHost));
     cudaFree(tmp);
   }
+  return WQL_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Allocation-free field read: FP32 planes are widened through this fixed
+// device array instead of a cudaMalloc'd temporary.  One s plane of pq*nr
+// pitched points at a time; nothing in it needs to start at zero (each
+// plane is written in full before it is copied out).
+constexpr long long kPlaneScratchWords = 1LL << 20;  // 8 MiB of doubles
+static __device__ __align__(256) double g_plane_scratch[kPlaneScratchWords];
+
+__global__ void widen_plane(const float* __restrict__ src, double* __restrict__ dst, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i];
+}
+
+// Device address of the scratch, resolved once per device with that device
+// current.
+int plane_scratch(int device, double** out) {
+  static std::mutex mu;
+  static double* addr[64] = {};
+  if (device < 0 || device >= 64) return fail(WQL_E_INPUT, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_plane_scratch);
+    if (e != cudaSuccess) return fail(WQL_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    addr[device] = (double*)p;
+  }
+  *out = addr[device];
+  return WQL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wql_get_field_noalloc(wql_scn* scn, int block, int comp, double* host_out) {
+  if (!scn || !host_out || block < 0 || block > 1 || comp < 0 || comp > 8)
+    return fail(WQL_E_INPUT, "bad argument");
+  auto& B = scn->B[block];
+  const int dev = scn->ctx->device;
+  CK(cudaSetDevice(dev));
+  CK(cudaStreamSynchronize(scn->stream));
+  if (scn->prec == WQL_FP64) {
+    CK(cudaMemcpy2D(host_out, B.nq * sizeof(double), (const double*)B.F[scn->cur] + comp * B.np,
+                    B.pq * sizeof(double), B.nq * sizeof(double), (size_t)B.nr * B.ns, cudaMemcpyDeviceToHost));
+    return WQL_OK;
+  }
+  const long long plane = (long long)B.pq * B.nr;
+  if (plane > kPlaneScratchWords)
+    return fail(WQL_E_INPUT, "wql_get_field_noalloc: a plane of " + std::to_string(plane) +
+                                 " pitched points exceeds the " + std::to_string(kPlaneScratchWords) +
+                                 "-point device scratch; use wql_get_field");
+  double* scr = nullptr;
+  int rc = plane_scratch(dev, &scr);
+  if (rc) return rc;
+  const float* src = (const float*)B.F[scn->cur] + comp * B.np;
+  for (int k = 0; k < B.ns; ++k) {
+    widen_plane<<<(unsigned)((plane + 255) / 256), 256, 0, scn->stream>>>(src + k * plane, scr, plane);
+    CK(cudaMemcpy2DAsync(host_out + (size_t)k * B.nq * B.nr, B.nq * sizeof(double), scr, B.pq * sizeof(double),
+                         B.nq * sizeof(double), B.nr, cudaMemcpyDeviceToHost, scn->stream));
+  }
+  CK(cudaStreamSynchronize(scn->stream));
+  CK(cudaGetLastError());
   return WQL_OK;
 }
 

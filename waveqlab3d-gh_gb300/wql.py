@@ -23,7 +23,7 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_scenario_create_from_text", "wql_scenario_create_ex", "wql_scenario_destroy", "wql_step", "wql_sync",
            "wql_get_info", "wql_get_field", "wql_set_field", "wql_get_iface", "wql_frame_count",
            "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step", "wql_profile",
-           "wql_kernel_times", "wql_set_tuning"]
+           "wql_kernel_times", "wql_set_tuning", "wql_get_field_noalloc"]
 
 
 class Media(ctypes.Structure):
@@ -67,6 +67,7 @@ def lib():
         L.wql_get_info.argtypes = [vp, ctypes.POINTER(Info)]
         L.wql_get_field.argtypes = [vp, ci, ci, vp]
         L.wql_set_field.argtypes = [vp, ci, ci, vp]
+        L.wql_get_field_noalloc.argtypes = [vp, ci, ci, vp]
         L.wql_get_iface.argtypes = [vp, ci, ci, vp]
         L.wql_frame_count.argtypes = [vp, ctypes.POINTER(ci)]
         L.wql_get_frames.argtypes = [vp, ci, vp]
@@ -175,6 +176,13 @@ class Scenario:
         nq, nr, ns = self.dims[block]
         out = np.empty(nq * nr * ns, np.float64)
         _check(lib().wql_get_field(self.h, block, comp, out.ctypes.data))
+        return out.reshape(ns, nr, nq)
+
+    def field_noalloc(self, block, comp):
+        """As field(), through wql_get_field_noalloc (no device allocation)."""
+        nq, nr, ns = self.dims[block]
+        out = np.empty(nq * nr * ns, np.float64)
+        _check(lib().wql_get_field_noalloc(self.h, block, comp, out.ctypes.data))
         return out.reshape(ns, nr, nq)
 
     def fields(self, block):
