@@ -130,6 +130,20 @@ int wql_get_iface(wql_scn* scn, int copy, int what, double* host_out);
 int wql_frame_count(wql_scn* scn, int* frames);
 int wql_get_frames(wql_scn* scn, int what, float* host_out);
 
+/* Seismogram stations (src/seismogram.f90): with output_seismograms = T in
+ * &output_list, the positions of '!---begin:station_list---' (both blocks)
+ * or of station_listU / station_listV (block 1 / 2) are mapped to grid
+ * points as Find_Coordinates does (src/seismogram.f90:531-650; positions
+ * with no grid point within half a cell diagonal are dropped), and every
+ * output step (w_stride) records t and (vx, vy, vz) there at stage 1
+ * (write_seismogram, src/seismogram.f90:460-474).  wql_station_count gives
+ * the stations found in a block and the records so far; wql_station_index
+ * their 1-based grid indices (3 ints each); wql_get_seismograms the records
+ * as records x stations x (t, vx, vy, vz) doubles. */
+int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords);
+int wql_station_index(wql_scn* scn, int block, int* ijk);
+int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
+
 /* The CUDA stream the scenario's kernels run on (cudaStream_t as integer),
  * for callers that time or order work around wql_step. */
 int wql_scenario_stream(wql_scn* scn, uintptr_t* stream);

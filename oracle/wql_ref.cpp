@@ -412,6 +412,14 @@ struct Frames {
   vector<float> Uface, Vface, S, Uhat, Vhat, Svel, trup, state;
 };
 
+// Seismogram stations of one block: 1-based grid indices of the stations
+// that were found, and per output step (t, vx, vy, vz) of each.
+struct Stations {
+  vector<int> i, j, k;
+  vector<wp> rec;
+  int count = 0;
+};
+
 // D6 derivative along one axis at (i,j,k) of component comp of x, summed in
 // the order of src/metrics.f90:29-150; axis 0/1/2 = q/r/s.
 wp d6(const RBlock& B, const vector<wp>& u, int axis, int i, int j, int k) {
@@ -728,8 +736,60 @@ struct Domain {
   bool weighted_bc = false;
   wp pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
   Frames fr;
+  Stations st[2];
   std::string err;
 };
+
+// Find_Coordinates (src/seismogram.f90:531-650): for each requested
+// position the grid point with the smallest distance among those within
+// half the local cell diagonal (forward differences of x along q, y along r,
+// z along s; backward at the last point), scanning s, r, q in that nesting
+// and keeping the last point at equal distance.  Stations with no such
+// point are not recorded (src/seismogram.f90:357, 471).
+void find_stations(const RBlock& B, const vector<wp>& xyz, Stations& S) {
+  const size_t ns_ = xyz.size() / 3;
+  for (size_t c = 0; c < ns_; ++c) {
+    int i0 = -9999, j0 = -9999, k0 = -9999;
+    wp mindist = 1.0e8;
+    for (int k = 1; k <= B.ns; ++k)
+      for (int j = 1; j <= B.nr; ++j)
+        for (int i = 1; i <= B.nq; ++i) {
+          const size_t p = B.id(i, j, k);
+          wp hx = B.X[0][B.id(B.nq, j, k)] - B.X[0][B.id(B.nq - 1, j, k)];
+          wp hy = B.X[1][B.id(i, B.nr, k)] - B.X[1][B.id(i, B.nr - 1, k)];
+          wp hz = B.X[2][B.id(i, j, B.ns)] - B.X[2][B.id(i, j, B.ns - 1)];
+          if (i < B.nq) hx = B.X[0][B.id(i + 1, j, k)] - B.X[0][p];
+          if (j < B.nr) hy = B.X[1][B.id(i, j + 1, k)] - B.X[1][p];
+          if (k < B.ns) hz = B.X[2][B.id(i, j, k + 1)] - B.X[2][p];
+          const wp v0 = B.X[0][p] - xyz[3 * c], v1 = B.X[1][p] - xyz[3 * c + 1], v2 = B.X[2][p] - xyz[3 * c + 2];
+          const wp dist = std::sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+          const wp dist0 = std::sqrt(hx * hx + hy * hy + hz * hz);
+          if (dist <= mindist && dist <= 0.5 * dist0) {
+            i0 = i; j0 = j; k0 = k;
+            mindist = dist;
+          }
+        }
+    if (i0 > 0 && j0 > 0 && k0 > 0) {
+      S.i.push_back(i0);
+      S.j.push_back(j0);
+      S.k.push_back(k0);
+    }
+  }
+}
+
+// write_seismogram (src/seismogram.f90:460-474): t and F(i,j,k,1:3).
+void record_stations(Domain& D) {
+  for (int b = 0; b < 2; ++b) {
+    Stations& S = D.st[b];
+    RBlock& B = D.Bk[b];
+    for (size_t n = 0; n < S.i.size(); ++n) {
+      const size_t p = B.id(S.i[n], S.j[n], S.k[n]);
+      S.rec.push_back(D.t);
+      for (int c = 0; c < 3; ++c) S.rec.push_back(B.F[c][p]);
+    }
+    S.count += 1;
+  }
+}
 
 // Seeded surfaces and media handed in by the caller (the product's
 // wql_scenario_create_ex extension); all pointers may be null.
@@ -1627,6 +1687,7 @@ void time_step(Domain& D) {
       write_fault_frame(D);
       D.fr.count += 1;
     }
+    if (stage == 1 && D.P.output_seismograms && (n - 1) % std::max(D.P.w_stride, 1) == 0) record_stations(D);
     D.t = t0 + D.rk.C[stage] * D.dt;
     wp Bdt = D.rk.B[stage] * D.dt;
     // update_fields
@@ -1808,6 +1869,10 @@ static void* create_domain(Domain* D, const Media& md) {
   }
   D->fr.nr = nr;
   D->fr.ns = ns;
+  if (D->P.output_seismograms)
+    for (int b = 0; b < 2; ++b)
+      find_stations(D->Bk[b], !D->P.stations.empty() ? D->P.stations : (b == 0 ? D->P.stationsU : D->P.stationsV),
+                    D->st[b]);
   return D;
 }
 
@@ -1879,6 +1944,31 @@ int wqlref_get_iface(void* h, int block, int what, double* out) {
 }
 
 int wqlref_frame_count(void* h) { return ((Domain*)h)->fr.count; }
+
+// Stations of a block: number found, the recorded step count and their
+// 1-based grid indices (ijk: 3 per station).
+int wqlref_station_count(void* h, int block, int* nrec) {
+  const Stations& S = ((Domain*)h)->st[block];
+  if (nrec) *nrec = S.count;
+  return (int)S.i.size();
+}
+
+int wqlref_station_index(void* h, int block, int* ijk) {
+  const Stations& S = ((Domain*)h)->st[block];
+  for (size_t n = 0; n < S.i.size(); ++n) {
+    ijk[3 * n] = S.i[n];
+    ijk[3 * n + 1] = S.j[n];
+    ijk[3 * n + 2] = S.k[n];
+  }
+  return 0;
+}
+
+// Records x stations x (t, vx, vy, vz).
+int wqlref_get_seismograms(void* h, int block, double* out) {
+  const Stations& S = ((Domain*)h)->st[block];
+  std::memcpy(out, S.rec.data(), S.rec.size() * sizeof(double));
+  return 0;
+}
 
 // Frames in the reference's file layout: frame-major, then component,
 // then (r fastest, s).  what: 0 Uface,1 Vface,2 S,3 Uhat,4 Vhat,5 Svel,6 trup,7 state

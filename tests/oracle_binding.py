@@ -30,6 +30,9 @@ def lib():
         L.wqlref_info.argtypes = [vp, vp, vp, vp, vp, vp]
         L.wqlref_create_ex.restype = ctypes.c_void_p
         L.wqlref_create_ex.argtypes = [ctypes.c_char_p] + [vp] * 9
+        L.wqlref_station_count.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.wqlref_station_index.argtypes = [vp, ctypes.c_int, vp]
+        L.wqlref_get_seismograms.argtypes = [vp, ctypes.c_int, vp]
         _LIB = L
     return _LIB
 
@@ -100,6 +103,16 @@ class Oracle:
         out = np.empty(nr * ns, np.float64)
         lib().wqlref_get_iface(self.h, block, what, out.ctypes.data)
         return out.reshape(ns, nr)
+
+    def stations(self, block):
+        """(1-based grid indices (n, 3), seismograms (records, n, 4) of t, vx, vy, vz)."""
+        nrec = ctypes.c_int()
+        n = lib().wqlref_station_count(self.h, block, ctypes.byref(nrec))
+        ijk = np.empty(3 * n, np.int32)
+        lib().wqlref_station_index(self.h, block, ijk.ctypes.data)
+        rec = np.empty(nrec.value * n * 4, np.float64)
+        lib().wqlref_get_seismograms(self.h, block, rec.ctypes.data)
+        return ijk.reshape(n, 3), rec.reshape(nrec.value, n, 4)
 
     def frames(self, name):
         nf = lib().wqlref_frame_count(self.h)

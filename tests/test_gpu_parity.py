@@ -45,6 +45,15 @@ def test_truth1_fault_streams(ctx, wqlmod, oracle_lib, tmp_path):
         assert np.abs(got - ref).max() <= 1e-9 * scale, name
     for e in field_errors(s, o):
         assert e < TOL
+    # station seismograms: grid points, the oracle's records, and the truth
+    # files (printed to 6 decimals)
+    for block, name in ((0, "station_21_11_11"), (1, "station_1_11_11")):
+        idx, rec = s.stations(block)
+        oidx, orec = o.stations(block)
+        assert idx.tolist() == oidx.tolist()
+        assert rec.shape == orec.shape == (46, 1, 4)
+        assert np.abs(rec - orec).max() <= 1e-11 * max(np.abs(orec).max(), 1.0)
+        assert np.abs(rec[:, 0, :] - truth[name]).max() <= 5.1e-7
 
 
 def test_cartesian_characteristic_bc(ctx, wqlmod, oracle_lib, tmp_path):

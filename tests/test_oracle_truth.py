@@ -43,6 +43,20 @@ def test_cartesian_truth_bitwise(oracle_lib, tmp_path, truth_cart):
         assert diff <= 1e-10 * scale, (name, diff)
 
 
+def test_station_seismograms_match_truth(oracle_lib, tmp_path, truth_cart):
+    """The station lists of test_rup_cart_fric.in resolve to grid points
+    (21,11,11) of block 1 and (1,11,11) of block 2 (Find_Coordinates,
+    src/seismogram.f90:531-650), and their (t, vx, vy, vz) records match the
+    truth/1 station files, which are printed to 6 decimals."""
+    p = write(tmp_path, "cart.in", with_groups(golden_in("test_rup_cart_fric"), WEIGHTED))
+    o = run(oracle_lib, p)
+    for block, name, ijk in ((0, "station_21_11_11", (21, 11, 11)), (1, "station_1_11_11", (1, 11, 11))):
+        idx, rec = o.stations(block)
+        assert idx.tolist() == [list(ijk)]
+        assert rec.shape == (46, 1, 4)
+        assert np.abs(rec[:, 0, :] - truth_cart[name]).max() <= 5.1e-7, name
+
+
 def test_curvilinear_path_on_flat_grid_matches_truth(oracle_lib, tmp_path, truth_cart):
     """The curvilinear operator (transfinite grid, full metric terms,
     JU:16230-16356) on the flat truth/1 geometry reproduces truth/1."""

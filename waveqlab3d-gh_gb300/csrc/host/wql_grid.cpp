@@ -238,4 +238,31 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
   return 0;
 }
 
+void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk) {
+  const int nq = G.nq, nr = G.nr, ns = G.ns;
+  auto at = [&](int c, int i, int j, int k) {  // 1-based point
+    return G.x[c][(size_t)(i - 1) + (size_t)nq * ((size_t)(j - 1) + (size_t)nr * (k - 1))];
+  };
+  for (size_t st = 0; st + 2 < xyz.size(); st += 3) {
+    int best[3] = {-1, -1, -1};
+    double mind = 1.0e8;
+    // scan order s, r, q with "<=": the last point at equal distance wins
+    for (int k = 1; k <= ns; ++k)
+      for (int j = 1; j <= nr; ++j)
+        for (int i = 1; i <= nq; ++i) {
+          const double hx = i < nq ? at(0, i + 1, j, k) - at(0, i, j, k) : at(0, nq, j, k) - at(0, nq - 1, j, k);
+          const double hy = j < nr ? at(1, i, j + 1, k) - at(1, i, j, k) : at(1, i, nr, k) - at(1, i, nr - 1, k);
+          const double hz = k < ns ? at(2, i, j, k + 1) - at(2, i, j, k) : at(2, i, j, ns) - at(2, i, j, ns - 1);
+          const double dx = at(0, i, j, k) - xyz[st], dy = at(1, i, j, k) - xyz[st + 1],
+                       dz = at(2, i, j, k) - xyz[st + 2];
+          const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+          if (d <= mind && d <= 0.5 * std::sqrt(hx * hx + hy * hy + hz * hz)) {
+            best[0] = i; best[1] = j; best[2] = k;
+            mind = d;
+          }
+        }
+    if (best[0] > 0) ijk.insert(ijk.end(), best, best + 3);
+  }
+}
+
 }  // namespace wql

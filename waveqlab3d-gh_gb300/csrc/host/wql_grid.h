@@ -33,4 +33,10 @@ struct SurfaceMods {
 int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockGrid& G,
                     std::string& err);
 
+// Seismogram stations (Find_Coordinates, src/seismogram.f90:531-650): for
+// each requested (x, y, z) the grid point nearest to it among the points
+// within half their local cell diagonal; requests with no such point are
+// dropped.  Appends 1-based (i, j, k) triples to ijk.
+void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk);
+
 }  // namespace wql

@@ -364,6 +364,7 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
   }
   P.stationsU = marker_block(text, "station_listU");
   P.stationsV = marker_block(text, "station_listV");
+  P.stations = marker_block(text, "station_list");
 
   if (P.nblocks != 2) {
     err = "only two blocks joined by one q-interface are supported (src/domain.f90:243-244)";

@@ -75,6 +75,9 @@ struct Problem {
   bool output_seismograms = false;
   // station marker blocks (src/seismogram.f90:181-202): x y z per line
   std::vector<double> stationsU, stationsV;
+  // one list for both blocks ('!---begin:station_list---', src/seismogram.f90:157-176);
+  // when present it replaces the per-block lists
+  std::vector<double> stations;
   // &gb300_list: boundary SAT penalty weights.  'characteristic' is the form
   // compiled by the reference (src/BoundaryConditions.f90:777-918 followed by
   // structure(), src/RHS_Interior.f90:2203-2223); 'weighted' is the

@@ -133,6 +133,17 @@ struct wql_scn {
   int frame_cap = 0, frame_fill = 0;
   std::vector<float> frames_host;
   int nframes = 0;
+  // seismogram stations per block (src/seismogram.f90): 1-based grid
+  // indices, device point offsets, a device ring of velocity records
+  // (same capacity as the frame ring) and the flushed host records
+  struct Stations {
+    std::vector<int> ijk;
+    long long* idx_dev = nullptr;
+    double* ring = nullptr;        // cap x n x 3
+    std::vector<double> host;      // records x n x 4 (t, vx, vy, vz)
+  } st[2];
+  int st_cap = 0, st_fill = 0, st_records = 0;
+  std::vector<double> st_times;    // times of the records still in the ring
   // optional per-launch timing (CUDA events on the scenario stream)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -206,6 +217,17 @@ template <typename T>
 __global__ void pad_rows(const double* in, T* out, int nq, int pq, long long npd) {
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p < npd) out[p % nq + (long long)pq * (p / nq)] = (T)in[p];
+}
+
+// write_seismogram (src/seismogram.f90:460-474): velocities at the stations.
+template <typename T>
+__global__ void station_kernel(const T* __restrict__ F, long long np, const long long* __restrict__ idx, int n,
+                               double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long p = idx[i];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[i * 3 + c] = (double)F[c * np + p];
 }
 
 template <typename T>
@@ -333,6 +355,21 @@ int setup_block(wql_scn* S, int b) {
       pad_rows<double><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(x + np, (double*)B.y, B.nq, B.pq, np);
     else
       pad_rows<float><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(x + np, (float*)B.y, B.nq, B.pq, np);
+  }
+  // seismogram stations: nearest grid points, as pitched offsets
+  if (S->P.output_seismograms) {
+    const std::vector<double>& req = !S->P.stations.empty() ? S->P.stations : (b == 0 ? S->P.stationsU : S->P.stationsV);
+    auto& T = S->st[b];
+    find_station_points(G, req, T.ijk);
+    const int n = (int)T.ijk.size() / 3;
+    if (n > 0) {
+      std::vector<long long> off(n);
+      for (int i = 0; i < n; ++i)
+        off[i] = (T.ijk[3 * i] - 1) + (long long)B.pq * ((T.ijk[3 * i + 1] - 1) + (long long)B.nr * (T.ijk[3 * i + 2] - 1));
+      if ((rc = S->alloc((void**)&T.idx_dev, n * sizeof(long long), false))) return rc;
+      CK(cudaMemcpy(T.idx_dev, off.data(), n * sizeof(long long), cudaMemcpyHostToDevice));
+      if ((rc = S->alloc((void**)&T.ring, (size_t)64 * n * 3 * sizeof(double)))) return rc;
+    }
   }
   // interface coordinates of this block's fault face
   {
@@ -513,6 +550,7 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
     if ((rc = precompute_fault(S.get()))) return rc;
   if (fp.coupling == CPL_RS)
     if ((rc = init_rate_state(S.get()))) return rc;
+  S->st_cap = 64;
   if (Pr.w_fault) {
     S->frame_cap = 64;
     if ((rc = S->alloc((void**)&S->frame_dev, (size_t)S->frame_cap * kFrameWords * nf * sizeof(float)))) return rc;
@@ -533,7 +571,29 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   return WQL_OK;
 }
 
+int flush_stations(wql_scn* S) {
+  if (S->st_fill == 0) return WQL_OK;
+  for (int b = 0; b < 2; ++b) {
+    auto& T = S->st[b];
+    const int n = (int)T.ijk.size() / 3;
+    if (n == 0) continue;
+    std::vector<double> tmp((size_t)S->st_fill * n * 3);
+    CK(cudaMemcpyAsync(tmp.data(), T.ring, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, S->stream));
+    CK(cudaStreamSynchronize(S->stream));
+    for (int r = 0; r < S->st_fill; ++r)
+      for (int i = 0; i < n; ++i) {
+        T.host.push_back(S->st_times[r]);
+        for (int c = 0; c < 3; ++c) T.host.push_back(tmp[((size_t)r * n + i) * 3 + c]);
+      }
+  }
+  S->st_fill = 0;
+  S->st_times.clear();
+  return WQL_OK;
+}
+
 int flush_frames(wql_scn* S) {
+  int rc = flush_stations(S);
+  if (rc) return rc;
   if (S->frame_fill == 0) return WQL_OK;
   const long long nf = (long long)S->B[0].nr * S->B[0].ns;
   const size_t words = (size_t)S->frame_fill * kFrameWords * nf;
@@ -592,6 +652,8 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
 int run_step(wql_scn* S) {
   const long long nf = (long long)S->B[0].nr * S->B[0].ns;
   const bool want_frame = S->frame_dev && (S->nstep % std::max(S->P.w_stride, 1) == 0);
+  const bool want_station = S->P.output_seismograms && (S->st[0].ijk.size() + S->st[1].ijk.size() > 0) &&
+                            (S->nstep % std::max(S->P.w_stride, 1) == 0);
   const double t0 = S->t;
   int launches = 0;
   for (int stage = 1; stage <= 5; ++stage) {
@@ -631,6 +693,20 @@ int run_step(wql_scn* S) {
     launch_interface(ia, S->stream);
     launches += 1;
     if (S->profiling) mark_end();
+    if (stage == 1 && want_station) {
+      // stage-1 fields are the fields at t0 (write_output, src/time_step.f90:137)
+      for (int b = 0; b < 2; ++b) {
+        auto& T = S->st[b];
+        const int n = (int)T.ijk.size() / 3;
+        if (n == 0) continue;
+        double* out = T.ring + (size_t)S->st_fill * n * 3;
+        if (S->prec == WQL_FP64)
+          station_kernel<double><<<(n + 127) / 128, 128, 0, S->stream>>>((const double*)S->B[b].F[S->cur], S->B[b].np, T.idx_dev, n, out);
+        else
+          station_kernel<float><<<(n + 127) / 128, 128, 0, S->stream>>>((const float*)S->B[b].F[S->cur], S->B[b].np, T.idx_dev, n, out);
+        launches += 1;
+      }
+    }
     for (int b = 0; b < 2; ++b) {
       if (S->profiling) mark(2);
       if (S->prec == WQL_FP64) launches += launch_pre<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->stream);
@@ -652,6 +728,15 @@ int run_step(wql_scn* S) {
   S->launches_last_step = launches;
   S->t = t0 + S->rk.C[5] * S->dt;
   S->nstep += 1;
+  if (want_station) {
+    S->st_times.push_back(t0);
+    S->st_fill += 1;
+    S->st_records += 1;
+    if (S->st_fill == S->st_cap) {
+      const int rc = flush_stations(S);
+      if (rc) return rc;
+    }
+  }
   if (want_frame) {
     S->frame_fill += 1;
     S->nframes += 1;
@@ -916,6 +1001,27 @@ int wql_get_frames(wql_scn* scn, int what, float* host_out) {
     const float* src = scn->frames_host.data() + (size_t)fr * kFrameWords * nf + (size_t)off * nf;
     std::memcpy(host_out + (size_t)fr * nc * nf, src, (size_t)nc * nf * sizeof(float));
   }
+  return WQL_OK;
+}
+
+int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords) {
+  if (!scn || block < 0 || block > 1 || !nstations) return fail(WQL_E_INPUT, "bad argument");
+  *nstations = (int)scn->st[block].ijk.size() / 3;
+  if (nrecords) *nrecords = scn->st_records;
+  return WQL_OK;
+}
+
+int wql_station_index(wql_scn* scn, int block, int* ijk) {
+  if (!scn || block < 0 || block > 1 || !ijk) return fail(WQL_E_INPUT, "bad argument");
+  std::memcpy(ijk, scn->st[block].ijk.data(), scn->st[block].ijk.size() * sizeof(int));
+  return WQL_OK;
+}
+
+int wql_get_seismograms(wql_scn* scn, int block, double* host_out) {
+  if (!scn || block < 0 || block > 1 || !host_out) return fail(WQL_E_INPUT, "bad argument");
+  const int rc = flush_stations(scn);
+  if (rc) return rc;
+  std::memcpy(host_out, scn->st[block].host.data(), scn->st[block].host.size() * sizeof(double));
   return WQL_OK;
 }
 

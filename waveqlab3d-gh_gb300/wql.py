@@ -23,7 +23,8 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_scenario_create_from_text", "wql_scenario_create_ex", "wql_scenario_destroy", "wql_step", "wql_sync",
            "wql_get_info", "wql_get_field", "wql_set_field", "wql_get_iface", "wql_frame_count",
            "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step", "wql_profile",
-           "wql_kernel_times", "wql_set_tuning", "wql_get_field_noalloc"]
+           "wql_kernel_times", "wql_set_tuning", "wql_get_field_noalloc", "wql_station_count",
+           "wql_station_index", "wql_get_seismograms"]
 
 
 class Media(ctypes.Structure):
@@ -68,6 +69,9 @@ def lib():
         L.wql_get_field.argtypes = [vp, ci, ci, vp]
         L.wql_set_field.argtypes = [vp, ci, ci, vp]
         L.wql_get_field_noalloc.argtypes = [vp, ci, ci, vp]
+        L.wql_station_count.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
+        L.wql_station_index.argtypes = [vp, ci, vp]
+        L.wql_get_seismograms.argtypes = [vp, ci, vp]
         L.wql_get_iface.argtypes = [vp, ci, ci, vp]
         L.wql_frame_count.argtypes = [vp, ctypes.POINTER(ci)]
         L.wql_get_frames.argtypes = [vp, ci, vp]
@@ -177,6 +181,16 @@ class Scenario:
         out = np.empty(nq * nr * ns, np.float64)
         _check(lib().wql_get_field(self.h, block, comp, out.ctypes.data))
         return out.reshape(ns, nr, nq)
+
+    def stations(self, block):
+        """(1-based grid indices (n, 3), records (nrec, n, 4) of t, vx, vy, vz)."""
+        n, nrec = ctypes.c_int(), ctypes.c_int()
+        _check(lib().wql_station_count(self.h, block, ctypes.byref(n), ctypes.byref(nrec)))
+        ijk = np.empty(3 * n.value, np.int32)
+        _check(lib().wql_station_index(self.h, block, ijk.ctypes.data))
+        rec = np.empty(nrec.value * n.value * 4, np.float64)
+        _check(lib().wql_get_seismograms(self.h, block, rec.ctypes.data))
+        return ijk.reshape(n.value, 3), rec.reshape(nrec.value, n.value, 4)
 
     def field_noalloc(self, block, comp):
         """As field(), through wql_get_field_noalloc (no device allocation)."""
