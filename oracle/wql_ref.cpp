@@ -412,6 +412,18 @@ struct Frames {
   vector<float> Uface, Vface, S, Uhat, Vhat, Svel, trup, state;
 };
 
+// Moment-tensor point sources of one block (src/moment_tensor.f90): the
+// source, its nearest grid point (1-based) and that point's coordinates.
+struct MTSource {
+  wql::MomentSource s;
+  int i = -1, j = -1, k = -1;
+  wp px = 0, py = 0, pz = 0;
+};
+struct MTBlock {
+  vector<MTSource> src;
+  int alpha1 = 0;  // alpha of the first listed source selects the 9-point table
+};
+
 // Seismogram stations of one block: 1-based grid indices of the stations
 // that were found, and per output step (t, vx, vy, vz) of each.
 struct Stations {
@@ -737,8 +749,161 @@ struct Domain {
   wp pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
   Frames fr;
   Stations st[2];
+  MTBlock mt[2];
   std::string err;
 };
+
+// source_time (src/moment_tensor.f90:958-1011).  Returns false for an
+// unknown type (the reference stops).
+bool source_time(const std::string& type, wp t, wp t0, wp w, wp& A) {
+  const wp pi = 3.141592653589793;
+  if (type == "gaussian") A = (w / std::sqrt(2.0 * pi)) * std::exp((-(w * w) * ((t - t0) * (t - t0))) / 2.0);
+  else if (type == "LOH_discontinuity") A = (t / (w * w)) * std::exp(-t / w);
+  else if (type == "Brune") A = (w * w) * t * std::exp(-w * t);
+  else if (type == "Cos-Bell") A = t < t0 ? (1.0 - std::cos(2.0 * pi * t / t0)) / t0 : 0.0;
+  else if (type == "cosine") A = (t >= 0.0 && t <= w) ? 1.0 - std::cos(2.0 * pi * t / w) : 0.0;
+  else if (type == "LOH_moment_time_history") A = 1.0 - (1.0 + t / w) * std::exp(-t / w);
+  else if (type == "sine_moment_time_history") A = t <= w ? t - w / (2.0 * pi) * std::sin(2.0 * pi * t / w) : w;
+  else return false;
+  return true;
+}
+
+// singular_source (src/moment_tensor.f90:1081-1265): discrete delta at
+// index i for a source at grid index i0 offset by a (in units of h); order
+// 2 (5 points, depends on a) or 4 (9 points, tables for alpha 0/25/50/100).
+wp singular_source(int i, int i0, wp h, wp a, int order, int alpha) {
+  if (order == 2) {
+    const wp beta = (1.0 - 2.0 * a) / 4.0 + 0.25, gam = (2.0 * a - 1.0) / 16.0, gap = (2.0 * a + 1.0) / 16.0;
+    if (i == i0 - 2) return (-gam) / h;
+    if (i == i0 - 1) return (beta + 3.0 * gam - gap) / h;
+    if (i == i0) return (1.0 - a - 2.0 * beta - 3.0 * gam + 3.0 * gap) / h;
+    if (i == i0 + 1) return (a + beta + gam - 3.0 * gap) / h;
+    if (i == i0 + 2) return gap / h;
+    return 0.0;
+  }
+  static const wp tab[4][9] = {
+      {-0.01171875, -0.03125, 0.046875, 0.28125, 0.4296875, 0.28125, 0.046875, -0.03125, -0.01171875},
+      {-0.00246875, -0.02275, -0.014125, 0.16575, 0.4171875, 0.38675, 0.117875, -0.02975, -0.01846875},
+      {-0.00728125, -0.028, 0.014875, 0.224, 0.4265625, 0.336, 0.081375, -0.032, -0.01553125},
+      {-0.0095625, -0.02990625, 0.03053125, 0.25284375, 0.42890625, 0.30903125, 0.06384375, -0.03196875, -0.01371875}};
+  const int row = alpha == 0 ? 0 : (alpha == 25 ? 1 : (alpha == 50 ? 2 : 3));
+  const int o = i - i0;
+  if (o < -4 || o > 4) return 0.0;
+  return tab[row][o + 4] / h;
+}
+
+// Find_Coordinates_moment (src/seismogram.f90:652-727): nearest grid point
+// of a position inside the block's coordinate range, last one on ties.
+bool nearest_point(const RBlock& B, wp x, wp y, wp z, int& i0, int& j0, int& k0) {
+  wp lo[3], hi[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = *std::min_element(B.X[c].begin(), B.X[c].end());
+    hi[c] = *std::max_element(B.X[c].begin(), B.X[c].end());
+  }
+  if (!(lo[0] <= x && x <= hi[0] && lo[1] <= y && y <= hi[1] && lo[2] <= z && z <= hi[2])) return false;
+  wp mind = 1.0e8;
+  i0 = j0 = k0 = -9999;
+  for (int k = 1; k <= B.ns; ++k)
+    for (int j = 1; j <= B.nr; ++j)
+      for (int i = 1; i <= B.nq; ++i) {
+        const size_t p = B.id(i, j, k);
+        const wp v0 = B.X[0][p] - x, v1 = B.X[1][p] - y, v2 = B.X[2][p] - z;
+        const wp d = std::sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+        if (d <= mind) {
+          i0 = i; j0 = j; k0 = k;
+          mind = d;
+        }
+      }
+  return true;
+}
+
+// The block test of init_moment_tensor (src/moment_tensor.f90:304-306): the
+// position lies between the coordinates of the first and the last point.
+bool in_block_box(const RBlock& B, wp x, wp y, wp z) {
+  const size_t a = B.id(1, 1, 1), b = B.id(B.nq, B.nr, B.ns);
+  return B.X[0][a] <= x && x <= B.X[0][b] && B.X[1][a] <= y && y <= B.X[1][b] && B.X[2][a] <= z && z <= B.X[2][b];
+}
+
+// Assign the listed sources to the blocks.  The unified list goes to the
+// preferred block when the source lies in its box, else to the other block
+// when it lies in that one; per-block lists stay with their block.  A source
+// in no block is not applied.  (The reference keeps such a source at grid
+// index -1, where the discrete delta still reaches points 1..3 of each axis
+// -- src/moment_tensor.f90:318-345 with singular_source -- a spurious
+// source in the block corner that this restatement does not reproduce.)
+void resolve_sources(Domain& D) {
+  const wql::Problem& P = D.P;
+  for (int b = 0; b < 2; ++b) D.mt[b].src.clear();
+  auto add = [&](int b, const wql::MomentSource& m) {
+    MTSource s;
+    s.s = m;
+    if (!nearest_point(D.Bk[b], m.x, m.y, m.z, s.i, s.j, s.k)) return;
+    const size_t p = D.Bk[b].id(s.i, s.j, s.k);
+    s.px = D.Bk[b].X[0][p];
+    s.py = D.Bk[b].X[1][p];
+    s.pz = D.Bk[b].X[2][p];
+    D.mt[b].src.push_back(s);
+  };
+  if (P.mt_unified) {
+    const int pref = P.mt_block_preference == 2 ? 1 : 0;
+    for (const auto& m : P.tensors) {
+      if (in_block_box(D.Bk[pref], m.x, m.y, m.z)) add(pref, m);
+      else if (in_block_box(D.Bk[1 - pref], m.x, m.y, m.z)) add(1 - pref, m);
+    }
+    for (int b = 0; b < 2; ++b) D.mt[b].alpha1 = P.tensors.empty() ? 0 : P.tensors[0].alpha;
+  } else {
+    const vector<wql::MomentSource>* L[2] = {&P.tensorsU, &P.tensorsV};
+    for (int b = 0; b < 2; ++b) {
+      for (const auto& m : *L[b])
+        if (in_block_box(D.Bk[b], m.x, m.y, m.z)) add(b, m);
+      D.mt[b].alpha1 = L[b]->empty() ? 0 : (*L[b])[0].alpha;
+    }
+  }
+}
+
+// set_moment_tensor / set_moment_tensor_smooth (src/moment_tensor.f90:
+// 1014-1078, 1400-1475), once per stage after the interior rates:
+// DF(4:9) -= A(t) * M * delta.
+void apply_sources(Domain& D, int b, wp t) {
+  RBlock& B = D.Bk[b];
+  const MTBlock& T = D.mt[b];
+  for (const MTSource& s : T.src) {
+    wp A = 0;
+    source_time(s.s.type, t, s.s.t_init, s.s.duration, A);
+    if (D.P.mollify_source) {
+      const wp pi = 3.14159265359;
+      for (int n = 1; n <= B.ns; ++n)
+        for (int m = 1; m <= B.nr; ++m)
+          for (int l = 1; l <= B.nq; ++l) {
+            const size_t p = B.id(l, m, n);
+            wp hx = l == 1 ? B.X[0][B.id(2, m, n)] - B.X[0][p] : B.X[0][p] - B.X[0][B.id(l - 1, m, n)];
+            wp hy = m == 1 ? B.X[1][B.id(l, 2, n)] - B.X[1][p] : B.X[1][p] - B.X[1][B.id(l, m - 1, n)];
+            wp hz = n == 1 ? B.X[2][B.id(l, m, 2)] - B.X[2][p] : B.X[2][p] - B.X[2][B.id(l, m, n - 1)];
+            const wp sx = 2.0 * hx, sy = 2.0 * hy, sz = 2.0 * hz;
+            const wp ex = (B.X[0][p] - s.s.x) / sx, ey = (B.X[1][p] - s.s.y) / sy, ez = (B.X[2][p] - s.s.z) / sz;
+            const wp dx = std::exp(-0.5 * (ex * ex)) / (sx * std::sqrt(2.0 * pi));
+            const wp dy = std::exp(-0.5 * (ey * ey)) / (sy * std::sqrt(2.0 * pi));
+            const wp dz = std::exp(-0.5 * (ez * ez)) / (sz * std::sqrt(2.0 * pi));
+            const wp delta = dx * dy * dz;
+            for (int c = 0; c < 6; ++c) B.DF[3 + c][p] = B.DF[3 + c][p] - A * s.s.m[c] * delta;
+          }
+    } else {
+      const int R = D.P.mt_order == 2 ? 2 : 4;
+      for (int n = std::max(1, s.k - R); n <= std::min(B.ns, s.k + R); ++n)
+        for (int m = std::max(1, s.j - R); m <= std::min(B.nr, s.j + R); ++m)
+          for (int l = std::max(1, s.i - R); l <= std::min(B.nq, s.i + R); ++l) {
+            const size_t p = B.id(l, m, n);
+            const wp hx = B.hq / B.mx[0][p], hy = B.hr / B.my[1][p], hz = B.hs / B.mz[2][p];
+            const wp ax = (s.s.x - s.px) / hx, ay = (s.s.y - s.py) / hy, az = (s.s.z - s.pz) / hz;
+            const wp dx = singular_source(l, s.i, hx, ax, D.P.mt_order, T.alpha1);
+            const wp dy = singular_source(m, s.j, hy, ay, D.P.mt_order, T.alpha1);
+            const wp dz = singular_source(n, s.k, hz, az, D.P.mt_order, T.alpha1);
+            const wp delta = dx * dy * dz;
+            for (int c = 0; c < 6; ++c) B.DF[3 + c][p] = B.DF[3 + c][p] - A * s.s.m[c] * delta;
+          }
+    }
+  }
+}
 
 // Find_Coordinates (src/seismogram.f90:531-650): for each requested
 // position the grid point with the smallest distance among those within
@@ -1675,6 +1840,7 @@ void time_step(Domain& D) {
     for (int b = 0; b < 2; ++b) {
       rhs_interior(D.Bk[b], D.cart);
       rhs_near_boundaries(D.Bk[b]);
+      if (D.P.use_moment_tensor) apply_sources(D, b, D.t);
     }
     // enforce_bound_iface_conditions (block 1 then block 2)
     bool frame = want_frame && stage == 1;
@@ -1869,6 +2035,27 @@ static void* create_domain(Domain* D, const Media& md) {
   }
   D->fr.nr = nr;
   D->fr.ns = ns;
+  if (D->P.use_moment_tensor) {
+    const wql::Problem& P = D->P;
+    std::string bad;
+    if (P.mt_order != 2 && P.mt_order != 4) bad = "moment_list order must be 2 or 4";
+    for (const auto* L : {&P.tensors, &P.tensorsU, &P.tensorsV}) {
+      for (const auto& m : *L) {
+        wp A;
+        if (!source_time(m.type, 0.0, m.t_init, m.duration, A)) bad = "invalid source type '" + m.type + "'";
+      }
+      if (P.mt_order == 4 && !L->empty()) {
+        const int a = (*L)[0].alpha;
+        if (a != 0 && a != 25 && a != 50 && a != 100) bad = "order-4 sources need alpha 0, 25, 50 or 100";
+      }
+    }
+    if (!bad.empty()) {
+      std::snprintf(g_err, sizeof(g_err), "%s", bad.c_str());
+      delete D;
+      return nullptr;
+    }
+    resolve_sources(*D);
+  }
   if (D->P.output_seismograms)
     for (int b = 0; b < 2; ++b)
       find_stations(D->Bk[b], !D->P.stations.empty() ? D->P.stations : (b == 0 ? D->P.stationsU : D->P.stationsV),

@@ -85,4 +85,31 @@ def case_text(name):
         return problem("TPV101", "rate-and-state_friction", "curvilinear") + block_list()
     if name == "locked":
         return problem("TPV5", "locked") + block_list()
+    if name in MT_CASES:
+        mesh, order, mollify, lists = MT_CASES[name]
+        extra = ",\n mollify_source = T" if mollify else ""
+        return (problem("TPV5", "locked", mesh, extra=extra) + block_list() +
+                f"&moment_list\n use_moment_tensor = T,\n order = {order} /\n" + lists)
     raise KeyError(name)
+
+
+# moment-tensor point sources in a locked two-block domain: per-block lists
+# (order 4, Gaussian moment rate, off-grid positions), a unified list across
+# both blocks (order 2, mixed time functions), and a mollified source
+_MT_U = ("!---begin:tensor_listU---\n"
+         "'gaussian' 20d0 0.1d0 1d0 0.5d0 -0.7d0 0.3d0 -0.2d0 0.4d0 -1.63d0 7.31d0 0.22d0 0\n"
+         "!---end:tensor_listU---\n"
+         "!---begin:tensor_listV---\n"
+         "'Brune' 15d0 0d0 0d0 0d0 0d0 1d0 0d0 0d0 1.21d0 7.74d0 -0.37d0 0\n"
+         "!---end:tensor_listV---\n")
+_MT_UNIFIED = ("! source_type duration t_init mXX mYY mZZ mXY mXZ mYZ x y z alpha\n"
+               "!---begin:tensor_list---\n"
+               "'gaussian' 25d0 0.08d0 0d0 0d0 0d0 0d0 1d0 0d0 -1.07d0 7.5d0 0.05d0 0\n"
+               "'cosine' 0.2d0 0d0 0.5d0 0.5d0 0.5d0 0d0 0d0 0d0 1.52d0 6.93d0 0.31d0 0\n"
+               "!---end:tensor_list---\n")
+MT_CASES = {
+    "mt4": ("cartesian", 4, False, _MT_U),
+    "mt4_curv": ("curvilinear", 4, False, _MT_U),
+    "mt2_unified": ("cartesian", 2, False, _MT_UNIFIED),
+    "mt_mollified": ("cartesian", 2, True, _MT_U),
+}

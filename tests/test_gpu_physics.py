@@ -28,7 +28,9 @@ def wqlmod():
 
 
 @pytest.mark.parametrize("case,steps", [("pml", 40), ("pml_curv", 20), ("plastic", 46),
-                                        ("rs", 46), ("rs_curv", 20), ("locked", 30)])
+                                        ("rs", 46), ("rs_curv", 20), ("locked", 30),
+                                        ("mt4", 30), ("mt4_curv", 20), ("mt2_unified", 30),
+                                        ("mt_mollified", 20)])
 def test_case_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, steps):
     p = write(tmp_path, case + ".in", case_text(case))
     s, o = run_pair(wqlmod, oracle_lib, ctx, p, steps)
@@ -101,3 +103,15 @@ def test_seeded_configs_fp64_parity(ctx, wqlmod, oracle_lib, cfg, kw, steps):
             assert rs_close(s.fields(b), o.fields(b)), errs
     else:
         assert max(errs) < TOL, errs
+
+
+def test_moment_tensor_fp32c(ctx, wqlmod, tmp_path):
+    """Moment-tensor sources in the FP32-compensated mode against FP64."""
+    p = write(tmp_path, "mt.in", case_text("mt4"))
+    d = wqlmod.Scenario(ctx, p, precision=wqlmod.FP64)
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    d.step(30)
+    f.step(30)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), d.fields(b)) < 1e-5

@@ -226,6 +226,45 @@ std::vector<double> marker_block(const std::string& text, const std::string& tag
   return out;
 }
 
+bool has_marker(const std::string& text, const std::string& tag) {
+  std::istringstream is(text);
+  std::string line;
+  while (std::getline(is, line))
+    if (trim(line) == "!---begin:" + tag + "---") return true;
+  return false;
+}
+
+// Moment-tensor lines between markers (blank and '!' lines skipped,
+// src/moment_tensor.f90:24-30).
+std::vector<MomentSource> tensor_block(const std::string& text, const std::string& tag) {
+  std::vector<MomentSource> out;
+  std::istringstream is(text);
+  std::string line;
+  bool in = false;
+  while (std::getline(is, line)) {
+    std::string t = trim(line);
+    if (t == "!---begin:" + tag + "---") {
+      in = true;
+      continue;
+    }
+    if (t == "!---end:" + tag + "---") break;
+    if (!in || t.empty() || t[0] == '!') continue;
+    auto v = split_values(t);
+    if (v.size() < 13) continue;
+    MomentSource m;
+    m.type = v[0];
+    m.duration = to_double(v[1]);
+    m.t_init = to_double(v[2]);
+    for (int c = 0; c < 6; ++c) m.m[c] = to_double(v[3 + c]);
+    m.x = to_double(v[9]);
+    m.y = to_double(v[10]);
+    m.z = to_double(v[11]);
+    m.alpha = (int)to_double(v[12]);
+    out.push_back(m);
+  }
+  return out;
+}
+
 }  // namespace
 
 int parse_in_text(const std::string& text, const std::string& base_dir,
@@ -313,7 +352,12 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
     auto s = it.values.empty() ? std::string() : it.values[0];
     if (it.key == "use_moment_tensor") P.use_moment_tensor = to_bool(s);
     else if (it.key == "order") P.mt_order = (int)to_double(s);
+    else if (it.key == "tensor_block_preference") P.mt_block_preference = (int)to_double(s);
   }
+  P.mt_unified = has_marker(text, "tensor_list");
+  P.tensors = tensor_block(text, "tensor_list");
+  P.tensorsU = tensor_block(text, "tensor_listU");
+  P.tensorsV = tensor_block(text, "tensor_listV");
   for (auto& it : items_of("output_list")) {
     auto s = it.values.empty() ? std::string() : it.values[0];
     if (it.key == "output_seismograms") P.output_seismograms = to_bool(s);

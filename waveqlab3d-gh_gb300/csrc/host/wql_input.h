@@ -57,6 +57,17 @@ struct PlasticExt {
   double cohesion = 1.36, friction = 0.1934, Tv = 0.03;   // src/plastic.f90:174-176
 };
 
+// One moment-tensor point source, a line of a tensor list
+// (src/moment_tensor.f90:232-246): source_type duration t_init
+// mXX mYY mZZ mXY mXZ mYZ x y z alpha.
+struct MomentSource {
+  std::string type = "gaussian";
+  double duration = 0.0, t_init = 0.0;
+  double m[6] = {0, 0, 0, 0, 0, 0};  // XX, YY, ZZ, XY, XZ, YZ (stress components 4..9)
+  double x = 0.0, y = 0.0, z = 0.0;
+  int alpha = 0;
+};
+
 struct Problem {
   // &problem_list (defaults from src/domain.f90:115-133)
   std::string name = "default", problem = "TPV5", response = "elastic",
@@ -71,6 +82,11 @@ struct Problem {
   // &moment_list (src/block.f90:63)
   bool use_moment_tensor = false;
   int mt_order = 2;
+  int mt_block_preference = 1;
+  // tensor lists (src/moment_tensor.f90:106-260): the unified
+  // '!---begin:tensor_list---' for both blocks, else tensor_listU / tensor_listV
+  bool mt_unified = false;
+  std::vector<MomentSource> tensors, tensorsU, tensorsV;
   // &output_list (src/seismogram.f90:58)
   bool output_seismograms = false;
   // station marker blocks (src/seismogram.f90:181-202): x y z per line

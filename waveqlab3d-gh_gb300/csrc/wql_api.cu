@@ -2,6 +2,7 @@
 // (time_step_RK, src/time_step.f90:68-150) over the device kernels.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -144,6 +145,21 @@ struct wql_scn {
   } st[2];
   int st_cap = 0, st_fill = 0, st_records = 0;
   std::vector<double> st_times;    // times of the records still in the ring
+  // moment-tensor point sources (src/moment_tensor.f90): per block, every
+  // listed source's placement (found at set-up), then the applied ones with
+  // their discrete delta on a box of grid points
+  struct MTCand {
+    bool found = false, in_box = false;
+    int lo[3] = {0, 0, 0}, dim[3] = {0, 0, 0};  // delta box (0-based origin, extents)
+    std::vector<double> delta;                  // box points, q fastest
+  };
+  struct MTSrc {
+    MomentSource src;
+    int lo[3], dim[3];
+    double* delta = nullptr;  // device, box points
+  };
+  std::vector<MTCand> mt_cand[2][2];  // [block][0: unified list, 1: the block's own list]
+  std::vector<MTSrc> mt[2];
   // optional per-launch timing (CUDA events on the scenario stream)
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -234,6 +250,121 @@ template <typename T>
 __global__ void count_nonfinite(const T* a, long long n, unsigned int* cnt) {
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p < n && !isfinite((double)a[p])) atomicAdd(cnt, 1u);
+}
+
+// source_time (src/moment_tensor.f90:958-1011); false for an unknown type.
+bool source_time(const std::string& type, double t, double t0, double w, double& A) {
+  const double pi = 3.141592653589793;
+  if (type == "gaussian") A = (w / std::sqrt(2.0 * pi)) * std::exp((-(w * w) * ((t - t0) * (t - t0))) / 2.0);
+  else if (type == "LOH_discontinuity") A = (t / (w * w)) * std::exp(-t / w);
+  else if (type == "Brune") A = (w * w) * t * std::exp(-w * t);
+  else if (type == "Cos-Bell") A = t < t0 ? (1.0 - std::cos(2.0 * pi * t / t0)) / t0 : 0.0;
+  else if (type == "cosine") A = (t >= 0.0 && t <= w) ? 1.0 - std::cos(2.0 * pi * t / w) : 0.0;
+  else if (type == "LOH_moment_time_history") A = 1.0 - (1.0 + t / w) * std::exp(-t / w);
+  else if (type == "sine_moment_time_history") A = t <= w ? t - w / (2.0 * pi) * std::sin(2.0 * pi * t / w) : w;
+  else return false;
+  return true;
+}
+
+// Discrete delta weight at index i of a source at grid index i0 offset by a
+// cells (singular_source, src/moment_tensor.f90:1081-1265): 5 points for
+// order 2, the 9-point tables (alpha 0/25/50/100) for order 4.
+double point_delta(int i, int i0, double h, double a, int order, int alpha) {
+  if (order == 2) {
+    const double beta = (1.0 - 2.0 * a) / 4.0 + 0.25, gam = (2.0 * a - 1.0) / 16.0, gap = (2.0 * a + 1.0) / 16.0;
+    switch (i - i0) {
+      case -2: return (-gam) / h;
+      case -1: return (beta + 3.0 * gam - gap) / h;
+      case 0: return (1.0 - a - 2.0 * beta - 3.0 * gam + 3.0 * gap) / h;
+      case 1: return (a + beta + gam - 3.0 * gap) / h;
+      case 2: return gap / h;
+      default: return 0.0;
+    }
+  }
+  static const double w9[4][9] = {
+      {-0.01171875, -0.03125, 0.046875, 0.28125, 0.4296875, 0.28125, 0.046875, -0.03125, -0.01171875},
+      {-0.00246875, -0.02275, -0.014125, 0.16575, 0.4171875, 0.38675, 0.117875, -0.02975, -0.01846875},
+      {-0.00728125, -0.028, 0.014875, 0.224, 0.4265625, 0.336, 0.081375, -0.032, -0.01553125},
+      {-0.0095625, -0.02990625, 0.03053125, 0.25284375, 0.42890625, 0.30903125, 0.06384375, -0.03196875,
+       -0.01371875}};
+  const int row = alpha == 0 ? 0 : (alpha == 25 ? 1 : (alpha == 50 ? 2 : 3));
+  const int o = i - i0;
+  return (o < -4 || o > 4) ? 0.0 : w9[row][o + 4] / h;
+}
+
+// Placement of one listed source in a block and its time-independent
+// delta: the nearest grid point of a position inside the block's coordinate
+// range (Find_Coordinates_moment, src/seismogram.f90:652-727, last point on
+// ties), the block test between the first and last point's coordinates
+// (src/moment_tensor.f90:304-306), and the weights of set_moment_tensor
+// (local spacing h/metric at each point, src/moment_tensor.f90:1014-1078)
+// or set_moment_tensor_smooth (Gaussian of width 2h, :1400-1475; evaluated
+// on the points within 28 cells, beyond which the weight is below 1e-42 of
+// its peak).  metric_at(p, d) gives metric_d(d) (q_x, r_y, s_z) at point p.
+template <typename MetricAt>
+void place_source(const BlockGrid& G, const MomentSource& m, int order, int alpha1, bool mollify,
+                  MetricAt metric_at, wql_scn::MTCand& C) {
+  const int nq = G.nq, nr = G.nr, ns = G.ns;
+  auto X = [&](int c, int i, int j, int k) {  // 0-based
+    return G.x[c][(size_t)i + (size_t)nq * ((size_t)j + (size_t)nr * k)];
+  };
+  const double pos[3] = {m.x, m.y, m.z};
+  double lo[3], hi[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = *std::min_element(G.x[c].begin(), G.x[c].end());
+    hi[c] = *std::max_element(G.x[c].begin(), G.x[c].end());
+  }
+  C.found = lo[0] <= pos[0] && pos[0] <= hi[0] && lo[1] <= pos[1] && pos[1] <= hi[1] && lo[2] <= pos[2] && pos[2] <= hi[2];
+  C.in_box = true;
+  for (int c = 0; c < 3; ++c)
+    if (!(X(c, 0, 0, 0) <= pos[c] && pos[c] <= X(c, nq - 1, nr - 1, ns - 1))) C.in_box = false;
+  if (!C.found) return;
+  int n0[3] = {0, 0, 0};
+  double mind = 1.0e8;
+  for (int k = 0; k < ns; ++k)
+    for (int j = 0; j < nr; ++j)
+      for (int i = 0; i < nq; ++i) {
+        const double dx = X(0, i, j, k) - pos[0], dy = X(1, i, j, k) - pos[1], dz = X(2, i, j, k) - pos[2];
+        const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (d <= mind) {
+          n0[0] = i; n0[1] = j; n0[2] = k;
+          mind = d;
+        }
+      }
+  const int nn[3] = {nq, nr, ns};
+  const int R = mollify ? 28 : (order == 2 ? 2 : 4);
+  for (int c = 0; c < 3; ++c) {
+    C.lo[c] = std::max(0, n0[c] - R);
+    C.dim[c] = std::min(nn[c] - 1, n0[c] + R) - C.lo[c] + 1;
+  }
+  const double near[3] = {X(0, n0[0], n0[1], n0[2]), X(1, n0[0], n0[1], n0[2]), X(2, n0[0], n0[1], n0[2])};
+  const double hq = 1.0 / (nq - 1), hr = 1.0 / (nr - 1), hs = 1.0 / (ns - 1);
+  C.delta.assign((size_t)C.dim[0] * C.dim[1] * C.dim[2], 0.0);
+  size_t e = 0;
+  for (int n = C.lo[2]; n < C.lo[2] + C.dim[2]; ++n)
+    for (int mm = C.lo[1]; mm < C.lo[1] + C.dim[1]; ++mm)
+      for (int l = C.lo[0]; l < C.lo[0] + C.dim[0]; ++l, ++e) {
+        if (mollify) {
+          const double pi = 3.14159265359;
+          const double hx = l == 0 ? X(0, 1, mm, n) - X(0, l, mm, n) : X(0, l, mm, n) - X(0, l - 1, mm, n);
+          const double hy = mm == 0 ? X(1, l, 1, n) - X(1, l, mm, n) : X(1, l, mm, n) - X(1, l, mm - 1, n);
+          const double hz = n == 0 ? X(2, l, mm, 1) - X(2, l, mm, n) : X(2, l, mm, n) - X(2, l, mm, n - 1);
+          const double sx = 2.0 * hx, sy = 2.0 * hy, sz = 2.0 * hz;
+          const double ex = (X(0, l, mm, n) - m.x) / sx, ey = (X(1, l, mm, n) - m.y) / sy, ez = (X(2, l, mm, n) - m.z) / sz;
+          const double dx = std::exp(-0.5 * (ex * ex)) / (sx * std::sqrt(2.0 * pi));
+          const double dy = std::exp(-0.5 * (ey * ey)) / (sy * std::sqrt(2.0 * pi));
+          const double dz = std::exp(-0.5 * (ez * ez)) / (sz * std::sqrt(2.0 * pi));
+          C.delta[e] = dx * dy * dz;
+        } else {
+          const size_t p = (size_t)l + (size_t)nq * ((size_t)mm + (size_t)nr * n);
+          const double hx = hq / metric_at(p, 0), hy = hr / metric_at(p, 1), hz = hs / metric_at(p, 2);
+          const double ax = (m.x - near[0]) / hx, ay = (m.y - near[1]) / hy, az = (m.z - near[2]) / hz;
+          const double dx = point_delta(l, n0[0], hx, ax, order, alpha1);
+          const double dy = point_delta(mm, n0[1], hy, ay, order, alpha1);
+          const double dz = point_delta(n, n0[2], hz, az, order, alpha1);
+          C.delta[e] = dx * dy * dz;
+        }
+      }
 }
 
 int setup_block(wql_scn* S, int b) {
@@ -385,6 +516,30 @@ int setup_block(wql_scn* S, int b) {
                        cudaMemcpyHostToDevice, S->stream));
     CK(cudaStreamSynchronize(S->stream));
   }
+  // moment-tensor sources: placement and delta of every listed source
+  if (S->P.use_moment_tensor) {
+    const Problem& Pr = S->P;
+    // q_x, r_y, s_z on the host (the discrete delta uses the local spacing
+    // h/metric at each point of its support)
+    std::vector<double> diag[3];
+    if (!Pr.mollify_source) {
+      const int di[3] = {0, 4, 8};
+      for (int d = 0; d < 3; ++d) {
+        diag[d].resize(np);
+        CK(cudaMemcpy(diag[d].data(), metric + (size_t)di[d] * np, np * sizeof(double), cudaMemcpyDeviceToHost));
+      }
+    }
+    auto metric_at = [&](size_t p, int d) { return diag[d][p]; };
+    const std::vector<MomentSource>& own = b == 0 ? Pr.tensorsU : Pr.tensorsV;
+    const std::vector<MomentSource>* lists[2] = {&Pr.tensors, &own};
+    for (int li = 0; li < 2; ++li) {
+      const auto& L = *lists[li];
+      const int alpha1 = L.empty() ? 0 : L[0].alpha;
+      S->mt_cand[b][li].resize(L.size());
+      for (size_t i = 0; i < L.size(); ++i)
+        place_source(G, L[i], Pr.mt_order, alpha1, Pr.mollify_source, metric_at, S->mt_cand[b][li][i]);
+    }
+  }
   CK(cudaStreamSynchronize(S->stream));
   S->release(x);
   S->release(metric);
@@ -483,7 +638,21 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   if (Pr.fd_type != "traditional")
     return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' is not supported (6th-order traditional SBP only)");
   if (Pr.response == "anelastic") return fail(WQL_E_INPUT, "response='anelastic' is not supported");
-  if (Pr.use_moment_tensor) return fail(WQL_E_INPUT, "moment-tensor sources are not supported by this entry point");
+  if (Pr.use_moment_tensor) {
+    if (Pr.mt_order != 2 && Pr.mt_order != 4) return fail(WQL_E_INPUT, "moment_list order must be 2 or 4");
+    for (const auto* L : {&Pr.tensors, &Pr.tensorsU, &Pr.tensorsV}) {
+      for (const auto& m : *L) {
+        double A;
+        if (!source_time(m.type, 0.0, m.t_init, m.duration, A))
+          return fail(WQL_E_INPUT, "invalid source type '" + m.type + "' (src/moment_tensor.f90:970)");
+      }
+      if (Pr.mt_order == 4 && !L->empty()) {
+        const int a = (*L)[0].alpha;
+        if (a != 0 && a != 25 && a != 50 && a != 100)
+          return fail(WQL_E_INPUT, "order-4 sources need alpha 0, 25, 50 or 100 (src/moment_tensor.f90:1129-1262)");
+      }
+    }
+  }
   S->curv = Pr.type_of_mesh == "curvilinear";
   S->bc_form = Pr.bc_penalty == "weighted" ? BC_WEIGHTED : BC_CHARACTERISTIC;
   S->plastic = Pr.response == "plastic";
@@ -534,6 +703,45 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   if ((rc = S->alloc((void**)&S->xij, 2 * 3 * nf * sizeof(double)))) return rc;
   for (int b = 0; b < 2; ++b)
     if ((rc = setup_block(S.get(), b))) return rc;
+  // moment-tensor sources: the unified list goes to the preferred block when
+  // the source lies in its box, else to the other block when it lies in
+  // that one; per-block lists stay with their block; a source in no block is
+  // not applied (the reference keeps it at grid index -1, where its discrete
+  // delta still reaches the block's corner points 1..3 of each axis,
+  // src/moment_tensor.f90:318-345 -- not reproduced here)
+  if (Pr.use_moment_tensor) {
+    auto take = [&](int b, const MomentSource& m, const wql_scn::MTCand& C) -> int {
+      if (!C.found) return WQL_OK;
+      wql_scn::MTSrc T;
+      T.src = m;
+      for (int c = 0; c < 3; ++c) {
+        T.lo[c] = C.lo[c];
+        T.dim[c] = C.dim[c];
+      }
+      int r2;
+      if ((r2 = S->alloc((void**)&T.delta, C.delta.size() * sizeof(double), false))) return r2;
+      CK(cudaMemcpy(T.delta, C.delta.data(), C.delta.size() * sizeof(double), cudaMemcpyHostToDevice));
+      S->mt[b].push_back(T);
+      return WQL_OK;
+    };
+    if (Pr.mt_unified) {
+      const int pref = Pr.mt_block_preference == 2 ? 1 : 0;
+      for (size_t i = 0; i < Pr.tensors.size(); ++i) {
+        int b = -1;
+        if (S->mt_cand[pref][0][i].in_box) b = pref;
+        else if (S->mt_cand[1 - pref][0][i].in_box) b = 1 - pref;
+        if (b >= 0 && (rc = take(b, Pr.tensors[i], S->mt_cand[b][0][i]))) return rc;
+      }
+    } else {
+      for (int b = 0; b < 2; ++b) {
+        const auto& L = b == 0 ? Pr.tensorsU : Pr.tensorsV;
+        for (size_t i = 0; i < L.size(); ++i)
+          if (S->mt_cand[b][1][i].in_box && (rc = take(b, L[i], S->mt_cand[b][1][i]))) return rc;
+      }
+    }
+    for (int b = 0; b < 2; ++b)
+      for (int li = 0; li < 2; ++li) S->mt_cand[b][li].clear();
+  }
   if ((rc = S->alloc((void**)&S->S, 2 * 4 * nf * sizeof(double)))) return rc;
   if ((rc = S->alloc((void**)&S->DS, 2 * 4 * nf * sizeof(double)))) return rc;
   if ((rc = S->alloc((void**)&S->W, 2 * nf * sizeof(double)))) return rc;
@@ -717,6 +925,18 @@ int run_step(wql_scn* S) {
       else launch_volume<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       if (S->profiling) mark_end();
       if (S->profiling) mark(2);
+      // moment-tensor sources (set_rates, src/domain.f90:926-952) at the stage time
+      for (const auto& T : S->mt[b]) {
+        double At = 0.0;
+        source_time(T.src.type, ts, T.src.t_init, T.src.duration, At);
+        double am[6];
+        for (int c = 0; c < 6; ++c) am[c] = At * T.src.m[c];
+        if (S->prec == WQL_FP64)
+          launch_source<double>(volume_args<double>(S, b, A, Bdt, stage == 5), T.lo, T.dim, T.delta, am, S->stream);
+        else
+          launch_source<float>(volume_args<float>(S, b, A, Bdt, stage == 5), T.lo, T.dim, T.delta, am, S->stream);
+        launches += 1;
+      }
       if (S->prec == WQL_FP64) launches += launch_corrections<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       else launches += launch_corrections<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
       if (S->profiling) mark_end();

@@ -139,6 +139,11 @@ template <typename T>
 int launch_pre(const VolumeArgs<T>& a, void* stream);
 template <typename T>
 int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream);
+// One moment-tensor source: DF(4:9) -= am * delta on a box of points
+// (0-based origin lo, extents dim, delta q fastest), F_out to match.
+template <typename T>
+void launch_source(const VolumeArgs<T>& a, const int lo[3], const int dim[3], const double* delta,
+                   const double am[6], void* stream);
 void launch_interface(const InterfaceArgs& a, void* stream);
 void launch_metrics(int nq, int nr, int ns, const double* x, double* metric, double* J,
                     void* stream);

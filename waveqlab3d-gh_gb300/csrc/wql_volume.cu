@@ -643,6 +643,35 @@ __global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ V
 }
 
 // ---------------------------------------------------------------------------
+// Moment-tensor point source (set_moment_tensor / set_moment_tensor_smooth,
+// src/moment_tensor.f90:1014-1078, 1400-1475): DF(4:9) -= (A(t) M) * delta
+// on the source's box of points, with the matching update of F_out.
+struct SourceArgs {
+  int lo[3], dim[3];
+  const double* delta;
+  double am[6];
+};
+
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(256) source_kernel(const __grid_constant__ VolumeArgs<T> a,
+                                                     const __grid_constant__ SourceArgs s) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n = (long long)s.dim[0] * s.dim[1] * s.dim[2];
+  if (e >= n) return;
+  const int i = s.lo[0] + (int)(e % s.dim[0]);
+  const int j = s.lo[1] + (int)((e / s.dim[0]) % s.dim[1]);
+  const int k = s.lo[2] + (int)(e / ((long long)s.dim[0] * s.dim[1]));
+  const long long p = i + (long long)a.pq * (j + (long long)a.nr * k);
+  const double d = s.delta[e];
+  T corr[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) corr[c] = T(0);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) corr[3 + c] = (T)(-(s.am[c] * d));
+  add_correction<T, KAHAN>(a, p, corr);
+}
+
+// ---------------------------------------------------------------------------
 // Plastic return map after the last stage (update_fields_plastic,
 // src/plastic.f90:11-151, plastic_flow2 :153-217), on points outside the PML
 // slabs, applied to the updated stresses.
@@ -794,6 +823,27 @@ int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream) {
   return kahan ? launch_corr<T, false, true>(a, s) : launch_corr<T, false, false>(a, s);
 }
 
+template <typename T>
+void launch_source(const VolumeArgs<T>& a, const int lo[3], const int dim[3], const double* delta,
+                   const double am[6], void* stream) {
+  SourceArgs s;
+  for (int c = 0; c < 3; ++c) {
+    s.lo[c] = lo[c];
+    s.dim[c] = dim[c];
+  }
+  for (int c = 0; c < 6; ++c) s.am[c] = am[c];
+  s.delta = delta;
+  const long long n = (long long)dim[0] * dim[1] * dim[2];
+  if (n <= 0) return;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  if (a.C) source_kernel<T, true><<<g, 256, 0, (cudaStream_t)stream>>>(a, s);
+  else source_kernel<T, false><<<g, 256, 0, (cudaStream_t)stream>>>(a, s);
+}
+
+template void launch_source<double>(const VolumeArgs<double>&, const int*, const int*, const double*,
+                                    const double*, void*);
+template void launch_source<float>(const VolumeArgs<float>&, const int*, const int*, const double*,
+                                   const double*, void*);
 template void launch_volume<double>(const VolumeArgs<double>&, bool, void*);
 template void launch_volume<float>(const VolumeArgs<float>&, bool, void*);
 template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
