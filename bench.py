@@ -231,6 +231,40 @@ def cpu_sample(text, media, steps, warmup=0):
     return t1 - t0, os.cpu_count()
 
 
+def accuracy(wql, ctx, text, media, steps, stride=20):
+    """FP32C against FP64 on the same workload after `steps` steps: relative
+    L2 of the velocity fields and of the slip, relative error of the peak
+    slip rate (over fault frames every `stride` steps) and the largest
+    rupture-time difference in time steps over points that ruptured in both."""
+    import numpy as np
+    text_f = text.replace("w_fault = F", "w_fault = T").replace("w_stride = 1", f"w_stride = {stride}")
+    out = {}
+    runs = {}
+    for name, prec in (("fp64", wql.FP64), ("fp32c", wql.FP32C)):
+        s = wql.Scenario(ctx, text=text_f, precision=prec, media=media)
+        for _ in range(0, steps, 100):
+            s.step(min(100, steps - _))
+        s.sync(check_nan=True)
+        runs[name] = dict(v=[np.concatenate([s.field(b, c).ravel() for c in range(3)]) for b in range(2)],
+                          slip=s.iface(0, 3), trup=s.iface(0, 5),
+                          peak=float(np.sqrt((s.frames("Svel")[:, 1:3].astype(np.float64) ** 2).sum(axis=1)).max()),
+                          dt=s.info().dt)
+        s.close()
+    d, f = runs["fp64"], runs["fp32c"]
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
+    rup_d, rup_f = d["trup"] < 1e8, f["trup"] < 1e8
+    both = rup_d & rup_f
+    out["steps"] = steps
+    out["velocity_rel_l2"] = max(rel(f["v"][b], d["v"][b]) for b in range(2))
+    out["slip_rel_l2"] = rel(f["slip"], d["slip"])
+    out["peak_slip_rate_rel"] = abs(f["peak"] - d["peak"]) / max(abs(d["peak"]), 1e-300)
+    out["peak_slip_rate_fp64"] = d["peak"]
+    out["ruptured_points_fp64"] = int(rup_d.sum())
+    out["ruptured_points_fp32c"] = int(rup_f.sum())
+    out["rupture_time_err_dt"] = float(np.abs(f["trup"][both] - d["trup"][both]).max() / d["dt"]) if both.any() else None
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -242,6 +276,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="instead of timing, run FP32C and FP64 this many steps and report their differences")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     text, media, ups = workload(args)
@@ -271,6 +307,12 @@ def main():
     import wql_build
     wql_build.build()
     import wql
+    if args.accuracy_steps > 0:
+        ctx = wql.Context(local)
+        res = accuracy(wql, ctx, text, media, args.accuracy_steps)
+        if rank == 0:
+            print(json.dumps({"workload": wl, "fp32c_vs_fp64": res}))
+        return
     ctx = wql.Context(local)
     res = {}
     with Clocks(local) as clk:
