@@ -144,6 +144,26 @@ int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords);
 int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 
+/* Continuous batching of scenarios on one device.  wql_batch_step advances
+ * every member by nsteps steps: per RK stage, the stencil of every eligible
+ * block of every member (FP32C, default or TMA stencil variant) is one
+ * kernel launch over a packed table of (block, tile, s chunk) work, and the
+ * members' fault, boundary, source and correction kernels run on their own
+ * streams around it.  Members may have different sizes, physics and time
+ * steps; each advances exactly as wql_step would advance it alone.  Members
+ * join (wql_batch_add) and leave (wql_batch_remove) between calls; a member
+ * must not be stepped on its own while it is in a batch.  wql_batch_stream
+ * gives the stream that every member's work of a call joins into (for
+ * timing with events).  No counterpart in the reference, which runs one
+ * domain per MPI job. */
+typedef struct wql_batch wql_batch;
+int wql_batch_create(wql_ctx* ctx, wql_batch** out);
+int wql_batch_destroy(wql_batch* b);
+int wql_batch_add(wql_batch* b, wql_scn* scn);
+int wql_batch_remove(wql_batch* b, wql_scn* scn);
+int wql_batch_step(wql_batch* b, int nsteps);
+int wql_batch_stream(wql_batch* b, uintptr_t* stream);
+
 /* The CUDA stream the scenario's kernels run on (cudaStream_t as integer),
  * for callers that time or order work around wql_step. */
 int wql_scenario_stream(wql_scn* scn, uintptr_t* stream);

@@ -857,99 +857,129 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   return a;
 }
 
-int run_step(wql_scn* S) {
-  const long long nf = (long long)S->B[0].nr * S->B[0].ns;
-  const bool want_frame = S->frame_dev && (S->nstep % std::max(S->P.w_stride, 1) == 0);
-  const bool want_station = S->P.output_seismograms && (S->st[0].ijk.size() + S->st[1].ijk.size() > 0) &&
-                            (S->nstep % std::max(S->P.w_stride, 1) == 0);
-  const double t0 = S->t;
+// One time step split into phases so that a batch can interleave the
+// phases of many scenarios: per stage the interface kernel (and the stage-1
+// station gather), per block the face pre-kernel, the stencil, then the
+// sources and correction kernels.  run_step strings them together for one
+// scenario.
+struct StepCtx {
+  bool want_frame = false, want_station = false;
+  double t0 = 0.0;
   int launches = 0;
-  for (int stage = 1; stage <= 5; ++stage) {
-    const double A = S->rk.A[stage], Bdt = S->rk.B[stage] * S->dt;
-    const double ts = t0 + S->rk.C[stage - 1] * S->dt;
-    InterfaceArgs ia;
-    std::memset(&ia, 0, sizeof(ia));
-    ia.nr = S->B[0].nr; ia.ns = S->B[0].ns;
-    ia.np0 = S->B[0].np; ia.np1 = S->B[1].np; ia.nq0 = S->B[0].nq;
-    ia.pq0 = S->B[0].pq; ia.pq1 = S->B[1].pq;
-    ia.fp64 = S->prec == WQL_FP64;
-    ia.F0 = S->B[0].F[S->cur];
-    ia.F1 = S->B[1].F[S->cur];
-    ia.face0 = S->B[0].face[1];
-    ia.face1 = S->B[1].face[0];
-    ia.xij = S->xij;
-    ia.S = S->S; ia.DS = S->DS; ia.W = S->W; ia.DW = S->DW; ia.trup = S->trup;
-    ia.sat = S->sat;
-    ia.tau_h[0] = S->B[0].tau_h[0];
-    ia.tau_h[1] = S->B[1].tau_h[0];
-    ia.A = A; ia.Bdt = Bdt; ia.t = ts; ia.stage = stage;
-    ia.pre = S->pre;
-    ia.ramp = nucleation_ramp(S->fp, ts);
-    {
-      const double x0[3] = {0.0, 0.0, 0.0};  // V0 does not vary along the fault
-      ia.lnV0h = std::log(0.5 / rs_params(S->fp, x0, 0.0).V0);
-    }
-    ia.fp = S->fp;
-    ia.frame = (want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
-    ia.solver_fail = S->solver_fail;
-    auto mark = [&](int kind) {
-      S->ev_marks.push_back({S->ev_used, kind});
-      cudaEventRecord(S->next_event(), S->stream);
-    };
-    auto mark_end = [&]() { cudaEventRecord(S->next_event(), S->stream); };
-    if (S->profiling) mark(0);
-    launch_interface(ia, S->stream);
-    launches += 1;
-    if (S->profiling) mark_end();
-    if (stage == 1 && want_station) {
-      // stage-1 fields are the fields at t0 (write_output, src/time_step.f90:137)
-      for (int b = 0; b < 2; ++b) {
-        auto& T = S->st[b];
-        const int n = (int)T.ijk.size() / 3;
-        if (n == 0) continue;
-        double* out = T.ring + (size_t)S->st_fill * n * 3;
-        if (S->prec == WQL_FP64)
-          station_kernel<double><<<(n + 127) / 128, 128, 0, S->stream>>>((const double*)S->B[b].F[S->cur], S->B[b].np, T.idx_dev, n, out);
-        else
-          station_kernel<float><<<(n + 127) / 128, 128, 0, S->stream>>>((const float*)S->B[b].F[S->cur], S->B[b].np, T.idx_dev, n, out);
-        launches += 1;
-      }
-    }
-    for (int b = 0; b < 2; ++b) {
-      if (S->profiling) mark(2);
-      if (S->prec == WQL_FP64) launches += launch_pre<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->stream);
-      else launches += launch_pre<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->stream);
-      if (S->profiling) mark_end();
-      if (S->profiling) mark(1);
-      if (S->prec == WQL_FP64) launch_volume<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
-      else launch_volume<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
-      if (S->profiling) mark_end();
-      if (S->profiling) mark(2);
-      // moment-tensor sources (set_rates, src/domain.f90:926-952) at the stage time
-      for (const auto& T : S->mt[b]) {
-        double At = 0.0;
-        source_time(T.src.type, ts, T.src.t_init, T.src.duration, At);
-        double am[6];
-        for (int c = 0; c < 6; ++c) am[c] = At * T.src.m[c];
-        if (S->prec == WQL_FP64)
-          launch_source<double>(volume_args<double>(S, b, A, Bdt, stage == 5), T.lo, T.dim, T.delta, am, S->stream);
-        else
-          launch_source<float>(volume_args<float>(S, b, A, Bdt, stage == 5), T.lo, T.dim, T.delta, am, S->stream);
-        launches += 1;
-      }
-      if (S->prec == WQL_FP64) launches += launch_corrections<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
-      else launches += launch_corrections<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
-      if (S->profiling) mark_end();
-      launches += 1;
-    }
-    S->cur ^= 1;
+};
+
+StepCtx step_begin(wql_scn* S) {
+  StepCtx c;
+  c.want_frame = S->frame_dev && (S->nstep % std::max(S->P.w_stride, 1) == 0);
+  c.want_station = S->P.output_seismograms && (S->st[0].ijk.size() + S->st[1].ijk.size() > 0) &&
+                   (S->nstep % std::max(S->P.w_stride, 1) == 0);
+  c.t0 = S->t;
+  return c;
+}
+
+double stage_A(const wql_scn* S, int stage) { return S->rk.A[stage]; }
+double stage_Bdt(const wql_scn* S, int stage) { return S->rk.B[stage] * S->dt; }
+double stage_time(const wql_scn* S, const StepCtx& c, int stage) { return c.t0 + S->rk.C[stage - 1] * S->dt; }
+
+void mark_begin(wql_scn* S, int kind) {
+  if (!S->profiling) return;
+  S->ev_marks.push_back({S->ev_used, kind});
+  cudaEventRecord(S->next_event(), S->stream);
+}
+void mark_end(wql_scn* S) {
+  if (S->profiling) cudaEventRecord(S->next_event(), S->stream);
+}
+
+void stage_head(wql_scn* S, StepCtx& c, int stage) {
+  const long long nf = (long long)S->B[0].nr * S->B[0].ns;
+  const double ts = stage_time(S, c, stage);
+  InterfaceArgs ia;
+  std::memset(&ia, 0, sizeof(ia));
+  ia.nr = S->B[0].nr; ia.ns = S->B[0].ns;
+  ia.np0 = S->B[0].np; ia.np1 = S->B[1].np; ia.nq0 = S->B[0].nq;
+  ia.pq0 = S->B[0].pq; ia.pq1 = S->B[1].pq;
+  ia.fp64 = S->prec == WQL_FP64;
+  ia.F0 = S->B[0].F[S->cur];
+  ia.F1 = S->B[1].F[S->cur];
+  ia.face0 = S->B[0].face[1];
+  ia.face1 = S->B[1].face[0];
+  ia.xij = S->xij;
+  ia.S = S->S; ia.DS = S->DS; ia.W = S->W; ia.DW = S->DW; ia.trup = S->trup;
+  ia.sat = S->sat;
+  ia.tau_h[0] = S->B[0].tau_h[0];
+  ia.tau_h[1] = S->B[1].tau_h[0];
+  ia.A = stage_A(S, stage); ia.Bdt = stage_Bdt(S, stage); ia.t = ts; ia.stage = stage;
+  ia.pre = S->pre;
+  ia.ramp = nucleation_ramp(S->fp, ts);
+  {
+    const double x0[3] = {0.0, 0.0, 0.0};  // V0 does not vary along the fault
+    ia.lnV0h = std::log(0.5 / rs_params(S->fp, x0, 0.0).V0);
   }
+  ia.fp = S->fp;
+  ia.frame = (c.want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
+  ia.solver_fail = S->solver_fail;
+  mark_begin(S, 0);
+  launch_interface(ia, S->stream);
+  c.launches += 1;
+  mark_end(S);
+  if (stage == 1 && c.want_station) {
+    // stage-1 fields are the fields at t0 (write_output, src/time_step.f90:137)
+    for (int b = 0; b < 2; ++b) {
+      auto& T = S->st[b];
+      const int n = (int)T.ijk.size() / 3;
+      if (n == 0) continue;
+      double* out = T.ring + (size_t)S->st_fill * n * 3;
+      if (S->prec == WQL_FP64)
+        station_kernel<double><<<(n + 127) / 128, 128, 0, S->stream>>>((const double*)S->B[b].F[S->cur], S->B[b].np, T.idx_dev, n, out);
+      else
+        station_kernel<float><<<(n + 127) / 128, 128, 0, S->stream>>>((const float*)S->B[b].F[S->cur], S->B[b].np, T.idx_dev, n, out);
+      c.launches += 1;
+    }
+  }
+}
+
+void stage_block_pre(wql_scn* S, StepCtx& c, int stage, int b) {
+  mark_begin(S, 2);
+  if (S->prec == WQL_FP64) c.launches += launch_pre<double>(volume_args<double>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->stream);
+  else c.launches += launch_pre<float>(volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->stream);
+  mark_end(S);
+}
+
+void stage_block_stencil(wql_scn* S, StepCtx& c, int stage, int b) {
+  mark_begin(S, 1);
+  if (S->prec == WQL_FP64) launch_volume<double>(volume_args<double>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->curv, S->stream);
+  else launch_volume<float>(volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->curv, S->stream);
+  mark_end(S);
+  c.launches += 1;
+}
+
+void stage_block_post(wql_scn* S, StepCtx& c, int stage, int b) {
+  const double A = stage_A(S, stage), Bdt = stage_Bdt(S, stage), ts = stage_time(S, c, stage);
+  mark_begin(S, 2);
+  // moment-tensor sources (set_rates, src/domain.f90:926-952) at the stage time
+  for (const auto& T : S->mt[b]) {
+    double At = 0.0;
+    source_time(T.src.type, ts, T.src.t_init, T.src.duration, At);
+    double am[6];
+    for (int k = 0; k < 6; ++k) am[k] = At * T.src.m[k];
+    if (S->prec == WQL_FP64)
+      launch_source<double>(volume_args<double>(S, b, A, Bdt, stage == 5), T.lo, T.dim, T.delta, am, S->stream);
+    else
+      launch_source<float>(volume_args<float>(S, b, A, Bdt, stage == 5), T.lo, T.dim, T.delta, am, S->stream);
+    c.launches += 1;
+  }
+  if (S->prec == WQL_FP64) c.launches += launch_corrections<double>(volume_args<double>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+  else c.launches += launch_corrections<float>(volume_args<float>(S, b, A, Bdt, stage == 5), S->curv, S->stream);
+  mark_end(S);
+}
+
+int step_end(wql_scn* S, StepCtx& c) {
   CK(cudaGetLastError());
-  S->launches_last_step = launches;
-  S->t = t0 + S->rk.C[5] * S->dt;
+  S->launches_last_step = c.launches;
+  S->t = c.t0 + S->rk.C[5] * S->dt;
   S->nstep += 1;
-  if (want_station) {
-    S->st_times.push_back(t0);
+  if (c.want_station) {
+    S->st_times.push_back(c.t0);
     S->st_fill += 1;
     S->st_records += 1;
     if (S->st_fill == S->st_cap) {
@@ -957,12 +987,140 @@ int run_step(wql_scn* S) {
       if (rc) return rc;
     }
   }
-  if (want_frame) {
+  if (c.want_frame) {
     S->frame_fill += 1;
     S->nframes += 1;
     if (S->frame_fill == S->frame_cap) return flush_frames(S);
   }
   return WQL_OK;
+}
+
+int run_step(wql_scn* S);
+
+}  // namespace
+
+// Scenarios advanced together (continuous batching): per stage each member's
+// interface and face pre-kernels run on the member's own stream, the stencil
+// of every TMA-eligible block of every member is one launch from a packed
+// table on the batch stream, and the members' source and correction kernels
+// run on their own streams again.  Members join and leave between steps.
+struct wql_batch {
+  wql_ctx* ctx = nullptr;
+  std::vector<wql_scn*> members;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t joined = nullptr;
+  std::vector<cudaEvent_t> ev;
+  TmaBatchDesc* d_dev = nullptr;
+  size_t d_cap = 0;
+  std::vector<TmaBatchDesc> d_host;
+  ~wql_batch() {
+    for (auto e : ev) cudaEventDestroy(e);
+    if (joined) cudaEventDestroy(joined);
+    if (d_dev) cudaFree(d_dev);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+bool batch_tma(const wql_scn* S) {
+  return S->prec == WQL_FP32C && (S->kernel_variant == 0 || S->kernel_variant == 5 || S->kernel_variant == 6);
+}
+
+int batch_step(wql_batch* B) {
+  const size_t n = B->members.size();
+  while (B->ev.size() < n) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    B->ev.push_back(e);
+  }
+  std::vector<StepCtx> c(n);
+  for (size_t i = 0; i < n; ++i) c[i] = step_begin(B->members[i]);
+  for (int stage = 1; stage <= 5; ++stage) {
+    for (size_t i = 0; i < n; ++i) {
+      wql_scn* S = B->members[i];
+      stage_head(S, c[i], stage);
+      for (int b = 0; b < 2; ++b) stage_block_pre(S, c[i], stage, b);
+    }
+    // the packed stencil table: one group per (curvilinear, compensated)
+    for (int curv = 0; curv < 2; ++curv) {
+      B->d_host.clear();
+      std::vector<size_t> who;
+      long long total = 0;
+      for (size_t i = 0; i < n; ++i) {
+        wql_scn* S = B->members[i];
+        if (!batch_tma(S) || (int)S->curv != curv) continue;
+        bool any = false;
+        for (int b = 0; b < 2; ++b) {
+          VolumeArgs<float> a = volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5);
+          if (!tma_eligible(a)) continue;
+          TmaBatchDesc d;
+          const long long k = fill_tma_desc(a, d);
+          d.cta0 = total;
+          total += k;
+          B->d_host.push_back(d);
+          any = true;
+        }
+        if (any) who.push_back(i);
+      }
+      if (B->d_host.empty()) continue;
+      if (B->d_host.size() > B->d_cap) {
+        if (B->d_dev) cudaFree(B->d_dev);
+        B->d_cap = B->d_host.size() * 2;
+        CK(cudaMalloc(&B->d_dev, B->d_cap * sizeof(TmaBatchDesc)));
+      }
+      for (size_t i : who) {
+        CK(cudaEventRecord(B->ev[i], B->members[i]->stream));
+        CK(cudaStreamWaitEvent(B->stream, B->ev[i], 0));
+      }
+      CK(cudaMemcpyAsync(B->d_dev, B->d_host.data(), B->d_host.size() * sizeof(TmaBatchDesc),
+                         cudaMemcpyHostToDevice, B->stream));
+      launch_stencil_tma_batch(B->d_dev, (int)B->d_host.size(), total, curv == 1, true, 3, B->stream);
+      CK(cudaEventRecord(B->joined, B->stream));
+      for (size_t i : who) {
+        CK(cudaStreamWaitEvent(B->members[i]->stream, B->joined, 0));
+        c[i].launches += 1;
+      }
+    }
+    // blocks outside the packed launch: their own stencil launch
+    for (size_t i = 0; i < n; ++i) {
+      wql_scn* S = B->members[i];
+      for (int b = 0; b < 2; ++b) {
+        bool packed = false;
+        if (batch_tma(S)) packed = tma_eligible(volume_args<float>(S, b, 0.0, 0.0, false));
+        if (!packed) stage_block_stencil(S, c[i], stage, b);
+      }
+    }
+    for (size_t i = 0; i < n; ++i) {
+      wql_scn* S = B->members[i];
+      for (int b = 0; b < 2; ++b) stage_block_post(S, c[i], stage, b);
+      S->cur ^= 1;
+    }
+  }
+  for (size_t i = 0; i < n; ++i) {
+    const int rc = step_end(B->members[i], c[i]);
+    if (rc) return rc;
+  }
+  // the batch stream ends after every member's step
+  for (size_t i = 0; i < n; ++i) {
+    CK(cudaEventRecord(B->ev[i], B->members[i]->stream));
+    CK(cudaStreamWaitEvent(B->stream, B->ev[i], 0));
+  }
+  return WQL_OK;
+}
+
+int run_step(wql_scn* S) {
+  StepCtx c = step_begin(S);
+  for (int stage = 1; stage <= 5; ++stage) {
+    stage_head(S, c, stage);
+    for (int b = 0; b < 2; ++b) {
+      stage_block_pre(S, c, stage, b);
+      stage_block_stencil(S, c, stage, b);
+      stage_block_post(S, c, stage, b);
+    }
+    S->cur ^= 1;
+  }
+  return step_end(S, c);
 }
 
 }  // namespace
@@ -1242,6 +1400,66 @@ int wql_get_seismograms(wql_scn* scn, int block, double* host_out) {
   const int rc = flush_stations(scn);
   if (rc) return rc;
   std::memcpy(host_out, scn->st[block].host.data(), scn->st[block].host.size() * sizeof(double));
+  return WQL_OK;
+}
+
+int wql_batch_create(wql_ctx* ctx, wql_batch** out) {
+  if (!ctx || !out) return fail(WQL_E_INPUT, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  std::unique_ptr<wql_batch> B(new wql_batch());
+  B->ctx = ctx;
+  CK(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&B->joined, cudaEventDisableTiming));
+  *out = B.release();
+  return WQL_OK;
+}
+
+int wql_batch_destroy(wql_batch* b) {
+  if (b) {
+    cudaStreamSynchronize(b->stream);
+    delete b;
+  }
+  return WQL_OK;
+}
+
+int wql_batch_add(wql_batch* b, wql_scn* scn) {
+  if (!b || !scn) return fail(WQL_E_INPUT, "null argument");
+  if (scn->ctx->device != b->ctx->device) return fail(WQL_E_INPUT, "scenario is on another device");
+  for (auto* m : b->members)
+    if (m == scn) return fail(WQL_E_STATE, "scenario is already in the batch");
+  b->members.push_back(scn);
+  return WQL_OK;
+}
+
+int wql_batch_remove(wql_batch* b, wql_scn* scn) {
+  if (!b || !scn) return fail(WQL_E_INPUT, "null argument");
+  for (size_t i = 0; i < b->members.size(); ++i)
+    if (b->members[i] == scn) {
+      CK(cudaStreamSynchronize(b->stream));
+      b->members.erase(b->members.begin() + i);
+      return WQL_OK;
+    }
+  return fail(WQL_E_STATE, "scenario is not in the batch");
+}
+
+int wql_batch_step(wql_batch* b, int nsteps) {
+  if (!b) return fail(WQL_E_INPUT, "null batch");
+  if (nsteps < 0) return fail(WQL_E_INPUT, "negative step count");
+  CK(cudaSetDevice(b->ctx->device));
+  for (int k = 0; k < nsteps; ++k) {
+    const int rc = batch_step(b);
+    if (rc) return rc;
+  }
+  for (auto* m : b->members) {
+    const int rc = flush_frames(m);
+    if (rc) return rc;
+  }
+  return WQL_OK;
+}
+
+int wql_batch_stream(wql_batch* b, uintptr_t* stream) {
+  if (!b || !stream) return fail(WQL_E_INPUT, "null argument");
+  *stream = (uintptr_t)b->stream;
   return WQL_OK;
 }
 

@@ -127,6 +127,26 @@ int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, vo
 // 3-deep ring of shared-memory stages.
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int stages, void* stream);
 
+// One entry of the packed table of the batched TMA stencil launch: one block
+// at one stage (its tensor maps for the stage's input buffer, its arguments)
+// and the range of CTAs [cta0, cta0 + tq*tr*nchunk) that work on it.
+struct TmaBatchDesc {
+  CUtensorMap m[8];  // field box, lead fields, coefficient boxes (q, r, tile, lead), DF, C
+  VolumeArgs<float> a;
+  int schunk, tq, tr, nchunk;
+  long long cta0;
+};
+// Fills d for one block (a.tma must point at the block's StencilMaps) and
+// returns the number of CTAs it needs.
+long long fill_tma_desc(const VolumeArgs<float>& a, TmaBatchDesc& d);
+// Whether a block can go through the TMA stencil (FP32, r extent that keeps
+// the closure rows of the shifted last r tile inside the halo).
+bool tma_eligible(const VolumeArgs<float>& a);
+// One launch over nd table entries (all curvilinear or all Cartesian, all
+// with or all without compensation).
+void launch_stencil_tma_batch(const TmaBatchDesc* d_dev, int nd, long long total_ctas, bool curv, bool kahan,
+                              int stages, void* stream);
+
 // One stage on one block: launch_volume runs the stencil kernel (DF and the
 // updated fields for every point); launch_corrections then adds the PML,
 // boundary/fault penalty and plastic kernels and returns how many it issued.

@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "wql_internal.h"
 #include "wql_stencil.cuh"
@@ -159,9 +160,10 @@ struct MapArgs {
   CUtensorMap fbox, flead, ca, cb, cc, cl, df, ck;
 };
 
+// The work of one CTA: tile (bx, by) of the block, s chunk bz.
 template <bool CURV, bool KAHAN, int NS>
-__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
-    stencil_kernel_tma(const __grid_constant__ VolumeArgs<float> a, const __grid_constant__ MapArgs m, int schunk) {
+__device__ __forceinline__ void tma_body(const VolumeArgs<float>& a, const MapArgs& m, int schunk, int bx, int by,
+                                         int bz) {
   using TL = TmaTile<CURV, KAHAN>;
   constexpr int TQ = TL::TQ, TR = TL::TR, NC = TL::NC, BQ = TL::BQ, BR = TL::BR;
   constexpr int NCW = NC / 32;
@@ -175,10 +177,10 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
 
   const int tid = threadIdx.x;
   const int nq = a.nq, nr = a.nr, ns = a.ns;
-  const int q0 = blockIdx.x * TQ;
-  const TileSpan spr = tile_span(blockIdx.y, nr, TR);
+  const int q0 = bx * TQ;
+  const TileSpan spr = tile_span(by, nr, TR);
   const int r0 = spr.origin;
-  const int s_begin = blockIdx.z * schunk;
+  const int s_begin = bz * schunk;
   const int s_end = min(ns, s_begin + schunk);
   const int nstep = s_end - s_begin;
 
@@ -476,26 +478,41 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
 }
 
 template <bool CURV, bool KAHAN, int NS>
-void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t s) {
-  using TL = TmaTile<CURV, KAHAN>;
-  const int ncen = a.ns;
-  const size_t smem = sizeof(float) * (size_t)NS * TL::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
-  auto kern = stencil_kernel_tma<CURV, KAHAN, NS>;
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_done = true;
+__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
+    stencil_kernel_tma(const __grid_constant__ VolumeArgs<float> a, const __grid_constant__ MapArgs m, int schunk) {
+  tma_body<CURV, KAHAN, NS>(a, m, schunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One launch over many blocks (of one or many scenarios): CTA i works on the
+// descriptor whose CTA range holds i, found by binary search in the packed
+// table (descriptors sorted by cta0).
+template <bool CURV, bool KAHAN, int NS>
+__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
+    stencil_kernel_tma_batch(const TmaBatchDesc* __restrict__ d, int nd) {
+  const long long cta = blockIdx.x;
+  int lo = 0, hi = nd - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (d[mid].cta0 <= cta) lo = mid;
+    else hi = mid - 1;
   }
-  const int tq = (a.nq + TL::TQ - 1) / TL::TQ, tr = (a.nr + TL::TR - 1) / TL::TR;
-  int schunk = a.schunk;
-  if (schunk <= 0) {
-    // about 24 planes per chunk, equal chunks: measured on 2 x 201^3 blocks,
-    // shorter chunks balance the SMs better than fewer waves do, down to
-    // where the per-chunk start (the first six planes of the s window)
-    // shows
-    const int nc = std::max(1, (ncen + 12) / 24);
-    schunk = (ncen + nc - 1) / nc;
-  }
+  const TmaBatchDesc& D = d[lo];
+  const long long l = cta - D.cta0;
+  tma_body<CURV, KAHAN, NS>(D.a, *reinterpret_cast<const MapArgs*>(&D.m), D.schunk, (int)(l % D.tq),
+                            (int)((l / D.tq) % D.tr), (int)(l / ((long long)D.tq * D.tr)));
+}
+
+// Planes per s chunk: the tuned value, else about 24 in equal chunks
+// (measured on 2 x 201^3 blocks, shorter chunks balance the SMs better than
+// fewer waves do, down to where the per-chunk start -- the first six planes
+// of the s window -- shows).
+int chunk_planes(const VolumeArgs<float>& a) {
+  if (a.schunk > 0) return a.schunk;
+  const int nc = std::max(1, (a.ns + 12) / 24);
+  return (a.ns + nc - 1) / nc;
+}
+
+MapArgs stage_maps(const StencilMaps& sm) {
   MapArgs m;
   m.fbox = sm.fbox[sm.cur];
   m.flead = sm.flead[sm.cur];
@@ -505,8 +522,34 @@ void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t 
   m.cl = sm.cl;
   m.df = sm.df;
   m.ck = sm.ck;
-  dim3 grd(tq, tr, (ncen + schunk - 1) / schunk);
-  kern<<<grd, TL::NC + 32, smem, s>>>(a, m, schunk);
+  return m;
+}
+
+template <typename K>
+size_t prepare(K kern, int NS, int stage_words) {
+  const size_t smem = sizeof(float) * (size_t)NS * stage_words + (2 * NS + 1) * sizeof(uint64_t) + 128;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return smem;
+}
+
+template <bool CURV, bool KAHAN, int NS>
+void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t s) {
+  using TL = TmaTile<CURV, KAHAN>;
+  auto kern = stencil_kernel_tma<CURV, KAHAN, NS>;
+  static const size_t smem = prepare(kern, NS, TL::STAGE_W);
+  const int tq = (a.nq + TL::TQ - 1) / TL::TQ, tr = (a.nr + TL::TR - 1) / TL::TR;
+  const int schunk = chunk_planes(a);
+  dim3 grd(tq, tr, (a.ns + schunk - 1) / schunk);
+  kern<<<grd, TL::NC + 32, smem, s>>>(a, stage_maps(sm), schunk);
+}
+
+template <bool CURV, bool KAHAN, int NS>
+void launch_tma_batch(const TmaBatchDesc* d, int nd, long long total, cudaStream_t s) {
+  using TL = TmaTile<CURV, KAHAN>;
+  auto kern = stencil_kernel_tma_batch<CURV, KAHAN, NS>;
+  static const size_t smem = prepare(kern, NS, TL::STAGE_W);
+  if (total <= 0) return;
+  kern<<<(unsigned)total, TL::NC + 32, smem, s>>>(d, nd);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -566,6 +609,38 @@ int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, vo
   }
   m.ok = rc == 0;
   return rc;
+}
+
+long long fill_tma_desc(const VolumeArgs<float>& a, TmaBatchDesc& d) {
+  static_assert(sizeof(MapArgs) == sizeof(d.m), "map set layout");
+  const StencilMaps& sm = *static_cast<const StencilMaps*>(a.tma);
+  const MapArgs m = stage_maps(sm);
+  std::memcpy(d.m, &m, sizeof(m));
+  d.a = a;
+  d.schunk = chunk_planes(a);
+  d.tq = (a.nq + kTmaTQ - 1) / kTmaTQ;
+  d.tr = (a.nr + kTmaTR - 1) / kTmaTR;
+  d.nchunk = (a.ns + d.schunk - 1) / d.schunk;
+  d.cta0 = 0;
+  return (long long)d.tq * d.tr * d.nchunk;
+}
+
+bool tma_eligible(const VolumeArgs<float>& a) {
+  // tile_span keeps every r closure row inside tile + halo unless the
+  // shifted last tile starts at 4 or 5
+  return a.tma != nullptr && (a.nr <= kTmaTR + 3 || a.nr >= kTmaTR + 6);
+}
+
+void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bool curv, bool kahan, int stages,
+                              void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (stages == 2) {
+    if (curv) kahan ? launch_tma_batch<true, true, 2>(d, nd, total, s) : launch_tma_batch<true, false, 2>(d, nd, total, s);
+    else kahan ? launch_tma_batch<false, true, 2>(d, nd, total, s) : launch_tma_batch<false, false, 2>(d, nd, total, s);
+  } else {
+    if (curv) kahan ? launch_tma_batch<true, true, 3>(d, nd, total, s) : launch_tma_batch<true, false, 3>(d, nd, total, s);
+    else kahan ? launch_tma_batch<false, true, 3>(d, nd, total, s) : launch_tma_batch<false, false, 3>(d, nd, total, s);
+  }
 }
 
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int stages, void* stream) {

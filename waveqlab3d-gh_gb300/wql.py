@@ -24,7 +24,8 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_get_info", "wql_get_field", "wql_set_field", "wql_get_iface", "wql_frame_count",
            "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step", "wql_profile",
            "wql_kernel_times", "wql_set_tuning", "wql_get_field_noalloc", "wql_station_count",
-           "wql_station_index", "wql_get_seismograms"]
+           "wql_station_index", "wql_get_seismograms", "wql_batch_create", "wql_batch_destroy",
+           "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream"]
 
 
 class Media(ctypes.Structure):
@@ -70,6 +71,12 @@ def lib():
         L.wql_set_field.argtypes = [vp, ci, ci, vp]
         L.wql_get_field_noalloc.argtypes = [vp, ci, ci, vp]
         L.wql_station_count.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
+        L.wql_batch_create.argtypes = [vp, ctypes.POINTER(vp)]
+        L.wql_batch_destroy.argtypes = [vp]
+        L.wql_batch_add.argtypes = [vp, vp]
+        L.wql_batch_remove.argtypes = [vp, vp]
+        L.wql_batch_step.argtypes = [vp, ci]
+        L.wql_batch_stream.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
         L.wql_station_index.argtypes = [vp, ci, vp]
         L.wql_get_seismograms.argtypes = [vp, ci, vp]
         L.wql_get_iface.argtypes = [vp, ci, ci, vp]
@@ -248,3 +255,41 @@ class Scenario:
 
     def set_tuning(self, kernel=0, schunk=0):
         _check(lib().wql_set_tuning(self.h, kernel, schunk))
+
+
+class Batch:
+    """Scenarios advanced together (wql_batch_*): one packed stencil launch
+    per stage for all members."""
+
+    def __init__(self, ctx):
+        h = ctypes.c_void_p()
+        _check(lib().wql_batch_create(ctx.h, ctypes.byref(h)))
+        self.h = h.value
+        self.members = []
+
+    def add(self, scn):
+        _check(lib().wql_batch_add(self.h, scn.h))
+        self.members.append(scn)
+
+    def remove(self, scn):
+        _check(lib().wql_batch_remove(self.h, scn.h))
+        self.members.remove(scn)
+
+    def step(self, n=1):
+        _check(lib().wql_batch_step(self.h, n))
+
+    def stream(self):
+        s = ctypes.c_size_t()
+        _check(lib().wql_batch_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def close(self):
+        if self.h:
+            lib().wql_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
