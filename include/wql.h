@@ -144,6 +144,13 @@ int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords);
 int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 
+/* Device memory a scenario of this `.in` text would hold once created
+ * (resident) and at most while it is being created (peak: resident plus the
+ * FP64 set-up arrays of one block), without allocating anything.  For
+ * admission control by HBM footprint. */
+int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int precision, long long* resident,
+                              long long* peak);
+
 /* Continuous batching of scenarios on one device.  wql_batch_step advances
  * every member by nsteps steps: per RK stage, the stencil of every eligible
  * block of every member (FP32C, default or TMA stencil variant) is one
@@ -163,6 +170,34 @@ int wql_batch_add(wql_batch* b, wql_scn* scn);
 int wql_batch_remove(wql_batch* b, wql_scn* scn);
 int wql_batch_step(wql_batch* b, int nsteps);
 int wql_batch_stream(wql_batch* b, uintptr_t* stream);
+
+/* Request server (continuous batching with admission by device memory).
+ * A worker thread admits submitted scenarios in arrival order while the
+ * head request's peak footprint (wql_estimate_device_bytes) fits within
+ * hbm_budget_bytes next to the resident bytes of the running scenarios
+ * (the head is always admitted when nothing runs), advances all running
+ * scenarios together with wql_batch_step (at most round_steps steps per
+ * round, never past a member's step count), and retires each scenario when
+ * it reaches its step count, keeping its station seismograms.  Requests that
+ * arrive while others run join the batch at the next round.  submit copies
+ * the text and media arrays and returns at once; wait blocks until the
+ * request is done (status 1) or failed (status < 0: minus its WQL_E_* code)
+ * or the timeout passes (status 0); result gives one block's seismograms
+ * (as wql_get_seismograms, may be NULL) and the request's arrival,
+ * admission and completion times in seconds since the server started;
+ * release frees a finished request's record; destroy finishes all submitted
+ * work and stops the worker.  No counterpart in the reference. */
+typedef struct wql_server wql_server;
+int wql_server_create(wql_ctx* ctx, long long hbm_budget_bytes, int round_steps, wql_server** out);
+int wql_server_submit(wql_server* s, const char* in_text, int precision, const wql_media* media, int nsteps,
+                      long long* id);
+int wql_server_wait(wql_server* s, long long id, double timeout_s, int* status);
+int wql_server_result(wql_server* s, long long id, int block, int* nstations, int* nrecords, double* seis,
+                      double* times);
+int wql_server_release(wql_server* s, long long id);
+int wql_server_stats(wql_server* s, long long* completed, long long* queued, long long* active,
+                     long long* bytes_in_use);
+int wql_server_destroy(wql_server* s);
 
 /* The CUDA stream the scenario's kernels run on (cudaStream_t as integer),
  * for callers that time or order work around wql_step. */

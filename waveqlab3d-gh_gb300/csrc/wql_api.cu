@@ -1403,6 +1403,44 @@ int wql_get_seismograms(wql_scn* scn, int block, double* host_out) {
   return WQL_OK;
 }
 
+int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int precision, long long* resident,
+                              long long* peak) {
+  if (!in_text || !resident || !peak) return fail(WQL_E_INPUT, "null argument");
+  if (precision != WQL_FP64 && precision != WQL_FP32C) return fail(WQL_E_INPUT, "unknown precision");
+  Problem P;
+  std::string err;
+  if (parse_in_text(in_text, base_dir ? base_dir : "", P, err)) return fail(WQL_E_INPUT, err);
+  // the allocations of create() / setup_block(), rounded up as cudaMalloc does
+  const long long esz = precision == WQL_FP64 ? 8 : 4;
+  auto al = [](long long b) { return (b + 511) / 512 * 512; };
+  long long res = 0, transient = 0;
+  const long long nf = (long long)P.btp[0].nqrs[1] * P.btp[0].nqrs[2];
+  for (int b = 0; b < 2; ++b) {
+    const BlockParams& bp = P.btp[b];
+    const long long nq = bp.nqrs[0], nr = bp.nqrs[1], ns = bp.nqrs[2];
+    const long long per16 = 16 / esz, pq = (nq + per16 - 1) / per16 * per16;
+    const long long npd = nq * nr * ns, np = pq * nr * ns;
+    const bool curv = P.type_of_mesh == "curvilinear";
+    res += 2 * al(9 * np * esz) + al(9 * np * esz) + al((curv ? kCurvCoef : kCartCoef) * np * esz);
+    if (precision == WQL_FP32C) res += al(9 * np * esz);
+    const long long nfs[3] = {nr * ns, nq * ns, nq * nr};
+    for (int s2 = 0; s2 < 6; ++s2) res += al(kFaceWords * nfs[s2 / 2] * 8);
+    const int dims[3] = {(int)nq, (int)nr, (int)ns};
+    for (int s2 = 0; s2 < 6; ++s2) {
+      const bool pml = (s2 % 2 == 0) ? bp.pml_lqrs[s2 / 2] : bp.pml_rqrs[s2 / 2];
+      if (pml && bp.npml > 0) res += 2 * al(9 * (npd / dims[s2 / 2]) * bp.npml * esz);
+    }
+    if (P.response == "plastic") res += al(np * esz);
+    // set-up arrays of one block: x, metric, J, material (FP64)
+    transient = std::max(transient, al(3 * npd * 8) + al(9 * npd * 8) + al(npd * 8) + al(3 * npd * 8));
+  }
+  res += al(6 * nf * 8) + 2 * al(8 * nf * 8) + 3 * al(2 * nf * 8) + al(18 * nf * esz) + al(10 * nf * 8) + 2 * 512;
+  if (P.w_fault) res += al(64LL * kFrameWords * nf * 4);
+  *resident = res;
+  *peak = res + transient;
+  return WQL_OK;
+}
+
 int wql_batch_create(wql_ctx* ctx, wql_batch** out) {
   if (!ctx || !out) return fail(WQL_E_INPUT, "null argument");
   CK(cudaSetDevice(ctx->device));

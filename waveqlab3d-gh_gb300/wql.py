@@ -25,7 +25,9 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_get_frames", "wql_scenario_stream", "wql_launches_per_step", "wql_profile",
            "wql_kernel_times", "wql_set_tuning", "wql_get_field_noalloc", "wql_station_count",
            "wql_station_index", "wql_get_seismograms", "wql_batch_create", "wql_batch_destroy",
-           "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream"]
+           "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream",
+           "wql_estimate_device_bytes", "wql_server_create", "wql_server_submit", "wql_server_wait",
+           "wql_server_result", "wql_server_release", "wql_server_stats", "wql_server_destroy"]
 
 
 class Media(ctypes.Structure):
@@ -72,6 +74,17 @@ def lib():
         L.wql_get_field_noalloc.argtypes = [vp, ci, ci, vp]
         L.wql_station_count.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
         L.wql_batch_create.argtypes = [vp, ctypes.POINTER(vp)]
+        ll = ctypes.c_longlong
+        L.wql_estimate_device_bytes.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ci, ctypes.POINTER(ll),
+                                                ctypes.POINTER(ll)]
+        L.wql_server_create.argtypes = [vp, ll, ci, ctypes.POINTER(vp)]
+        L.wql_server_submit.argtypes = [vp, ctypes.c_char_p, ci, vp, ci, ctypes.POINTER(ll)]
+        L.wql_server_wait.argtypes = [vp, ll, ctypes.c_double, ctypes.POINTER(ci)]
+        L.wql_server_result.argtypes = [vp, ll, ci, ctypes.POINTER(ci), ctypes.POINTER(ci), vp, vp]
+        L.wql_server_release.argtypes = [vp, ll]
+        L.wql_server_stats.argtypes = [vp, ctypes.POINTER(ll), ctypes.POINTER(ll), ctypes.POINTER(ll),
+                                       ctypes.POINTER(ll)]
+        L.wql_server_destroy.argtypes = [vp]
         L.wql_batch_destroy.argtypes = [vp]
         L.wql_batch_add.argtypes = [vp, vp]
         L.wql_batch_remove.argtypes = [vp, vp]
@@ -97,6 +110,28 @@ def _check(rc):
         buf = ctypes.create_string_buffer(1024)
         lib().wql_last_error(buf, 1024)
         raise WqlError(rc, buf.value.decode())
+
+
+def _media_struct(media):
+    """A Media struct over contiguous FP64 copies of the arrays (returned
+    alongside so they stay alive for the call)."""
+    keep = []
+
+    def ptr(a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        keep.append(a)
+        return a.ctypes.data
+
+    m = Media()
+    m.fault_offset = ptr(media.get("fault_offset"))
+    for key in ("topo_offset", "lam", "mu", "rho"):
+        pair = media.get(key) or (None, None)
+        arr = getattr(m, key)
+        for b in range(2):
+            arr[b] = ptr(pair[b])
+    return m, keep
 
 
 class Context:
@@ -128,22 +163,7 @@ class Scenario:
             if text is None:
                 with open(in_path) as f:
                     text = f.read()
-            keep = []
-
-            def ptr(a):
-                if a is None:
-                    return None
-                a = np.ascontiguousarray(a, dtype=np.float64).ravel()
-                keep.append(a)
-                return a.ctypes.data
-
-            m = Media()
-            m.fault_offset = ptr(media.get("fault_offset"))
-            for key in ("topo_offset", "lam", "mu", "rho"):
-                pair = media.get(key) or (None, None)
-                arr = getattr(m, key)
-                for b in range(2):
-                    arr[b] = ptr(pair[b])
+            m, keep = _media_struct(media)
             _check(lib().wql_scenario_create_ex(ctx.h, text.encode(),
                                                 base_dir.encode() if base_dir else None, precision,
                                                 ctypes.byref(m), ctypes.byref(self.h)))
@@ -286,6 +306,69 @@ class Batch:
     def close(self):
         if self.h:
             lib().wql_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def estimate_device_bytes(text, precision=FP32C):
+    """(resident, peak) device bytes a scenario of this .in text would need."""
+    r, p = ctypes.c_longlong(), ctypes.c_longlong()
+    _check(lib().wql_estimate_device_bytes(text.encode(), None, precision, ctypes.byref(r), ctypes.byref(p)))
+    return r.value, p.value
+
+
+class Server:
+    """Request server (wql_server_*): admission by device-memory footprint and
+    continuous batching on a worker thread."""
+
+    def __init__(self, ctx, hbm_budget_bytes, round_steps=10):
+        h = ctypes.c_void_p()
+        _check(lib().wql_server_create(ctx.h, int(hbm_budget_bytes), round_steps, ctypes.byref(h)))
+        self.h = h.value
+        self._keep = {}
+
+    def submit(self, text, nsteps, precision=FP32C, media=None):
+        mp = None
+        if media:
+            mobj, keep = _media_struct(media)
+            mp = ctypes.byref(mobj)
+        rid = ctypes.c_longlong()
+        _check(lib().wql_server_submit(self.h, text.encode(), precision, mp, nsteps, ctypes.byref(rid)))
+        return rid.value
+
+    def wait(self, rid, timeout=600.0):
+        st = ctypes.c_int()
+        _check(lib().wql_server_wait(self.h, rid, timeout, ctypes.byref(st)))
+        return st.value
+
+    def result(self, rid, block):
+        """(seismograms (records, n, 4), (t_arrive, t_admit, t_done))."""
+        n, nrec = ctypes.c_int(), ctypes.c_int()
+        times = np.zeros(3)
+        rc = lib().wql_server_result(self.h, rid, block, ctypes.byref(n), ctypes.byref(nrec), None,
+                                     times.ctypes.data)
+        if rc:
+            raise WqlError(rc, "request %d failed" % rid)
+        seis = np.empty(nrec.value * n.value * 4)
+        _check(lib().wql_server_result(self.h, rid, block, None, None, seis.ctypes.data, None))
+        return seis.reshape(nrec.value, n.value, 4), tuple(times)
+
+    def release(self, rid):
+        _check(lib().wql_server_release(self.h, rid))
+
+    def stats(self):
+        v = [ctypes.c_longlong() for _ in range(4)]
+        _check(lib().wql_server_stats(self.h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("completed", "queued", "active", "bytes_in_use"), (x.value for x in v)))
+
+    def close(self):
+        if self.h:
+            lib().wql_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -16,8 +16,8 @@ LIB = os.path.join(BUILD, "libwql.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["wql_api.cu", "wql_setup.cu", "wql_volume.cu", "wql_stencil_tma.cu", "wql_interface.cu"]
-CPP = ["host/wql_input.cpp", "host/wql_grid.cpp"]
-HEADERS = ["wql_internal.h", "wql_sbp.cuh", "wql_presets.cuh", "host/wql_input.h",
+CPP = ["host/wql_input.cpp", "host/wql_grid.cpp", "host/wql_serve.cpp"]
+HEADERS = ["wql_internal.h", "wql_sbp.cuh", "wql_presets.cuh", "wql_stencil.cuh", "host/wql_input.h",
            "host/wql_grid.h", os.path.join("..", "..", "include", "wql.h")]
 
 
@@ -34,7 +34,7 @@ def _compile(src):
         cmd = [NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                "--expt-relaxed-constexpr", "-I" + CSRC, "-c", path, "-o", obj]
     else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-I" + CSRC, "-c", path, "-o", obj]
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + CSRC, "-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return obj, " ".join(cmd) + "\n" + r.stdout + r.stderr
@@ -50,7 +50,7 @@ def build(verbose=False):
         raise RuntimeError("libwql build failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [NVCC, *ARCH, "-shared", "-cudart", "static", "-o", LIB + ".tmp", *objs]
+        cmd = [NVCC, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-pthread", "-o", LIB + ".tmp", *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("libwql link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)

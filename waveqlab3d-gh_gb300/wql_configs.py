@@ -180,3 +180,84 @@ def updates_per_step(text):
     for m in re.finditer(r"btp\(\d\)%nqrs\s*=\s*(\d+),\s*(\d+),\s*(\d+)", text):
         tot += int(m.group(1)) * int(m.group(2)) * int(m.group(3))
     return 5 * tot
+
+
+# --------------------------------------------------- served point sources ----
+
+def moment_tensor(strike, dip, rake, m0):
+    """Moment tensor (XX, YY, ZZ, XY, XZ, YZ) of a double couple in the frame
+    x = east, y = down, z = north, from strike/dip/rake in degrees (the
+    Aki-Richards expressions in north-east-down, with the axes permuted)."""
+    f, d, l = (np.radians(v) for v in (strike, dip, rake))
+    nn = -m0 * (np.sin(d) * np.cos(l) * np.sin(2 * f) + np.sin(2 * d) * np.sin(l) * np.sin(f) ** 2)
+    ne = m0 * (np.sin(d) * np.cos(l) * np.cos(2 * f) + 0.5 * np.sin(2 * d) * np.sin(l) * np.sin(2 * f))
+    nd = -m0 * (np.cos(d) * np.cos(l) * np.cos(f) + np.cos(2 * d) * np.sin(l) * np.sin(f))
+    ee = m0 * (np.sin(d) * np.cos(l) * np.sin(2 * f) - np.sin(2 * d) * np.sin(l) * np.cos(f) ** 2)
+    ed = -m0 * (np.cos(d) * np.cos(l) * np.sin(f) - np.cos(2 * d) * np.sin(l) * np.cos(f))
+    dd = m0 * np.sin(2 * d) * np.sin(l)
+    return ee, dd, nn, ed, ne, nd
+
+
+def config4_request(i, seed=4242, n_lo=96, n_hi=256, steps=100, medium=None):
+    """Request i of the served stream: an n^3 grid (n uniform in n_lo..n_hi)
+    as two blocks joined by a locked interface at x = 0, absorbing sides and
+    a free surface at y = 0, a double-couple point source (strike 0-360,
+    dip 10-90, rake -180-180, Mw 4-6 -> M0 = 10^(1.5 Mw + 9.1) N m, in
+    MPa km^3 = 1e15 N m) with a Gaussian moment rate of rise time 0.1-0.5 s
+    at 2-15 km depth, and 32 seeded stations on the free surface.  The
+    domain is a cube of side max(depth + 5, 12) km.  `medium`, if given, is a
+    von Karman perturbation field at least n^3, cropped to the grid."""
+    rng = np.random.default_rng([seed, i])
+    n = int(rng.integers(n_lo, n_hi + 1))
+    depth = float(rng.uniform(2.0, 15.0))
+    side = max(depth + 5.0, 12.0)
+    strike, dip, rake = rng.uniform(0, 360), rng.uniform(10, 90), rng.uniform(-180, 180)
+    mw = rng.uniform(4.0, 6.0)
+    m0 = 10 ** (1.5 * mw + 9.1) / 1e15
+    rise = rng.uniform(0.1, 0.5)
+    w = 2.0 / rise
+    t0 = 1.5 * rise
+    mt = moment_tensor(strike, dip, rake, m0)
+    h = side / (n - 1)
+    nq1 = n // 2 + 1
+    nq2 = n - nq1 + 1
+    x1 = -h * (nq1 - 1)
+    x2 = h * (nq2 - 1)
+    # source inside block 1, off the grid points
+    sx = float(rng.uniform(0.3, 0.7)) * x1
+    sz = float(rng.uniform(-0.2, 0.2)) * side
+    dt = 0.5 * h / math.sqrt(CS * CS + CP * CP)
+    text = (f"&problem_list\n name = 'request{i}',\n problem = 'TPV5',\n nblocks = 2,\n"
+            f" t_final = {(steps + 0.5) * dt!r},\n CFL = 0.5d0,\n coupling = 'locked',\n"
+            f" type_of_mesh = 'cartesian',\n w_stride = 1,\n w_fault = F /\n")
+    text += "&block_list\n" + _block(1, (nq1, n, n), (x1, 0.0, -side / 2), (0.0, side, side / 2), (1, 2, 1), (0, 1, 1))
+    text += _block(2, (nq2, n, n), (0.0, 0.0, -side / 2), (x2, side, side / 2), (0, 2, 1), (1, 1, 1)) + " /\n"
+    text += "&moment_list\n use_moment_tensor = T,\n order = 2 /\n"
+    text += "!---begin:tensor_listU---\n"
+    text += (f"'gaussian' {w!r} {t0!r} " + " ".join(repr(float(v)) for v in mt) +
+             f" {sx!r} {depth!r} {sz!r} 0\n")
+    text += "!---end:tensor_listU---\n"
+    text += "&output_list\n output_seismograms = T /\n!---begin:station_list---\n"
+    for k in range(32):
+        text += f"{rng.uniform(x1, x2)!r} 0d0 {rng.uniform(-side / 2, side / 2)!r}\n"
+    text += "!---end:station_list---\n"
+    media = None
+    if medium is not None:
+        sl = medium[:n, :n, :n]
+        media = {"lam": [], "mu": [], "rho": []}
+        for b, (q0, nq) in enumerate(((0, nq1), (nq1 - 1, nq2))):
+            p = sl[q0:q0 + nq]
+            cp, cs = CP * (1.0 + p), CS * (1.0 + p)
+            rho = nafe_drake_rho(cp)
+            mu = rho * cs * cs
+            lam = rho * cp * cp - 2.0 * mu
+            for key, val in (("lam", lam), ("mu", mu), ("rho", rho)):
+                media[key].append(np.asfortranarray(val).ravel(order="F"))
+        media = {k: tuple(v) for k, v in media.items()}
+    return text, media, n
+
+
+def config4_medium(n=256, seed=4242, h=0.05):
+    """One von Karman perturbation field (a = 2 km, H = 0.2, 5 %) that the
+    requests crop to their size."""
+    return von_karman((n, n, n), (h, h, h), 2.0, 0.2, 0.05, seed, kmax=np.pi / h)
