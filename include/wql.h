@@ -144,6 +144,14 @@ int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords);
 int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 
+/* Autotuner: times the stencil-kernel candidates (WQL_FP32C: the TMA
+ * kernel with 3 or 2 stages and s chunks of 12..48 planes or automatic;
+ * WQL_FP64: tiled and per-point) on the scenario's own blocks, reps
+ * launches each, into scratch arrays (the scenario's state is not
+ * changed), applies the fastest with wql_set_tuning and returns it.
+ * Results are cached per block shape, mesh type and precision. */
+int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk);
+
 /* Device memory a scenario of this `.in` text would hold once created
  * (resident) and at most while it is being created (peak: resident plus the
  * FP64 set-up arrays of one block), without allocating anything.  For

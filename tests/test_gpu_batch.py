@@ -91,3 +91,25 @@ def test_members_join_and_leave(ctx, wqlmod, tmp_path):
     _same(a0, m0)
     _same(a1, m1)
     batch.close()
+
+
+def test_autotune_keeps_state(ctx, wqlmod):
+    """The autotuner leaves the scenario's state alone and its choice steps
+    like the per-point kernel."""
+    import wql_configs
+    text, media = wql_configs.config1(n=45, steps=10)
+    s = wqlmod.Scenario(ctx, text=text, precision=wqlmod.FP32C, media=media)
+    r = wqlmod.Scenario(ctx, text=text, precision=wqlmod.FP32C, media=media)
+    s.step(2)
+    r.step(2)
+    before = [s.fields(b) for b in range(2)]
+    v, c = s.autotune(reps=2)
+    assert v in (5, 6)
+    for b in range(2):
+        assert np.array_equal(s.fields(b), before[b])
+    r.set_tuning(1, 0)
+    s.step(4)
+    r.step(4)
+    for b in range(2):
+        a, ref = s.fields(b), r.fields(b)
+        assert np.linalg.norm(a - ref) <= 2e-6 * np.linalg.norm(ref)

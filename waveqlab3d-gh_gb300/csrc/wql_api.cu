@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -1400,6 +1401,128 @@ int wql_get_seismograms(wql_scn* scn, int block, double* host_out) {
   const int rc = flush_stations(scn);
   if (rc) return rc;
   std::memcpy(host_out, scn->st[block].host.data(), scn->st[block].host.size() * sizeof(double));
+  return WQL_OK;
+}
+
+int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
+  if (!scn || reps <= 0) return fail(WQL_E_INPUT, "bad argument");
+  CK(cudaSetDevice(scn->ctx->device));
+  // results are kept per block shape, mesh and precision
+  static std::mutex mu;
+  static std::map<std::vector<int>, std::pair<int, int>> cache;
+  std::vector<int> key = {scn->prec, (int)scn->curv};
+  for (int b = 0; b < 2; ++b) {
+    key.push_back(scn->B[b].nq);
+    key.push_back(scn->B[b].nr);
+    key.push_back(scn->B[b].ns);
+  }
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      scn->kernel_variant = it->second.first;
+      scn->schunk = it->second.second;
+      if (variant) *variant = scn->kernel_variant;
+      if (schunk) *schunk = scn->schunk;
+      return WQL_OK;
+    }
+  }
+  // candidates: the TMA kernel with 3 or 2 stages and several s chunk sizes
+  // (FP32C), the tiled and per-point kernels (FP64)
+  std::vector<std::pair<int, int>> cand;
+  if (scn->prec == WQL_FP32C) {
+    for (int v : {5, 6})
+      for (int c : {0, 12, 16, 24, 32, 48})
+        if (c <= scn->B[0].ns) cand.push_back({v, c});
+  } else {
+    for (int c : {8, 16, 32}) cand.push_back({2, c});
+    cand.push_back({1, 0});
+  }
+  // scratch rates, compensation and output so the scenario state is untouched
+  void* scratch[2][3] = {};
+  int rc = WQL_OK;
+  for (int b = 0; b < 2 && !rc; ++b)
+    for (int k = 0; k < 3 && !rc; ++k) {
+      if (k == 1 && scn->prec != WQL_FP32C) continue;
+      if (cudaMalloc(&scratch[b][k], 9 * scn->B[b].np * scn->esz) != cudaSuccess) rc = fail(WQL_E_OOM, "autotune scratch");
+      else CK(cudaMemsetAsync(scratch[b][k], 0, 9 * scn->B[b].np * scn->esz, scn->stream));
+    }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int keep_v = scn->kernel_variant, keep_c = scn->schunk;
+  float best = 1e30f;
+  std::pair<int, int> choice = {keep_v, keep_c};
+  for (auto& c : cand) {
+    if (rc) break;
+    scn->kernel_variant = c.first;
+    scn->schunk = c.second;
+    auto run = [&]() {
+      for (int b = 0; b < 2; ++b) {
+        if (scn->prec == WQL_FP64) {
+          VolumeArgs<double> a = volume_args<double>(scn, b, 0.5, 1e-4, false);
+          a.DF = (double*)scratch[b][0];
+          a.Fout = (double*)scratch[b][2];
+          a.C = nullptr;
+          launch_volume<double>(a, scn->curv, scn->stream);
+        } else {
+          VolumeArgs<float> a = volume_args<float>(scn, b, 0.5, 1e-4, false);
+          a.DF = (float*)scratch[b][0];
+          a.C = (float*)scratch[b][1];
+          a.Fout = (float*)scratch[b][2];
+          if (c.first == 5 || c.first == 6) {
+            // the TMA kernel reads DF and C through the block's tensor maps:
+            // point them at the scratch arrays for the trial
+            StencilMaps m = scn->B[b].maps;
+            void* Fs[2] = {scn->B[b].F[0], scn->B[b].F[1]};
+            if (make_stencil_maps(m, Fs, scn->B[b].coef, scratch[b][0], scratch[b][1], scn->B[b].nq, scn->B[b].nr,
+                                  scn->B[b].ns, scn->B[b].pq, scn->curv)) {
+              rc = fail(WQL_E_CUDA, "autotune tensor maps");
+              return;
+            }
+            m.cur = scn->cur;
+            a.tma = &m;
+            launch_volume<float>(a, scn->curv, scn->stream);
+          } else {
+            launch_volume<float>(a, scn->curv, scn->stream);
+          }
+        }
+      }
+    };
+    run();  // warm-up
+    cudaEventRecord(e0, scn->stream);
+    for (int r = 0; r < reps; ++r) run();
+    cudaEventRecord(e1, scn->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(WQL_E_CUDA, "autotune trial failed");
+      break;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      choice = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int b = 0; b < 2; ++b)
+    for (int k = 0; k < 3; ++k)
+      if (scratch[b][k]) cudaFree(scratch[b][k]);
+  if (rc) {
+    scn->kernel_variant = keep_v;
+    scn->schunk = keep_c;
+    return rc;
+  }
+  CK(cudaGetLastError());
+  scn->kernel_variant = choice.first;
+  scn->schunk = choice.second;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = choice;
+  }
+  if (variant) *variant = choice.first;
+  if (schunk) *schunk = choice.second;
   return WQL_OK;
 }
 

@@ -27,7 +27,8 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_station_index", "wql_get_seismograms", "wql_batch_create", "wql_batch_destroy",
            "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream",
            "wql_estimate_device_bytes", "wql_server_create", "wql_server_submit", "wql_server_wait",
-           "wql_server_result", "wql_server_release", "wql_server_stats", "wql_server_destroy"]
+           "wql_server_result", "wql_server_release", "wql_server_stats", "wql_server_destroy",
+           "wql_autotune"]
 
 
 class Media(ctypes.Structure):
@@ -85,6 +86,7 @@ def lib():
         L.wql_server_stats.argtypes = [vp, ctypes.POINTER(ll), ctypes.POINTER(ll), ctypes.POINTER(ll),
                                        ctypes.POINTER(ll)]
         L.wql_server_destroy.argtypes = [vp]
+        L.wql_autotune.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(ci)]
         L.wql_batch_destroy.argtypes = [vp]
         L.wql_batch_add.argtypes = [vp, vp]
         L.wql_batch_remove.argtypes = [vp, vp]
@@ -272,6 +274,12 @@ class Scenario:
             _check(lib().wql_kernel_times(self.h, kind, ctypes.byref(ms), ctypes.byref(n)))
             out[name] = (ms.value, n.value)
         return out
+
+    def autotune(self, reps=3):
+        """Time the stencil candidates and keep the fastest: (variant, schunk)."""
+        v, c = ctypes.c_int(), ctypes.c_int()
+        _check(lib().wql_autotune(self.h, reps, ctypes.byref(v), ctypes.byref(c)))
+        return v.value, c.value
 
     def set_tuning(self, kernel=0, schunk=0):
         _check(lib().wql_set_tuning(self.h, kernel, schunk))
