@@ -265,6 +265,123 @@ def accuracy(wql, ctx, text, media, steps, stride=20):
     return out
 
 
+def batch_mode(wql, device, args):
+    """Config 3: an ensemble of uneven scenarios advanced as one batch (one
+    packed stencil launch per stage, tile chunks from the autotuner), against
+    the same scenarios stepped one after another, and FP64 stepped alone."""
+    import numpy as np
+    import torch
+    import wql_configs
+    ctx = wql.Context(device)
+    n_hi = 160
+    medium = wql_configs.von_karman((2 * n_hi - 1, n_hi, n_hi), (0.1, 0.1, 0.1), 2.0, 0.2, 0.05, 3131)
+    members, points = [], 0
+    t0 = time.perf_counter()
+    for i in range(args.members):
+        text, media, npts = wql_configs.config3_scenario(i, medium=medium)
+        s = wql.Scenario(ctx, text=text, precision=wql.FP32C, media=media)
+        s.autotune(reps=2)
+        members.append((s, text, media, npts))
+        points += npts
+    setup_s = time.perf_counter() - t0
+    batch = wql.Batch(ctx)
+    for s, *_ in members:
+        batch.add(s)
+    batch.step(args.warmup)
+    torch.cuda.synchronize()
+    st = torch.cuda.ExternalStream(batch.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(device) as clk:
+        e0.record(st)
+        batch.step(args.steps)
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    batched = points * 5 * args.steps / (ms * 1e-3)
+    for s, *_ in members:
+        s.sync(check_nan=True)
+    batch.close()
+    # the same members stepped one after another
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s, *_ in members:
+        s.step(args.steps)
+    for s, *_ in members:
+        s.sync()
+    seq = points * 5 * args.steps / (time.perf_counter() - t0)
+    for s, *_ in members:
+        s.close()
+    # FP64 on a few members, one after another
+    fp64_pts, fp64_s = 0, 0.0
+    for s_, text, media, npts in members[:4]:
+        d = wql.Scenario(ctx, text=text, precision=wql.FP64, media=media)
+        d.step(1)
+        d.sync()
+        t0 = time.perf_counter()
+        d.step(3)
+        d.sync()
+        fp64_s += time.perf_counter() - t0
+        fp64_pts += npts * 5 * 3
+        d.close()
+    fp64 = fp64_pts / fp64_s
+    return {"mode": "batch", "metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "dtype": "f32 fields, Kahan-compensated RK update, f64 fault solve",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"config3: {args.members} slip-weakening scenarios, blocks of 64^3..160^3 "
+                                   f"points, planar/rough faults, homogeneous/von Karman media, 10-point PML, "
+                                   f"{points} grid points", "setup_s": setup_s},
+            "sequential_fp32c": seq, "batched_over_sequential": batched / seq,
+            "fp64_alone": fp64, "batched_fp32c_over_fp64": batched / fp64, "clocks": clk.summary()}
+
+
+def serve_mode(wql, device, args):
+    """Config 4: a Poisson stream of point-source requests (n^3 grids, n in
+    96..256, von Karman media, 32 stations) served with admission by device
+    memory and continuous batching; latency from each request's scheduled
+    arrival to its completion."""
+    import numpy as np
+    import torch
+    import wql_configs
+    ctx = wql.Context(device)
+    medium = wql_configs.config4_medium(256, h=0.05)
+    free, total = torch.cuda.mem_get_info(device)
+    budget = int(0.6 * free)
+    rng = np.random.default_rng(4242)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
+    srv = wql.Server(ctx, hbm_budget_bytes=budget, round_steps=10)
+    t_base = time.perf_counter()  # the server clock starts with the server (within ms)
+    ids, sizes = [], []
+    with Clocks(device) as clk:
+        for i, ta in enumerate(arrivals):
+            text, media, n = wql_configs.config4_request(i, steps=args.serve_steps, medium=medium)
+            wait = ta - (time.perf_counter() - t_base)
+            if wait > 0:
+                time.sleep(wait)
+            ids.append(srv.submit(text, args.serve_steps, media=media))
+            sizes.append(n)
+            del media
+        status = [srv.wait(rid, 3600.0) for rid in ids]
+    lat, done = [], []
+    for rid, ta in zip(ids, arrivals):
+        _, (t_arr, t_adm, t_done) = srv.result(rid, 0)
+        lat.append(t_done - ta)
+        done.append(t_done)
+    srv.close()
+    lat = np.array(lat)
+    span = max(done) - arrivals[0]
+    upd = sum(2 * (n // 2 + 1) * n * n for n in sizes) * 5 * args.serve_steps
+    return {"mode": "serve", "metric": METRIC, "value": len(ids) / span, "unit": "solves/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32 fields, Kahan-compensated RK update, f64 sources",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"config4: {args.requests} point-source requests, n^3 grids n in 96..256, "
+                                   f"von Karman media, 32 stations, {args.serve_steps} steps each",
+                       "arrival_rate_per_s": args.rate, "hbm_budget_bytes": budget},
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "updates_per_s": upd / span, "completed": int(sum(1 for x in status if x == 1)),
+            "clocks": clk.summary()}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -276,6 +393,12 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
+                    help="step: config 1 (default); batch: config 3 ensemble in one batch; serve: config 4 stream")
+    ap.add_argument("--members", type=int, default=64, help="batch mode: ensemble size")
+    ap.add_argument("--requests", type=int, default=32, help="serve mode: number of requests")
+    ap.add_argument("--rate", type=float, default=4.0, help="serve mode: Poisson arrival rate (requests/s)")
+    ap.add_argument("--serve-steps", type=int, default=100, help="serve mode: time steps per request")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing, run FP32C and FP64 this many steps and report their differences")
     args = ap.parse_args()
@@ -307,6 +430,17 @@ def main():
     import wql_build
     wql_build.build()
     import wql
+    if args.mode == "batch":
+        if rank == 0 or world > 1:
+            line = batch_mode(wql, local, args)
+            if rank == 0:
+                print(json.dumps(line))
+        return
+    if args.mode == "serve":
+        line = serve_mode(wql, local, args)
+        if rank == 0:
+            print(json.dumps(line))
+        return
     if args.accuracy_steps > 0:
         ctx = wql.Context(local)
         res = accuracy(wql, ctx, text, media, args.accuracy_steps)

@@ -261,3 +261,56 @@ def config4_medium(n=256, seed=4242, h=0.05):
     """One von Karman perturbation field (a = 2 km, H = 0.2, 5 %) that the
     requests crop to their size."""
     return von_karman((n, n, n), (h, h, h), 2.0, 0.2, 0.05, seed, kmax=np.pi / h)
+
+
+# --------------------------------------------------- batched ensemble ----
+
+def config3_scenario(i, seed=3131, n_lo=64, n_hi=160, steps=1500, medium=None, npml=10):
+    """Member i of the batched ensemble: blocks of n^3 points (n^3 uniform in
+    n_lo^3..n_hi^3), 15 km deep, slip weakening (fs 0.677, fd 0.525,
+    Dc 0.4 m) under sigma_n = 120 MPa and tau_0 = fd*sigma_n + (fs - fd)*
+    sigma_n/(1 + S) with S uniform in [0.5, 1.5], a nucleation patch
+    (R = 1.5 km, just above peak strength) centred at a depth of 2-12 km
+    and uniform along strike, a planar fault (Cartesian mesh) or a rough
+    one (alpha 0.005-0.01, curvilinear mesh), a homogeneous or von Karman
+    medium (cropped from `medium`), and npml-point PML on the five sides
+    other than the free surface."""
+    rng = np.random.default_rng([seed, i])
+    n = int(np.floor(rng.uniform(n_lo ** 3, n_hi ** 3) ** (1.0 / 3.0)))
+    h = 15.0 / (n - 1)
+    ext = (n - 1) * h
+    S = rng.uniform(0.5, 1.5)
+    fs, fd, sn = 0.677, 0.525, 120.0
+    tau0 = fd * sn + (fs - fd) * sn / (1.0 + S)
+    ny = rng.uniform(2.0, 12.0)
+    nz = rng.uniform(-0.35, 0.35) * ext
+    rough = bool(rng.integers(0, 2))
+    hetero = bool(rng.integers(0, 2)) and medium is not None
+    mesh = "curvilinear" if rough else "cartesian"
+    dt = dt_of((n, n, n), (ext, ext, ext))
+    text = _problem(f"member{i}", "sw_param", "slip-weakening_friction", mesh, (steps + 0.5) * dt)
+    text += "&block_list\n" + _block(1, (n, n, n), (-ext, 0.0, -ext / 2), (0.0, ext, ext / 2), (1, 2, 1), (0, 1, 1),
+                                     (True, False, True), (False, True, True), npml)
+    text += _block(2, (n, n, n), (0.0, 0.0, -ext / 2), (ext, ext, ext / 2), (0, 2, 1), (1, 1, 1),
+                   (False, False, True), (True, True, True), npml) + " /\n"
+    amp = (fs * sn - tau0) + 1.0
+    text += (f"&fault_list\n fs = {fs}d0, fd = {fd}d0, Dc = 0.4d0,\n"
+             f" s0 = -120d0, 0d0, -120d0, 0d0, {tau0!r}, 0d0,\n"
+             f" nuc_amp = {amp!r}, nuc_radius = 1.5d0, nuc_y = {ny!r}, nuc_z = {nz!r}, nuc_rise = 0d0 /\n")
+    media = {}
+    if rough:
+        alpha = rng.uniform(0.005, 0.01)
+        fault = self_similar_surface((n, n), (h, h), alpha, max(2 * h, 0.2), seed + 7 * i + 1)
+        media["fault_offset"] = np.asfortranarray(fault).ravel(order="F")
+    if hetero:
+        m = {"lam": [], "mu": [], "rho": []}
+        for b in range(2):
+            p = medium[b * (n - 1): b * (n - 1) + n, :n, :n] if medium.shape[0] >= 2 * n - 1 else medium[:n, :n, :n]
+            cp, cs = CP * (1.0 + p), CS * (1.0 + p)
+            rho = nafe_drake_rho(cp)
+            mu = rho * cs * cs
+            lam = rho * cp * cp - 2.0 * mu
+            for key, val in (("lam", lam), ("mu", mu), ("rho", rho)):
+                m[key].append(np.asfortranarray(val).ravel(order="F"))
+        media.update({k: tuple(v) for k, v in m.items()})
+    return text, (media or None), 2 * n ** 3
