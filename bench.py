@@ -127,7 +127,10 @@ def allsum(world, v):
 
 def workload(args):
     import wql_configs
-    text, media = wql_configs.config1(n=args.n, steps=10 ** 6, seed=args.seed)
+    if args.workload == "config2":
+        text, media = wql_configs.config2(steps=10 ** 6, seed=args.seed)
+    else:
+        text, media = wql_configs.config1(n=args.n, steps=10 ** 6, seed=args.seed)
     return text, media, wql_configs.updates_per_step(text)
 
 
@@ -395,6 +398,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
                     help="step: config 1 (default); batch: config 3 ensemble in one batch; serve: config 4 stream")
+    ap.add_argument("--workload", default="config1", choices=["config1", "config2"],
+                    help="step mode: config1 (2 x n^3 curvilinear, rate and state) or config2 (2 x 401x201x201, "
+                         "PML, von Karman, plasticity)")
     ap.add_argument("--members", type=int, default=64, help="batch mode: ensemble size")
     ap.add_argument("--requests", type=int, default=32, help="serve mode: number of requests")
     ap.add_argument("--rate", type=float, default=4.0, help="serve mode: Poisson arrival rate (requests/s)")
@@ -406,6 +412,9 @@ def main():
     text, media, ups = workload(args)
     wl = (f"config1: 2 x {args.n}^3 curvilinear blocks, seeded topography + self-similar rough fault, "
           f"aging-law rate-and-state, {ups // 5} grid points")
+    if args.workload == "config2":
+        wl = (f"config2: 2 x 401x201x201 curvilinear blocks, 20-point PML on 5 sides, von Karman medium, "
+              f"scec viscoplasticity, TPV26 stress, slip weakening, {ups // 5} grid points")
 
     if args.impl == "reference":
         if rank != 0:
@@ -464,7 +473,7 @@ def main():
     peak, peak_kind = peaks()
     vol_ms, vol_n = main_r["kt"]["stencil"]
     kernel_name = "stencil_kernel_tma<float,curv,kahan>"
-    pts_per_launch = (args.n ** 3)
+    pts_per_launch = (401 * 201 * 201) if args.workload == "config2" else (args.n ** 3)
     algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
     traffic = None

@@ -852,7 +852,11 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   for (int c = 0; c < 6; ++c) a.s0u[c] = S->fp.s0[c];
   a.ycoord = (const T*)B.y;
   a.pl_c = S->pl_c; a.pl_nu = S->pl_nu; a.pl_Tv = S->pl_Tv; a.dt = S->dt;
+  a.pl_ccos = S->pl_c * std::cos(std::atan(S->pl_nu));
+  a.pl_sin = std::sin(std::atan(S->pl_nu));
+  a.pl_decay = std::exp(-S->dt / S->pl_Tv);
   a.err = S->err_dev;
+  a.pml_d0 = 6.0 / (2.0 * 1.0) * std::log(1.0 / 1.0e-3);
   B.maps.cur = S->cur;
   a.tma = &B.maps;
   return a;

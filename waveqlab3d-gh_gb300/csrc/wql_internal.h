@@ -66,7 +66,9 @@ struct VolumeArgs {
   double s0u[6];       // uniform initial stress
   const T* __restrict__ ycoord;  // depth coordinate for the initial stress
   double pl_c, pl_nu, pl_Tv, dt;
+  double pl_ccos, pl_sin, pl_decay;  // c*cos(atan nu), sin(atan nu), exp(-dt/Tv)
   int* err;                      // device error word (pipeline wait timeouts)
+  double pml_d0;                 // PML damping scale 3 ln(1000)
   const void* tma;               // host pointer to the block's StencilMaps (FP32 only)
 };
 

@@ -97,6 +97,47 @@ WQL_HD bool initial_stress(int preset, const double x[3], double s0[6]) {
   }
 }
 
+// initial_stress for the plastic update in the field precision R: the same
+// expressions on the depth y (R = double gives the values above).
+template <typename R>
+WQL_HD bool initial_stress_y(int preset, R y, R s0[6]) {
+  switch (preset) {
+    case PRE_TPV26:
+    case PRE_TPV27:
+    case PRE_TPV29:
+    case PRE_TPV30: {
+      const bool p29 = preset == PRE_TPV29 || preset == PRE_TPV30;
+      const R y1 = p29 ? R(17.0) : R(15.0), y2 = p29 ? R(22.0) : R(20.0);
+      R Om = R(0.0);
+      if (y <= y1) Om = R(1.0);
+      else if (y >= y1 && y <= y2) Om = (y2 - y) / R(5.0);
+      const R b11 = p29 ? R(1.025837) : R(0.926793), b33 = p29 ? R(0.974162) : R(1.073206);
+      const R b13 = p29 ? R(-0.158649) : R(-0.169029);
+      const R Pf = R(9.8) * y, s22 = R(-2.67) * R(9.8) * y;
+      s0[0] = Om * (b33 * (s22 + Pf) - Pf) + (R(1.0) - Om) * s22 + Pf;
+      s0[1] = s22 + Pf;
+      s0[2] = Om * (b11 * (s22 + Pf) - Pf) + (R(1.0) - Om) * s22 + Pf;
+      s0[3] = R(0.0);
+      s0[4] = Om * (b13 * (s22 + Pf));
+      s0[5] = R(0.0);
+      return true;
+    }
+    case PRE_TPV28:
+      s0[0] = R(-60.0); s0[1] = R(0.0); s0[2] = R(60.0); s0[3] = R(0.0); s0[4] = R(29.38); s0[5] = R(0.0);
+      return true;
+    case PRE_TPV101:
+    case PRE_TPV102:
+      s0[0] = R(-120.0); s0[1] = R(0.0); s0[2] = R(-120.0); s0[3] = R(0.0); s0[4] = R(75.0); s0[5] = R(0.0);
+      return true;
+    case PRE_TPV10:
+      s0[0] = R(-7.378) * y; s0[1] = R(0.0); s0[2] = R(-7.378) * y; s0[3] = R(0.0);
+      s0[4] = R(-0.55) * s0[0]; s0[5] = R(0.0);
+      return true;
+    default:
+      return false;
+  }
+}
+
 WQL_HD void tensor_traction(const double s0[6], const double n[3], const double m[3],
                             const double l[3], double& Tn, double& Tm, double& Tl) {
   const double Tx = n[0] * s0[0] + n[1] * s0[3] + n[2] * s0[4];

@@ -97,6 +97,39 @@ __device__ __forceinline__ void diff6(const T* __restrict__ F, const T* __restri
   }
 }
 
+// SBP-6 derivative along one axis of the three velocities only (no flux).
+template <typename T>
+__device__ __forceinline__ void diff_v(const T* __restrict__ F, long long np, long long p, int i, int n, long long st,
+                                       T r[3]) {
+  r[0] = r[1] = r[2] = T(0);
+  const int kind = sbp_kind(i, n);
+  if (kind == 0) {
+    const T cs[3] = {T(kC1), T(kC2), T(kC3)};
+#pragma unroll
+    for (int s = 1; s <= 3; ++s)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[c] += cs[s - 1] * (F[c * np + p + s * st] - F[c * np + p - s * st]);
+  } else if (kind < 0) {
+    const int row = -kind - 1;
+    const long long p0 = p - (long long)i * st;
+    for (int col = 0; col < 9; ++col) {
+      const T w = sbp_w<T>(row, col);
+      if (w != T(0))
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + p0 + col * st];
+    }
+  } else {
+    const int row = kind - 1;
+    const long long pn = p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < 9; ++col) {
+      const T w = -sbp_w<T>(row, col);
+      if (w != T(0))
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + pn - col * st];
+    }
+  }
+}
+
 // D_d of the three fluxes J*metric_j(d)*sigma_{c,j} (fixed physical axis j),
 // needed only inside PML slabs (the per-axis split of the divergence).
 template <typename T>
@@ -460,8 +493,8 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
   T g[3][3];
   const T Jinv = CURV ? coef[9 * np + p] : T(1);
   for (int d = 0; d < 3; ++d) {
-    T o[6];
-    diff6<T, CURV>(F, coef, np, p, idx[d], nn[d], st[d], d, o);
+    T o[3];
+    diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
     const T rh = a.rh[d];
     for (int c = 0; c < 3; ++c) {
       if (CURV) {
@@ -480,7 +513,7 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
   const T rinv = CURV ? coef[12 * np + p] : coef[2 * np + p];
   const T rhoinv = CURV ? rinv / Jinv : rinv;
   const T l2m = lam + T(2) * mu;
-  const double d0 = 6.0 / (2.0 * 1.0) * log(1.0 / 1.0e-3);
+  const double d0 = a.pml_d0;  // 6/(2*1) * ln(1/1e-3), src/RHS_Interior.f90:1815
   const T cfs = T(1);
   T corr[9];
 #pragma unroll
@@ -493,10 +526,10 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
     const bool hi = side & 1;
     const int ii = idx[axis], n = nn[axis];
     if (!(hi ? (ii >= n - npml) : (ii < npml))) continue;
-    double dd;  // damping profile in grid-index units (src/RHS_Interior.f90:1855,1973,2092)
-    if (axis == 2) dd = hi ? fabs((double)(ii + 1 - (n - npml)) / npml) : fabs((double)(ii + 1 - npml) / npml);
-    else dd = hi ? fabs((double)(ii + 1 - (n - npml)) / npml) : fabs((double)(ii - npml) / npml);
-    const T damp = (T)(d0 * dd);
+    // damping profile in grid-index units (src/RHS_Interior.f90:1855,1973,2092),
+    // in the field precision
+    const int off = hi ? ii + 1 - (n - npml) : (axis == 2 ? ii + 1 - npml : ii - npml);
+    const T damp = (T)d0 * (fabs((T)off / (T)npml));
     long long sp;
     if (axis == 0) sp = (hi ? ii - (n - npml) : ii) + (long long)npml * (j + (long long)nr * k);
     else if (axis == 1) sp = i + (long long)nq * ((hi ? ii - (n - npml) : ii) + (long long)npml * k);
@@ -688,24 +721,25 @@ __global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ Vo
   }
   const long long np = a.np;
   const long long p = i + (long long)a.pq * (j + (long long)a.nr * k);
-  double xs[3] = {0.0, (double)a.ycoord[p], 0.0}, s0[6];
-  if (!initial_stress(a.preset, xs, s0))
-    for (int c = 0; c < 6; ++c) s0[c] = a.s0u[c];
+  T s0[6];
+  if (!initial_stress_y<T>(a.preset, a.ycoord[p], s0))
+    for (int c = 0; c < 6; ++c) s0[c] = (T)a.s0u[c];
   T sa[6];
-  for (int c = 0; c < 6; ++c) sa[c] = a.Fout[(3 + c) * np + p] + (T)s0[c];
+  for (int c = 0; c < 6; ++c) sa[c] = a.Fout[(3 + c) * np + p] + s0[c];
   const T sigma = (sa[0] + sa[1] + sa[2]) / T(3);
   const T J2 = ((sa[0] - sa[1]) * (sa[0] - sa[1]) + (sa[1] - sa[2]) * (sa[1] - sa[2]) +
                 (sa[2] - sa[0]) * (sa[2] - sa[0])) / T(6) +
                sa[3] * sa[3] + sa[4] * sa[4] + sa[5] * sa[5];
   const T tau = sqrt(J2);
-  const T Ys = fmax(T(0), (T)(a.pl_c * cos(atan(a.pl_nu))) - sigma * (T)sin(atan(a.pl_nu)));
+  // c cos(atan nu), sin(atan nu) and exp(-dt/Tv) are uniform: set on the host
+  const T Ys = fmax(T(0), (T)a.pl_ccos - sigma * (T)a.pl_sin);
   if (!(tau - Ys > T(0))) return;
-  const T e = (T)exp(-a.dt / a.pl_Tv);
+  const T e = (T)a.pl_decay;
   const T rr = e + (T(1) - e) * Ys / tau;
   for (int c = 0; c < 6; ++c) {
     const T dlt = c < 3 ? T(1) : T(0);
     const T sd = sa[c] - sigma * dlt;
-    a.Fout[(3 + c) * np + p] = (sigma * dlt + rr * sd) - (T)s0[c];
+    a.Fout[(3 + c) * np + p] = (sigma * dlt + rr * sd) - s0[c];
     if (KAHAN) a.C[(3 + c) * np + p] = T(0);
   }
 }
