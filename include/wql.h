@@ -145,7 +145,7 @@ int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 
 /* Autotuner: times the stencil-kernel candidates (WQL_FP32C: the TMA
- * kernel with 3 or 2 stages and s chunks of 12..48 planes or automatic;
+ * kernel with s chunks of 12..48 planes or automatic;
  * WQL_FP64: tiled and per-point) on the scenario's own blocks, reps
  * launches each, into scratch arrays (the scenario's state is not
  * changed), applies the fastest with wql_set_tuning and returns it.
@@ -223,8 +223,8 @@ int wql_kernel_times(wql_scn* scn, int kind, double* ms, int* launches);
  * in WQL_FP32C, tiled 32x8 in WQL_FP64), 1 = per-point form (every
  * neighbour read through the caches), 2 = tiled shared-memory kernel with
  * 32x8 tiles, 3 = the same at three blocks per SM (FP32), 4 = 64x8 tiles
- * (WQL_FP32C only), 5 = TMA-pipelined kernel with a 3-deep stage ring
- * (WQL_FP32C only), 6 = the same with 2 stages; schunk = planes per thread
+ * (WQL_FP32C only), 5 = TMA-pipelined kernel (32x12 tiles, two-deep stage
+ * ring; WQL_FP32C only), 6 = accepted as 5; schunk = planes per thread
  * block along s (0 = automatic). */
 int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk);
 

@@ -1080,7 +1080,7 @@ int batch_step(wql_batch* B) {
       }
       CK(cudaMemcpyAsync(B->d_dev, B->d_host.data(), B->d_host.size() * sizeof(TmaBatchDesc),
                          cudaMemcpyHostToDevice, B->stream));
-      launch_stencil_tma_batch(B->d_dev, (int)B->d_host.size(), total, curv == 1, true, 3, B->stream);
+      launch_stencil_tma_batch(B->d_dev, (int)B->d_host.size(), total, curv == 1, true, B->stream);
       CK(cudaEventRecord(B->joined, B->stream));
       for (size_t i : who) {
         CK(cudaStreamWaitEvent(B->members[i]->stream, B->joined, 0));
@@ -1431,13 +1431,12 @@ int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
       return WQL_OK;
     }
   }
-  // candidates: the TMA kernel with 3 or 2 stages and several s chunk sizes
-  // (FP32C), the tiled and per-point kernels (FP64)
+  // candidates: the TMA kernel with several s chunk sizes (FP32C), the
+  // tiled and per-point kernels (FP64)
   std::vector<std::pair<int, int>> cand;
   if (scn->prec == WQL_FP32C) {
-    for (int v : {5, 6})
-      for (int c : {0, 12, 16, 24, 32, 48})
-        if (c <= scn->B[0].ns) cand.push_back({v, c});
+    for (int c : {0, 12, 14, 16, 24, 32, 48})
+      if (c <= scn->B[0].ns) cand.push_back({5, c});
   } else {
     for (int c : {8, 16, 32}) cand.push_back({2, c});
     cand.push_back({1, 0});

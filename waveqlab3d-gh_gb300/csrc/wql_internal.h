@@ -114,7 +114,10 @@ constexpr int kFrameOff[9] = {FR_UFACE, FR_VFACE, FR_S, FR_UHAT, FR_VHAT, FR_SVE
 // Tensor maps of one block for the TMA stencil kernel (FP32 fields): the
 // field box with halo and the lead-plane tile for each of the two field
 // buffers, and the coefficient boxes.  Built once at set-up.
-constexpr int kTmaTQ = 32, kTmaTR = 8;
+// Tile 32 (q) x 12 (r): twelve consumer warps and a two-deep ring of
+// stages fill one SM's shared memory (measured faster than 32 x 8 tiles with
+// three stages, 32 x 10 and 64 x 6 on 2 x 201^3 blocks).
+constexpr int kTmaTQ = 32, kTmaTR = 12, kTmaStages = 2;
 struct StencilMaps {
   CUtensorMap fbox[2], flead[2];  // per field buffer
   CUtensorMap ca, cb, cc, cl;     // coefficients: q-halo rows, r-halo columns, tile, lead plane
@@ -125,9 +128,8 @@ struct StencilMaps {
 // Fills m for a block; returns 0 or a CUDA driver error code.
 int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
                       bool curv);
-// Launches the TMA stencil kernel (every plane of the block) with a 2- or
-// 3-deep ring of shared-memory stages.
-void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int stages, void* stream);
+// Launches the TMA stencil kernel (every plane of the block).
+void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream);
 
 // One entry of the packed table of the batched TMA stencil launch: one block
 // at one stage (its tensor maps for the stage's input buffer, its arguments)
@@ -147,7 +149,7 @@ bool tma_eligible(const VolumeArgs<float>& a);
 // One launch over nd table entries (all curvilinear or all Cartesian, all
 // with or all without compensation).
 void launch_stencil_tma_batch(const TmaBatchDesc* d_dev, int nd, long long total_ctas, bool curv, bool kahan,
-                              int stages, void* stream);
+                              void* stream);
 
 // One stage on one block: launch_volume runs the stencil kernel (DF and the
 // updated fields for every point); launch_corrections then adds the PML,

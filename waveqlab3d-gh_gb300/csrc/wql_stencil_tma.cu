@@ -9,7 +9,7 @@
 // 1516-1703, 1757-1772) are folded into DF beforehand by the face
 // pre-kernel, so this kernel has no face-dependent work.
 //
-// A CTA owns a 32 x 8 (q, r) tile and marches along a chunk of s planes.  One
+// A CTA owns a 32 x 12 (q, r) tile and marches along a chunk of s planes.  One
 // producer thread streams each plane into shared memory with
 // cp.async.bulk.tensor (TMA) through an NS-deep ring of stages guarded by
 // mbarriers ("full" completes on the transaction bytes, "empty" when all
@@ -497,6 +497,11 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
     else hi = mid - 1;
   }
   const TmaBatchDesc& D = d[lo];
+  // the table was written by a host copy: order that write before the
+  // tensor-map proxy reads the maps (in every thread that issues copies)
+  if (threadIdx.x == kTmaTQ * kTmaTR)
+    for (int i = 0; i < 8; ++i)
+      asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(&D.m[i]) : "memory");
   const long long l = cta - D.cta0;
   tma_body<CURV, KAHAN, NS>(D.a, *reinterpret_cast<const MapArgs*>(&D.m), D.schunk, (int)(l % D.tq),
                             (int)((l / D.tq) % D.tr), (int)(l / ((long long)D.tq * D.tr)));
@@ -524,6 +529,14 @@ MapArgs stage_maps(const StencilMaps& sm) {
   m.ck = sm.ck;
   return m;
 }
+
+template <bool CURV, bool KAHAN>
+constexpr size_t tma_smem_bytes(int NS) {
+  return sizeof(float) * (size_t)NS * TmaTile<CURV, KAHAN>::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
+}
+static_assert(tma_smem_bytes<true, true>(kTmaStages) <= 227 * 1024 &&
+                  tma_smem_bytes<false, true>(kTmaStages) <= 227 * 1024,
+              "the stage ring must fit in the shared memory of one CTA");
 
 template <typename K>
 size_t prepare(K kern, int NS, int stage_words) {
@@ -631,28 +644,19 @@ bool tma_eligible(const VolumeArgs<float>& a) {
   return a.tma != nullptr && (a.nr <= kTmaTR + 3 || a.nr >= kTmaTR + 6);
 }
 
-void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bool curv, bool kahan, int stages,
-                              void* stream) {
+void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bool curv, bool kahan, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
-  if (stages == 2) {
-    if (curv) kahan ? launch_tma_batch<true, true, 2>(d, nd, total, s) : launch_tma_batch<true, false, 2>(d, nd, total, s);
-    else kahan ? launch_tma_batch<false, true, 2>(d, nd, total, s) : launch_tma_batch<false, false, 2>(d, nd, total, s);
-  } else {
-    if (curv) kahan ? launch_tma_batch<true, true, 3>(d, nd, total, s) : launch_tma_batch<true, false, 3>(d, nd, total, s);
-    else kahan ? launch_tma_batch<false, true, 3>(d, nd, total, s) : launch_tma_batch<false, false, 3>(d, nd, total, s);
-  }
+  if (curv) kahan ? launch_tma_batch<true, true, kTmaStages>(d, nd, total, s)
+                  : launch_tma_batch<true, false, kTmaStages>(d, nd, total, s);
+  else kahan ? launch_tma_batch<false, true, kTmaStages>(d, nd, total, s)
+             : launch_tma_batch<false, false, kTmaStages>(d, nd, total, s);
 }
 
-void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, int stages, void* stream) {
+void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream) {
   const StencilMaps& sm = *static_cast<const StencilMaps*>(a.tma);
   cudaStream_t s = (cudaStream_t)stream;
-  if (stages == 2) {
-    if (curv) kahan ? launch_tma<true, true, 2>(a, sm, s) : launch_tma<true, false, 2>(a, sm, s);
-    else kahan ? launch_tma<false, true, 2>(a, sm, s) : launch_tma<false, false, 2>(a, sm, s);
-  } else {
-    if (curv) kahan ? launch_tma<true, true, 3>(a, sm, s) : launch_tma<true, false, 3>(a, sm, s);
-    else kahan ? launch_tma<false, true, 3>(a, sm, s) : launch_tma<false, false, 3>(a, sm, s);
-  }
+  if (curv) kahan ? launch_tma<true, true, kTmaStages>(a, sm, s) : launch_tma<true, false, kTmaStages>(a, sm, s);
+  else kahan ? launch_tma<false, true, kTmaStages>(a, sm, s) : launch_tma<false, false, kTmaStages>(a, sm, s);
 }
 
 }  // namespace wql

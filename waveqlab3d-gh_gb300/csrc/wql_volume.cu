@@ -762,7 +762,7 @@ void launch_tiled(const VolumeArgs<T>& a, cudaStream_t s) {
 
 // Stencil-kernel variants (the tuning table): 1 per-point, 2 tiled 32x8 at
 // 1 CTA/SM, 3 tiled 32x8 at 3 CTAs/SM in FP32, 4 tiled 64x8 at 1 CTA/SM,
-// 5 TMA-pipelined (FP32) with 3 stages, 6 the same with 2; 0 picks the
+// 5 TMA-pipelined (FP32), 6 accepted as 5; 0 picks the
 // fastest measured on a 2 x 201^3 curvilinear block pair (TMA in FP32,
 // tiled 32x8 in FP64).
 //
@@ -805,7 +805,7 @@ void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
     case 5:
     case 6:
       if constexpr (f32) {
-        launch_stencil_tma(a, CURV, KAHAN, v == 6 ? 2 : 3, s);
+        launch_stencil_tma(a, CURV, KAHAN, s);
         return;
       }
       [[fallthrough]];
