@@ -368,7 +368,12 @@ __device__ __forceinline__ void tma_body(const VolumeArgs<float>& a, const MapAr
             for (int c = 0; c < 6; ++c)
               o[c] = c1 * (qv[4][c] - qv[2][c]) + c2 * (qv[5][c] - qv[1][c]) + c3 * (qv[6][c] - qv[0][c]);
           } else {
-            s_closure<CURV>(a, p, s, ks, o);
+            // a separate array: only it goes through memory for the call,
+            // o stays in registers
+            float os[6];
+            s_closure<CURV>(a, p, s, ks, os);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) o[c] = os[c];
           }
         } else {
           const int kind = d == 0 ? kq : kr;
@@ -507,13 +512,13 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
                             (int)((l / D.tq) % D.tr), (int)(l / ((long long)D.tq * D.tr)));
 }
 
-// Planes per s chunk: the tuned value, else about 24 in equal chunks
-// (measured on 2 x 201^3 blocks, shorter chunks balance the SMs better than
-// fewer waves do, down to where the per-chunk start -- the first six planes
-// of the s window -- shows).
+// Planes per s chunk: the tuned value, else about 16 in equal chunks
+// (measured on 2 x 201^3 blocks with 32 x 12 tiles: 14-24 planes within 1 %,
+// longer chunks leave a longer tail of the last wave, shorter ones pay the
+// per-chunk start -- the first six planes of the s window -- more often).
 int chunk_planes(const VolumeArgs<float>& a) {
   if (a.schunk > 0) return a.schunk;
-  const int nc = std::max(1, (a.ns + 12) / 24);
+  const int nc = std::max(1, (a.ns + 8) / 16);
   return (a.ns + nc - 1) / nc;
 }
 
