@@ -492,6 +492,9 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
   // velocity gradient at the point
   T g[3][3];
   const T Jinv = CURV ? coef[9 * np + p] : T(1);
+  // every loop over axes and sides is unrolled so that the per-axis index,
+  // extent and stride are compile-time selections (no local-memory arrays)
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
     T o[3];
     diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
@@ -519,6 +522,7 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
 #pragma unroll
   for (int c = 0; c < 9; ++c) corr[c] = T(0);
   // reference order of the layers: s-low, s-high, r-low, r-high, q-low, q-high
+#pragma unroll
   for (int oi = 0; oi < 6; ++oi) {
     const int side = oi < 2 ? 4 + oi : (oi < 4 ? oi : oi - 4);
     if (!a.pml[side]) continue;
@@ -543,6 +547,7 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
     T sd[3];
     if (CURV) {
       T acc3[3] = {T(0), T(0), T(0)};
+#pragma unroll
       for (int d = 0; d < 3; ++d) {
         T r3[3];
         diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
