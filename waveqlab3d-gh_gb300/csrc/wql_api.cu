@@ -112,6 +112,7 @@ struct wql_scn {
     void* Q[6] = {};
     void* DQ[6] = {};
     long long slab_np[6] = {};
+    void* G = nullptr;  // PML velocity gradient hand-off (FP32C with PML)
     void* y = nullptr;
     double cart_metric[3] = {1, 1, 1};
     double tau_h[3] = {};
@@ -476,6 +477,7 @@ int setup_block(wql_scn* S, int b) {
       if ((rc = S->alloc(&B.Q[s], 9 * slab * S->esz))) return rc;
       if ((rc = S->alloc(&B.DQ[s], 9 * slab * S->esz))) return rc;
     }
+    if (S->prec == WQL_FP32C && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   }
   const double tau0 = 1.0 / (0.315949074074074);  // src/block.f90:191
   const int dims[3] = {B.nq, B.nr, B.ns};
@@ -839,6 +841,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
     a.DQ[s] = (T*)B.DQ[s];
     a.slab_np[s] = B.slab_np[s];
   }
+  a.G = (T*)B.G;  // used only when the block's stencil is the TMA kernel
   a.bc_form = S->bc_form;
   a.kernel = S->kernel_variant;
   a.schunk = S->schunk;
@@ -1556,6 +1559,9 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
       const bool pml = (s2 % 2 == 0) ? bp.pml_lqrs[s2 / 2] : bp.pml_rqrs[s2 / 2];
       if (pml && bp.npml > 0) res += 2 * al(9 * (npd / dims[s2 / 2]) * bp.npml * esz);
     }
+    bool any_pml = false;
+    for (int s2 = 0; s2 < 3; ++s2) any_pml = any_pml || bp.pml_lqrs[s2] || bp.pml_rqrs[s2];
+    if (any_pml && bp.npml > 0 && precision == WQL_FP32C) res += al(9 * np * esz);
     if (P.response == "plastic") res += al(np * esz);
     // set-up arrays of one block: x, metric, J, material (FP64)
     transient = std::max(transient, al(3 * npd * 8) + al(9 * npd * 8) + al(npd * 8) + al(3 * npd * 8));

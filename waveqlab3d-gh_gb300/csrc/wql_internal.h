@@ -56,6 +56,10 @@ struct VolumeArgs {
   T* Q[6];
   T* DQ[6];
   long long slab_np[6];
+  // velocity gradient g[c][j] (component c*3+j, stride np) of the PML points,
+  // written by the TMA stencil kernel and read by the PML kernel of the same
+  // stage; nullptr where the PML kernel forms it itself
+  T* G;
   int kernel;         // stencil variant: 0 default, 1 per-point, 2..4 tiled
   int schunk;         // planes per CTA along s for the tiled kernel (0: default)
   // RK

@@ -234,6 +234,10 @@ __device__ __forceinline__ void tma_body(const VolumeArgs<float>& a, const MapAr
   const int q = q0 + tx, r = r0 + ty;
   const bool own = q < nq && r >= spr.own_lo && r < spr.own_hi;
   const int kq = sbp_kind(q, nq), kr = sbp_kind(r, nr);
+  // PML points hand their velocity gradient to the PML kernel (a.G)
+  const int npml = a.npml;
+  const bool pml_qr = a.G != nullptr && ((a.pml[0] && q < npml) || (a.pml[1] && q >= nq - npml) ||
+                                         (a.pml[2] && r < npml) || (a.pml[3] && r >= nr - npml));
   const long long np = a.np;
   const long long sts = (long long)a.pq * nr;
   const long long col = q + (long long)a.pq * r;
@@ -433,6 +437,12 @@ __device__ __forceinline__ void tma_body(const VolumeArgs<float>& a, const MapAr
             g[c][d] = sc * o[c];
           }
         }
+      }
+      if (a.G != nullptr && (pml_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) a.G[(c * 3 + jj) * np + p] = g[c][jj];
       }
       const int ci = ty * TQ + tx;
       const float lam = CURV ? CC[4 * NC + ci] : CC[0 * NC + ci];

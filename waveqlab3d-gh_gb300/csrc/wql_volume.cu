@@ -489,27 +489,36 @@ __global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ Volume
   const long long st[3] = {1, a.pq, (long long)a.pq * nr};
   const T* __restrict__ F = a.Fin;
   const T* __restrict__ coef = a.coef;
-  // velocity gradient at the point
+  // velocity gradient at the point: from the TMA stencil of this stage
+  // (a.G), else formed here
   T g[3][3];
   const T Jinv = CURV ? coef[9 * np + p] : T(1);
+  const bool have_g = a.G != nullptr;
+  if (have_g) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj) g[c][jj] = a.G[(c * 3 + jj) * np + p];
+  }
   // every loop over axes and sides is unrolled so that the per-axis index,
   // extent and stride are compile-time selections (no local-memory arrays)
+  if (!have_g) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    T o[3];
-    diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
-    const T rh = a.rh[d];
-    for (int c = 0; c < 3; ++c) {
-      if (CURV) {
-        for (int jj = 0; jj < 3; ++jj) {
-          const T m = coef[(d * 3 + jj) * np + p] * Jinv;
-          g[c][jj] = d == 0 ? m * (rh * o[c]) : g[c][jj] + m * (rh * o[c]);
+    for (int d = 0; d < 3; ++d) {
+      T o[3];
+      diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
+      const T rh = a.rh[d];
+      for (int c = 0; c < 3; ++c) {
+        if (CURV) {
+          for (int jj = 0; jj < 3; ++jj) {
+            const T m = coef[(d * 3 + jj) * np + p] * Jinv;
+            g[c][jj] = d == 0 ? m * (rh * o[c]) : g[c][jj] + m * (rh * o[c]);
+          }
+        } else {
+          g[c][d] = a.cart_metric[d] * rh * o[c];
         }
-      } else {
-        g[c][d] = a.cart_metric[d] * rh * o[c];
       }
     }
-    // Cartesian: the per-axis stress derivatives are the flux derivatives
   }
   const T lam = CURV ? coef[10 * np + p] : coef[0 * np + p];
   const T mu = CURV ? coef[11 * np + p] : coef[1 * np + p];
@@ -855,8 +864,12 @@ int launch_pre(const VolumeArgs<T>& a, void* stream) {
 }
 
 template <typename T>
-int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream) {
+int launch_corrections(const VolumeArgs<T>& a0, bool curv, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  // the PML velocity gradient comes from the stencil only when that was the
+  // TMA kernel (the only one that writes it)
+  VolumeArgs<T> a = a0;
+  if (!stencil_has_faces(a)) a.G = nullptr;
   const bool kahan = a.C != nullptr;
   if (curv) return kahan ? launch_corr<T, true, true>(a, s) : launch_corr<T, true, false>(a, s);
   return kahan ? launch_corr<T, false, true>(a, s) : launch_corr<T, false, false>(a, s);
