@@ -133,8 +133,8 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 template <bool CURV>
 __device__ __noinline__ void s_closure(const VolumeArgs<float>& a, long long p, int s, int ks, float o[6]) {
   const long long np = a.np, st = (long long)a.pq * a.nr;
-#pragma unroll
-  for (int c = 0; c < 6; ++c) o[c] = 0.0f;
+  float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // in registers; o is written once
+#pragma unroll 3
   for (int e = 0; e < 9; ++e) {
     float w;
     int off;
@@ -154,8 +154,10 @@ __device__ __noinline__ void s_closure(const VolumeArgs<float>& a, long long p, 
       for (int c = 0; c < 3; ++c) x[3 + c] = F[sig(c, 2) * np + pp];
     }
 #pragma unroll
-    for (int c = 0; c < 6; ++c) o[c] += w * x[c];
+    for (int c = 0; c < 6; ++c) acc[c] += w * x[c];
   }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) o[c] = acc[c];
 }
 
 struct MapArgs {
@@ -330,13 +332,12 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       float tmp[3];
       if (tx < 16) qflux(ty, tx < 8 ? tx : tx + TQ, tmp);     // q halo: 8 columns each side
       if (ty < 6) rflux(ty < 3 ? ty : ty + TR, tx, tmp);      // r halo: 3 rows each side
-      // every consumer thread arrives; the bounded wait makes the fluxes of
-      // all of them visible (arrive releases, the wait acquires)
+      // a warp forms every q flux of its own row (the q derivative needs
+      // only those: warp sync); the r fluxes of other rows come from other
+      // warps: every consumer thread arrives here and waits (bounded) just
+      // before the r derivative, so the q and s derivatives overlap the wait
+      __syncwarp();
       mbar_arrive(fluxbar);
-      if (!mbar_wait(fluxbar, T & 1)) {
-        atomicExch(a.err, 3);
-        return false;
-      }
     }
 
     if (work) {
@@ -356,7 +357,12 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       float g[3][3], dv[3];
       const float Jinv = CURV ? CC[3 * NC + ty * TQ + tx] : 1.0f;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
+      for (int k = 0; k < 3; ++k) {
+        const int d = k == 0 ? 0 : (k == 1 ? 2 : 1);  // q, s, then r
+        if (CURV && k == 2 && !mbar_wait(fluxbar, T & 1)) {
+          atomicExch(a.err, 3);
+          return false;
+        }
         float o[6];
         if (d == 2) {
           if (ks == 0) {
@@ -417,15 +423,15 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
           }
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            dv[c] = d == 0 ? rh * o[3 + c] : dv[c] + rh * o[3 + c];
+            dv[c] = k == 0 ? rh * o[3 + c] : dv[c] + rh * o[3 + c];
 #pragma unroll
-            for (int jj = 0; jj < 3; ++jj) g[c][jj] = d == 0 ? mt[jj] * (rh * o[c]) : g[c][jj] + mt[jj] * (rh * o[c]);
+            for (int jj = 0; jj < 3; ++jj) g[c][jj] = k == 0 ? mt[jj] * (rh * o[c]) : g[c][jj] + mt[jj] * (rh * o[c]);
           }
         } else {
           const float sc = a.cart_metric[d] * rh;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            dv[c] = d == 0 ? sc * o[3 + c] : dv[c] + sc * o[3 + c];
+            dv[c] = k == 0 ? sc * o[3 + c] : dv[c] + sc * o[3 + c];
             g[c][d] = sc * o[c];
           }
         }
@@ -470,6 +476,9 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
           a.Fout[c * np + p] = f0 + a.Bdt * df;
         }
       }
+    } else if (CURV && !mbar_wait(fluxbar, T & 1)) {  // the same phase for threads without a point
+      atomicExch(a.err, 3);
+      return false;
     }
     // order this thread's shared-memory writes (the fluxes) before the
     // producer's next bulk copy into the stage
