@@ -472,8 +472,9 @@ def main():
     main_r = res["fp32c"]
     peak, peak_kind = peaks()
     vol_ms, vol_n = main_r["kt"]["stencil"]
-    kernel_name = "stencil_kernel_tma<float,curv,kahan>"
-    pts_per_launch = (401 * 201 * 201) if args.workload == "config2" else (args.n ** 3)
+    # one launch per RK stage covers both blocks
+    kernel_name = "stencil_kernel_tma2<float,curv,kahan>"
+    pts_per_launch = ups * main_r["steps"] / vol_n if vol_n else 0
     algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
     traffic = None

@@ -1119,6 +1119,28 @@ int batch_step(wql_batch* B) {
 
 int run_step(wql_scn* S) {
   StepCtx c = step_begin(S);
+  bool pair = false;  // both blocks through the TMA kernel: one stencil launch per stage
+  if (S->prec == WQL_FP32C) {
+    pair = true;
+    for (int b = 0; b < 2; ++b) pair = pair && stencil_has_faces(volume_args<float>(S, b, 0.0, 0.0, false));
+  }
+  if (pair) {
+    // both blocks' pre-kernels, the stencil launch, both blocks'
+    // corrections (the blocks touch disjoint arrays)
+    for (int stage = 1; stage <= 5; ++stage) {
+      stage_head(S, c, stage);
+      for (int b = 0; b < 2; ++b) stage_block_pre(S, c, stage, b);
+      const double A = stage_A(S, stage), Bdt = stage_Bdt(S, stage);
+      mark_begin(S, 1);
+      launch_stencil_tma2(volume_args<float>(S, 0, A, Bdt, stage == 5), volume_args<float>(S, 1, A, Bdt, stage == 5),
+                          S->curv, true, S->stream);
+      mark_end(S);
+      c.launches += 1;
+      for (int b = 0; b < 2; ++b) stage_block_post(S, c, stage, b);
+      S->cur ^= 1;
+    }
+    return step_end(S, c);
+  }
   for (int stage = 1; stage <= 5; ++stage) {
     stage_head(S, c, stage);
     for (int b = 0; b < 2; ++b) {

@@ -134,6 +134,13 @@ int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, vo
                       bool curv);
 // Launches the TMA stencil kernel (every plane of the block).
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream);
+// The same for both blocks of a scenario in one launch.
+void launch_stencil_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, bool curv, bool kahan,
+                         void* stream);
+// Whether the block's stencil runs as the TMA kernel (the tuning and the
+// block shape allow it).
+template <typename T>
+bool stencil_has_faces(const VolumeArgs<T>& a);
 
 // One entry of the packed table of the batched TMA stencil launch: one block
 // at one stage (its tensor maps for the stage's input buffer, its arguments)

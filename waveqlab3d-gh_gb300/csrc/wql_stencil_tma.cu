@@ -575,6 +575,35 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
   ring.drain(tb);
 }
 
+// Both blocks of a scenario in one launch: CTAs [0, ntile0) take block 0's
+// tiles, the rest block 1's.  The arguments stay kernel parameters (two
+// inlined copies of the tile code, each with its own constant offsets), so
+// the block pair costs what two single launches cost minus one launch tail.
+struct TwoBlocks {
+  VolumeArgs<float> a[2];
+  MapArgs m[2];
+  int schunk[2], tq[2], tr[2];
+  int ntile0;
+};
+
+template <bool CURV, bool KAHAN, int NS>
+__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
+    stencil_kernel_tma2(const __grid_constant__ TwoBlocks P) {
+  Ring<CURV, KAHAN, NS> ring;
+  ring.init();
+  int tb = 0;
+  const int w = blockIdx.x;
+  if (w < P.ntile0) {
+    tma_body<CURV, KAHAN, NS>(P.a[0], P.m[0], P.schunk[0], w % P.tq[0], (w / P.tq[0]) % P.tr[0],
+                              w / (P.tq[0] * P.tr[0]), tb);
+  } else {
+    const int l = w - P.ntile0;
+    tma_body<CURV, KAHAN, NS>(P.a[1], P.m[1], P.schunk[1], l % P.tq[1], (l / P.tq[1]) % P.tr[1],
+                              l / (P.tq[1] * P.tr[1]), tb);
+  }
+  ring.drain(tb);
+}
+
 // Planes per s chunk: the tuned value, else about 16 in equal chunks
 // (measured on 2 x 201^3 blocks with 32 x 12 tiles: 14-24 planes within 1 %,
 // longer chunks leave a longer tail of the last wave, shorter ones pay the
@@ -627,6 +656,26 @@ void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t 
   const int schunk = chunk_planes(a);
   const int ntile = tq * tr * ((a.ns + schunk - 1) / schunk);
   kern<<<ntile, TL::NC + 32, smem, s>>>(a, stage_maps(sm), schunk, tq, tr, ntile);
+}
+
+template <bool CURV, bool KAHAN, int NS>
+void launch_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, cudaStream_t s) {
+  using TL = TmaTile<CURV, KAHAN>;
+  auto kern = stencil_kernel_tma2<CURV, KAHAN, NS>;
+  static const size_t smem = prepare(kern, NS, TL::STAGE_W);
+  TwoBlocks P;
+  const VolumeArgs<float>* a[2] = {&a0, &a1};
+  int ntile[2];
+  for (int b = 0; b < 2; ++b) {
+    P.a[b] = *a[b];
+    P.m[b] = stage_maps(*static_cast<const StencilMaps*>(a[b]->tma));
+    P.schunk[b] = chunk_planes(*a[b]);
+    P.tq[b] = (a[b]->nq + TL::TQ - 1) / TL::TQ;
+    P.tr[b] = (a[b]->nr + TL::TR - 1) / TL::TR;
+    ntile[b] = P.tq[b] * P.tr[b] * ((a[b]->ns + P.schunk[b] - 1) / P.schunk[b]);
+  }
+  P.ntile0 = ntile[0];
+  kern<<<ntile[0] + ntile[1], TL::NC + 32, smem, s>>>(P);
 }
 
 template <bool CURV, bool KAHAN, int NS>
@@ -723,6 +772,13 @@ void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bo
                   : launch_tma_batch<true, false, kTmaStages>(d, nd, total, s);
   else kahan ? launch_tma_batch<false, true, kTmaStages>(d, nd, total, s)
              : launch_tma_batch<false, false, kTmaStages>(d, nd, total, s);
+}
+
+void launch_stencil_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, bool curv, bool kahan,
+                         void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (curv) kahan ? launch_tma2<true, true, kTmaStages>(a0, a1, s) : launch_tma2<true, false, kTmaStages>(a0, a1, s);
+  else kahan ? launch_tma2<false, true, kTmaStages>(a0, a1, s) : launch_tma2<false, false, kTmaStages>(a0, a1, s);
 }
 
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream) {

@@ -902,5 +902,7 @@ template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
 template int launch_pre<double>(const VolumeArgs<double>&, void*);
 template int launch_pre<float>(const VolumeArgs<float>&, void*);
 template int launch_corrections<float>(const VolumeArgs<float>&, bool, void*);
+template bool stencil_has_faces<float>(const VolumeArgs<float>&);
+template bool stencil_has_faces<double>(const VolumeArgs<double>&);
 
 }  // namespace wql
