@@ -1018,9 +1018,23 @@ struct wql_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t joined = nullptr;
   std::vector<cudaEvent_t> ev;
+  // Packed stencil tables of the current membership, built once per
+  // membership (and tuning): every member's buffer index flips with every
+  // stage, so a step starts in one of two phases, and the tables hold
+  // [phase][stage][curvilinear] groups of descriptors in one device array.
   TmaBatchDesc* d_dev = nullptr;
   size_t d_cap = 0;
-  std::vector<TmaBatchDesc> d_host;
+  struct Group {
+    size_t off = 0;
+    int nd = 0;
+    long long total = 0;
+    std::vector<size_t> who;  // members with a block in the group
+  };
+  Group groups[2][5][2];
+  std::vector<wql_scn*> key_members;
+  std::vector<int> key_tuning;  // variant, schunk per member
+  std::vector<int> cur0;        // members' buffer index when the tables were built
+  bool built = false;
   ~wql_batch() {
     for (auto e : ev) cudaEventDestroy(e);
     if (joined) cudaEventDestroy(joined);
@@ -1035,6 +1049,74 @@ bool batch_tma(const wql_scn* S) {
   return S->prec == WQL_FP32C && (S->kernel_variant == 0 || S->kernel_variant == 5 || S->kernel_variant == 6);
 }
 
+// (Re)builds the packed tables when the membership or a member's tuning
+// changed, and returns the phase of this step.
+int batch_tables(wql_batch* B, int* phase) {
+  const size_t n = B->members.size();
+  std::vector<int> tun;
+  for (auto* S : B->members) {
+    tun.push_back(S->kernel_variant);
+    tun.push_back(S->schunk);
+  }
+  bool same = B->built && B->key_members == B->members && B->key_tuning == tun;
+  int p = 0;
+  if (same && n) {
+    p = B->members[0]->cur ^ B->cur0[0];
+    for (size_t i = 0; i < n; ++i) same = same && ((B->members[i]->cur ^ B->cur0[i]) == p);
+  }
+  if (same) {
+    *phase = p;
+    return WQL_OK;
+  }
+  std::vector<TmaBatchDesc> h;
+  B->cur0.assign(n, 0);
+  for (size_t i = 0; i < n; ++i) B->cur0[i] = B->members[i]->cur;
+  for (int ph = 0; ph < 2; ++ph)
+    for (int stage = 1; stage <= 5; ++stage)
+      for (int curv = 0; curv < 2; ++curv) {
+        wql_batch::Group& g = B->groups[ph][stage - 1][curv];
+        g = wql_batch::Group();
+        g.off = h.size();
+        for (size_t i = 0; i < n; ++i) {
+          wql_scn* S = B->members[i];
+          if (!batch_tma(S) || (int)S->curv != curv) continue;
+          const int keep = S->cur;
+          S->cur = B->cur0[i] ^ ph ^ ((stage - 1) & 1);
+          bool any = false;
+          for (int b = 0; b < 2; ++b) {
+            VolumeArgs<float> a = volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5);
+            if (!tma_eligible(a)) continue;
+            TmaBatchDesc d;
+            const long long k = fill_tma_desc(a, d);
+            d.cta0 = g.total;
+            g.total += k;
+            h.push_back(d);
+            any = true;
+          }
+          S->cur = keep;
+          if (any) g.who.push_back(i);
+        }
+        g.nd = (int)(h.size() - g.off);
+      }
+  if (h.size() > B->d_cap) {
+    CK(cudaStreamSynchronize(B->stream));
+    if (B->d_dev) cudaFree(B->d_dev);
+    B->d_dev = nullptr;
+    B->d_cap = h.size();
+    CK(cudaMalloc(&B->d_dev, B->d_cap * sizeof(TmaBatchDesc)));
+  }
+  if (!h.empty()) {
+    // the previous tables may still be in use by launches in flight
+    CK(cudaStreamSynchronize(B->stream));
+    CK(cudaMemcpy(B->d_dev, h.data(), h.size() * sizeof(TmaBatchDesc), cudaMemcpyHostToDevice));
+  }
+  B->key_members = B->members;
+  B->key_tuning = tun;
+  B->built = true;
+  *phase = 0;
+  return WQL_OK;
+}
+
 int batch_step(wql_batch* B) {
   const size_t n = B->members.size();
   while (B->ev.size() < n) {
@@ -1042,6 +1124,9 @@ int batch_step(wql_batch* B) {
     CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     B->ev.push_back(e);
   }
+  int phase = 0;
+  int trc = batch_tables(B, &phase);
+  if (trc) return trc;
   std::vector<StepCtx> c(n);
   for (size_t i = 0; i < n; ++i) c[i] = step_begin(B->members[i]);
   for (int stage = 1; stage <= 5; ++stage) {
@@ -1050,42 +1135,17 @@ int batch_step(wql_batch* B) {
       stage_head(S, c[i], stage);
       for (int b = 0; b < 2; ++b) stage_block_pre(S, c[i], stage, b);
     }
-    // the packed stencil table: one group per (curvilinear, compensated)
+    // the packed stencil launches: one group per mesh kind
     for (int curv = 0; curv < 2; ++curv) {
-      B->d_host.clear();
-      std::vector<size_t> who;
-      long long total = 0;
-      for (size_t i = 0; i < n; ++i) {
-        wql_scn* S = B->members[i];
-        if (!batch_tma(S) || (int)S->curv != curv) continue;
-        bool any = false;
-        for (int b = 0; b < 2; ++b) {
-          VolumeArgs<float> a = volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5);
-          if (!tma_eligible(a)) continue;
-          TmaBatchDesc d;
-          const long long k = fill_tma_desc(a, d);
-          d.cta0 = total;
-          total += k;
-          B->d_host.push_back(d);
-          any = true;
-        }
-        if (any) who.push_back(i);
-      }
-      if (B->d_host.empty()) continue;
-      if (B->d_host.size() > B->d_cap) {
-        if (B->d_dev) cudaFree(B->d_dev);
-        B->d_cap = B->d_host.size() * 2;
-        CK(cudaMalloc(&B->d_dev, B->d_cap * sizeof(TmaBatchDesc)));
-      }
-      for (size_t i : who) {
+      const wql_batch::Group& g = B->groups[phase][stage - 1][curv];
+      if (g.nd == 0) continue;
+      for (size_t i : g.who) {
         CK(cudaEventRecord(B->ev[i], B->members[i]->stream));
         CK(cudaStreamWaitEvent(B->stream, B->ev[i], 0));
       }
-      CK(cudaMemcpyAsync(B->d_dev, B->d_host.data(), B->d_host.size() * sizeof(TmaBatchDesc),
-                         cudaMemcpyHostToDevice, B->stream));
-      launch_stencil_tma_batch(B->d_dev, (int)B->d_host.size(), total, curv == 1, true, B->stream);
+      launch_stencil_tma_batch(B->d_dev + g.off, g.nd, g.total, curv == 1, true, B->stream);
       CK(cudaEventRecord(B->joined, B->stream));
-      for (size_t i : who) {
+      for (size_t i : g.who) {
         CK(cudaStreamWaitEvent(B->members[i]->stream, B->joined, 0));
         c[i].launches += 1;
       }

@@ -129,9 +129,10 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 
 // s derivative of the six differenced quantities on a closure row (planes
 // 0..5 and ns-6..ns-1), read from global memory: the s window in registers
-// holds only the 7 planes of a central row.
+// holds only the 7 planes of a central row.  Inlined: as a call, its
+// argument passing put values on the stack and made the caller spill.
 template <bool CURV>
-__device__ __noinline__ void s_closure(const VolumeArgs<float>& a, long long p, int s, int ks, float o[6]) {
+__device__ __forceinline__ void s_closure(const VolumeArgs<float>& a, long long p, int s, int ks, float o[6]) {
   const long long np = a.np, st = (long long)a.pq * a.nr;
   float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // in registers; o is written once
 #pragma unroll 3
@@ -549,29 +550,33 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
 template <bool CURV, bool KAHAN, int NS>
 __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
     stencil_kernel_tma_batch(const TmaBatchDesc* __restrict__ d, int nd, long long total) {
+  // the entry's arguments are copied to shared memory: read from there they
+  // cost no registers across the plane loop (held in registers they spill)
+  __shared__ VolumeArgs<float> sa;
   Ring<CURV, KAHAN, NS> ring;
-  ring.init();
-  int tb = 0, last = -1;
-  for (long long cta = blockIdx.x; cta < total; cta += gridDim.x) {
-    int lo = 0, hi = nd - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) / 2;
-      if (d[mid].cta0 <= cta) lo = mid;
-      else hi = mid - 1;
-    }
-    const TmaBatchDesc& D = d[lo];
-    // the table was written by a host copy: order that write before the
-    // tensor-map proxy reads an entry's maps (in the thread that issues
-    // copies, once per entry change)
-    if (lo != last && threadIdx.x == kTmaTQ * kTmaTR)
-      for (int i = 0; i < 8; ++i)
-        asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(&D.m[i]) : "memory");
-    last = lo;
-    const long long l = cta - D.cta0;
-    if (!tma_body<CURV, KAHAN, NS>(D.a, *reinterpret_cast<const MapArgs*>(&D.m), D.schunk, (int)(l % D.tq),
-                                   (int)((l / D.tq) % D.tr), (int)(l / ((long long)D.tq * D.tr)), tb))
-      break;
+  const long long cta = blockIdx.x;
+  int lo = 0, hi = nd - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (d[mid].cta0 <= cta) lo = mid;
+    else hi = mid - 1;
   }
+  const TmaBatchDesc& D = d[lo];
+  {
+    const int* src = reinterpret_cast<const int*>(&D.a);
+    int* dst = reinterpret_cast<int*>(&sa);
+    for (int i = threadIdx.x; i < (int)(sizeof(VolumeArgs<float>) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  }
+  // the table was written by a host copy: order that write before the
+  // tensor-map proxy reads the entry's maps (in the thread that issues copies)
+  if (threadIdx.x == kTmaTQ * kTmaTR)
+    for (int i = 0; i < 8; ++i)
+      asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(&D.m[i]) : "memory");
+  ring.init();  // its barrier also publishes sa
+  int tb = 0;
+  const long long l = cta - D.cta0;
+  tma_body<CURV, KAHAN, NS>(sa, *reinterpret_cast<const MapArgs*>(&D.m), D.schunk, (int)(l % D.tq),
+                            (int)((l / D.tq) % D.tr), (int)(l / ((long long)D.tq * D.tr)), tb);
   ring.drain(tb);
 }
 
