@@ -478,7 +478,7 @@ def main():
     algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_stencil_tma_fp32c_curv.json")
+    tpath = os.path.join(ROOT, "profiles", "traffic_stencil_tma2_fp32c_curv.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             t = json.load(f)
