@@ -1,6 +1,7 @@
 // Block coordinates on the host (one-time FP64 setup); see wql_grid.h.
 #include "wql_grid.h"
 
+#include <algorithm>
 #include <cmath>
 
 namespace wql {
@@ -238,31 +239,121 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
   return 0;
 }
 
+namespace {
+
+// Bounding box of every q row (j, k) of a block: min x, y, z then max x, y, z.
+std::vector<double> row_boxes(const BlockGrid& G) {
+  const int nq = G.nq, nr = G.nr, ns = G.ns;
+  std::vector<double> box(6 * (size_t)nr * ns);
+  for (size_t row = 0; row < (size_t)nr * ns; ++row) {
+    double* b = &box[6 * row];
+    for (int c = 0; c < 3; ++c) {
+      const double* x = &G.x[c][row * nq];
+      b[c] = *std::min_element(x, x + nq);
+      b[3 + c] = *std::max_element(x, x + nq);
+    }
+  }
+  return box;
+}
+
+// Distance from p to a row's box: no point of the row is closer.  Each step
+// (difference, square, sum, root) rounds monotonically, so the floating-point
+// value is also at most that of any point of the row.
+double box_distance(const double* b, const double* p) {
+  double s = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    const double e = p[c] < b[c] ? b[c] - p[c] : (p[c] > b[3 + c] ? p[c] - b[3 + c] : 0.0);
+    s += e * e;
+  }
+  return std::sqrt(s);
+}
+
+}  // namespace
+
 void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk) {
   const int nq = G.nq, nr = G.nr, ns = G.ns;
   auto at = [&](int c, int i, int j, int k) {  // 1-based point
     return G.x[c][(size_t)(i - 1) + (size_t)nq * ((size_t)(j - 1) + (size_t)nr * (k - 1))];
   };
+  auto half_diag = [&](int i, int j, int k) {
+    const double hx = i < nq ? at(0, i + 1, j, k) - at(0, i, j, k) : at(0, nq, j, k) - at(0, nq - 1, j, k);
+    const double hy = j < nr ? at(1, i, j + 1, k) - at(1, i, j, k) : at(1, i, nr, k) - at(1, i, nr - 1, k);
+    const double hz = k < ns ? at(2, i, j, k + 1) - at(2, i, j, k) : at(2, i, j, ns) - at(2, i, j, ns - 1);
+    return 0.5 * std::sqrt(hx * hx + hy * hy + hz * hz);
+  };
+  // A point is admissible only within half its local cell diagonal, so a
+  // station scans only the rows whose box lies within the block's largest
+  // half diagonal; the rows it skips hold no admissible point, and the scan
+  // order (s, r, q with "<=": the last point at equal distance wins) is the
+  // reference's, so the chosen point is the one the full scan picks.
+  double reach = 0.0;
+  for (int k = 1; k <= ns; ++k)
+    for (int j = 1; j <= nr; ++j)
+      for (int i = 1; i <= nq; ++i) reach = std::max(reach, half_diag(i, j, k));
+  const std::vector<double> box = row_boxes(G);
   for (size_t st = 0; st + 2 < xyz.size(); st += 3) {
+    const double* p = &xyz[st];
     int best[3] = {-1, -1, -1};
     double mind = 1.0e8;
-    // scan order s, r, q with "<=": the last point at equal distance wins
     for (int k = 1; k <= ns; ++k)
-      for (int j = 1; j <= nr; ++j)
+      for (int j = 1; j <= nr; ++j) {
+        if (box_distance(&box[6 * ((size_t)(j - 1) + (size_t)nr * (k - 1))], p) > reach) continue;
         for (int i = 1; i <= nq; ++i) {
-          const double hx = i < nq ? at(0, i + 1, j, k) - at(0, i, j, k) : at(0, nq, j, k) - at(0, nq - 1, j, k);
-          const double hy = j < nr ? at(1, i, j + 1, k) - at(1, i, j, k) : at(1, i, nr, k) - at(1, i, nr - 1, k);
-          const double hz = k < ns ? at(2, i, j, k + 1) - at(2, i, j, k) : at(2, i, j, ns) - at(2, i, j, ns - 1);
-          const double dx = at(0, i, j, k) - xyz[st], dy = at(1, i, j, k) - xyz[st + 1],
-                       dz = at(2, i, j, k) - xyz[st + 2];
+          const double dx = at(0, i, j, k) - p[0], dy = at(1, i, j, k) - p[1], dz = at(2, i, j, k) - p[2];
           const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
-          if (d <= mind && d <= 0.5 * std::sqrt(hx * hx + hy * hy + hz * hz)) {
+          if (d <= mind && d <= half_diag(i, j, k)) {
             best[0] = i; best[1] = j; best[2] = k;
             mind = d;
           }
         }
+      }
     if (best[0] > 0) ijk.insert(ijk.end(), best, best + 3);
   }
+}
+
+void nearest_grid_point(const BlockGrid& G, const double p[3], int n0[3]) {
+  const int nq = G.nq, nr = G.nr, ns = G.ns;
+  auto X = [&](int c, int i, int j, int k) {  // 0-based
+    return G.x[c][(size_t)i + (size_t)nq * ((size_t)j + (size_t)nr * k)];
+  };
+  const std::vector<double> box = row_boxes(G);
+  const size_t nrow = (size_t)nr * ns;
+  auto row_min = [&](size_t row) {
+    const int j = (int)(row % nr), k = (int)(row / nr);
+    double m = 1.0e300;
+    for (int i = 0; i < nq; ++i) {
+      const double dx = X(0, i, j, k) - p[0], dy = X(1, i, j, k) - p[1], dz = X(2, i, j, k) - p[2];
+      m = std::min(m, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    return m;
+  };
+  // an upper bound on the nearest distance from the row whose box is
+  // closest, then the reference's scan (s, r, q with "<=") over the rows
+  // that can hold a point that near
+  size_t r0 = 0;
+  double b0 = 1.0e300;
+  for (size_t row = 0; row < nrow; ++row) {
+    const double b = box_distance(&box[6 * row], p);
+    if (b < b0) {
+      b0 = b;
+      r0 = row;
+    }
+  }
+  const double bound = row_min(r0);
+  n0[0] = n0[1] = n0[2] = 0;
+  double mind = 1.0e8;
+  for (int k = 0; k < ns; ++k)
+    for (int j = 0; j < nr; ++j) {
+      if (box_distance(&box[6 * ((size_t)j + (size_t)nr * k)], p) > bound) continue;
+      for (int i = 0; i < nq; ++i) {
+        const double dx = X(0, i, j, k) - p[0], dy = X(1, i, j, k) - p[1], dz = X(2, i, j, k) - p[2];
+        const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (d <= mind) {
+          n0[0] = i; n0[1] = j; n0[2] = k;
+          mind = d;
+        }
+      }
+    }
 }
 
 }  // namespace wql

@@ -39,4 +39,8 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
 // dropped.  Appends 1-based (i, j, k) triples to ijk.
 void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk);
 
+// The 0-based grid point nearest to p (scan order s, r, q; the last point at
+// equal distance wins), the rule of the moment-tensor source placement.
+void nearest_grid_point(const BlockGrid& G, const double p[3], int n0[3]);
+
 }  // namespace wql

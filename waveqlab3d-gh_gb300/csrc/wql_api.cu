@@ -321,18 +321,8 @@ void place_source(const BlockGrid& G, const MomentSource& m, int order, int alph
   for (int c = 0; c < 3; ++c)
     if (!(X(c, 0, 0, 0) <= pos[c] && pos[c] <= X(c, nq - 1, nr - 1, ns - 1))) C.in_box = false;
   if (!C.found) return;
-  int n0[3] = {0, 0, 0};
-  double mind = 1.0e8;
-  for (int k = 0; k < ns; ++k)
-    for (int j = 0; j < nr; ++j)
-      for (int i = 0; i < nq; ++i) {
-        const double dx = X(0, i, j, k) - pos[0], dy = X(1, i, j, k) - pos[1], dz = X(2, i, j, k) - pos[2];
-        const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
-        if (d <= mind) {
-          n0[0] = i; n0[1] = j; n0[2] = k;
-          mind = d;
-        }
-      }
+  int n0[3];
+  nearest_grid_point(G, pos, n0);
   const int nn[3] = {nq, nr, ns};
   const int R = mollify ? 28 : (order == 2 ? 2 : 4);
   for (int c = 0; c < 3; ++c) {
