@@ -113,3 +113,24 @@ def test_autotune_keeps_state(ctx, wqlmod):
     for b in range(2):
         a, ref = s.fields(b), r.fields(b)
         assert np.linalg.norm(a - ref) <= 2e-6 * np.linalg.norm(ref)
+
+
+def test_member_replaced(ctx, wqlmod, tmp_path):
+    """A member that leaves and is destroyed, then a new scenario (which may
+    reuse its host address) joins: the batch's packed tables follow the new
+    member, which steps as it does alone."""
+    specs, make = _members(wqlmod, ctx, tmp_path)
+    batch = wqlmod.Batch(ctx)
+    for _ in range(3):
+        m = make(specs[2])
+        batch.add(m)
+        batch.step(3)
+        batch.remove(m)
+        m.close()
+    fresh, ref = make(specs[2]), make(specs[2])
+    batch.add(fresh)
+    batch.step(5)
+    ref.step(5)
+    fresh.sync(check_nan=True)
+    _same(ref, fresh)
+    batch.close()

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -84,6 +85,12 @@ struct wql_ctx {
 };
 
 struct wql_scn {
+  // process-unique identity (an address can be reused by a later scenario)
+  const long long uid = next_uid();
+  static long long next_uid() {
+    static std::atomic<long long> n{0};
+    return ++n;
+  }
   wql_ctx* ctx = nullptr;
   Problem P;
   wql_media media{};
@@ -1021,7 +1028,7 @@ struct wql_batch {
     std::vector<size_t> who;  // members with a block in the group
   };
   Group groups[2][5][2];
-  std::vector<wql_scn*> key_members;
+  std::vector<long long> key_members;  // member uids
   std::vector<int> key_tuning;  // variant, schunk per member
   std::vector<int> cur0;        // members' buffer index when the tables were built
   bool built = false;
@@ -1048,7 +1055,9 @@ int batch_tables(wql_batch* B, int* phase) {
     tun.push_back(S->kernel_variant);
     tun.push_back(S->schunk);
   }
-  bool same = B->built && B->key_members == B->members && B->key_tuning == tun;
+  std::vector<long long> uids;
+  for (auto* S : B->members) uids.push_back(S->uid);
+  bool same = B->built && B->key_members == uids && B->key_tuning == tun;
   int p = 0;
   if (same && n) {
     p = B->members[0]->cur ^ B->cur0[0];
@@ -1100,7 +1109,7 @@ int batch_tables(wql_batch* B, int* phase) {
     CK(cudaStreamSynchronize(B->stream));
     CK(cudaMemcpy(B->d_dev, h.data(), h.size() * sizeof(TmaBatchDesc), cudaMemcpyHostToDevice));
   }
-  B->key_members = B->members;
+  B->key_members = uids;
   B->key_tuning = tun;
   B->built = true;
   *phase = 0;
