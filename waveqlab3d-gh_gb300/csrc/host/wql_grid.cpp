@@ -3,11 +3,33 @@
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
+#include <vector>
 
 namespace wql {
 namespace {
 
 const double kPi = 3.141592653589793;
+
+// f(k) for k in [0, n) on up to 16 host threads, each taking a contiguous
+// range (every k is independent: the result does not depend on the split).
+template <typename F>
+void parallel_k(int n, F&& f) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (n < 16 || hw == 1) {
+    for (int k = 0; k < n; ++k) f(k);
+    return;
+  }
+  const int per = (n + (int)hw - 1) / (int)hw;
+  std::vector<std::thread> th;
+  for (int lo = 0; lo < n; lo += per) {
+    const int hi = std::min(n, lo + per);
+    th.emplace_back([lo, hi, &f] {
+      for (int k = lo; k < hi; ++k) f(k);
+    });
+  }
+  for (auto& t : th) t.join();
+}
 
 // 2D transfinite interpolation of one face from its four edge curves
 // (Gen_Surf_Mesh, src/grid.f90:2418-2455).  L/R run along the second index
@@ -39,7 +61,7 @@ void block_tfi(int nq, int nr, int ns, const Faces& f, std::vector<double>& x) {
   auto LK = [&](const std::vector<double>& a, int j, int k) { return a[(size_t)j + (size_t)nr * k]; };
   auto IK = [&](const std::vector<double>& a, int i, int k) { return a[(size_t)i + (size_t)nq * k]; };
   auto IJ = [&](const std::vector<double>& a, int i, int j) { return a[(size_t)i + (size_t)nq * j]; };
-  for (int k = 0; k < ns; ++k)
+  parallel_k(ns, [&](int k) {
     for (int j = 0; j < nr; ++j)
       for (int i = 0; i < nq; ++i) {
         const double q = (double)i * hq, r = (double)j * hr, s = (double)k * hs;
@@ -58,6 +80,7 @@ void block_tfi(int nq, int nr, int ns, const Faces& f, std::vector<double>& x) {
                                r * ((1.0 - s) * IK(f.bottom, nq - 1, 0) + s * IK(f.bottom, nq - 1, ns - 1)));
         x[(size_t)i + (size_t)nq * ((size_t)j + (size_t)nr * k)] = U + V + W - UV - UW - VW + C1 + C2;
       }
+  });
 }
 
 int curvilinear(const BlockParams& bp, BlockGrid& G, std::string& err) {
@@ -189,7 +212,7 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
                           (bp.bqrs[1] - bp.aqrs[1]) / (double)(G.nr - 1),
                           (bp.bqrs[2] - bp.aqrs[2]) / (double)(G.ns - 1)};
     for (int c = 0; c < 3; ++c) G.x[c].resize(np);
-    for (int k = 0; k < G.ns; ++k)
+    parallel_k(G.ns, [&](int k) {
       for (int j = 0; j < G.nr; ++j)
         for (int i = 0; i < G.nq; ++i) {
           const size_t p = (size_t)i + (size_t)G.nq * ((size_t)j + (size_t)G.nr * k);
@@ -197,6 +220,7 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
           G.x[1][p] = bp.aqrs[1] + (double)j * bh[1];
           G.x[2][p] = bp.aqrs[2] + (double)k * bh[2];
         }
+    });
   } else if (P.type_of_mesh == "curvilinear") {
     if (P.use_topography) {
       err = "use_topography reads topography files; pass a seeded surface through the API instead";
@@ -214,7 +238,7 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
       err = "fault_offset has the wrong size";
       return 1;
     }
-    for (int k = 0; k < G.ns; ++k)
+    parallel_k(G.ns, [&](int k) {
       for (int j = 0; j < G.nr; ++j)
         for (int i = 0; i < G.nq; ++i) {
           const double q = (double)i / (double)(G.nq - 1);
@@ -222,19 +246,21 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
           G.x[0][(size_t)i + (size_t)G.nq * ((size_t)j + (size_t)G.nr * k)] +=
               w * mods.fault_offset[(size_t)j + (size_t)G.nr * k];
         }
+    });
   }
   if (!mods.topo_offset.empty()) {
     if (mods.topo_offset.size() != (size_t)G.nq * G.ns) {
       err = "topo_offset has the wrong size";
       return 1;
     }
-    for (int k = 0; k < G.ns; ++k)
+    parallel_k(G.ns, [&](int k) {
       for (int j = 0; j < G.nr; ++j)
         for (int i = 0; i < G.nq; ++i) {
           const double w = 1.0 - (double)j / (double)(G.nr - 1);
           G.x[1][(size_t)i + (size_t)G.nq * ((size_t)j + (size_t)G.nr * k)] +=
               w * mods.topo_offset[(size_t)i + (size_t)G.nq * k];
         }
+    });
   }
   return 0;
 }
@@ -245,14 +271,16 @@ namespace {
 std::vector<double> row_boxes(const BlockGrid& G) {
   const int nq = G.nq, nr = G.nr, ns = G.ns;
   std::vector<double> box(6 * (size_t)nr * ns);
-  for (size_t row = 0; row < (size_t)nr * ns; ++row) {
-    double* b = &box[6 * row];
-    for (int c = 0; c < 3; ++c) {
-      const double* x = &G.x[c][row * nq];
-      b[c] = *std::min_element(x, x + nq);
-      b[3 + c] = *std::max_element(x, x + nq);
+  parallel_k(ns, [&](int k) {
+    for (size_t row = (size_t)nr * k; row < (size_t)nr * (k + 1); ++row) {
+      double* b = &box[6 * row];
+      for (int c = 0; c < 3; ++c) {
+        const double* x = &G.x[c][row * nq];
+        b[c] = *std::min_element(x, x + nq);
+        b[3 + c] = *std::max_element(x, x + nq);
+      }
     }
-  }
+  });
   return box;
 }
 
@@ -286,10 +314,14 @@ void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std
   // half diagonal; the rows it skips hold no admissible point, and the scan
   // order (s, r, q with "<=": the last point at equal distance wins) is the
   // reference's, so the chosen point is the one the full scan picks.
-  double reach = 0.0;
-  for (int k = 1; k <= ns; ++k)
+  std::vector<double> plane_reach(ns, 0.0);
+  parallel_k(ns, [&](int k0) {
+    double m = 0.0;
     for (int j = 1; j <= nr; ++j)
-      for (int i = 1; i <= nq; ++i) reach = std::max(reach, half_diag(i, j, k));
+      for (int i = 1; i <= nq; ++i) m = std::max(m, half_diag(i, j, k0 + 1));
+    plane_reach[k0] = m;
+  });
+  const double reach = *std::max_element(plane_reach.begin(), plane_reach.end());
   const std::vector<double> box = row_boxes(G);
   for (size_t st = 0; st + 2 < xyz.size(); st += 3) {
     const double* p = &xyz[st];

@@ -225,17 +225,28 @@ __global__ void fill_comp(T* F, long long np, int comp, T val) {
   if (p < np) F[comp * np + p] = val;
 }
 
+
+// Pitched rows (pq per row) <-> dense FP64 rows (nq per row), so that the
+// host copy is one contiguous transfer (a 2-D copy of short rows runs at a
+// fraction of the link's rate).
 template <typename T>
-__global__ void to_double(const T* in, double* out, long long n) {
-  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p < n) out[p] = (double)in[p];
+__global__ void pitched_to_dense(const T* __restrict__ in, int pq, int nq, long long rows, double* __restrict__ out) {
+  const long long n = (long long)nq * rows;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const long long row = t / nq;
+    out[t] = (double)in[row * pq + (t - row * nq)];
+  }
+}
+template <typename T>
+__global__ void dense_to_pitched(const double* __restrict__ in, int pq, int nq, long long rows, T* __restrict__ out) {
+  const long long n = (long long)pq * rows;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const long long row = t / pq;
+    const int i = (int)(t - row * pq);
+    out[t] = i < nq ? (T)in[row * nq + i] : T(0);
+  }
 }
 
-template <typename T>
-__global__ void from_double(const double* in, T* out, long long n) {
-  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p < n) out[p] = (T)in[p];
-}
 
 // Dense (nq-pitched) FP64 array to a pq-pitched array of T.
 template <typename T>
@@ -1336,19 +1347,18 @@ int wql_get_field(wql_scn* scn, int block, int comp, double* host_out) {
     return fail(WQL_E_INPUT, "bad argument");
   auto& B = scn->B[block];
   CK(cudaStreamSynchronize(scn->stream));
-  const size_t rows = (size_t)B.nr * B.ns;
-  if (scn->prec == WQL_FP64) {
-    CK(cudaMemcpy2D(host_out, B.nq * sizeof(double), (const double*)B.F[scn->cur] + comp * B.np,
-                    B.pq * sizeof(double), B.nq * sizeof(double), rows, cudaMemcpyDeviceToHost));
-  } else {
-    double* tmp = nullptr;
-    CK(cudaMalloc(&tmp, B.np * sizeof(double)));
-    to_double<float><<<(unsigned)((B.np + 255) / 256), 256, 0, scn->stream>>>((const float*)B.F[scn->cur] + comp * B.np, tmp, B.np);
-    CK(cudaStreamSynchronize(scn->stream));
-    CK(cudaMemcpy2D(host_out, B.nq * sizeof(double), tmp, B.pq * sizeof(double), B.nq * sizeof(double), rows,
-                    cudaMemcpyDeviceToHost));
-    cudaFree(tmp);
-  }
+  const long long rows = (long long)B.nr * B.ns;
+  double* tmp = nullptr;
+  CK(cudaMalloc(&tmp, B.npd * sizeof(double)));
+  const unsigned grid = (unsigned)std::min<long long>((B.npd + 255) / 256, 4096);
+  if (scn->prec == WQL_FP64)
+    pitched_to_dense<double><<<grid, 256, 0, scn->stream>>>((const double*)B.F[scn->cur] + comp * B.np, B.pq, B.nq, rows, tmp);
+  else
+    pitched_to_dense<float><<<grid, 256, 0, scn->stream>>>((const float*)B.F[scn->cur] + comp * B.np, B.pq, B.nq, rows, tmp);
+  cudaError_t e = cudaStreamSynchronize(scn->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, tmp, B.npd * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail(WQL_E_CUDA, cudaGetErrorString(e));
   return WQL_OK;
 }
 
@@ -1425,18 +1435,20 @@ int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in) {
     return fail(WQL_E_INPUT, "bad argument");
   auto& B = scn->B[block];
   CK(cudaStreamSynchronize(scn->stream));
-  const size_t rows = (size_t)B.nr * B.ns;
+  const long long rows = (long long)B.nr * B.ns;
   double* tmp = nullptr;
-  CK(cudaMalloc(&tmp, B.np * sizeof(double)));
-  CK(cudaMemset(tmp, 0, B.np * sizeof(double)));
-  CK(cudaMemcpy2D(tmp, B.pq * sizeof(double), host_in, B.nq * sizeof(double), B.nq * sizeof(double), rows,
-                  cudaMemcpyHostToDevice));
-  if (scn->prec == WQL_FP64)
-    CK(cudaMemcpy((double*)B.F[scn->cur] + comp * B.np, tmp, B.np * sizeof(double), cudaMemcpyDeviceToDevice));
-  else
-    from_double<float><<<(unsigned)((B.np + 255) / 256), 256, 0, scn->stream>>>(tmp, (float*)B.F[scn->cur] + comp * B.np, B.np);
-  CK(cudaStreamSynchronize(scn->stream));
+  CK(cudaMalloc(&tmp, B.npd * sizeof(double)));
+  cudaError_t e = cudaMemcpy(tmp, host_in, B.npd * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    const unsigned grid = (unsigned)std::min<long long>((B.np + 255) / 256, 4096);
+    if (scn->prec == WQL_FP64)
+      dense_to_pitched<double><<<grid, 256, 0, scn->stream>>>(tmp, B.pq, B.nq, rows, (double*)B.F[scn->cur] + comp * B.np);
+    else
+      dense_to_pitched<float><<<grid, 256, 0, scn->stream>>>(tmp, B.pq, B.nq, rows, (float*)B.F[scn->cur] + comp * B.np);
+    e = cudaStreamSynchronize(scn->stream);
+  }
   cudaFree(tmp);
+  if (e != cudaSuccess) return fail(WQL_E_CUDA, cudaGetErrorString(e));
   return WQL_OK;
 }
 
