@@ -141,6 +141,15 @@ int wql_get_frames(wql_scn* scn, int what, float* host_out);
  * their 1-based grid indices (3 ints each); wql_get_seismograms the records
  * as records x stations x (t, vx, vy, vz) doubles. */
 int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords);
+/* Writes the outputs so far in the reference's file formats under out_dir
+ * (created if missing): the eight fault streams as raw float32 frames
+ * <name>_interface.{Uface,Vface,S,Uhat,Vhat,Svel,trup,state}
+ * (src/fault_output.f90:12-121) when w_fault = T, and one text file per
+ * station, lines (4f15.10) of t, vx, vy, vz, at
+ * <station_file_directory>/block<b>/<name>_<i>_<j>_<k>_block<b>.dat, or
+ * <name>_<x>_<y>_<z>.dat with station_xyz_index = T
+ * (src/seismogram.f90:98-114, 368-384, 460-474).  Replaces the files. */
+int wql_write_outputs(wql_scn* scn, const char* out_dir);
 int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 

@@ -129,3 +129,32 @@ def test_tma_matches_pointwise(ctx, wqlmod, cfg, schunk):
     b.sync(check_nan=True)
     for blk in range(2):
         assert rel_l2(b.fields(blk), a.fields(blk)) < 2e-6
+
+
+def test_output_files(ctx, wqlmod, tmp_path):
+    """wql_write_outputs: the eight fault streams as raw float32 frames and one
+    (4f15.10) text file per station, in the reference's names and layout;
+    their contents are the frames and records of the run (truth/1)."""
+    p = write(tmp_path, "cart.in", with_groups(golden_in("test_rup_cart_fric"), WEIGHTED))
+    s = wqlmod.Scenario(ctx, p)
+    s.step(46)
+    out = tmp_path / "out"
+    s.write_outputs(out)
+    truth = np.load(os.path.join(GOLDEN, "truth_cart.npz"))
+    ncomp = {"Uface": 9, "Vface": 9, "S": 4, "Uhat": 6, "Vhat": 6, "Svel": 3, "trup": 1, "state": 1}
+    for ext, nc in ncomp.items():
+        f = out / "data" / f"test_rup_cart_fric_interface.{ext}"
+        raw = np.fromfile(f, dtype="<f4")
+        assert raw.size == 46 * nc * 21 * 21, ext
+        assert np.array_equal(raw.reshape(46, nc, 21, 21), s.frames(ext)), ext
+        assert np.abs(raw.reshape(46, nc, 21, 21) - truth[ext]).max() <= 1e-9 * max(np.abs(truth[ext]).max(), 1.0)
+    for block, (ijk, tname) in enumerate((((21, 11, 11), "station_21_11_11"), ((1, 11, 11), "station_1_11_11"))):
+        b = block + 1
+        f = out / "seismogram" / f"block{b}" / "data" / f"test_rup_cart_fric_{ijk[0]}_{ijk[1]}_{ijk[2]}_block{b}.dat"
+        lines = f.read_text().splitlines()
+        assert len(lines) == 46 and all(len(l) == 60 for l in lines)
+        vals = np.array([[float(l[15 * c:15 * (c + 1)]) for c in range(4)] for l in lines])
+        _, rec = s.stations(block)
+        assert np.abs(vals - rec[:, 0, :]).max() <= 0.51e-10
+        assert np.abs(vals - truth[tname]).max() <= 5.1e-7
+    s.close()

@@ -298,7 +298,8 @@ double box_distance(const double* b, const double* p) {
 
 }  // namespace
 
-void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk) {
+void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk,
+                         std::vector<int>* which) {
   const int nq = G.nq, nr = G.nr, ns = G.ns;
   auto at = [&](int c, int i, int j, int k) {  // 1-based point
     return G.x[c][(size_t)(i - 1) + (size_t)nq * ((size_t)(j - 1) + (size_t)nr * (k - 1))];
@@ -339,7 +340,10 @@ void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std
           }
         }
       }
-    if (best[0] > 0) ijk.insert(ijk.end(), best, best + 3);
+    if (best[0] > 0) {
+      ijk.insert(ijk.end(), best, best + 3);
+      if (which) which->push_back((int)(st / 3));
+    }
   }
 }
 

@@ -37,7 +37,9 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
 // each requested (x, y, z) the grid point nearest to it among the points
 // within half their local cell diagonal; requests with no such point are
 // dropped.  Appends 1-based (i, j, k) triples to ijk.
-void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk);
+// which, if given, receives the request index of each point found.
+void find_station_points(const BlockGrid& G, const std::vector<double>& xyz, std::vector<int>& ijk,
+                         std::vector<int>* which = nullptr);
 
 // The 0-based grid point nearest to p (scan order s, r, q; the last point at
 // equal distance wins), the rule of the moment-tensor source placement.

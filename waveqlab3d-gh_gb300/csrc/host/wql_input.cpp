@@ -361,6 +361,8 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
   for (auto& it : items_of("output_list")) {
     auto s = it.values.empty() ? std::string() : it.values[0];
     if (it.key == "output_seismograms") P.output_seismograms = to_bool(s);
+    else if (it.key == "station_file_directory") P.station_file_directory = s;
+    else if (it.key == "station_xyz_index") P.station_xyz_index = to_bool(s);
   }
   for (auto& it : items_of("gb300_list")) {
     auto s = it.values.empty() ? std::string() : it.values[0];

@@ -87,8 +87,12 @@ struct Problem {
   // '!---begin:tensor_list---' for both blocks, else tensor_listU / tensor_listV
   bool mt_unified = false;
   std::vector<MomentSource> tensors, tensorsU, tensorsV;
-  // &output_list (src/seismogram.f90:58)
+  // &output_list (src/seismogram.f90:58-82): seismograms on/off, the station
+  // file directory (default 'seismogram') and the file naming by physical
+  // position instead of grid index
   bool output_seismograms = false;
+  std::string station_file_directory = "seismogram";
+  bool station_xyz_index = false;
   // station marker blocks (src/seismogram.f90:181-202): x y z per line
   std::vector<double> stationsU, stationsV;
   // one list for both blocks ('!---begin:station_list---', src/seismogram.f90:157-176);

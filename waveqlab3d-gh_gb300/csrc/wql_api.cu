@@ -6,6 +6,9 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <filesystem>
+#include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -148,6 +151,7 @@ struct wql_scn {
   // (same capacity as the frame ring) and the flushed host records
   struct Stations {
     std::vector<int> ijk;
+    std::vector<double> xyz;       // requested positions of the stations found
     long long* idx_dev = nullptr;
     double* ring = nullptr;        // cap x n x 3
     std::vector<double> host;      // records x n x 4 (t, vx, vy, vz)
@@ -502,7 +506,9 @@ int setup_block(wql_scn* S, int b) {
   if (S->P.output_seismograms) {
     const std::vector<double>& req = !S->P.stations.empty() ? S->P.stations : (b == 0 ? S->P.stationsU : S->P.stationsV);
     auto& T = S->st[b];
-    find_station_points(G, req, T.ijk);
+    std::vector<int> which;
+    find_station_points(G, req, T.ijk, &which);
+    for (int w : which) T.xyz.insert(T.xyz.end(), req.begin() + 3 * w, req.begin() + 3 * w + 3);
     const int n = (int)T.ijk.size() / 3;
     if (n > 0) {
       std::vector<long long> off(n);
@@ -1501,6 +1507,97 @@ int wql_get_seismograms(wql_scn* scn, int block, double* host_out) {
   const int rc = flush_stations(scn);
   if (rc) return rc;
   std::memcpy(host_out, scn->st[block].host.data(), scn->st[block].host.size() * sizeof(double));
+  return WQL_OK;
+}
+
+// Output files in the reference's formats, so that its tools read them:
+// the eight fault streams as raw float32 frames in <name>_interface.<ext>
+// (init_fault_output / write_fault / write_hats, src/fault_output.f90:12-121,
+// frame layout src/mpi3dio.f90:327-364), and one text file per station with
+// one line (4f15.10) of t, vx, vy, vz per record (init_seismogram /
+// write_seismogram, src/seismogram.f90:98-114, 368-384, 460-474) at
+// <station_file_directory>/block<b>/<name>_<i>_<j>_<k>_block<b>.dat, or
+// <name>_<x>_<y>_<z>.dat (f20.3 positions) with station_xyz_index.
+namespace {
+
+// Fortran Fw.d edit of one value (right-justified, w characters; asterisks
+// when it does not fit).
+std::string fortran_f(double v, int w, int d) {
+  char buf[64];
+  if (std::isnan(v)) std::snprintf(buf, sizeof(buf), "%*s", w, "NaN");
+  else if (std::isinf(v)) std::snprintf(buf, sizeof(buf), "%*s", w, v > 0 ? "Infinity" : "-Infinity");
+  else std::snprintf(buf, sizeof(buf), "%*.*f", w, d, v);
+  std::string s(buf);
+  if ((int)s.size() > w) s.assign(w, '*');
+  return s;
+}
+
+std::string trimmed_f(double v, int w, int d) {  // trim(adjustl(...)) of an Fw.d edit
+  std::string s = fortran_f(v, w, d);
+  const size_t i = s.find_first_not_of(' ');
+  return i == std::string::npos ? std::string() : s.substr(i);
+}
+
+}  // namespace
+
+int wql_write_outputs(wql_scn* scn, const char* out_dir) {
+  if (!scn || !out_dir) return fail(WQL_E_INPUT, "null argument");
+  namespace fs = std::filesystem;
+  const std::string name = scn->P.name;
+  std::error_code ec;
+  fs::create_directories(out_dir, ec);
+  if (ec) return fail(WQL_E_INPUT, std::string("cannot create ") + out_dir + ": " + ec.message());
+  int frames = 0, rc = wql_frame_count(scn, &frames);
+  if (rc) return rc;
+  if (frames > 0) {
+    static const char* ext[8] = {"Uface", "Vface", "S", "Uhat", "Vhat", "Svel", "trup", "state"};
+    const long long nf = (long long)scn->B[0].nr * scn->B[0].ns;
+    for (int what = 0; what < 8; ++what) {
+      const int nc = kFrameOff[what + 1] - kFrameOff[what];
+      std::vector<float> buf((size_t)frames * nc * nf);
+      if ((rc = wql_get_frames(scn, what, buf.data()))) return rc;
+      const fs::path path = fs::path(out_dir) / (name + "_interface." + ext[what]);
+      fs::create_directories(path.parent_path(), ec);  // the name may hold a directory part
+      std::FILE* f = std::fopen(path.c_str(), "wb");
+      if (!f) return fail(WQL_E_INPUT, "cannot write " + path.string());
+      const size_t n = std::fwrite(buf.data(), sizeof(float), buf.size(), f);
+      std::fclose(f);
+      if (n != buf.size()) return fail(WQL_E_INPUT, "short write to " + path.string());
+    }
+  }
+  if ((rc = flush_stations(scn))) return rc;
+  const std::string sdir = scn->P.station_file_directory;
+  for (int b = 0; b < 2; ++b) {
+    const auto& T = scn->st[b];
+    const int n = (int)T.ijk.size() / 3;
+    if (n == 0) continue;
+    const std::string bdir = "block" + std::to_string(b + 1);
+    const fs::path dir = (sdir.empty() || sdir == ".") ? fs::path(out_dir) / bdir : fs::path(out_dir) / sdir / bdir;
+    fs::create_directories(dir, ec);
+    if (ec) return fail(WQL_E_INPUT, "cannot create " + dir.string() + ": " + ec.message());
+    const size_t nrec = T.host.size() / (4 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+      std::string file;
+      if (scn->P.station_xyz_index)
+        file = name + "_" + trimmed_f(T.xyz[3 * i], 20, 3) + "_" + trimmed_f(T.xyz[3 * i + 1], 20, 3) + "_" +
+               trimmed_f(T.xyz[3 * i + 2], 20, 3) + ".dat";
+      else
+        file = name + "_" + std::to_string(T.ijk[3 * i]) + "_" + std::to_string(T.ijk[3 * i + 1]) + "_" +
+               std::to_string(T.ijk[3 * i + 2]) + "_block" + std::to_string(b + 1) + ".dat";
+      const fs::path path = dir / file;
+      fs::create_directories(path.parent_path(), ec);
+      std::FILE* f = std::fopen(path.c_str(), "w");
+      if (!f) return fail(WQL_E_INPUT, "cannot write " + path.string());
+      for (size_t r = 0; r < nrec; ++r) {
+        const double* rec = &T.host[(r * n + i) * 4];
+        std::string line;
+        for (int c = 0; c < 4; ++c) line += fortran_f(rec[c], 15, 10);
+        line += '\n';
+        std::fputs(line.c_str(), f);
+      }
+      std::fclose(f);
+    }
+  }
   return WQL_OK;
 }
 
