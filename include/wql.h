@@ -150,6 +150,16 @@ int wql_station_count(wql_scn* scn, int block, int* nstations, int* nrecords);
  * <name>_<x>_<y>_<z>.dat with station_xyz_index = T
  * (src/seismogram.f90:98-114, 368-384, 460-474).  Replaces the files. */
 int wql_write_outputs(wql_scn* scn, const char* out_dir);
+
+/* The grids of both blocks of an input, computed as wql_scenario_create
+ * would, written as the raw FP64 files block_grid_<id>.X/.Y/.Z (q fastest)
+ * that mesh_source = 'file' reads (init_grid_from_file,
+ * src/grid.f90:146-211) -- the role of the reference's preprocessor program
+ * (src/preprocessor.f90).  Host only: no device is touched.  With
+ * mesh_source = 'file' a scenario reads these files from base_dir, and with
+ * material_source = 'file' the files btp(i)%material_path(1:3) (lambda, mu,
+ * rho, raw FP64, q fastest; src/material.f90:706-747). */
+int wql_write_block_grids(const char* in_text, const char* base_dir, const char* out_dir);
 int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 

@@ -158,3 +158,36 @@ def test_output_files(ctx, wqlmod, tmp_path):
         assert np.abs(vals - rec[:, 0, :]).max() <= 0.51e-10
         assert np.abs(vals - truth[tname]).max() <= 5.1e-7
     s.close()
+
+
+def test_mesh_and_material_from_files(ctx, wqlmod, tmp_path):
+    """mesh_source = 'file' (block_grid_<id>.X/Y/Z) and material_source =
+    'file' (btp%material_path) give the same run as the computed grid and the
+    preset material they were written from (bitwise, FP64)."""
+    text = golden_in("test_rup_curv_fric")
+    wqlmod.write_block_grids(text, tmp_path)
+    n = 21 ** 3
+    rho, cs, cp = 2.67, 3.464, 6.0
+    lam, mu = rho * (cp * cp - 2.0 * cs * cs), rho * cs * cs
+    for b in (1, 2):
+        for name, v in (("lam", lam), ("mu", mu), ("rho", rho)):
+            np.full(n, v, dtype="<f8").tofile(tmp_path / f"{name}{b}.bin")
+    ftext = text.replace("type_of_mesh='curvilinear',",
+                         "type_of_mesh='curvilinear',\n mesh_source = 'file',\n material_source = 'file',")
+    assert ftext != text
+    for b in (1, 2):
+        ftext = ftext.replace(f"btp({b})%rho_s_p", f"btp({b})%material_path = 'lam{b}.bin', 'mu{b}.bin', "
+                                                   f"'rho{b}.bin',\nbtp({b})%rho_s_p")
+    a = wqlmod.Scenario(ctx, text=text)
+    f = wqlmod.Scenario(ctx, text=ftext, base_dir=str(tmp_path))
+    a.step(10)
+    f.step(10)
+    for blk in range(2):
+        assert np.array_equal(a.fields(blk), f.fields(blk))
+    assert np.array_equal(a.frames("Svel"), f.frames("Svel"))
+    a.close()
+    f.close()
+    # a missing grid file is an input error, not a crash
+    (tmp_path / "block_grid_2.Z").unlink()
+    with pytest.raises(wqlmod.WqlError):
+        wqlmod.Scenario(ctx, text=ftext, base_dir=str(tmp_path))

@@ -1,0 +1,77 @@
+"""Host-side logic of the library, run without a device: the block grid
+files that mesh_source = 'file' reads (wql_write_block_grids, the role of
+the reference's preprocessor) and the device-footprint estimate used for
+admission."""
+import numpy as np
+import pytest
+
+from inputs import golden_in, set_key
+
+
+@pytest.fixture(scope="module")
+def wqlmod():
+    import shutil
+    if shutil.which("nvcc") is None:
+        pytest.skip("nvcc not available")
+    import wql_build
+    wql_build.build()
+    import wql
+    return wql
+
+
+def _grid(path, n):
+    return np.fromfile(path, dtype="<f8").reshape(n[2], n[1], n[0])  # q fastest
+
+
+def test_block_grid_files_cartesian(wqlmod, tmp_path):
+    """Cartesian blocks: x = a + i*h per axis (src/grid.f90 cartesian_grid_3d),
+    written as raw FP64, q fastest, one file per coordinate and block."""
+    wqlmod.write_block_grids(golden_in("test_rup_cart_fric"), tmp_path)
+    n = (21, 21, 21)
+    boxes = {1: ((-3.0, 6.0, -1.5), (0.0, 9.0, 1.5)), 2: ((0.0, 6.0, -1.5), (3.0, 9.0, 1.5))}
+    for b, (lo, hi) in boxes.items():
+        for c, ext in enumerate("XYZ"):
+            f = tmp_path / f"block_grid_{b}.{ext}"
+            assert f.stat().st_size == 8 * 21 ** 3
+            x = _grid(f, n)
+            line = lo[c] + np.arange(21) * ((hi[c] - lo[c]) / 20.0)
+            shape = [1, 1, 1]
+            shape[2 - c] = 21
+            assert np.array_equal(x, np.broadcast_to(line.reshape(shape), x.shape)), (b, ext)
+
+
+def test_block_grid_files_curvilinear(wqlmod, tmp_path):
+    """Curvilinear blocks (transfinite interpolation with the bumpy fault of
+    truth/2): the faces away from the fault stay flat, the fault faces of the
+    two blocks coincide, and q increases along every row."""
+    wqlmod.write_block_grids(golden_in("test_rup_curv_fric"), tmp_path)
+    n = (21, 21, 21)
+    X1, X2 = _grid(tmp_path / "block_grid_1.X", n), _grid(tmp_path / "block_grid_2.X", n)
+    Y1, Y2 = _grid(tmp_path / "block_grid_1.Y", n), _grid(tmp_path / "block_grid_2.Y", n)
+    Z1, Z2 = _grid(tmp_path / "block_grid_1.Z", n), _grid(tmp_path / "block_grid_2.Z", n)
+    assert np.ptp(X1[:, :, 0]) < 1e-12 and np.ptp(X2[:, :, -1]) < 1e-12
+    assert np.ptp(X1[:, :, -1]) > 0.0  # the fault is not flat
+    assert np.allclose(X1[:, :, -1], X2[:, :, 0], rtol=0, atol=1e-12)
+    assert np.allclose(Y1[:, :, -1], Y2[:, :, 0], rtol=0, atol=1e-12)
+    assert np.allclose(Z1[:, :, -1], Z2[:, :, 0], rtol=0, atol=1e-12)
+    assert (np.diff(X1, axis=2) > 0).all() and (np.diff(X2, axis=2) > 0).all()
+
+
+def test_block_grid_files_bad_directory(wqlmod, tmp_path):
+    bad = tmp_path / "f"
+    bad.write_text("")
+    with pytest.raises(wqlmod.WqlError):
+        wqlmod.write_block_grids(golden_in("test_rup_cart_fric"), bad / "sub")
+
+
+def test_footprint_estimate_host(wqlmod):
+    """The admission estimate grows with the grid, is larger in FP64 than in
+    FP32C, and counts PML slabs."""
+    text = golden_in("test_rup_cart_fric")
+    r32, p32 = wqlmod.estimate_device_bytes(text, wqlmod.FP32C)
+    r64, p64 = wqlmod.estimate_device_bytes(text, wqlmod.FP64)
+    assert 0 < r32 < p32 and 0 < r64 < p64 and r64 > r32
+    big = text.replace("btp(1)%nqrs = 21, 21, 21", "btp(1)%nqrs = 41, 21, 21")
+    assert wqlmod.estimate_device_bytes(big, wqlmod.FP32C)[0] > r32
+    pml = text.replace("btp(1)%rqrs = 0, 1, 1,", "btp(1)%rqrs = 0, 1, 1,\nbtp(1)%pml_lqrs = T, F, F,\nbtp(1)%npml = 5,")
+    assert wqlmod.estimate_device_bytes(pml, wqlmod.FP32C)[0] > r32

@@ -3,6 +3,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -196,6 +198,53 @@ int curvilinear(const BlockParams& bp, BlockGrid& G, std::string& err) {
 
 }  // namespace
 
+std::string resolve_path(const std::string& base_dir, const std::string& name) {
+  if (name.empty() || name[0] == '/' || base_dir.empty()) return name;
+  return base_dir + "/" + name;
+}
+
+int read_f64(const std::string& path, size_t n, std::vector<double>& out, std::string& err) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    err = "cannot open " + path;
+    return 1;
+  }
+  out.resize(n);
+  const size_t got = std::fread(out.data(), sizeof(double), n, f);
+  const bool more = std::fgetc(f) != EOF;
+  std::fclose(f);
+  if (got != n || more) {
+    err = path + " does not hold " + std::to_string(n) + " FP64 values";
+    return 1;
+  }
+  return 0;
+}
+
+int write_block_grids(const Problem& P, const std::string& out_dir, std::string& err) {
+  Problem Q = P;
+  Q.mesh_source = "compute";
+  static const char ext[3] = {'X', 'Y', 'Z'};
+  for (int b = 0; b < 2; ++b) {
+    BlockGrid G;
+    if (make_block_grid(Q, b, SurfaceMods(), G, err)) return 1;
+    for (int c = 0; c < 3; ++c) {
+      const std::string path = resolve_path(out_dir, "block_grid_" + std::to_string(b + 1) + "." + ext[c]);
+      std::FILE* f = std::fopen(path.c_str(), "wb");
+      if (!f) {
+        err = "cannot write " + path;
+        return 1;
+      }
+      const size_t n = std::fwrite(G.x[c].data(), sizeof(double), G.x[c].size(), f);
+      std::fclose(f);
+      if (n != G.x[c].size()) {
+        err = "short write to " + path;
+        return 1;
+      }
+    }
+  }
+  return 0;
+}
+
 int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockGrid& G,
                     std::string& err) {
   const BlockParams& bp = P.btp[block];
@@ -203,8 +252,18 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
   G.nr = bp.nqrs[1];
   G.ns = bp.nqrs[2];
   const size_t np = (size_t)G.nq * G.nr * G.ns;
+  if (P.mesh_source == "file") {
+    // init_grid_from_file (src/grid.f90:146-211): block_grid_<id>.X/Y/Z,
+    // raw FP64 coordinates, q fastest; the seeded surface offsets do not apply
+    static const char ext[3] = {'X', 'Y', 'Z'};
+    for (int c = 0; c < 3; ++c) {
+      const std::string path = resolve_path(P.base_dir, "block_grid_" + std::to_string(block + 1) + "." + ext[c]);
+      if (read_f64(path, np, G.x[c], err)) return 1;
+    }
+    return 0;
+  }
   if (P.mesh_source != "compute") {
-    err = "mesh_source '" + P.mesh_source + "' is not supported (grids are computed)";
+    err = "mesh_source '" + P.mesh_source + "' is not supported ('compute' or 'file')";
     return 1;
   }
   if (P.type_of_mesh == "cartesian") {

@@ -33,6 +33,15 @@ struct SurfaceMods {
 int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockGrid& G,
                     std::string& err);
 
+// name relative to base_dir (unchanged when absolute or base_dir is empty).
+std::string resolve_path(const std::string& base_dir, const std::string& name);
+// Reads exactly n FP64 values from a raw file.
+int read_f64(const std::string& path, size_t n, std::vector<double>& out, std::string& err);
+// The computed grids of both blocks as block_grid_<id>.X/Y/Z in out_dir,
+// the files mesh_source = 'file' reads (what the reference's preprocessor
+// program prepares, src/preprocessor.f90).
+int write_block_grids(const Problem& P, const std::string& out_dir, std::string& err);
+
 // Seismogram stations (Find_Coordinates, src/seismogram.f90:531-650): for
 // each requested (x, y, z) the grid point nearest to it among the points
 // within half their local cell diagonal; requests with no such point are

@@ -206,6 +206,12 @@ void set_block_field(BlockParams& b, const std::string& field,
   else if (field == "pml_rqrs") bv(b.pml_rqrs, 3);
   else if (field == "npml") iv(&b.npml, 1);
   else if (field == "faultsize") iv(b.faultsize, 2);
+  else if (field == "material_path")
+    for (int i = 0; i < 3 && i < (int)v.size(); ++i) b.material_path[i] = v[i];
+  else if (field.rfind("material_path(", 0) == 0) {
+    const int i = std::atoi(field.c_str() + 14) - 1;
+    if (i >= 0 && i < 3) b.material_path[i] = sv();
+  }
 }
 
 std::vector<double> marker_block(const std::string& text, const std::string& tag) {
@@ -269,6 +275,7 @@ std::vector<MomentSource> tensor_block(const std::string& text, const std::strin
 
 int parse_in_text(const std::string& text, const std::string& base_dir,
                   Problem& P, std::string& err) {
+  P.base_dir = base_dir;
   auto groups = groups_of(text);
   auto items_of = [&](const char* g) {
     std::vector<Item> all;

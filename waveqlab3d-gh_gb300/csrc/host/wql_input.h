@@ -28,6 +28,9 @@ struct BlockParams {
   double mu_beta_eta[3] = {0, 0, 0};
   int lqrs[3] = {0, 0, 0}, rqrs[3] = {0, 0, 0};
   std::string profile_type, profile_path, topography_type, topography_path;
+  // material_source = 'file': lambda, mu, rho as raw FP64 arrays, q fastest
+  // (init_material_from_file, src/material.f90:706-747)
+  std::string material_path[3];
   bool pml_lqrs[3] = {false, false, false}, pml_rqrs[3] = {false, false, false};
   int npml = 0;
   int faultsize[2] = {0, 0};
@@ -74,6 +77,9 @@ struct Problem {
               plastic_model = "default", coupling = "locked",
               fd_type = "traditional", type_of_mesh = "cartesian",
               mesh_source = "compute", material_source = "hardcode";
+  // directory that relative file names of the input resolve against (the
+  // .in file's directory; empty: the process's working directory)
+  std::string base_dir;
   int nblocks = 2, nt = 0, order = 5, w_stride = 1;
   double CFL = 0.5, t_final = 0.0, topo = 1.0;
   bool w_fault = true, interpol = false, use_topography = false,

@@ -422,6 +422,17 @@ int setup_block(wql_scn* S, int b) {
     for (int c = 0; c < 3; ++c)
       CK(cudaMemcpyAsync(mat + c * np, user[c], np * sizeof(double), cudaMemcpyHostToDevice, S->stream));
     CK(cudaStreamSynchronize(S->stream));
+  } else if (S->P.material_source == "file") {
+    // init_material_from_file (src/material.f90:706-747): lambda, mu, rho
+    // as raw FP64 arrays, q fastest, named by btp(i)%material_path
+    std::vector<double> h;
+    for (int c = 0; c < 3; ++c) {
+      std::string e2;
+      if (bp.material_path[c].empty()) return fail(WQL_E_INPUT, "material_source = 'file' needs btp%material_path");
+      if (read_f64(resolve_path(S->P.base_dir, bp.material_path[c]), (size_t)np, h, e2)) return fail(WQL_E_INPUT, e2);
+      CK(cudaMemcpyAsync(mat + c * np, h.data(), np * sizeof(double), cudaMemcpyHostToDevice, S->stream));
+      CK(cudaStreamSynchronize(S->stream));
+    }
   } else if (S->P.material_source != "hardcode") {
     return fail(WQL_E_INPUT, "material_source '" + S->P.material_source + "' needs the media arrays");
   } else {
@@ -1598,6 +1609,18 @@ int wql_write_outputs(wql_scn* scn, const char* out_dir) {
       std::fclose(f);
     }
   }
+  return WQL_OK;
+}
+
+int wql_write_block_grids(const char* in_text, const char* base_dir, const char* out_dir) {
+  if (!in_text || !out_dir) return fail(WQL_E_INPUT, "null argument");
+  Problem P;
+  std::string err;
+  if (parse_in_text(in_text, base_dir ? base_dir : "", P, err)) return fail(WQL_E_INPUT, err);
+  std::error_code ec;
+  std::filesystem::create_directories(out_dir, ec);
+  if (ec) return fail(WQL_E_INPUT, std::string("cannot create ") + out_dir + ": " + ec.message());
+  if (write_block_grids(P, out_dir, err)) return fail(WQL_E_INPUT, err);
   return WQL_OK;
 }
 

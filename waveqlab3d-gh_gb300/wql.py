@@ -28,7 +28,7 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream",
            "wql_estimate_device_bytes", "wql_server_create", "wql_server_submit", "wql_server_wait",
            "wql_server_result", "wql_server_release", "wql_server_stats", "wql_server_destroy",
-           "wql_autotune", "wql_write_outputs"]
+           "wql_autotune", "wql_write_outputs", "wql_write_block_grids"]
 
 
 class Media(ctypes.Structure):
@@ -95,6 +95,7 @@ def lib():
         L.wql_station_index.argtypes = [vp, ci, vp]
         L.wql_get_seismograms.argtypes = [vp, ci, vp]
         L.wql_write_outputs.argtypes = [vp, ctypes.c_char_p]
+        L.wql_write_block_grids.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         L.wql_get_iface.argtypes = [vp, ci, ci, vp]
         L.wql_frame_count.argtypes = [vp, ctypes.POINTER(ci)]
         L.wql_get_frames.argtypes = [vp, ci, vp]
@@ -390,3 +391,11 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def write_block_grids(text, out_dir, base_dir=None):
+    """The grids of both blocks of an .in text as block_grid_<id>.X/.Y/.Z in
+    out_dir (raw FP64, q fastest), the files mesh_source = 'file' reads
+    (wql_write_block_grids; host only)."""
+    _check(lib().wql_write_block_grids(text.encode(), str(base_dir).encode() if base_dir else None,
+                                       os.fsencode(str(out_dir))))
