@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only.  Nothing in the product links or calls
 // this file; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-// leg load it, as the checker.
+// leg load it, to compare the product against and to time the CPU path.
 //
 // A plain FP64 CPU restatement of WaveQLab3D's time-stepping hot path, written
 // from the reference's Fortran in the same loop order and expression grouping
