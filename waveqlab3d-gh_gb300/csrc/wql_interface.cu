@@ -138,8 +138,11 @@ __device__ __forceinline__ void load_face(const void* F, long long np, long long
 // R is the arithmetic type of the characteristic algebra: the field type
 // (FP64 fields keep every operation of the FP64 restatement; FP32 fields do
 // the algebra in FP32 with the slip, state and their rates kept in FP64).
+// FP32 fields: capped at 96 registers so that five 128-thread CTAs share an
+// SM and a 201^2 fault (2 x 40401 threads) runs in about one round (measured
+// 0.092 -> 0.078 ms per launch on config 1 despite some spilling).
 template <typename T>
-__global__ void interface_kernel(const __grid_constant__ InterfaceArgs a) {
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(const __grid_constant__ InterfaceArgs a) {
   using R = T;
   constexpr bool F64 = sizeof(T) == 8;
   const long long nf = (long long)a.nr * a.ns;
