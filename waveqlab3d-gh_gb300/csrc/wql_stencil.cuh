@@ -173,9 +173,10 @@ __device__ __forceinline__ void add_correction(const VolumeArgs<T>& a, long long
 // point lies on, times that axis's tau0/h (src/RHS_Interior.f90:1516-1703),
 // plus the fault SAT on the interface face (src/RHS_Interior.f90:1757-1772).
 // The caller subtracts tot from the rates.  Returns false if the point has
-// no penalised face.
+// no penalised face.  Inlined: as a call its array arguments went through
+// the stack.
 template <typename T>
-__device__ __noinline__ bool face_penalty(const VolumeArgs<T>& a, int i, int j, int k, const T* u, T* tot) {
+__device__ __forceinline__ bool face_penalty(const VolumeArgs<T>& a, int i, int j, int k, const T* u, T* tot) {
   const int nq = a.nq, nr = a.nr, ns = a.ns;
   const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
   bool any = false;
