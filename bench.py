@@ -140,7 +140,6 @@ def time_gpu(wql, ctx, text, media, prec, steps, warmup, world):
     st = torch.cuda.ExternalStream(s.stream())
     s.step(warmup)
     s.sync(check_nan=True)
-    s.profile(True)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier(world)
@@ -152,7 +151,14 @@ def time_gpu(wql, ctx, text, media, prec, steps, warmup, world):
     torch.cuda.synchronize()
     barrier(world)
     ms = e0.elapsed_time(e1)
+    # per-kernel times from a separate pass with the library's event markers
+    # (their records would otherwise sit between the timed launches)
+    prof_steps = max(2, min(steps, 5))
+    s.profile(True)
+    s.step(prof_steps)
+    s.sync()
     kt = s.kernel_times()
+    kt["prof_steps"] = prof_steps
     s.profile(False)
     s.sync(check_nan=True)
     info = s.info()
@@ -474,7 +480,7 @@ def main():
     vol_ms, vol_n = main_r["kt"]["stencil"]
     # one launch per RK stage covers both blocks
     kernel_name = "stencil_kernel_tma2<float,curv,kahan>"
-    pts_per_launch = ups * main_r["steps"] / vol_n if vol_n else 0
+    pts_per_launch = ups * main_r["kt"]["prof_steps"] / vol_n if vol_n else 0
     algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
     traffic = None
