@@ -469,8 +469,11 @@ __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_con
 // rates, DQ <- A*DQ + sources - (d+cfs)*Q (plus the face penalty on the
 // slab's own boundary, src/RHS_Interior.f90:1560-1700) and Q <- Q + B*dt*DQ.
 // One thread per point of the block; points outside every slab exit.
+// FP32 fields: capped at 80 registers for three CTAs per SM (24 warps to
+// hide the latency of its dependent loads; measured 0.39 -> 0.31 ms per
+// correction launch on config 2 despite some spilling).
 template <typename T, bool CURV, bool KAHAN>
-__global__ void __launch_bounds__(256) pml_kernel(const __grid_constant__ VolumeArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const __grid_constant__ VolumeArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
