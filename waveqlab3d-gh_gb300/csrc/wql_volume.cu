@@ -469,16 +469,58 @@ __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_con
 // rates, DQ <- A*DQ + sources - (d+cfs)*Q (plus the face penalty on the
 // slab's own boundary, src/RHS_Interior.f90:1560-1700) and Q <- Q + B*dt*DQ.
 // One thread per point of the block; points outside every slab exit.
+// The PML slab union of a block as up to six disjoint boxes: the q slabs
+// over the whole (r, s) extent, the r slabs between them, the s slabs inside
+// both; start[b] is the number of points in boxes before b.
+struct PmlBoxes {
+  int n;
+  int lo[6][3], dim[6][3];
+  long long start[7];
+};
+
+template <typename T>
+PmlBoxes pml_boxes(const VolumeArgs<T>& a) {
+  PmlBoxes B;
+  B.n = 0;
+  B.start[0] = 0;
+  const int nq = a.nq, nr = a.nr, ns = a.ns, w = a.npml;
+  const int qlo = a.pml[0] ? w : 0, qhi = a.pml[1] ? nq - w : nq;
+  const int rlo = a.pml[2] ? w : 0, rhi = a.pml[3] ? nr - w : nr;
+  const int slo = a.pml[4] ? w : 0, shi = a.pml[5] ? ns - w : ns;
+  auto add = [&](int q0, int q1, int r0, int r1, int s0, int s1) {
+    if (q1 <= q0 || r1 <= r0 || s1 <= s0) return;
+    const int b = B.n++;
+    B.lo[b][0] = q0; B.lo[b][1] = r0; B.lo[b][2] = s0;
+    B.dim[b][0] = q1 - q0; B.dim[b][1] = r1 - r0; B.dim[b][2] = s1 - s0;
+    B.start[b + 1] = B.start[b] + (long long)(q1 - q0) * (r1 - r0) * (s1 - s0);
+  };
+  add(0, qlo, 0, nr, 0, ns);
+  add(qhi, nq, 0, nr, 0, ns);
+  add(qlo, qhi, 0, rlo, 0, ns);
+  add(qlo, qhi, rhi, nr, 0, ns);
+  add(qlo, qhi, rlo, rhi, 0, slo);
+  add(qlo, qhi, rlo, rhi, shi, ns);
+  for (int b = B.n; b < 6; ++b) B.start[b + 1] = B.start[b];
+  return B;
+}
+
 // FP32 fields: capped at 80 registers for three CTAs per SM (24 warps to
 // hide the latency of its dependent loads; measured 0.39 -> 0.31 ms per
 // correction launch on config 2 despite some spilling).
 template <typename T, bool CURV, bool KAHAN>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const __grid_constant__ VolumeArgs<T> a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const __grid_constant__ VolumeArgs<T> a,
+                                                                           const __grid_constant__ PmlBoxes bx) {
+  // one thread per point of the slab union, enumerated box by box (q
+  // fastest within a box)
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  int b = 0;
+  while (b < bx.n && t >= bx.start[b + 1]) ++b;
+  if (b >= bx.n) return;
+  const long long l = t - bx.start[b];
+  const int i = bx.lo[b][0] + (int)(l % bx.dim[b][0]);
+  const int j = bx.lo[b][1] + (int)((l / bx.dim[b][0]) % bx.dim[b][1]);
+  const int k = bx.lo[b][2] + (int)(l / ((long long)bx.dim[b][0] * bx.dim[b][1]));
   const int nq = a.nq, nr = a.nr, ns = a.ns, npml = a.npml;
-  if (i >= nq || j >= nr) return;
   const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
   bool any = false;
 #pragma unroll
@@ -835,7 +877,9 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
   int n = 0;
   dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
   if (a.npml > 0) {
-    pml_kernel<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a);
+    const PmlBoxes bx = pml_boxes(a);
+    if (bx.start[bx.n] > 0)
+      pml_kernel<T, CURV, KAHAN><<<(unsigned)((bx.start[bx.n] + 255) / 256), 256, 0, s>>>(a, bx);
     ++n;
   }
   if (!stencil_has_faces(a)) {
