@@ -945,8 +945,11 @@ void stage_head(wql_scn* S, StepCtx& c, int stage) {
   ia.pre = S->pre;
   ia.ramp = nucleation_ramp(S->fp, ts);
   {
-    const double x0[3] = {0.0, 0.0, 0.0};  // V0 does not vary along the fault
-    ia.lnV0h = std::log(0.5 / rs_params(S->fp, x0, 0.0).V0);
+    const double x0[3] = {0.0, 0.0, 0.0};  // V0, b and L do not vary along the fault
+    const RSParams r0 = rs_params(S->fp, x0, 0.0);
+    ia.lnV0h = std::log(0.5 / r0.V0);
+    ia.rs_bL = r0.b / r0.L0;
+    ia.rs_binv = 1.0 / r0.b;
   }
   ia.fp = S->fp;
   ia.frame = (c.want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;

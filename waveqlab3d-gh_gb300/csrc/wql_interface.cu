@@ -116,15 +116,17 @@ __device__ bool newton_mixed(double& V, double Phi, double eta, double sn, doubl
     u = un;
     if (fabsf(du) <= 1.0e-4f * fmaxf(1.0f, fabsf(u))) break;
   }
-  double ud = (double)u, du = 0.0;
+  double ud = (double)u, du = 0.0, v = 0.0;
   for (int it = 0; it < 2; ++it) {
-    const double v = exp(ud);
+    v = exp(ud);
     double A, dA;
     asinh_exp(ud + L, A, dA);
     du = -(v + c * A - target) / (v + c * dA);
     ud += du;
   }
-  V = exp(ud);
+  // exp(ud + du) from the last exp(ud): the series in du is exact to
+  // rounding once |du| <= 1e-9 (the acceptance bound below)
+  V = v * (1.0 + du * (1.0 + 0.5 * du));
   return fabs(du) <= 1.0e-9 * fmax(1.0, fabs(ud));
 }
 
@@ -284,8 +286,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(
       }
       tau_m_hat = (phi_1 - es * vv_m) - T0m;
       tau_l_hat = (phi_2 - es * vv_l) - T0l;
-      // aging law (src/Interface_Condition.f90:431-436)
-      DW[f] = a.A * DW[f] + (rs.b * rs.V0 / rs.L0 * exp(-(psi - rs.f0) / rs.b) - V * rs.b / rs.L0);
+      // aging law (src/Interface_Condition.f90:431-436); the FP32-field mode
+      // multiplies by the reciprocals (FP64 division is slow on this part)
+      if (F64) {
+        DW[f] = a.A * DW[f] + (rs.b * rs.V0 / rs.L0 * exp(-(psi - rs.f0) / rs.b) - V * rs.b / rs.L0);
+      } else {
+        DW[f] = a.A * DW[f] + (a.rs_bL * rs.V0 * exp((rs.f0 - psi) * a.rs_binv) - V * a.rs_bL);
+      }
     }
     const R tmh = (R)tau_m_hat, tlh = (R)tau_l_hat, vm = (R)vv_m, vl = (R)vv_l;
     P[0] = (q_n - phi_n) / Z2p;

@@ -96,6 +96,7 @@ struct InterfaceArgs {
   const double* pre;        // 2 x 5 x nf: static Tn, Tm, Tl, nucleation weight, rate-state a
   double ramp;              // nucleation ramp at this stage's time
   double lnV0h;             // ln(1/(2 V0)) of the rate-and-state law
+  double rs_bL, rs_binv;    // b/L and 1/b of the aging law (uniform along the fault)
   double tau_h[2];
   double A, Bdt, t;
   int stage;
