@@ -1212,7 +1212,7 @@ int run_step(wql_scn* S) {
   bool pair = false;  // both blocks through the TMA kernel: one stencil launch per stage
   if (S->prec == WQL_FP32C) {
     pair = true;
-    for (int b = 0; b < 2; ++b) pair = pair && stencil_has_faces(volume_args<float>(S, b, 0.0, 0.0, false));
+    for (int b = 0; b < 2; ++b) pair = pair && stencil_is_tma(volume_args<float>(S, b, 0.0, 0.0, false));
   }
   if (pair) {
     // both blocks' pre-kernels, the stencil launch, both blocks'

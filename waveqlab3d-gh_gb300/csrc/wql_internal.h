@@ -141,7 +141,7 @@ void launch_stencil_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a
 // Whether the block's stencil runs as the TMA kernel (the tuning and the
 // block shape allow it).
 template <typename T>
-bool stencil_has_faces(const VolumeArgs<T>& a);
+bool stencil_is_tma(const VolumeArgs<T>& a);
 
 // One entry of the packed table of the batched TMA stencil launch: one block
 // at one stage (its tensor maps for the stage's input buffer, its arguments)

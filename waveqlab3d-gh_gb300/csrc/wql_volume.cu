@@ -842,9 +842,11 @@ int effective_variant(const VolumeArgs<T>& a) {
   return v;
 }
 
-// The TMA kernel applies the boundary and fault penalties itself.
+// Whether the block's stencil runs as the TMA kernel.  Its penalties are
+// folded into DF beforehand by the face pre-kernel (launch_pre); the other
+// variants get them afterwards from the face kernel (launch_corrections).
 template <typename T>
-bool stencil_has_faces(const VolumeArgs<T>& a) {
+bool stencil_is_tma(const VolumeArgs<T>& a) {
   const int v = effective_variant(a);
   return v == 5 || v == 6;
 }
@@ -882,7 +884,7 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
       pml_kernel<T, CURV, KAHAN><<<(unsigned)((bx.start[bx.n] + 255) / 256), 256, 0, s>>>(a, bx);
     ++n;
   }
-  if (!stencil_has_faces(a)) {
+  if (!stencil_is_tma(a)) {
     const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
     face_kernel<T, KAHAN><<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(a);
     ++n;
@@ -904,7 +906,7 @@ void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream) {
 
 template <typename T>
 int launch_pre(const VolumeArgs<T>& a, void* stream) {
-  if (!stencil_has_faces(a)) return 0;
+  if (!stencil_is_tma(a)) return 0;
   const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
   face_pre_kernel<T><<<(unsigned)((nface + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a);
   return 1;
@@ -916,7 +918,7 @@ int launch_corrections(const VolumeArgs<T>& a0, bool curv, void* stream) {
   // the PML velocity gradient comes from the stencil only when that was the
   // TMA kernel (the only one that writes it)
   VolumeArgs<T> a = a0;
-  if (!stencil_has_faces(a)) a.G = nullptr;
+  if (!stencil_is_tma(a)) a.G = nullptr;
   const bool kahan = a.C != nullptr;
   if (curv) return kahan ? launch_corr<T, true, true>(a, s) : launch_corr<T, true, false>(a, s);
   return kahan ? launch_corr<T, false, true>(a, s) : launch_corr<T, false, false>(a, s);
@@ -949,7 +951,7 @@ template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
 template int launch_pre<double>(const VolumeArgs<double>&, void*);
 template int launch_pre<float>(const VolumeArgs<float>&, void*);
 template int launch_corrections<float>(const VolumeArgs<float>&, bool, void*);
-template bool stencil_has_faces<float>(const VolumeArgs<float>&);
-template bool stencil_has_faces<double>(const VolumeArgs<double>&);
+template bool stencil_is_tma<float>(const VolumeArgs<float>&);
+template bool stencil_is_tma<double>(const VolumeArgs<double>&);
 
 }  // namespace wql
