@@ -557,8 +557,35 @@ void surf_mesh(int mx, int my, const vector<wp>& XL, const vector<wp>& XR, const
 }
 
 // Curve_Grid_3D3, flat-topography branch: src/grid.f90:471-1160, 1873-1875,
+// read_2darray + reshape_2darray (src/grid.f90:2457-2500): my*mz rows of
+// (x, y, z), list-directed; returns the x column (r fastest).
+bool read_profile_rows(const std::string& path, size_t n, vector<wp>& x1, std::string& err) {
+  std::FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) {
+    err = "cannot open " + path;
+    return false;
+  }
+  x1.assign(n, 0.0);
+  size_t row = 0;
+  char buf[4096];
+  while (row < n && std::fgets(buf, sizeof(buf), f)) {
+    std::string line(buf);
+    for (auto& c : line)
+      if (c == 'd' || c == 'D') c = 'e';
+      else if (c == ',') c = ' ';
+    double a, b, c;
+    if (std::sscanf(line.c_str(), "%lf %lf %lf", &a, &b, &c) == 3) x1[row++] = a;
+  }
+  std::fclose(f);
+  if (row != n) {
+    err = path + ": too few rows";
+    return false;
+  }
+  return true;
+}
+
 // Gen3_Curve_Mesh src/grid.f90:2290-2416
-bool curve_grid(RBlock& B, const wql::BlockParams& bp, std::string& err) {
+bool curve_grid(RBlock& B, const wql::BlockParams& bp, const std::string& base_dir, std::string& err) {
   int mx = B.nq, my = B.nr, mz = B.ns;
   wp ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1], az = bp.aqrs[2], bz = bp.bqrs[2];
   wp lc = bp.lc, rc = bp.rc;
@@ -585,7 +612,34 @@ bool curve_grid(RBlock& B, const wql::BlockParams& bp, std::string& err) {
       Xl[I2(j, k)] = Xl[I2(j, k)] + fa * rc * f;
       Xr[I2(j, k)] = Xr[I2(j, k)] + fa * lc * f;
     }
-  if (pt == "analytical_test_problem") {
+  if (pt == "read_from_memomry_fractal") {  // src/grid.f90:832-924
+    vector<wp> X1;
+    std::string path = bp.profile_path;
+    if (!path.empty() && path[0] != '/' && !base_dir.empty()) path = base_dir + "/" + path;
+    if (!read_profile_rows(path, (size_t)my * mz, X1, err)) return false;
+    vector<wp> Y0xT(my), Y0xB(my), Z0xT(my), Z0xB(my), Z0xL(mz), Z0xR(mz), Y0xL(mz), Y0xR(mz);
+    for (int j = 1; j <= my; ++j) {
+      Y0xT[j - 1] = ay + (wp)(j - 1) * hy;
+      Y0xB[j - 1] = ay + (wp)(j - 1) * hy;
+      Z0xT[j - 1] = bz;
+      Z0xB[j - 1] = az;
+    }
+    for (int k = 1; k <= mz; ++k) {
+      Z0xL[k - 1] = az + (wp)(k - 1) * hz;
+      Z0xR[k - 1] = az + (wp)(k - 1) * hz;
+      Y0xL[k - 1] = ay;
+      Y0xR[k - 1] = by;
+    }
+    surf_mesh(my, mz, Y0xL, Y0xR, Y0xB, Y0xT, Z0xL, Z0xR, Z0xB, Z0xT, Yl, Zl);
+    surf_mesh(my, mz, Y0xL, Y0xR, Y0xB, Y0xT, Z0xL, Z0xR, Z0xB, Z0xT, Yr, Zr);
+    for (int k = 1; k <= mz; ++k)
+      for (int j = 1; j <= my; ++j) {
+        Xl[I2(j, k)] = ax;
+        if (rc != 0.0) Xl[I2(j, k)] = Xl[I2(j, k)] + rc * X1[I2(j, k)];
+        Xr[I2(j, k)] = bx;
+        if (lc != 0.0) Xr[I2(j, k)] = Xr[I2(j, k)] + lc * X1[I2(j, k)];
+      }
+  } else if (pt == "analytical_test_problem") {
     vector<wp> Y0xT(my), Y0xB(my), Z0xT(my), Z0xB(my), Z0xL(mz), Z0xR(mz), Y0xL(mz), Y0xR(mz);
     for (int j = 1; j <= my; ++j) {
       Y0xT[j - 1] = ay + (wp)(j - 1) * hy;
@@ -993,7 +1047,7 @@ int init_block(Domain& D, int b, const Media& md) {
       D.err = "topography grids are not supported by the oracle";
       return 1;
     }
-    if (!curve_grid(B, bp, D.err)) return 1;
+    if (!curve_grid(B, bp, D.P.base_dir, D.err)) return 1;
   } else {
     D.err = "unknown type_of_mesh " + D.P.type_of_mesh;
     return 1;

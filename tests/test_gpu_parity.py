@@ -191,3 +191,14 @@ def test_mesh_and_material_from_files(ctx, wqlmod, tmp_path):
     (tmp_path / "block_grid_2.Z").unlink()
     with pytest.raises(wqlmod.WqlError):
         wqlmod.Scenario(ctx, text=ftext, base_dir=str(tmp_path))
+
+
+def test_fault_profile_file_vs_oracle(ctx, wqlmod, oracle_lib, tmp_path):
+    """A fault surface read from a profile file (profile_type
+    'read_from_memomry_fractal'): GPU FP64 against the oracle."""
+    from test_host_cpu import _fractal_case
+    text, _ = _fractal_case(tmp_path)
+    p = write(tmp_path, "fractal.in", text)
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, 20)
+    for e in field_errors(s, o):
+        assert e < TOL

@@ -75,3 +75,36 @@ def test_footprint_estimate_host(wqlmod):
     assert wqlmod.estimate_device_bytes(big, wqlmod.FP32C)[0] > r32
     pml = text.replace("btp(1)%rqrs = 0, 1, 1,", "btp(1)%rqrs = 0, 1, 1,\nbtp(1)%pml_lqrs = T, F, F,\nbtp(1)%npml = 5,")
     assert wqlmod.estimate_device_bytes(pml, wqlmod.FP32C)[0] > r32
+
+
+def _fractal_case(tmp_path, n=21):
+    """The truth/2 curvilinear input with profile_type
+    'read_from_memomry_fractal': a fault surface file of n*n rows (x, y, z),
+    r fastest, written with Fortran exponents."""
+    rng = np.random.default_rng(7)
+    j, k = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")  # j fastest in ravel
+    x1 = 0.03 * np.sin(0.7 * j + 0.2) * np.cos(0.5 * k) + 0.005 * rng.standard_normal((n, n))
+    with open(tmp_path / "fault.dat", "w") as f:
+        for xv, yv, zv in zip(x1.ravel(), (6.0 + 0.15 * j).ravel(), (-1.5 + 0.15 * k).ravel()):
+            f.write(f"{xv:.17e} {yv:.6f} {zv:.6f}\n".replace("e", "d"))
+    text = golden_in("test_rup_curv_fric").replace("'analytical_test_problem'", "'read_from_memomry_fractal'") \
+                                          .replace("'No-path'", "'fault.dat'")
+    return text, x1
+
+
+def test_fault_profile_file(wqlmod, tmp_path):
+    """profile_type 'read_from_memomry_fractal': the fault faces are the block
+    faces plus lc (block 1, q = nq) or rc (block 2, q = 1) times the file's x
+    column (src/grid.f90:832-924)."""
+    text, x1 = _fractal_case(tmp_path)
+    out = tmp_path / "grids"
+    wqlmod.write_block_grids(text, out, base_dir=tmp_path)
+    n = (21, 21, 21)
+    X1 = _grid(out / "block_grid_1.X", n)
+    X2 = _grid(out / "block_grid_2.X", n)
+    assert np.allclose(X1[:, :, -1], 0.0 + x1, rtol=0, atol=1e-15)
+    assert np.allclose(X2[:, :, 0], 0.0 + x1, rtol=0, atol=1e-15)
+    assert np.ptp(X1[:, :, 0]) < 1e-12 and np.ptp(X2[:, :, -1]) < 1e-12
+    (tmp_path / "fault.dat").write_text("1 2 3\n")
+    with pytest.raises(wqlmod.WqlError):
+        wqlmod.write_block_grids(text, out, base_dir=tmp_path)

@@ -85,13 +85,42 @@ void block_tfi(int nq, int nr, int ns, const Faces& f, std::vector<double>& x) {
   });
 }
 
-int curvilinear(const BlockParams& bp, BlockGrid& G, std::string& err) {
+// The fault surface file of profile_type 'read_from_memomry_fractal'
+// (read_2darray + reshape_2darray, src/grid.f90:832-838, 2457-2500): n rows
+// of three list-directed numbers (x, y, z); the x column, r fastest.
+int read_fault_profile(const std::string& path, size_t n, std::vector<double>& x1, std::string& err) {
+  std::FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) {
+    err = "cannot open fault profile " + path;
+    return 1;
+  }
+  x1.resize(n);
+  char line[4096];
+  size_t row = 0;
+  while (row < n && std::fgets(line, sizeof(line), f)) {
+    for (char* c = line; *c; ++c)
+      if (*c == 'd' || *c == 'D') *c = 'e';  // Fortran exponent letters
+      else if (*c == ',') *c = ' ';
+    double v[3];
+    if (std::sscanf(line, "%lf %lf %lf", &v[0], &v[1], &v[2]) != 3) continue;  // blank or comment line
+    x1[row++] = v[0];
+  }
+  std::fclose(f);
+  if (row != n) {
+    err = path + " holds " + std::to_string(row) + " rows of x y z, not " + std::to_string(n);
+    return 1;
+  }
+  return 0;
+}
+
+int curvilinear(const BlockParams& bp, const std::string& base_dir, BlockGrid& G, std::string& err) {
   const int mx = G.nq, my = G.nr, mz = G.ns;
   const double ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1];
   const double az = bp.aqrs[2], bz = bp.bqrs[2];
   const std::string& pt = bp.profile_type;
   const bool flat = pt.empty() || pt == "No-path" || pt == "no_path" || pt == "none";
-  if (!(flat || pt == "analytical_tpv28" || pt == "analytical_test_problem")) {
+  const bool fractal = pt == "read_from_memomry_fractal";  // the reference's spelling
+  if (!(flat || fractal || pt == "analytical_tpv28" || pt == "analytical_test_problem")) {
     err = "profile_type '" + pt + "' is not supported";
     return 1;
   }
@@ -120,6 +149,26 @@ int curvilinear(const BlockParams& bp, BlockGrid& G, std::string& err) {
         X.right[p] += bp.lc * f;
       }
     }
+  if (fractal) {
+    // (y, z) meshed from straight edges, x = the face position plus rc (left)
+    // or lc (right) times the file's x column (src/grid.f90:832-924)
+    std::vector<double> x1;
+    if (read_fault_profile(resolve_path(base_dir, bp.profile_path), nx, x1, err)) return 1;
+    std::vector<double> eyL(mz, ay), eyR(mz, by), eyB(my), eyT(my), ezL(mz), ezR(mz), ezB(my, az),
+        ezT(my, bz);
+    for (int j = 0; j < my; ++j) eyB[j] = eyT[j] = ay + (double)j * hy;
+    for (int k = 0; k < mz; ++k) ezL[k] = ezR[k] = az + (double)k * hz;
+    face_tfi(my, mz, eyL, eyR, eyB, eyT, Y.left);
+    face_tfi(my, mz, ezL, ezR, ezB, ezT, Z.left);
+    Y.right = Y.left;
+    Z.right = Z.left;
+    for (size_t p = 0; p < nx; ++p) {
+      X.left[p] = ax;
+      if (bp.rc != 0.0) X.left[p] += bp.rc * x1[p];
+      X.right[p] = bx;
+      if (bp.lc != 0.0) X.right[p] += bp.lc * x1[p];
+    }
+  }
   if (pt == "analytical_test_problem") {
     // (y,z) meshed by Gen_Surf_Mesh from straight edges, then a Gaussian bump
     // plus a sine product on x (src/grid.f90:790-841)
@@ -285,7 +334,7 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
       err = "use_topography reads topography files; pass a seeded surface through the API instead";
       return 1;
     }
-    if (curvilinear(bp, G, err)) return 1;
+    if (curvilinear(bp, P.base_dir, G, err)) return 1;
   } else {
     err = "unknown type_of_mesh '" + P.type_of_mesh + "'";
     return 1;
