@@ -94,6 +94,12 @@ int wql_scenario_destroy(wql_scn* scn);
 
 /* Advance nsteps steps = nsteps calls of time_step_RK (src/time_step.f90:68). */
 int wql_step(wql_scn* scn, int nsteps);
+/* One RK stage (1..5, in order) of the current step: the body of one pass
+ * of the stage loop of time_step_RK (src/time_step.f90:109-147), for parity
+ * and debugging; stages 1..5 give the same result as one wql_step.
+ * WQL_E_STATE for a stage out of order, and for wql_step or wql_batch_add
+ * while a step is in progress. */
+int wql_stage(wql_scn* scn, int stage);
 
 /* Blocks until all queued work of the scenario finished; reports device
  * faults and non-finite state (when check_nan is nonzero). */

@@ -202,3 +202,34 @@ def test_fault_profile_file_vs_oracle(ctx, wqlmod, oracle_lib, tmp_path):
     s, o = run_pair(wqlmod, oracle_lib, ctx, p, 20)
     for e in field_errors(s, o):
         assert e < TOL
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32c"])
+def test_stage_by_stage_equals_step(ctx, wqlmod, tmp_path, prec):
+    """wql_stage 1..5 advances a step exactly as wql_step does (fields, fault
+    state and frames, bitwise); stages out of order and a step in the middle
+    of one are refused."""
+    p = write(tmp_path, "cart.in", golden_in("test_rup_cart_fric"))
+    precision = wqlmod.FP64 if prec == "fp64" else wqlmod.FP32C
+    a = wqlmod.Scenario(ctx, p, precision=precision)
+    b = wqlmod.Scenario(ctx, p, precision=precision)
+    a.step(3)
+    for _ in range(3):
+        for st in range(1, 6):
+            b.stage(st)
+    for blk in range(2):
+        assert np.array_equal(a.fields(blk), b.fields(blk))
+    for copy in range(2):
+        for what in range(6):
+            assert np.array_equal(a.iface(copy, what), b.iface(copy, what))
+    assert np.array_equal(a.frames("Svel"), b.frames("Svel"))
+    with pytest.raises(wqlmod.WqlError):
+        b.stage(2)
+    b.stage(1)
+    with pytest.raises(wqlmod.WqlError):
+        b.step(1)
+    for st in range(2, 6):
+        b.stage(st)
+    b.step(1)
+    a.close()
+    b.close()

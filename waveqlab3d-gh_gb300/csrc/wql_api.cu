@@ -137,6 +137,12 @@ struct wql_scn {
   int* err_dev = nullptr;  // kernel error word (bounded pipeline waits that ran out)
   FaultParams fp{};
   int bc_form = BC_CHARACTERISTIC;
+  // a step advanced stage by stage (wql_stage): the next stage to run (1:
+  // no step in progress) and the step's context
+  int next_stage = 1;
+  bool want_frame = false, want_station = false;
+  double stage_t0 = 0.0;
+  int stage_launches = 0;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
   int schunk = 0;          // planes per CTA along s (0: default)
   bool plastic = false;
@@ -1207,39 +1213,38 @@ int batch_step(wql_batch* B) {
   return WQL_OK;
 }
 
-int run_step(wql_scn* S) {
-  StepCtx c = step_begin(S);
+// One RK stage of the current step (stages 1..5 in order).
+void run_stage(wql_scn* S, StepCtx& c, int stage) {
   bool pair = false;  // both blocks through the TMA kernel: one stencil launch per stage
   if (S->prec == WQL_FP32C) {
     pair = true;
     for (int b = 0; b < 2; ++b) pair = pair && stencil_is_tma(volume_args<float>(S, b, 0.0, 0.0, false));
   }
+  stage_head(S, c, stage);
   if (pair) {
     // both blocks' pre-kernels, the stencil launch, both blocks'
     // corrections (the blocks touch disjoint arrays)
-    for (int stage = 1; stage <= 5; ++stage) {
-      stage_head(S, c, stage);
-      for (int b = 0; b < 2; ++b) stage_block_pre(S, c, stage, b);
-      const double A = stage_A(S, stage), Bdt = stage_Bdt(S, stage);
-      mark_begin(S, 1);
-      launch_stencil_tma2(volume_args<float>(S, 0, A, Bdt, stage == 5), volume_args<float>(S, 1, A, Bdt, stage == 5),
-                          S->curv, true, S->stream);
-      mark_end(S);
-      c.launches += 1;
-      for (int b = 0; b < 2; ++b) stage_block_post(S, c, stage, b);
-      S->cur ^= 1;
-    }
-    return step_end(S, c);
-  }
-  for (int stage = 1; stage <= 5; ++stage) {
-    stage_head(S, c, stage);
+    for (int b = 0; b < 2; ++b) stage_block_pre(S, c, stage, b);
+    const double A = stage_A(S, stage), Bdt = stage_Bdt(S, stage);
+    mark_begin(S, 1);
+    launch_stencil_tma2(volume_args<float>(S, 0, A, Bdt, stage == 5), volume_args<float>(S, 1, A, Bdt, stage == 5),
+                        S->curv, true, S->stream);
+    mark_end(S);
+    c.launches += 1;
+    for (int b = 0; b < 2; ++b) stage_block_post(S, c, stage, b);
+  } else {
     for (int b = 0; b < 2; ++b) {
       stage_block_pre(S, c, stage, b);
       stage_block_stencil(S, c, stage, b);
       stage_block_post(S, c, stage, b);
     }
-    S->cur ^= 1;
   }
+  S->cur ^= 1;
+}
+
+int run_step(wql_scn* S) {
+  StepCtx c = step_begin(S);
+  for (int stage = 1; stage <= 5; ++stage) run_stage(S, c, stage);
   return step_end(S, c);
 }
 
@@ -1304,9 +1309,40 @@ int wql_scenario_destroy(wql_scn* scn) {
   return WQL_OK;
 }
 
+int wql_stage(wql_scn* scn, int stage) {
+  if (!scn) return fail(WQL_E_INPUT, "null scenario");
+  if (stage != scn->next_stage)
+    return fail(WQL_E_STATE, "stage " + std::to_string(stage) + " requested, stage " +
+                                 std::to_string(scn->next_stage) + " is next");
+  CK(cudaSetDevice(scn->ctx->device));
+  StepCtx c;
+  if (stage == 1) {
+    c = step_begin(scn);
+  } else {
+    c.want_frame = scn->want_frame;
+    c.want_station = scn->want_station;
+    c.t0 = scn->stage_t0;
+    c.launches = scn->stage_launches;
+  }
+  run_stage(scn, c, stage);
+  if (stage < 5) {
+    scn->want_frame = c.want_frame;
+    scn->want_station = c.want_station;
+    scn->stage_t0 = c.t0;
+    scn->stage_launches = c.launches;
+    scn->next_stage = stage + 1;
+    return WQL_OK;
+  }
+  scn->next_stage = 1;
+  const int rc = step_end(scn, c);
+  if (rc) return rc;
+  return flush_frames(scn);
+}
+
 int wql_step(wql_scn* scn, int nsteps) {
   if (!scn) return fail(WQL_E_INPUT, "null scenario");
   if (nsteps < 0) return fail(WQL_E_INPUT, "negative step count");
+  if (scn->next_stage != 1) return fail(WQL_E_STATE, "a step is in progress (wql_stage)");
   CK(cudaSetDevice(scn->ctx->device));
   for (int n = 0; n < nsteps; ++n) {
     int rc = run_step(scn);
@@ -1813,6 +1849,7 @@ int wql_batch_add(wql_batch* b, wql_scn* scn) {
   if (scn->ctx->device != b->ctx->device) return fail(WQL_E_INPUT, "scenario is on another device");
   for (auto* m : b->members)
     if (m == scn) return fail(WQL_E_STATE, "scenario is already in the batch");
+  if (scn->next_stage != 1) return fail(WQL_E_STATE, "the scenario is in the middle of a step (wql_stage)");
   b->members.push_back(scn);
   return WQL_OK;
 }

@@ -28,7 +28,7 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream",
            "wql_estimate_device_bytes", "wql_server_create", "wql_server_submit", "wql_server_wait",
            "wql_server_result", "wql_server_release", "wql_server_stats", "wql_server_destroy",
-           "wql_autotune", "wql_write_outputs", "wql_write_block_grids"]
+           "wql_autotune", "wql_write_outputs", "wql_write_block_grids", "wql_stage"]
 
 
 class Media(ctypes.Structure):
@@ -95,6 +95,7 @@ def lib():
         L.wql_station_index.argtypes = [vp, ci, vp]
         L.wql_get_seismograms.argtypes = [vp, ci, vp]
         L.wql_write_outputs.argtypes = [vp, ctypes.c_char_p]
+        L.wql_stage.argtypes = [vp, ci]
         L.wql_write_block_grids.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         L.wql_get_iface.argtypes = [vp, ci, ci, vp]
         L.wql_frame_count.argtypes = [vp, ctypes.POINTER(ci)]
@@ -222,6 +223,10 @@ class Scenario:
         rec = np.empty(nrec.value * n.value * 4, np.float64)
         _check(lib().wql_get_seismograms(self.h, block, rec.ctypes.data))
         return ijk.reshape(n.value, 3), rec.reshape(nrec.value, n.value, 4)
+
+    def stage(self, stage):
+        """One RK stage (1..5, in order) of the current step (wql_stage)."""
+        _check(lib().wql_stage(self.h, stage))
 
     def write_outputs(self, out_dir):
         """The fault streams and station files so far, in the reference's
