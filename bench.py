@@ -129,6 +129,8 @@ def workload(args):
     import wql_configs
     if args.workload == "config2":
         text, media = wql_configs.config2(steps=10 ** 6, seed=args.seed)
+    elif args.workload == "upwind":
+        text, media = wql_configs.upwind_pml12(steps=10 ** 6)
     else:
         text, media = wql_configs.config1(n=args.n, steps=10 ** 6, seed=args.seed)
     return text, media, wql_configs.updates_per_step(text)
@@ -404,9 +406,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
                     help="step: config 1 (default); batch: config 3 ensemble in one batch; serve: config 4 stream")
-    ap.add_argument("--workload", default="config1", choices=["config1", "config2"],
-                    help="step mode: config1 (2 x n^3 curvilinear, rate and state) or config2 (2 x 401x201x201, "
-                         "PML, von Karman, plasticity)")
+    ap.add_argument("--workload", default="config1", choices=["config1", "config2", "upwind"],
+                    help="step mode: config1 (2 x n^3 curvilinear, rate and state), config2 (2 x 401x201x201, "
+                         "PML, von Karman, plasticity) or upwind (2 x 76x101x151 Cartesian, upwind SBP-6, PML, "
+                         "point source)")
     ap.add_argument("--members", type=int, default=64, help="batch mode: ensemble size")
     ap.add_argument("--requests", type=int, default=32, help="serve mode: number of requests")
     ap.add_argument("--rate", type=float, default=4.0, help="serve mode: Poisson arrival rate (requests/s)")
@@ -421,6 +424,9 @@ def main():
     if args.workload == "config2":
         wl = (f"config2: 2 x 401x201x201 curvilinear blocks, 20-point PML on 5 sides, von Karman medium, "
               f"scec viscoplasticity, TPV26 stress, slip weakening, {ups // 5} grid points")
+    if args.workload == "upwind":
+        wl = (f"upwind: 2 x 76x101x151 Cartesian blocks, upwind SBP-6 operators, 12-point PML on 5 sides, "
+              f"locked interface, one moment-tensor source, {ups // 5} grid points")
 
     if args.impl == "reference":
         if rank != 0:
@@ -478,13 +484,18 @@ def main():
     main_r = res["fp32c"]
     peak, peak_kind = peaks()
     vol_ms, vol_n = main_r["kt"]["stencil"]
-    # one launch per RK stage covers both blocks
+    # one launch per RK stage covers both blocks (the upwind operators: one
+    # per-point launch per block)
     kernel_name = "stencil_kernel_tma2<float,curv,kahan>"
+    mesh = "curv"
+    if args.workload == "upwind":
+        kernel_name, mesh = "stencil_kernel_pointwise<float,cart,kahan,upwind>", "cart"
     pts_per_launch = ups * main_r["kt"]["prof_steps"] / vol_n if vol_n else 0
-    algo = BYTES_PER_UPDATE[("curv", "fp32c")] * pts_per_launch
+    algo = BYTES_PER_UPDATE[(mesh, "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_stencil_tma2_fp32c_curv.json")
+    tpath = os.path.join(ROOT, "profiles", "traffic_stencil_tma2_fp32c_curv.json" if mesh == "curv"
+                         else "traffic_stencil_pointwise_upwind_fp32c_cart.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             t = json.load(f)
@@ -510,7 +521,9 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["fp32c"]["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 fields, Kahan-compensated RK update, f64 fault solve",
-        "data": "synthetic (seeded topography, fault roughness)",
+        "data": {"config1": "synthetic (seeded topography, fault roughness)",
+                 "config2": "synthetic (seeded von Karman medium)",
+                 "upwind": "synthetic (uniform medium, one point source)"}[args.workload],
         "config": {"workload": wl, "precision": "fp32c", "steps_timed": args.steps,
                    "l2": f"inputs larger than L2: {ws_bytes / 2**20:.0f} MiB resident per GPU vs 129 MiB L2",
                    "parallelism": f"{world} independent replica(s), no collective"},
@@ -520,7 +533,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_kind": peak_kind, "kernel": kernel_name,
-                     "bytes_per_update": BYTES_PER_UPDATE[("curv", "fp32c")],
+                     "bytes_per_update": BYTES_PER_UPDATE[(mesh, "fp32c")],
                      "avg_launch_ms": vol_ms / vol_n if vol_n else None,
                      "interface_avg_launch_ms": (main_r["kt"]["interface"][0] / main_r["kt"]["interface"][1])
                      if main_r["kt"]["interface"][1] else None,

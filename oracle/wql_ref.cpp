@@ -374,6 +374,66 @@ int stencil(int i, int n, int* pt, wp* c) {
   return r.n;
 }
 
+// ------------------------------------------------- upwind SBP-6 rows ----
+// fd_type 'upwind', order 6: the velocities are differenced with the forward
+// operator D+ and the stress fluxes with the backward operator D-
+// (src/JU_xJU_yJU_z6.f90:2680-3706 near boundaries, :17675-17983 interior).
+// Left closure rows 1..6, in the reference's summation order (point indices
+// descending); the right closure rows of D+ are the negated mirror images of
+// the left rows of D-, and those of D- of D+ (src/JU_xJU_yJU_z6.f90:2890-3043).
+struct URow {
+  int n;
+  int pt[10];
+  wp c[10];
+};
+const URow UPROW[6] = {  // D+ (src/JU_xJU_yJU_z6.f90:2759-2880, velocity parts)
+    {6, {6, 5, 4, 3, 2, 1}, {0.054021710000147, 0.023993033880123, -0.302855902188632, -0.275607596716317, 2.093702214477299, -1.593253459452621}},
+    {6, {6, 5, 4, 3, 2, 1}, {-0.039560344515975, 0.030739159126096, 0.105980141988699, 0.393228064437077, -0.029551468764759, -0.460835552271137}},
+    {7, {7, 6, 5, 4, 3, 2, 1}, {-0.026915887850467, 0.197069524204597, -0.589452745232692, 1.258766829227482, -0.306540940575249, -0.629259919521358, 0.096333139747688}},
+    {8, {8, 7, 6, 5, 4, 3, 2, 1}, {-0.013345690454124, 0.106765523632994, -0.330443502642251, 0.946962507015985, -0.318292975073623, -0.243684445410829, -0.240558007429252, 0.0925965903611}},
+    {9, {9, 8, 7, 6, 5, 4, 3, 2, 1}, {-0.018365004463716, 0.146920035709731, -0.550950133911491, 1.406282074938901, -0.593528379527062, -0.450132219590077, 0.041897570295664, 0.033485250803205, -0.015609194255155}},
+    {10, {10, 9, 8, 7, 6, 5, 4, 3, 2, 1}, {-0.016424481602299, 0.131395852818395, -0.492734448068983, 1.313958528183954, -0.572337434946968, -0.357460227911152, -0.025427590054054, -0.00533856744421, 0.040531470682718, -0.0161631016574}},
+};
+const URow UMROW[6] = {  // D- (the same lines, stress parts)
+    {6, {6, 5, 4, 3, 2, 1}, {0.05204891554804, 0.044953974933765, -0.366971721882124, -0.189297839436616, 2.039450367044345, -1.58018369620741}},
+    {6, {6, 5, 4, 3, 2, 1}, {-0.029492540133095, -0.021790841692085, 0.215422101432619, 0.279404147185598, 0.029551468764759, -0.473094335557797}},
+    {6, {6, 5, 4, 3, 2, 1}, {0.008748664712219, -0.061405392278187, 0.491468255323896, 0.306540940575249, -0.88560840157053, 0.140255933237354}},
+    {6, {6, 5, 4, 3, 2, 1}, {0.020661154127888, 0.327107204245208, 0.318292975073623, -0.624133691970994, -0.11834612889915, 0.076418487423426}},
+    {7, {7, 6, 5, 4, 3, 2, 1}, {-0.036730008927433, 0.399693508760138, 0.593528379527062, -1.303115093827634, 0.402190050630647, -0.047235828122731, -0.008331008040049}},
+    {8, {8, 7, 6, 5, 4, 3, 2, 1}, {-0.032848963204599, 0.394187558455186, 0.572337434946968, -1.257688453771463, 0.406675342006739, -0.120254802392339, 0.054367610816546, -0.016775726857039}},
+};
+// Interior rows (src/JU_xJU_yJU_z6.f90:2726-2746): D+ on points i-2..i+4,
+// D- on points i-4..i+2, summed from the lowest index upwards.
+const wp UP_CF[7] = {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0};
+const wp UP_CB[7] = {1.0 / 60.0, -2.0 / 15.0, 1.0 / 2.0, -4.0 / 3.0, 7.0 / 12.0, 2.0 / 5.0, -1.0 / 30.0};
+
+// Row of D+ (plus = true) or D- at 1-based index i of n points.
+int stencil_up(bool plus, int i, int n, int* pt, wp* c) {
+  if (i >= 7 && i <= n - 6) {
+    const wp* cc = plus ? UP_CF : UP_CB;
+    const int o0 = plus ? -2 : -4;
+    for (int k = 0; k < 7; ++k) {
+      pt[k] = i + o0 + k;
+      c[k] = cc[k];
+    }
+    return 7;
+  }
+  if (i <= 6) {
+    const URow& r = (plus ? UPROW : UMROW)[i - 1];
+    for (int k = 0; k < r.n; ++k) {
+      pt[k] = r.pt[k];
+      c[k] = r.c[k];
+    }
+    return r.n;
+  }
+  const URow& r = (plus ? UMROW : UPROW)[n - i];
+  for (int k = 0; k < r.n; ++k) {
+    pt[k] = n + 1 - r.pt[k];
+    c[k] = -r.c[k];
+  }
+  return r.n;
+}
+
 // ------------------------------------------------------------- blocks ----
 struct Face {
   vector<wp> n_l[3], n_m[3], n_n[3];
@@ -394,6 +454,7 @@ struct RBlock {
   int npml = 0;
   vector<wp> Q[7][9], DQ[7][9];    // full-size per active side
   wp tau0 = 0;
+  bool upwind = false;  // fd_type 'upwind', order 6
   size_t id(int i, int j, int k) const {
     return (size_t)(i - 1) + (size_t)nq * ((size_t)(j - 1) + (size_t)nr * (size_t)(k - 1));
   }
@@ -1098,7 +1159,9 @@ int init_block(Domain& D, int b, const Media& md) {
         B.Q[s][c].assign(B.np, 0.0);
         B.DQ[s][c].assign(B.np, 0.0);
       }
-  B.tau0 = 1.0 / (0.315949074074074);
+  // src/block.f90:189-214
+  B.upwind = D.P.fd_type == "upwind";
+  B.tau0 = B.upwind ? 42300.0 / 13613.0 : 1.0 / (0.315949074074074);
   return 0;
 }
 
@@ -1126,6 +1189,39 @@ void jju_x6(const RBlock& B, int x, int y, int z, const vector<wp>* Xm, wp Ju[9]
         s = (t == 0) ? term : s + term;
       }
       out[ax][comp] = (comp < 3) ? centre * s : s;
+    }
+  }
+  for (int comp = 0; comp < 9; ++comp)
+    Ju[comp] = (1.0 / B.hq) * Jq[comp] + (1.0 / B.hr) * Jr[comp] + (1.0 / B.hs) * Js[comp];
+}
+
+// JJU_x6_upwind: src/JU_xJU_yJU_z6.f90:2680-3706.  Velocities: centre
+// metric times the D+ row; stresses: the D- row of c*metric*J*sigma.
+void jju_x6_upwind(const RBlock& B, int x, int y, int z, const vector<wp>* Xm, wp Ju[9]) {
+  wp Jq[9], Jr[9], Js[9];
+  int ptp[10], ptm[10];
+  wp cp[10], cm[10];
+  const int dims[3] = {B.nq, B.nr, B.ns};
+  const int pos[3] = {x, y, z};
+  wp* out[3] = {Jq, Jr, Js};
+  for (int ax = 0; ax < 3; ++ax) {
+    const int mp = stencil_up(true, pos[ax], dims[ax], ptp, cp);
+    const int mm = stencil_up(false, pos[ax], dims[ax], ptm, cm);
+    const vector<wp>& Xa = Xm[ax];
+    const wp centre = Xa[B.id(x, y, z)];
+    for (int comp = 0; comp < 9; ++comp) {
+      const bool vel = comp < 3;
+      const int m = vel ? mp : mm;
+      const int* pt = vel ? ptp : ptm;
+      const wp* c = vel ? cp : cm;
+      wp s = 0;
+      for (int t = 0; t < m; ++t) {
+        const int i = ax == 0 ? pt[t] : x, j = ax == 1 ? pt[t] : y, k = ax == 2 ? pt[t] : z;
+        const size_t p = B.id(i, j, k);
+        const wp term = vel ? c[t] * B.F[comp][p] : c[t] * Xa[p] * B.J[p] * B.F[comp][p];
+        s = (t == 0) ? term : s + term;
+      }
+      out[ax][comp] = vel ? centre * s : s;
     }
   }
   for (int comp = 0; comp < 9; ++comp)
@@ -1289,7 +1385,72 @@ void rhs_interior(RBlock& B, bool cart) {
       }
 }
 
-// RHS_near_boundaries (traditional): src/RHS_Interior.f90:133-274
+// JJU_x6_interior_upwind: src/JU_xJU_yJU_z6.f90:17675-17983 (elastic)
+void rhs_interior_upwind(RBlock& B, bool cart) {
+  int ix, iy, iz, fx, fy, fz;
+  interior_limits(B, ix, iy, iz, fx, fy, fz);
+  wp cfx[7], cfy[7], cfz[7], cbx[7], cby[7], cbz[7];
+  for (int k = 0; k < 7; ++k) {
+    cfx[k] = UP_CF[k] / B.hq; cfy[k] = UP_CF[k] / B.hr; cfz[k] = UP_CF[k] / B.hs;
+    cbx[k] = UP_CB[k] / B.hq; cby[k] = UP_CB[k] / B.hr; cbz[k] = UP_CB[k] / B.hs;
+  }
+  const int nx = B.nq, ny = B.nr, nz = B.ns;
+#pragma omp parallel for schedule(static)
+  for (int z = 1; z <= nz; ++z)
+    for (int y = 1; y <= ny; ++y)
+      for (int x = 1; x <= nx; ++x) {
+        if ((iz + 1 > z) || (z > nz - fz) || (iy + 1 > y) || (y > ny - fy) || (ix + 1 > x) || (x > nx - fx))
+          continue;
+        const size_t p = B.id(x, y, z);
+        wp DFx[9] = {0}, DFy[9] = {0}, DFz[9] = {0};
+        for (int s = -2; s <= 4; ++s) {
+          const int k = s + 2;
+          const size_t xf = B.id(x + s, y, z), yf = B.id(x, y + s, z), zf = B.id(x, y, z + s);
+          const size_t xb = B.id(x + s - 2, y, z), yb = B.id(x, y + s - 2, z), zb = B.id(x, y, z + s - 2);
+          if (!cart) {
+            const vector<wp>* Ms[3] = {B.mx, B.my, B.mz};
+            wp* Ds[3] = {DFx, DFy, DFz};
+            for (int a = 0; a < 3; ++a) {
+              const vector<wp>* Mm = Ms[a];
+              wp* D = Ds[a];
+              for (int c = 0; c < 3; ++c)
+                D[c] = D[c] + Mm[0][p] * cfx[k] * B.F[c][xf] + Mm[1][p] * cfy[k] * B.F[c][yf] +
+                       Mm[2][p] * cfz[k] * B.F[c][zf];
+              for (int c = 3; c < 9; ++c)
+                D[c] = D[c] + cbx[k] * B.F[c][xb] * Mm[0][xb] * B.J[xb] + cby[k] * B.F[c][yb] * Mm[1][yb] * B.J[yb] +
+                       cbz[k] * B.F[c][zb] * Mm[2][zb] * B.J[zb];
+            }
+          } else {
+            for (int c = 0; c < 3; ++c) {
+              DFx[c] = DFx[c] + B.mx[0][p] * cfx[k] * B.F[c][xf];
+              DFy[c] = DFy[c] + B.my[1][p] * cfy[k] * B.F[c][yf];
+              DFz[c] = DFz[c] + B.mz[2][p] * cfz[k] * B.F[c][zf];
+            }
+            for (int c = 3; c < 9; ++c) {
+              DFx[c] = DFx[c] + B.mx[0][p] * cbx[k] * B.F[c][xb];
+              DFy[c] = DFy[c] + B.my[1][p] * cby[k] * B.F[c][yb];
+              DFz[c] = DFz[c] + B.mz[2][p] * cbz[k] * B.F[c][zb];
+            }
+          }
+        }
+        wp a1 = cart ? 1.0 / (B.M[2][p]) : 1.0 / (B.M[2][p] * B.J[p]);
+        wp a2 = (2.0 * B.M[1][p] + B.M[0][p]);
+        wp a3 = B.M[0][p];
+        wp a4 = B.M[1][p];
+        B.DF[0][p] = B.DF[0][p] + a1 * (DFx[3] + DFy[6] + DFz[7]);
+        B.DF[1][p] = B.DF[1][p] + a1 * (DFx[6] + DFy[4] + DFz[8]);
+        B.DF[2][p] = B.DF[2][p] + a1 * (DFx[7] + DFy[8] + DFz[5]);
+        B.DF[3][p] = B.DF[3][p] + a2 * DFx[0] + a3 * (DFy[1] + DFz[2]);
+        B.DF[4][p] = B.DF[4][p] + a2 * DFy[1] + a3 * (DFx[0] + DFz[2]);
+        B.DF[5][p] = B.DF[5][p] + a2 * DFz[2] + a3 * (DFx[0] + DFy[1]);
+        B.DF[6][p] = B.DF[6][p] + a4 * (DFy[0] + DFx[1]);
+        B.DF[7][p] = B.DF[7][p] + a4 * (DFz[0] + DFx[2]);
+        B.DF[8][p] = B.DF[8][p] + a4 * (DFz[1] + DFy[2]);
+      }
+}
+
+// RHS_near_boundaries: src/RHS_Interior.f90:133-274 (traditional),
+// 595-662 (upwind, order 6)
 void rhs_near_boundaries(RBlock& B) {
   int ix, iy, iz, fx, fy, fz;
   interior_limits(B, ix, iy, iz, fx, fy, fz);
@@ -1302,9 +1463,15 @@ void rhs_near_boundaries(RBlock& B) {
             ((ix + 1 <= x) && (x <= nx - fx)))
           continue;
         wp Ux[9], Uy[9], Uz[9], DU[9];
-        jju_x6(B, x, y, z, B.mx, Ux);
-        jju_x6(B, x, y, z, B.my, Uy);
-        jju_x6(B, x, y, z, B.mz, Uz);
+        if (B.upwind) {
+          jju_x6_upwind(B, x, y, z, B.mx, Ux);
+          jju_x6_upwind(B, x, y, z, B.my, Uy);
+          jju_x6_upwind(B, x, y, z, B.mz, Uz);
+        } else {
+          jju_x6(B, x, y, z, B.mx, Ux);
+          jju_x6(B, x, y, z, B.my, Uy);
+          jju_x6(B, x, y, z, B.mz, Uz);
+        }
         size_t p = B.id(x, y, z);
         wp rhoJ_inv = 1.0 / (B.M[2][p] * B.J[p]);
         wp lambda2mu = B.M[0][p] + 2.0 * B.M[1][p];
@@ -1892,7 +2059,8 @@ void time_step(Domain& D) {
     }
     // set_rates
     for (int b = 0; b < 2; ++b) {
-      rhs_interior(D.Bk[b], D.cart);
+      if (D.Bk[b].upwind) rhs_interior_upwind(D.Bk[b], D.cart);
+      else rhs_interior(D.Bk[b], D.cart);
       rhs_near_boundaries(D.Bk[b]);
       if (D.P.use_moment_tensor) apply_sources(D, b, D.t);
     }
@@ -1978,6 +2146,21 @@ static char g_err[512];
 
 const char* wqlref_last_error() { return g_err; }
 
+// Dense n x n matrix (row-major, row i = derivative at point i+1, times h)
+// of a first-derivative operator: fd 0 the traditional SBP-6 D, fd 1 the
+// upwind D+ (plus != 0) or D- of order 6.  Returns 0, or -1 for n < 12.
+int wqlref_fd_matrix(int fd, int plus, int n, double* D) {
+  if (n < 12 || !D) return -1;
+  int pt[10];
+  wp c[10];
+  for (size_t k = 0; k < (size_t)n * n; ++k) D[k] = 0.0;
+  for (int i = 1; i <= n; ++i) {
+    const int m = fd ? stencil_up(plus != 0, i, n, pt, c) : stencil(i, n, pt, c);
+    for (int t = 0; t < m; ++t) D[(size_t)(i - 1) * n + (pt[t] - 1)] += c[t];
+  }
+  return 0;
+}
+
 static void* create_domain(Domain* D, const Media& md);
 
 void* wqlref_create(const char* in_path) {
@@ -2023,6 +2206,14 @@ static void* create_domain(Domain* D, const Media& md) {
   D->rs = cp == "rate-and-state_friction";
   D->locked = cp == "locked";
   D->linear = cp == "linear_friction";
+  // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator, or the
+  // upwind operators of order 6 (the other orders and the DRP variants are
+  // not restated)
+  if (!(D->P.fd_type == "traditional" || (D->P.fd_type == "upwind" && D->P.order == 6))) {
+    std::snprintf(g_err, sizeof(g_err), "fd_type %s with order %d is not restated", D->P.fd_type.c_str(), D->P.order);
+    delete D;
+    return nullptr;
+  }
   if (!(D->sw || D->rs || D->locked || D->linear)) {
     std::snprintf(g_err, sizeof(g_err), "invalid coupling condition %s", cp.c_str());
     delete D;

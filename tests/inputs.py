@@ -85,6 +85,9 @@ def case_text(name):
         return problem("TPV101", "rate-and-state_friction", "curvilinear") + block_list()
     if name == "locked":
         return problem("TPV5", "locked") + block_list()
+    if name.startswith("up_"):
+        # the upwind operators of order 6 (fd_type = 'upwind')
+        return case_text(name[3:]).replace(" w_stride = 1,", " w_stride = 1,\n fd_type = 'upwind',\n order = 6,", 1)
     if name in MT_CASES:
         mesh, order, mollify, lists = MT_CASES[name]
         extra = ",\n mollify_source = T" if mollify else ""

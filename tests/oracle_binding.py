@@ -33,6 +33,7 @@ def lib():
         L.wqlref_station_count.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         L.wqlref_station_index.argtypes = [vp, ctypes.c_int, vp]
         L.wqlref_get_seismograms.argtypes = [vp, ctypes.c_int, vp]
+        L.wqlref_fd_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         _LIB = L
     return _LIB
 
@@ -120,3 +121,11 @@ class Oracle:
         out = np.empty(nf * NCOMP[name] * nr * ns, np.float32)
         lib().wqlref_get_frames(self.h, STREAMS.index(name), out.ctypes.data)
         return out.reshape(nf, NCOMP[name], ns, nr)
+
+
+def fd_matrix(fd, plus, n):
+    """Dense n x n first-derivative operator of the oracle (times h): fd 0
+    the traditional SBP-6 D, fd 1 the upwind D+ (plus) or D- of order 6."""
+    D = np.zeros((n, n))
+    assert lib().wqlref_fd_matrix(fd, int(plus), n, D.ctypes.data) == 0
+    return D

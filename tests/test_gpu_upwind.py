@@ -1,0 +1,81 @@
+"""The upwind SBP operators of order 6 (fd_type = 'upwind', order = 6) on the
+GPU against the oracle: FP64 fields to 1e-11 relative L2 (rate and state to
+its solver tolerance), and the FP32-compensated mode against FP64 to 1e-5."""
+import numpy as np
+import pytest
+
+from gpu_helpers import field_errors, rel_l2, rs_close, run_pair
+from inputs import case_text, write
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-11
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import wql_build
+    wql_build.build()
+    import wql
+    c = wql.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def wqlmod():
+    import wql
+    return wql
+
+
+@pytest.mark.parametrize("case,steps", [("up_pml", 40), ("up_pml_curv", 20), ("up_plastic", 46),
+                                        ("up_rs_curv", 20), ("up_mt4", 30), ("up_mt4_curv", 20)])
+def test_upwind_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, steps):
+    p = write(tmp_path, case + ".in", case_text(case))
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, steps)
+    errs = field_errors(s, o)
+    if case.startswith("up_rs"):
+        for b in range(2):
+            assert rs_close(s.fields(b), o.fields(b)), errs
+    else:
+        assert max(errs) < TOL, errs
+    # and the run differs from the traditional operator's
+    t = wqlmod.Scenario(ctx, write(tmp_path, "t.in", case_text(case[3:])))
+    t.step(steps)
+    assert rel_l2(t.fields(0), s.fields(0)) > 1e-6
+
+
+@pytest.mark.parametrize("case,steps", [("up_pml", 40), ("up_pml_curv", 20), ("up_mt4_curv", 20)])
+def test_upwind_fp32c_vs_fp64(ctx, wqlmod, tmp_path, case, steps):
+    p = write(tmp_path, case + ".in", case_text(case))
+    d = wqlmod.Scenario(ctx, p, precision=wqlmod.FP64)
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    d.step(steps)
+    f.step(steps)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), d.fields(b)) < 1e-5
+
+
+def test_upwind_in_batch_equals_alone(ctx, wqlmod, tmp_path):
+    """An upwind scenario stepped in a batch next to a traditional one gives
+    the same fields as stepped alone (its stencil stays outside the packed
+    TMA launch)."""
+    pu = write(tmp_path, "u.in", case_text("up_pml_curv"))
+    pt = write(tmp_path, "t.in", case_text("pml_curv"))
+    alone = wqlmod.Scenario(ctx, pu, precision=wqlmod.FP32C)
+    alone.step(10)
+    a = wqlmod.Scenario(ctx, pu, precision=wqlmod.FP32C)
+    b = wqlmod.Scenario(ctx, pt, precision=wqlmod.FP32C)
+    bt = wqlmod.Batch(ctx)
+    bt.add(a)
+    bt.add(b)
+    bt.step(10)
+    for k in range(2):
+        assert np.array_equal(a.fields(k), alone.fields(k))
+    bt.close()
+
+
+def test_upwind_other_orders_rejected(ctx, wqlmod, tmp_path):
+    p = write(tmp_path, "u5.in", case_text("up_pml").replace("order = 6", "order = 5"))
+    with pytest.raises(Exception, match="order = 6"):
+        wqlmod.Scenario(ctx, p)

@@ -20,6 +20,7 @@
 #include "host/wql_grid.h"
 #include "host/wql_input.h"
 #include "wql_internal.h"
+#include "wql_sbp.cuh"
 
 using namespace wql;
 
@@ -144,6 +145,7 @@ struct wql_scn {
   double stage_t0 = 0.0;
   int stage_launches = 0;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
+  int fd = 0;              // 0: traditional SBP-6; 1: upwind SBP-6 (per-point stencil)
   int schunk = 0;          // planes per CTA along s (0: default)
   bool plastic = false;
   double pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
@@ -506,9 +508,10 @@ int setup_block(wql_scn* S, int b) {
       if ((rc = S->alloc(&B.Q[s], 9 * slab * S->esz))) return rc;
       if ((rc = S->alloc(&B.DQ[s], 9 * slab * S->esz))) return rc;
     }
-    if (S->prec == WQL_FP32C && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
+    if (S->prec == WQL_FP32C && !S->fd && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   }
-  const double tau0 = 1.0 / (0.315949074074074);  // src/block.f90:191
+  // src/block.f90:189-214
+  const double tau0 = S->fd ? kTau0Upwind6 : 1.0 / (0.315949074074074);
   const int dims[3] = {B.nq, B.nr, B.ns};
   for (int d = 0; d < 3; ++d) B.tau_h[d] = tau0 / (1.0 / (double)(dims[d] - 1));
   // depth coordinate for the plastic update
@@ -669,8 +672,12 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
   const Problem& Pr = S->P;
-  if (Pr.fd_type != "traditional")
-    return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' is not supported (6th-order traditional SBP only)");
+  // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator or the
+  // upwind operators of order 6
+  if (Pr.fd_type == "upwind" && Pr.order == 6) S->fd = 1;
+  else if (Pr.fd_type != "traditional")
+    return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' with order " + std::to_string(Pr.order) +
+                                 " is not supported (traditional SBP-6, or upwind with order = 6)");
   if (Pr.response == "anelastic") return fail(WQL_E_INPUT, "response='anelastic' is not supported");
   if (Pr.use_moment_tensor) {
     if (Pr.mt_order != 2 && Pr.mt_order != 4) return fail(WQL_E_INPUT, "moment_list order must be 2 or 4");
@@ -875,6 +882,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.G = (T*)B.G;  // used only when the block's stencil is the TMA kernel
   a.bc_form = S->bc_form;
   a.kernel = S->kernel_variant;
+  a.fd = S->fd;
   a.schunk = S->schunk;
   a.fault_sat = (const T*)S->sat + (long long)b * 9 * B.nr * B.ns;
   a.npml = B.npml;
@@ -892,7 +900,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.err = S->err_dev;
   a.pml_d0 = 6.0 / (2.0 * 1.0) * std::log(1.0 / 1.0e-3);
   B.maps.cur = S->cur;
-  a.tma = &B.maps;
+  a.tma = S->fd ? nullptr : &B.maps;  // the TMA stencil has the central operator only
   return a;
 }
 
@@ -1080,7 +1088,7 @@ struct wql_batch {
 namespace {
 
 bool batch_tma(const wql_scn* S) {
-  return S->prec == WQL_FP32C && (S->kernel_variant == 0 || S->kernel_variant == 5 || S->kernel_variant == 6);
+  return S->prec == WQL_FP32C && !S->fd && (S->kernel_variant == 0 || S->kernel_variant == 5 || S->kernel_variant == 6);
 }
 
 // (Re)builds the packed tables when the membership or a member's tuning
@@ -1669,7 +1677,7 @@ int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
   // results are kept per block shape, mesh and precision
   static std::mutex mu;
   static std::map<std::vector<int>, std::pair<int, int>> cache;
-  std::vector<int> key = {scn->prec, (int)scn->curv};
+  std::vector<int> key = {scn->prec, (int)scn->curv, scn->fd};
   for (int b = 0; b < 2; ++b) {
     key.push_back(scn->B[b].nq);
     key.push_back(scn->B[b].nr);

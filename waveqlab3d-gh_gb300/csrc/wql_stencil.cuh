@@ -22,6 +22,17 @@ __device__ __forceinline__ double sbp_w<double>(int row, int col) { return c_sbp
 template <>
 __device__ __forceinline__ float sbp_w<float>(int row, int col) { return c_sbp_f[row][col]; }
 
+// Upwind SBP-6 closure rows: [0] D+, [1] D-.
+__constant__ double c_up_d[2][6][10] = WQL_UP_TABLE;
+__constant__ float c_up_f[2][6][10] = WQL_UP_TABLE;
+
+template <typename T>
+__device__ __forceinline__ T up_w(int op, int row, int col);
+template <>
+__device__ __forceinline__ double up_w<double>(int op, int row, int col) { return c_up_d[op][row][col]; }
+template <>
+__device__ __forceinline__ float up_w<float>(int op, int row, int col) { return c_up_f[op][row][col]; }
+
 // sigma_{c,j} component index in F: rows x,y,z of the symmetric stress.
 __host__ __device__ constexpr int sig(int c, int j) {
   // sxx=3 syy=4 szz=5 sxy=6 sxz=7 syz=8

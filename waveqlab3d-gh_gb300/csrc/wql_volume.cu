@@ -166,6 +166,135 @@ __device__ void diff_pml_flux(const T* __restrict__ F, const T* __restrict__ coe
 }
 
 
+// ---------------------------------------------------------------------------
+// Upwind SBP-6 (fd 1, src/JU_xJU_yJU_z6.f90:2680-3706, 17675-17983): D+ on
+// the velocities, D- on the fluxes.  Interior D+ weights on offsets -2..4
+// and D- weights on offsets -4..2; the closure rows of both operators cover
+// the same columns, so one load per column serves both.
+#define WQL_UP_CF {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0}
+
+template <typename T, bool CURV>
+__device__ __forceinline__ void diff6_up(const T* __restrict__ F, const T* __restrict__ coef, long long np,
+                                         long long p, int i, int n, long long st, int d, T r[6]) {
+  T t[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) r[c] = T(0);
+  const int kind = sbp_kind(i, n);
+  if (kind == 0) {
+    const T cf[7] = WQL_UP_CF;
+#pragma unroll
+    for (int o = -4; o <= 4; ++o) {
+      load6<T, CURV>(F, coef, np, p + o * st, d, t);
+      if (o >= -2)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += cf[o + 2] * t[c];
+      if (o <= 2)
+#pragma unroll
+        for (int c = 3; c < 6; ++c) r[c] -= cf[2 - o] * t[c];
+    }
+  } else if (kind < 0) {
+    const int row = -kind - 1;
+    const long long p0 = p - (long long)i * st;
+    for (int col = 0; col < 10; ++col) {
+      const T wv = up_w<T>(0, row, col), wf = up_w<T>(1, row, col);
+      if (wv != T(0) || wf != T(0)) {
+        load6<T, CURV>(F, coef, np, p0 + col * st, d, t);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += wv * t[c];
+#pragma unroll
+        for (int c = 3; c < 6; ++c) r[c] += wf * t[c];
+      }
+    }
+  } else {
+    const int row = kind - 1;
+    const long long pn = p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < 10; ++col) {
+      const T wv = -up_w<T>(1, row, col), wf = -up_w<T>(0, row, col);
+      if (wv != T(0) || wf != T(0)) {
+        load6<T, CURV>(F, coef, np, pn - col * st, d, t);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += wv * t[c];
+#pragma unroll
+        for (int c = 3; c < 6; ++c) r[c] += wf * t[c];
+      }
+    }
+  }
+}
+
+// D+ of the three velocities only.
+template <typename T>
+__device__ __forceinline__ void diff_v_up(const T* __restrict__ F, long long np, long long p, int i, int n,
+                                          long long st, T r[3]) {
+  r[0] = r[1] = r[2] = T(0);
+  const int kind = sbp_kind(i, n);
+  if (kind == 0) {
+    const T cf[7] = WQL_UP_CF;
+#pragma unroll
+    for (int o = -2; o <= 4; ++o)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[c] += cf[o + 2] * F[c * np + p + o * st];
+  } else if (kind < 0) {
+    const int row = -kind - 1;
+    const long long p0 = p - (long long)i * st;
+    for (int col = 0; col < 10; ++col) {
+      const T w = up_w<T>(0, row, col);
+      if (w != T(0))
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + p0 + col * st];
+    }
+  } else {
+    const int row = kind - 1;
+    const long long pn = p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < 10; ++col) {
+      const T w = -up_w<T>(1, row, col);
+      if (w != T(0))
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + pn - col * st];
+    }
+  }
+}
+
+// D- of the three fluxes J*metric_j(d)*sigma_{c,j} (PML split, as
+// diff_pml_flux).
+template <typename T>
+__device__ void diff_pml_flux_up(const T* __restrict__ F, const T* __restrict__ coef, long long np, long long p,
+                                 int i, int n, long long st, int d, int j, T r[3]) {
+  r[0] = r[1] = r[2] = T(0);
+  const int kind = sbp_kind(i, n);
+  auto acc = [&](long long q, T w) {
+    const T a = coef[(d * 3 + j) * np + q];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c] += w * (a * F[sig(c, j) * np + q]);
+  };
+  if (kind == 0) {
+    const T cf[7] = WQL_UP_CF;
+    for (int o = -4; o <= 2; ++o) acc(p + o * st, -cf[2 - o]);
+  } else if (kind < 0) {
+    const int row = -kind - 1;
+    const long long p0 = p - (long long)i * st;
+    for (int col = 0; col < 10; ++col) {
+      const T w = up_w<T>(1, row, col);
+      if (w != T(0)) acc(p0 + col * st, w);
+    }
+  } else {
+    const int row = kind - 1;
+    const long long pn = p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < 10; ++col) {
+      const T w = -up_w<T>(0, row, col);
+      if (w != T(0)) acc(pn - col * st, w);
+    }
+  }
+}
+
+// Operator dispatch on the compile-time fd of a kernel.
+template <typename T, bool CURV, int FD>
+__device__ __forceinline__ void diff6_op(const T* __restrict__ F, const T* __restrict__ coef, long long np,
+                                         long long p, int i, int n, long long st, int d, T r[6]) {
+  if (FD) diff6_up<T, CURV>(F, coef, np, p, i, n, st, d, r);
+  else diff6<T, CURV>(F, coef, np, p, i, n, st, d, r);
+}
+
+
 
 // ---------------------------------------------------------------------------
 // Main stencil kernel (2.5-D tiled).  Computes, for every point of the block,
@@ -396,7 +525,7 @@ __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __gr
 // through L1/L2 (kept for cross-checks of the tiled kernel).
 // smode 1 restricts it to the 12 s-boundary planes (grid z = 12), the part
 // the TMA kernel leaves out.
-template <typename T, bool CURV, bool KAHAN>
+template <typename T, bool CURV, bool KAHAN, int FD = 0>
 __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_constant__ VolumeArgs<T> a, int smode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -411,7 +540,7 @@ __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_con
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     T o[6];
-    diff6<T, CURV>(a.Fin, a.coef, np, p, idx[d], nn[d], st[d], d, o);
+    diff6_op<T, CURV, FD>(a.Fin, a.coef, np, p, idx[d], nn[d], st[d], d, o);
     const T rh = a.rh[d];
     if (CURV) {
       T m[3];
@@ -507,7 +636,7 @@ PmlBoxes pml_boxes(const VolumeArgs<T>& a) {
 // FP32 fields: capped at 80 registers for three CTAs per SM (24 warps to
 // hide the latency of its dependent loads; measured 0.39 -> 0.31 ms per
 // correction launch on config 2 despite some spilling).
-template <typename T, bool CURV, bool KAHAN>
+template <typename T, bool CURV, bool KAHAN, int FD>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const __grid_constant__ VolumeArgs<T> a,
                                                                            const __grid_constant__ PmlBoxes bx) {
   // one thread per point of the slab union, enumerated box by box (q
@@ -551,7 +680,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T o[3];
-      diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
+      if (FD) diff_v_up<T>(F, np, p, idx[d], nn[d], st[d], o);
+      else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
       const T rh = a.rh[d];
       for (int c = 0; c < 3; ++c) {
         if (CURV) {
@@ -604,13 +734,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         T r3[3];
-        diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
+        if (FD) diff_pml_flux_up<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
+        else diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
         for (int c = 0; c < 3; ++c) acc3[c] += a.rh[d] * r3[c];
       }
       for (int c = 0; c < 3; ++c) sd[c] = acc3[c] * Jinv;
     } else {
       T o[6];
-      diff6<T, false>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, o);
+      diff6_op<T, false, FD>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, o);
       for (int c = 0; c < 3; ++c) sd[c] = a.cart_metric[axis] * a.rh[axis] * o[3 + c];
     }
     corr[0] -= damp * qv[0] * rhoinv;
@@ -834,6 +965,7 @@ inline bool tiles_ok(int n, int T) { return n <= T + 3 || n >= T + 6; }
 template <typename T>
 int effective_variant(const VolumeArgs<T>& a) {
   constexpr bool f32 = sizeof(T) == 4;
+  if (a.fd) return 1;  // the upwind operators run per point
   int v = a.kernel != 0 ? a.kernel : (f32 ? 5 : 2);
   if ((v == 5 || v == 6) && !f32) v = 2;
   if ((v == 5 || v == 6) && !tiles_ok(a.nr, kTmaTR)) v = 1;
@@ -858,7 +990,8 @@ void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
   switch (v) {
     case 1: {
       dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
-      stencil_kernel_pointwise<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a, 0);
+      if (a.fd) stencil_kernel_pointwise<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a, 0);
+      else stencil_kernel_pointwise<T, CURV, KAHAN, 0><<<grd, blk, 0, s>>>(a, 0);
       return;
     }
     case 3: launch_tiled<T, CURV, KAHAN, 32, 8, f32 ? 3 : 1>(a, s); return;
@@ -880,8 +1013,11 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
   dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
   if (a.npml > 0) {
     const PmlBoxes bx = pml_boxes(a);
-    if (bx.start[bx.n] > 0)
-      pml_kernel<T, CURV, KAHAN><<<(unsigned)((bx.start[bx.n] + 255) / 256), 256, 0, s>>>(a, bx);
+    const unsigned nblk = (unsigned)((bx.start[bx.n] + 255) / 256);
+    if (bx.start[bx.n] > 0) {
+      if (a.fd) pml_kernel<T, CURV, KAHAN, 1><<<nblk, 256, 0, s>>>(a, bx);
+      else pml_kernel<T, CURV, KAHAN, 0><<<nblk, 256, 0, s>>>(a, bx);
+    }
     ++n;
   }
   if (!stencil_is_tma(a)) {
