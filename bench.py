@@ -489,13 +489,13 @@ def main():
     kernel_name = "stencil_kernel_tma2<float,curv,kahan>"
     mesh = "curv"
     if args.workload == "upwind":
-        kernel_name, mesh = "stencil_kernel_pointwise<float,cart,kahan,upwind>", "cart"
+        kernel_name, mesh = "stencil_kernel_tma2<float,cart,kahan,upwind>", "cart"
     pts_per_launch = ups * main_r["kt"]["prof_steps"] / vol_n if vol_n else 0
     algo = BYTES_PER_UPDATE[(mesh, "fp32c")] * pts_per_launch
     achieved = algo / (vol_ms / vol_n * 1e-3) / 1e9 if vol_n else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_stencil_tma2_fp32c_curv.json" if mesh == "curv"
-                         else "traffic_stencil_pointwise_upwind_fp32c_cart.json")
+                         else "traffic_stencil_tma2_upwind_fp32c_cart.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             t = json.load(f)

@@ -67,7 +67,9 @@ int wql_ctx_destroy(wql_ctx* ctx);
 /* Build a scenario from a reference `.in` file: init_domain
  * (src/domain.f90:31-564) -- namelists, grids, metrics, materials, normals,
  * boundary codes, PML slabs, interface state (src/Interface_Condition.f90:
- * 2722-2850).  precision is WQL_FP64 or WQL_FP32C. */
+ * 2722-2850).  precision is WQL_FP64 or WQL_FP32C.  The difference operator
+ * follows &problem_list fd_type (src/RHS_Interior.f90:31-125): 'traditional'
+ * (SBP-6) or 'upwind' with order = 6; other operators return WQL_E_INPUT. */
 int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision, wql_scn** out);
 
 /* Same, from the text of a `.in` file (relative paths resolve against

@@ -56,10 +56,39 @@ def test_upwind_fp32c_vs_fp64(ctx, wqlmod, tmp_path, case, steps):
         assert rel_l2(f.fields(b), d.fields(b)) < 1e-5
 
 
+def _mt_text(n, mesh):
+    from inputs import MT_CASES, block_list, problem
+    _, order, _, lists = MT_CASES["mt4"]
+    t = (problem("TPV5", "locked", mesh) + block_list(n) +
+         f"&moment_list\n use_moment_tensor = T,\n order = {order} /\n" + lists)
+    return t.replace(" w_stride = 1,", " w_stride = 1,\n fd_type = 'upwind',\n order = 6,", 1)
+
+
+@pytest.mark.parametrize("case,steps", [("up_pml", 40), ("up_pml_curv", 20), ("n16_cartesian", 30),
+                                        ("n16_curvilinear", 20), ("n17_curvilinear", 20)])
+def test_upwind_tma_vs_pointwise(ctx, wqlmod, tmp_path, case, steps):
+    """FP32C: the TMA kernel with the upwind pair (its PML gradient handed to
+    the PML kernel) against the per-point kernel.  n = 16 puts the last r
+    tile at 4, so it owns left closure rows read from its 4-row halo; n = 17
+    (last tile at 5) runs per point in both."""
+    text = case_text(case) if case.startswith("up_") else _mt_text(int(case[1:3]), case[4:])
+    p = write(tmp_path, case + ".in", text)
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    g = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    g.set_tuning(1, 0)
+    d = wqlmod.Scenario(ctx, p, precision=wqlmod.FP64)
+    for s in (f, g, d):
+        s.step(steps)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), g.fields(b)) < 1e-6
+        assert rel_l2(f.fields(b), d.fields(b)) < 1e-5
+
+
 def test_upwind_in_batch_equals_alone(ctx, wqlmod, tmp_path):
     """An upwind scenario stepped in a batch next to a traditional one gives
     the same fields as stepped alone (its stencil stays outside the packed
-    TMA launch)."""
+    launch, which runs the central operator)."""
     pu = write(tmp_path, "u.in", case_text("up_pml_curv"))
     pt = write(tmp_path, "t.in", case_text("pml_curv"))
     alone = wqlmod.Scenario(ctx, pu, precision=wqlmod.FP32C)

@@ -145,7 +145,7 @@ struct wql_scn {
   double stage_t0 = 0.0;
   int stage_launches = 0;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
-  int fd = 0;              // 0: traditional SBP-6; 1: upwind SBP-6 (per-point stencil)
+  int fd = 0;              // 0: traditional SBP-6; 1: upwind SBP-6
   int schunk = 0;          // planes per CTA along s (0: default)
   bool plastic = false;
   double pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
@@ -486,7 +486,7 @@ int setup_block(wql_scn* S, int b) {
   if ((rc = S->alloc(&B.DF, 9 * B.np * S->esz))) return rc;
   if (S->prec == WQL_FP32C) {
     if ((rc = S->alloc(&B.C, 9 * B.np * S->esz))) return rc;
-    const int erc = make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, S->curv);
+    const int erc = make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, S->curv, S->fd);
     if (erc) return fail(WQL_E_CUDA, "cuTensorMapEncodeTiled failed for the stencil maps (error " + std::to_string(erc) + ")");
   }
   // boundary codes (src/BoundaryConditions.f90:15-48) and PML slabs (src/block.f90:163-178)
@@ -508,7 +508,7 @@ int setup_block(wql_scn* S, int b) {
       if ((rc = S->alloc(&B.Q[s], 9 * slab * S->esz))) return rc;
       if ((rc = S->alloc(&B.DQ[s], 9 * slab * S->esz))) return rc;
     }
-    if (S->prec == WQL_FP32C && !S->fd && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
+    if (S->prec == WQL_FP32C && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   }
   // src/block.f90:189-214
   const double tau0 = S->fd ? kTau0Upwind6 : 1.0 / (0.315949074074074);
@@ -900,7 +900,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.err = S->err_dev;
   a.pml_d0 = 6.0 / (2.0 * 1.0) * std::log(1.0 / 1.0e-3);
   B.maps.cur = S->cur;
-  a.tma = S->fd ? nullptr : &B.maps;  // the TMA stencil has the central operator only
+  a.tma = &B.maps;
   return a;
 }
 
@@ -1742,7 +1742,7 @@ int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
             StencilMaps m = scn->B[b].maps;
             void* Fs[2] = {scn->B[b].F[0], scn->B[b].F[1]};
             if (make_stencil_maps(m, Fs, scn->B[b].coef, scratch[b][0], scratch[b][1], scn->B[b].nq, scn->B[b].nr,
-                                  scn->B[b].ns, scn->B[b].pq, scn->curv)) {
+                                  scn->B[b].ns, scn->B[b].pq, scn->curv, scn->fd)) {
               rc = fail(WQL_E_CUDA, "autotune tensor maps");
               return;
             }

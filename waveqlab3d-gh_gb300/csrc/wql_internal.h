@@ -128,12 +128,16 @@ struct StencilMaps {
   CUtensorMap fbox[2], flead[2];  // per field buffer
   CUtensorMap ca, cb, cc, cl;     // coefficients: q-halo rows, r-halo columns, tile, lead plane
   CUtensorMap df, ck;             // rates and compensation on the tile
+  CUtensorMap flead2[2];          // upwind pair: the stress lead tile (else = flead)
   int cur;                        // which field buffer is the stage input
+  int fd;                         // operator the boxes are shaped for (0 central, 1 upwind)
   int ok;
 };
-// Fills m for a block; returns 0 or a CUDA driver error code.
+// Fills m for a block (fd: 0 the central SBP-6 operator, 1 the upwind pair:
+// r halo of 4 rows, velocity and stress lead tiles from different planes);
+// returns 0 or a CUDA driver error code.
 int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
-                      bool curv);
+                      bool curv, int fd);
 // Launches the TMA stencil kernel (every plane of the block).
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream);
 // The same for both blocks of a scenario in one launch.
@@ -148,7 +152,7 @@ bool stencil_is_tma(const VolumeArgs<T>& a);
 // at one stage (its tensor maps for the stage's input buffer, its arguments)
 // and the range of CTAs [cta0, cta0 + tq*tr*nchunk) that work on it.
 struct TmaBatchDesc {
-  CUtensorMap m[8];  // field box, lead fields, coefficient boxes (q, r, tile, lead), DF, C
+  CUtensorMap m[9];  // field box, lead fields, coefficient boxes (q, r, tile, lead), DF, C, stress lead
   VolumeArgs<float> a;
   int schunk, tq, tr, nchunk;
   long long cta0;

@@ -62,6 +62,29 @@ __device__ __forceinline__ void row_entry(int kind, int t, T& w, int& off) {
   }
 }
 
+// Closure entry t (0..9) of the upwind pair at a closure row (kind as
+// sbp_kind, nonzero): the D+ weight wv (velocities), the D- weight wf
+// (fluxes) and the offset from the point.  Left rows read points 0..9,
+// right rows the mirror images; the right rows of D+ are the negated left
+// rows of D- and the other way round.
+template <typename T>
+__device__ __forceinline__ void up_entry(int kind, int t, T& wv, T& wf, int& off) {
+  if (kind < 0) {
+    const int i = -kind - 1;
+    wv = up_w<T>(0, i, t);
+    wf = up_w<T>(1, i, t);
+    off = t - i;
+  } else {
+    const int k = kind - 1;
+    wv = -up_w<T>(1, k, t);
+    wf = -up_w<T>(0, k, t);
+    off = k - t;
+  }
+}
+
+// Interior weights of D+ on offsets -2..4 (D- at offset o is -UP_CF[2-o]).
+#define WQL_UP_CF {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0}
+
 struct TileSpan {
   int origin, own_lo, own_hi;
 };

@@ -51,16 +51,18 @@
 namespace wql {
 namespace {
 
-template <bool CURV, bool KAHAN>
+template <bool CURV, bool KAHAN, int FD>
 struct TmaTile {
   static constexpr int TQ = kTmaTQ, TR = kTmaTR, NC = TQ * TR;
-  static constexpr int BQ = TQ + 16, BR = TR + 6;  // field box: q from q0-8, r from r0-3
+  // r halo: 3 rows for the central operator, 4 for the upwind pair
+  static constexpr int HR = FD ? 4 : 3;
+  static constexpr int BQ = TQ + 16, BR = TR + 2 * HR;  // field box: q from q0-8, r from r0-HR
   static constexpr int NCC = CURV ? 7 : 3;         // tile coefficients: 6..12 or lambda, mu, 1/rho
   static constexpr int F_W = 9 * BR * BQ;
   static constexpr int CA_W = CURV ? 3 * TR * BQ : 0;
   static constexpr int CB_W = CURV ? 3 * BR * TQ : 0;
   static constexpr int CC_W = NCC * NC;
-  static constexpr int LF_W = 9 * NC;
+  static constexpr int LF_W = 9 * NC;  // lead fields (FD 1: velocities of s+4, then stresses of s+2)
   static constexpr int LC_W = CURV ? 3 * NC : 0;
   static constexpr int DF_W = 9 * NC;            // rates of the main plane
   static constexpr int CK_W = KAHAN ? 9 * NC : 0;  // compensation of the main plane
@@ -131,15 +133,20 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 // 0..5 and ns-6..ns-1), read from global memory: the s window in registers
 // holds only the 7 planes of a central row.  Inlined: as a call, its
 // argument passing put values on the stack and made the caller spill.
-template <bool CURV>
+template <bool CURV, int FD>
 __device__ __forceinline__ void s_closure(const VolumeArgs<float>& a, long long p, int s, int ks, float o[6]) {
   const long long np = a.np, st = (long long)a.pq * a.nr;
   float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // in registers; o is written once
 #pragma unroll 3
-  for (int e = 0; e < 9; ++e) {
-    float w;
+  for (int e = 0; e < (FD ? 10 : 9); ++e) {
+    float w, wf;
     int off;
-    row_entry<float>(ks, e, w, off);
+    if (FD) {
+      up_entry<float>(ks, e, w, wf, off);
+    } else {
+      row_entry<float>(ks, e, w, off);
+      wf = w;
+    }
     const long long pp = p + off * st;
     float x[6];
     const float* F = a.Fin;
@@ -155,14 +162,16 @@ __device__ __forceinline__ void s_closure(const VolumeArgs<float>& a, long long 
       for (int c = 0; c < 3; ++c) x[3 + c] = F[sig(c, 2) * np + pp];
     }
 #pragma unroll
-    for (int c = 0; c < 6; ++c) acc[c] += w * x[c];
+    for (int c = 0; c < 3; ++c) acc[c] += w * x[c];
+#pragma unroll
+    for (int c = 3; c < 6; ++c) acc[c] += wf * x[c];
   }
 #pragma unroll
   for (int c = 0; c < 6; ++c) o[c] = acc[c];
 }
 
 struct MapArgs {
-  CUtensorMap fbox, flead, ca, cb, cc, cl, df, ck;
+  CUtensorMap fbox, flead, ca, cb, cc, cl, df, ck, flead2;
 };
 
 // The work of one CTA: tile (bx, by) of the block, s chunk bz.
@@ -170,11 +179,11 @@ struct MapArgs {
 // the CTA has used before this tile (the same count in every thread), so a
 // persistent CTA keeps its mbarriers and the producer runs ahead into the
 // next tile.  Returns false after a wait ran out (the error word is set).
-template <bool CURV, bool KAHAN, int NS>
+template <bool CURV, bool KAHAN, int NS, int FD>
 __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapArgs& m, int schunk, int bx, int by,
                                          int bz, int& tb) {
-  using TL = TmaTile<CURV, KAHAN>;
-  constexpr int TQ = TL::TQ, TR = TL::TR, NC = TL::NC, BQ = TL::BQ, BR = TL::BR;
+  using TL = TmaTile<CURV, KAHAN, FD>;
+  constexpr int TQ = TL::TQ, TR = TL::TR, NC = TL::NC, BQ = TL::BQ, BR = TL::BR, HR = TL::HR;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   // 128-byte aligned start, derived from the shared array itself so the
   // compiler keeps every access in the shared address space
@@ -205,14 +214,20 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
         const int sp = s_begin + t;  // main plane
         mbar_expect_tx(&full[st], TL::LEAD_BYTES + TL::MAIN_BYTES);
         float* S = sm + st * TL::STAGE_W;
-        tma_load_4d(S + TL::OFF_LF, &m.flead, &full[st], q0, r0, sp + 3, 0);
-        if (CURV) tma_load_4d(S + TL::OFF_LC, &m.cl, &full[st], q0, r0, sp + 3, 6);
-        tma_load_4d(S + TL::OFF_F, &m.fbox, &full[st], q0 - 8, r0 - 3, sp, 0);
+        if (FD) {  // velocities of plane s+4, stresses and J*metric_s of plane s+2
+          tma_load_4d(S + TL::OFF_LF, &m.flead, &full[st], q0, r0, sp + 4, 0);
+          tma_load_4d(S + TL::OFF_LF + 3 * NC, &m.flead2, &full[st], q0, r0, sp + 2, 3);
+          if (CURV) tma_load_4d(S + TL::OFF_LC, &m.cl, &full[st], q0, r0, sp + 2, 6);
+        } else {
+          tma_load_4d(S + TL::OFF_LF, &m.flead, &full[st], q0, r0, sp + 3, 0);
+          if (CURV) tma_load_4d(S + TL::OFF_LC, &m.cl, &full[st], q0, r0, sp + 3, 6);
+        }
+        tma_load_4d(S + TL::OFF_F, &m.fbox, &full[st], q0 - 8, r0 - HR, sp, 0);
         tma_load_4d(S + TL::OFF_DF, &m.df, &full[st], q0, r0, sp, 0);
         if (KAHAN) tma_load_4d(S + TL::OFF_CK, &m.ck, &full[st], q0, r0, sp, 0);
         if (CURV) {
           tma_load_4d(S + TL::OFF_CA, &m.ca, &full[st], q0 - 8, r0, sp, 0);
-          tma_load_4d(S + TL::OFF_CB, &m.cb, &full[st], q0, r0 - 3, sp, 3);
+          tma_load_4d(S + TL::OFF_CB, &m.cb, &full[st], q0, r0 - HR, sp, 3);
           tma_load_4d(S + TL::OFF_CC, &m.cc, &full[st], q0, r0, sp, 6);
         } else {
           tma_load_4d(S + TL::OFF_CC, &m.cc, &full[st], q0, r0, sp, 0);
@@ -235,23 +250,30 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
   const long long np = a.np;
   const long long sts = (long long)a.pq * nr;
   const long long col = q + (long long)a.pq * r;
-  const int lq = tx + 8, lr = ty + 3;
+  const int lq = tx + 8, lr = ty + HR;
   const float c1 = float(kC1), c2 = float(kC2), c3 = float(kC3);
+  const float cf[7] = WQL_UP_CF;
 
-  float qv[7][6];  // velocities and s-face flux, planes s-3..s+3
-  // the window's first six planes (s_begin-3 .. s_begin+2) straight from
-  // global memory, all loads in flight at once; planes outside the block
-  // stay zero (only central rows read the window)
+  // s window: velocities of planes s-3..s+3 and the s-face flux of the same
+  // planes (central operator), or velocities of s-2..s+4 and fluxes of
+  // s-4..s+2 (upwind pair: the planes D+ and D- read)
+  float qv[7][6];
+  // the window's first six entries straight from global memory, all loads
+  // in flight at once; planes outside the block stay zero (only central
+  // rows read the window)
 #pragma unroll
   for (int i = 0; i < 7; ++i) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) qv[i][c] = 0.0f;
-    const int pl = s_begin - 3 + i;
-    if (i < 6 && pl >= 0 && pl < ns && q < nq && r < nr) {
-      const long long pp = col + sts * pl;
-      const float* F = a.Fin;
+    const int plv = s_begin + (FD ? -2 : -3) + i, pl = s_begin + (FD ? -4 : -3) + i;
+    const float* F = a.Fin;
+    if (i < 6 && plv >= 0 && plv < ns && q < nq && r < nr) {
+      const long long pp = col + sts * plv;
 #pragma unroll
       for (int c = 0; c < 3; ++c) qv[i][c] = F[c * np + pp];
+    }
+    if (i < 6 && pl >= 0 && pl < ns && q < nq && r < nr) {
+      const long long pp = col + sts * pl;
       if (CURV) {
         const float a0 = a.coef[6 * np + pp], a1 = a.coef[7 * np + pp], a2 = a.coef[8 * np + pp];
 #pragma unroll
@@ -276,7 +298,7 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       return false;
     }
     const float* S = sm + st * TL::STAGE_W;
-    // push the lead plane s+3 into the s window
+    // push the lead plane(s) into the s window
     {
       const float* LF = S + TL::OFF_LF;
       const int li = ty * TQ + tx;
@@ -311,7 +333,7 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       auto qflux = [&](int row, int l, float m[3]) {
         float sg[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sg[c] = fb(3 + c, row + 3, l);
+        for (int c = 0; c < 6; ++c) sg[c] = fb(3 + c, row + HR, l);
 #pragma unroll
         for (int j = 0; j < 3; ++j) m[j] = CA[(j * TR + row) * BQ + l];
 #pragma unroll
@@ -332,7 +354,7 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       rflux(lr, tx, mr);
       float tmp[3];
       if (tx < 16) qflux(ty, tx < 8 ? tx : tx + TQ, tmp);     // q halo: 8 columns each side
-      if (ty < 6) rflux(ty < 3 ? ty : ty + TR, tx, tmp);      // r halo: 3 rows each side
+      if (ty < 2 * HR) rflux(ty < HR ? ty : ty + TR, tx, tmp);  // r halo: HR rows each side
       // a warp forms every q flux of its own row (the q derivative needs
       // only those: warp sync); the r fluxes of other rows come from other
       // warps: every consumer thread arrives here and waits (bounded) just
@@ -366,7 +388,17 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
         }
         float o[6];
         if (d == 2) {
-          if (ks == 0) {
+          if (ks == 0 && FD) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) o[c] = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 7; ++i) {
+#pragma unroll
+              for (int c = 0; c < 3; ++c) o[c] += cf[i] * qv[i][c];
+#pragma unroll
+              for (int c = 3; c < 6; ++c) o[c] -= cf[6 - i] * qv[i][c];
+            }
+          } else if (ks == 0) {
 #pragma unroll
             for (int c = 0; c < 6; ++c)
               o[c] = c1 * (qv[4][c] - qv[2][c]) + c2 * (qv[5][c] - qv[1][c]) + c3 * (qv[6][c] - qv[0][c]);
@@ -374,14 +406,29 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
             // a separate array: only it goes through memory for the call,
             // o stays in registers
             float os[6];
-            s_closure<CURV>(a, p, s, ks, os);
+            s_closure<CURV, FD>(a, p, s, ks, os);
 #pragma unroll
             for (int c = 0; c < 6; ++c) o[c] = os[c];
           }
         } else {
           const int kind = d == 0 ? kq : kr;
           const int l0 = d == 0 ? lq : lr;
-          if (kind == 0) {
+          if (kind == 0 && FD) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) o[c] = 0.0f;
+#pragma unroll
+            for (int of = -4; of <= 4; ++of) {
+              float x[6];
+              if (d == 0) qvals(l0 + of, x);
+              else rvals(l0 + of, x);
+              if (of >= -2)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) o[c] += cf[of + 2] * x[c];
+              if (of <= 2)
+#pragma unroll
+                for (int c = 3; c < 6; ++c) o[c] -= cf[2 - of] * x[c];
+            }
+          } else if (kind == 0) {
             float xp[6], xm[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) o[c] = 0.0f;
@@ -402,15 +449,22 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
 #pragma unroll
             for (int c = 0; c < 6; ++c) o[c] = 0.0f;
 #pragma unroll 1
-            for (int e = 0; e < 9; ++e) {
-              float w;
+            for (int e = 0; e < (FD ? 10 : 9); ++e) {
+              float w, wf;
               int off;
-              row_entry<float>(kind, e, w, off);
+              if (FD) {
+                up_entry<float>(kind, e, w, wf, off);
+              } else {
+                row_entry<float>(kind, e, w, off);
+                wf = w;
+              }
               float x[6];
               if (d == 0) qvals(l0 + off, x);
               else rvals(l0 + off, x);
 #pragma unroll
-              for (int c = 0; c < 6; ++c) o[c] += w * x[c];
+              for (int c = 0; c < 3; ++c) o[c] += w * x[c];
+#pragma unroll
+              for (int c = 3; c < 6; ++c) o[c] += wf * x[c];
             }
           }
         }
@@ -496,12 +550,12 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
 }
 
 // Shared-memory ring of a persistent CTA: NS stages then the mbarriers.
-template <bool CURV, bool KAHAN, int NS>
+template <bool CURV, bool KAHAN, int NS, int FD>
 struct Ring {
   float* sm;
   uint64_t *full, *empty, *fluxbar;
   __device__ Ring() {
-    using TL = TmaTile<CURV, KAHAN>;
+    using TL = TmaTile<CURV, KAHAN, FD>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     sm = reinterpret_cast<float*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
     full = reinterpret_cast<uint64_t*>(sm + NS * TL::STAGE_W);
@@ -510,7 +564,7 @@ struct Ring {
   }
   // one thread initialises the barriers once per CTA
   __device__ void init() {
-    using TL = TmaTile<CURV, KAHAN>;
+    using TL = TmaTile<CURV, KAHAN, FD>;
     if (threadIdx.x == 0) {
       for (int i = 0; i < NS; ++i) {
         mbar_init(&full[i], 1);
@@ -524,7 +578,7 @@ struct Ring {
   // the producer's copies of the last stages land before the CTA leaves
   // (tb = stages issued)
   __device__ void drain(int tb) {
-    if (threadIdx.x == TmaTile<CURV, KAHAN>::NC)
+    if (threadIdx.x == TmaTile<CURV, KAHAN, FD>::NC)
       for (int T = max(0, tb - NS); T < tb; ++T) mbar_wait(&full[T % NS], (T / NS) & 1);
   }
 };
@@ -532,15 +586,15 @@ struct Ring {
 // Each CTA takes tiles w = blockIdx.x, blockIdx.x + gridDim.x, ... of the
 // tq x tr x nchunk tiles of the block (q fastest, so neighbouring CTAs share
 // halos in L2); with one CTA per tile that is one tile each.
-template <bool CURV, bool KAHAN, int NS>
+template <bool CURV, bool KAHAN, int NS, int FD>
 __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
     stencil_kernel_tma(const __grid_constant__ VolumeArgs<float> a, const __grid_constant__ MapArgs m, int schunk,
                        int tq, int tr, int ntile) {
-  Ring<CURV, KAHAN, NS> ring;
+  Ring<CURV, KAHAN, NS, FD> ring;
   ring.init();
   int tb = 0;
   for (int w = blockIdx.x; w < ntile; w += gridDim.x)
-    if (!tma_body<CURV, KAHAN, NS>(a, m, schunk, w % tq, (w / tq) % tr, w / (tq * tr), tb)) break;
+    if (!tma_body<CURV, KAHAN, NS, FD>(a, m, schunk, w % tq, (w / tq) % tr, w / (tq * tr), tb)) break;
   ring.drain(tb);
 }
 
@@ -553,7 +607,7 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
   // the entry's arguments are copied to shared memory: read from there they
   // cost no registers across the plane loop (held in registers they spill)
   __shared__ VolumeArgs<float> sa;
-  Ring<CURV, KAHAN, NS> ring;
+  Ring<CURV, KAHAN, NS, 0> ring;
   const long long cta = blockIdx.x;
   int lo = 0, hi = nd - 1;
   while (lo < hi) {
@@ -570,12 +624,12 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
   // the table was written by a host copy: order that write before the
   // tensor-map proxy reads the entry's maps (in the thread that issues copies)
   if (threadIdx.x == kTmaTQ * kTmaTR)
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < 9; ++i)
       asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(&D.m[i]) : "memory");
   ring.init();  // its barrier also publishes sa
   int tb = 0;
   const long long l = cta - D.cta0;
-  tma_body<CURV, KAHAN, NS>(sa, *reinterpret_cast<const MapArgs*>(&D.m), D.schunk, (int)(l % D.tq),
+  tma_body<CURV, KAHAN, NS, 0>(sa, *reinterpret_cast<const MapArgs*>(&D.m), D.schunk, (int)(l % D.tq),
                             (int)((l / D.tq) % D.tr), (int)(l / ((long long)D.tq * D.tr)), tb);
   ring.drain(tb);
 }
@@ -591,19 +645,19 @@ struct TwoBlocks {
   int ntile0;
 };
 
-template <bool CURV, bool KAHAN, int NS>
+template <bool CURV, bool KAHAN, int NS, int FD>
 __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
     stencil_kernel_tma2(const __grid_constant__ TwoBlocks P) {
-  Ring<CURV, KAHAN, NS> ring;
+  Ring<CURV, KAHAN, NS, FD> ring;
   ring.init();
   int tb = 0;
   const int w = blockIdx.x;
   if (w < P.ntile0) {
-    tma_body<CURV, KAHAN, NS>(P.a[0], P.m[0], P.schunk[0], w % P.tq[0], (w / P.tq[0]) % P.tr[0],
+    tma_body<CURV, KAHAN, NS, FD>(P.a[0], P.m[0], P.schunk[0], w % P.tq[0], (w / P.tq[0]) % P.tr[0],
                               w / (P.tq[0] * P.tr[0]), tb);
   } else {
     const int l = w - P.ntile0;
-    tma_body<CURV, KAHAN, NS>(P.a[1], P.m[1], P.schunk[1], l % P.tq[1], (l / P.tq[1]) % P.tr[1],
+    tma_body<CURV, KAHAN, NS, FD>(P.a[1], P.m[1], P.schunk[1], l % P.tq[1], (l / P.tq[1]) % P.tr[1],
                               l / (P.tq[1] * P.tr[1]), tb);
   }
   ring.drain(tb);
@@ -629,15 +683,18 @@ MapArgs stage_maps(const StencilMaps& sm) {
   m.cl = sm.cl;
   m.df = sm.df;
   m.ck = sm.ck;
+  m.flead2 = sm.flead2[sm.cur];
   return m;
 }
 
-template <bool CURV, bool KAHAN>
+template <bool CURV, bool KAHAN, int FD>
 constexpr size_t tma_smem_bytes(int NS) {
-  return sizeof(float) * (size_t)NS * TmaTile<CURV, KAHAN>::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
+  return sizeof(float) * (size_t)NS * TmaTile<CURV, KAHAN, FD>::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
 }
-static_assert(tma_smem_bytes<true, true>(kTmaStages) <= 227 * 1024 &&
-                  tma_smem_bytes<false, true>(kTmaStages) <= 227 * 1024,
+static_assert(tma_smem_bytes<true, true, 0>(kTmaStages) <= 227 * 1024 &&
+                  tma_smem_bytes<false, true, 0>(kTmaStages) <= 227 * 1024 &&
+                  tma_smem_bytes<true, true, 1>(kTmaStages) <= 227 * 1024 &&
+                  tma_smem_bytes<false, true, 1>(kTmaStages) <= 227 * 1024,
               "the stage ring must fit in the shared memory of one CTA");
 
 template <typename K>
@@ -652,10 +709,10 @@ size_t prepare(K kern, int NS, int stage_words) {
 // tiles statically interleaved that measured slower on 2 x 201^3 blocks
 // (0.54 ms against 0.50 ms per launch): the chunks holding the s closure
 // rows take longer, and the hardware's dynamic CTA scheduling balances them.
-template <bool CURV, bool KAHAN, int NS>
+template <bool CURV, bool KAHAN, int NS, int FD>
 void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t s) {
-  using TL = TmaTile<CURV, KAHAN>;
-  auto kern = stencil_kernel_tma<CURV, KAHAN, NS>;
+  using TL = TmaTile<CURV, KAHAN, FD>;
+  auto kern = stencil_kernel_tma<CURV, KAHAN, NS, FD>;
   static const size_t smem = prepare(kern, NS, TL::STAGE_W);
   const int tq = (a.nq + TL::TQ - 1) / TL::TQ, tr = (a.nr + TL::TR - 1) / TL::TR;
   const int schunk = chunk_planes(a);
@@ -663,10 +720,10 @@ void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t 
   kern<<<ntile, TL::NC + 32, smem, s>>>(a, stage_maps(sm), schunk, tq, tr, ntile);
 }
 
-template <bool CURV, bool KAHAN, int NS>
+template <bool CURV, bool KAHAN, int NS, int FD>
 void launch_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, cudaStream_t s) {
-  using TL = TmaTile<CURV, KAHAN>;
-  auto kern = stencil_kernel_tma2<CURV, KAHAN, NS>;
+  using TL = TmaTile<CURV, KAHAN, FD>;
+  auto kern = stencil_kernel_tma2<CURV, KAHAN, NS, FD>;
   static const size_t smem = prepare(kern, NS, TL::STAGE_W);
   TwoBlocks P;
   const VolumeArgs<float>* a[2] = {&a0, &a1};
@@ -685,7 +742,7 @@ void launch_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, cudaS
 
 template <bool CURV, bool KAHAN, int NS>
 void launch_tma_batch(const TmaBatchDesc* d, int nd, long long total, cudaStream_t s) {
-  using TL = TmaTile<CURV, KAHAN>;
+  using TL = TmaTile<CURV, KAHAN, 0>;
   auto kern = stencil_kernel_tma_batch<CURV, KAHAN, NS>;
   static const size_t smem = prepare(kern, NS, TL::STAGE_W);
   if (total <= 0) return;
@@ -727,20 +784,26 @@ int encode4(CUtensorMap* map, void* base, int nq, int nr, int ns, int ncomp, int
 }  // namespace
 
 int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
-                      bool curv) {
+                      bool curv, int fd) {
   constexpr int TQ = kTmaTQ, TR = kTmaTR;
+  const int hr = fd ? 4 : 3;  // r halo rows
   int rc = 0;
   m.ok = 0;
   m.cur = 0;
+  m.fd = fd;
   for (int i = 0; i < 2 && !rc; ++i) {
-    rc = encode4(&m.fbox[i], F[i], nq, nr, ns, 9, pq, TQ + 16, TR + 6, 9);
-    if (!rc) rc = encode4(&m.flead[i], F[i], nq, nr, ns, 9, pq, TQ, TR, 9);
+    rc = encode4(&m.fbox[i], F[i], nq, nr, ns, 9, pq, TQ + 16, TR + 2 * hr, 9);
+    // lead tiles: all 9 components of one plane, or (upwind) the 3
+    // velocities and, from another plane, the 6 stresses
+    if (!rc) rc = encode4(&m.flead[i], F[i], nq, nr, ns, 9, pq, TQ, TR, fd ? 3 : 9);
+    if (!rc && fd) rc = encode4(&m.flead2[i], F[i], nq, nr, ns, 9, pq, TQ, TR, 6);
+    if (!fd) m.flead2[i] = m.flead[i];
   }
   if (!rc) rc = encode4(&m.df, DF, nq, nr, ns, 9, pq, TQ, TR, 9);
   if (!rc) rc = encode4(&m.ck, C ? C : DF, nq, nr, ns, 9, pq, TQ, TR, 9);
   if (curv) {
     if (!rc) rc = encode4(&m.ca, coef, nq, nr, ns, kCurvCoef, pq, TQ + 16, TR, 3);
-    if (!rc) rc = encode4(&m.cb, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR + 6, 3);
+    if (!rc) rc = encode4(&m.cb, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR + 2 * hr, 3);
     if (!rc) rc = encode4(&m.cc, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR, 7);
     if (!rc) rc = encode4(&m.cl, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR, 3);
   } else {
@@ -766,9 +829,10 @@ long long fill_tma_desc(const VolumeArgs<float>& a, TmaBatchDesc& d) {
 }
 
 bool tma_eligible(const VolumeArgs<float>& a) {
-  // tile_span keeps every r closure row inside tile + halo unless the
-  // shifted last tile starts at 4 or 5
-  return a.tma != nullptr && (a.nr <= kTmaTR + 3 || a.nr >= kTmaTR + 6);
+  // the packed launch runs the central operator; tile_span keeps every r
+  // closure row inside tile + halo unless the shifted last tile starts at 4
+  // or 5
+  return a.tma != nullptr && a.fd == 0 && (a.nr <= kTmaTR + 3 || a.nr >= kTmaTR + 6);
 }
 
 void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bool curv, bool kahan, void* stream) {
@@ -779,18 +843,31 @@ void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bo
              : launch_tma_batch<false, false, kTmaStages>(d, nd, total, s);
 }
 
+// The upwind pair runs with the compensated update only (the FP32 mode
+// always carries C); stencil_is_tma sends an uncompensated upwind block to
+// the per-point kernel.
 void launch_stencil_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, bool curv, bool kahan,
                          void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
-  if (curv) kahan ? launch_tma2<true, true, kTmaStages>(a0, a1, s) : launch_tma2<true, false, kTmaStages>(a0, a1, s);
-  else kahan ? launch_tma2<false, true, kTmaStages>(a0, a1, s) : launch_tma2<false, false, kTmaStages>(a0, a1, s);
+  if (a0.fd) {
+    if (curv) launch_tma2<true, true, kTmaStages, 1>(a0, a1, s);
+    else launch_tma2<false, true, kTmaStages, 1>(a0, a1, s);
+    return;
+  }
+  if (curv) kahan ? launch_tma2<true, true, kTmaStages, 0>(a0, a1, s) : launch_tma2<true, false, kTmaStages, 0>(a0, a1, s);
+  else kahan ? launch_tma2<false, true, kTmaStages, 0>(a0, a1, s) : launch_tma2<false, false, kTmaStages, 0>(a0, a1, s);
 }
 
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream) {
   const StencilMaps& sm = *static_cast<const StencilMaps*>(a.tma);
   cudaStream_t s = (cudaStream_t)stream;
-  if (curv) kahan ? launch_tma<true, true, kTmaStages>(a, sm, s) : launch_tma<true, false, kTmaStages>(a, sm, s);
-  else kahan ? launch_tma<false, true, kTmaStages>(a, sm, s) : launch_tma<false, false, kTmaStages>(a, sm, s);
+  if (a.fd) {
+    if (curv) launch_tma<true, true, kTmaStages, 1>(a, sm, s);
+    else launch_tma<false, true, kTmaStages, 1>(a, sm, s);
+    return;
+  }
+  if (curv) kahan ? launch_tma<true, true, kTmaStages, 0>(a, sm, s) : launch_tma<true, false, kTmaStages, 0>(a, sm, s);
+  else kahan ? launch_tma<false, true, kTmaStages, 0>(a, sm, s) : launch_tma<false, false, kTmaStages, 0>(a, sm, s);
 }
 
 }  // namespace wql

@@ -171,8 +171,6 @@ __device__ void diff_pml_flux(const T* __restrict__ F, const T* __restrict__ coe
 // the velocities, D- on the fluxes.  Interior D+ weights on offsets -2..4
 // and D- weights on offsets -4..2; the closure rows of both operators cover
 // the same columns, so one load per column serves both.
-#define WQL_UP_CF {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0}
-
 template <typename T, bool CURV>
 __device__ __forceinline__ void diff6_up(const T* __restrict__ F, const T* __restrict__ coef, long long np,
                                          long long p, int i, int n, long long st, int d, T r[6]) {
@@ -960,14 +958,21 @@ void launch_tiled(const VolumeArgs<T>& a, cudaStream_t s) {
 // the tile that owns it plus a 3-point halo unless the shifted last tile
 // starts at 4 or 5 (then it would own left closure rows whose stencil
 // reaches point 0 from outside the halo); such sizes run per point.
+// With the upwind pair (halo 4, closure rows reading points 0..9) only a
+// last tile starting at 5 is excluded.
 inline bool tiles_ok(int n, int T) { return n <= T + 3 || n >= T + 6; }
+inline bool tiles_ok_up(int n, int T) { return n <= T + 4 || n >= T + 6; }
 
 template <typename T>
 int effective_variant(const VolumeArgs<T>& a) {
   constexpr bool f32 = sizeof(T) == 4;
-  if (a.fd) return 1;  // the upwind operators run per point
   int v = a.kernel != 0 ? a.kernel : (f32 ? 5 : 2);
   if ((v == 5 || v == 6) && !f32) v = 2;
+  if (a.fd) {
+    // the upwind pair: the TMA kernel (compensated FP32) or per point
+    if (!(v == 5 || v == 6) || a.C == nullptr || !tiles_ok_up(a.nr, kTmaTR)) v = 1;
+    return v;
+  }
   if ((v == 5 || v == 6) && !tiles_ok(a.nr, kTmaTR)) v = 1;
   if ((v == 2 || v == 3) && !(tiles_ok(a.nq, 32) && tiles_ok(a.nr, 8))) v = 1;
   if (v == 4 && !(tiles_ok(a.nq, 64) && tiles_ok(a.nr, 8))) v = 1;
