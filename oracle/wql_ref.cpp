@@ -455,6 +455,12 @@ struct RBlock {
   vector<wp> Q[7][9], DQ[7][9];    // full-size per active side
   wp tau0 = 0;
   bool upwind = false;  // fd_type 'upwind', order 6
+  // response = 'anelastic' (src/datatypes.f90:38-50): four relaxation
+  // mechanisms per stress component 4..9
+  bool anelastic = false;
+  vector<wp> Qs_inv, Qp_inv;
+  vector<wp> eta[6][4], Deta[6][4];
+  wp tau[4] = {0, 0, 0, 0}, weight[4] = {0, 0, 0, 0};
   size_t id(int i, int j, int k) const {
     return (size_t)(i - 1) + (size_t)nq * ((size_t)(j - 1) + (size_t)nr * (size_t)(k - 1));
   }
@@ -1079,6 +1085,54 @@ struct Media {
   const double* mat[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
 };
 
+// init_anelastic_properties: src/material.f90:11-142.  Q from the relaxed
+// shear speed, the relaxation times and weights of the selected set, and
+// the moduli replaced by their unrelaxed values at the reference frequency.
+void init_anelastic(RBlock& B, const wql::AnelasticParams& ap) {
+  const wp pi = 3.141592653589793;
+  const int N = 4;
+  B.anelastic = true;
+  B.Qs_inv.assign(B.np, 0.0);
+  B.Qp_inv.assign(B.np, 0.0);
+  for (int c = 0; c < 6; ++c)
+    for (int i = 0; i < N; ++i) {
+      B.eta[c][i].assign(B.np, 0.0);
+      B.Deta[c][i].assign(B.np, 0.0);
+    }
+  for (size_t p = 0; p < B.np; ++p) {
+    B.Qs_inv[p] = 1.0 / (ap.c * std::sqrt(B.M[1][p] / B.M[2][p]));
+    B.Qp_inv[p] = 0.5 * B.Qs_inv[p];
+  }
+  const wp w0[4] = {1.6126, 0.6255, 0.6382, 1.5969}, w6[4] = {0.0336, 0.6873, 0.8767, 1.5202};
+  const wp* w = ap.weight_exp < 0.01 ? w0 : w6;  // the caller has checked weight_exp
+  const wp FAC = 1.0;
+  const wp taumin = 1.0 / (2.0 * pi * 15.0) * 1.0 * FAC;
+  const wp taumax = 1.0 / (2.0 * pi * 0.08) * 200.0 * FAC;
+  for (int k = 1; k <= N; ++k) {
+    B.tau[k - 1] = std::exp(std::log(taumin) + (2.0 * k - 1.0) / 16.0 * (std::log(taumax) - std::log(taumin)));
+    B.weight[k - 1] = w[k - 1];
+  }
+  const wp wref = 2.0 * pi * ap.fref;
+  const wp facex = 1.0;
+  for (size_t p = 0; p < B.np; ++p) {
+    wp val_S = 0.0, val_P = 0.0;
+    for (int l = 0; l < N; ++l) {
+      const wp denom_S = ((wref * wref) * (B.tau[l] * B.tau[l]) + 1.0) * (1.0 / B.Qs_inv[p]) * facex;
+      const wp denom_P = ((wref * wref) * (B.tau[l] * B.tau[l]) + 1.0) * (1.0 / B.Qp_inv[p]) * facex;
+      val_S = val_S + B.weight[l] / denom_S;
+      val_P = val_P + B.weight[l] / denom_P;
+    }
+    wp vs = std::sqrt(B.M[1][p] / B.M[2][p]);
+    wp vp = std::sqrt((B.M[0][p] + 2.0 * B.M[1][p]) / B.M[2][p]);
+    const wp mu_S = B.M[2][p] * (vs * vs) / (1.0 - val_S);
+    const wp mu_P = B.M[2][p] * (vp * vp) / (1.0 - val_P);
+    vs = std::sqrt(mu_S / B.M[2][p]);
+    vp = std::sqrt(mu_P / B.M[2][p]);
+    B.M[1][p] = (vs * vs) * B.M[2][p];
+    B.M[0][p] = (vp * vp) * B.M[2][p] - 2.0 * B.M[1][p];
+  }
+}
+
 int init_block(Domain& D, int b, const Media& md) {
   RBlock& B = D.Bk[b];
   const wql::BlockParams& bp = D.P.btp[b];
@@ -1141,6 +1195,7 @@ int init_block(Domain& D, int b, const Media& md) {
     B.M[1][p] = md.mat[b][1] ? md.mat[b][1][p] : mu;
     B.M[2][p] = md.mat[b][2] ? md.mat[b][2][p] : bp.rho_s_p[0];
   }
+  if (D.P.response == "anelastic") init_anelastic(B, D.P.anel);  // src/block.f90:150-151
   for (int c = 0; c < 9; ++c) {
     B.F[c].assign(B.np, 0.0);
     B.DF[c].assign(B.np, 0.0);  // 1e40 in the reference; A(1)=0 clears it
@@ -1293,6 +1348,64 @@ void pml_point(RBlock& B, wp DU[9], const wp Ux[9], const wp Uy[9], const wp Uz[
   }
 }
 
+// Memory-variable terms of one point (src/RHS_Interior.f90:2390-2441, and
+// :2444-2509 inside a PML, where the strain rates lose the damped auxiliary
+// fields of pml_damping_and_q, :2287-2387): D[0..5] (the point's rates of
+// stress components 4..9) -= the sum of its four memory variables, and
+// Deta += (relaxed strain-rate forcing - eta) / tau.  g[c][j] = dv_c/dx_j.
+void anelastic_point(RBlock& B, size_t p, int x, int y, int z, const wp Ux[9], const wp Uy[9], const wp Uz[9],
+                     wp* D0, wp* D1, wp* D2, wp* D3, wp* D4, wp* D5) {
+  wp dxyz[3] = {0, 0, 0};
+  wp Qv[3][9] = {{0}};
+  const wp Rf = 1.0e-3;
+  const wp d0 = 6.0 / (2.0 * 1.0) * std::log(1.0 / Rf);
+  const int npml = B.npml, nx = B.nq, ny = B.nr, nz = B.ns;
+  auto take = [&](int side, int ax, wp d) {
+    dxyz[ax] = d;
+    for (int c = 0; c < 9; ++c) Qv[ax][c] = B.Q[side][c][p];
+  };
+  if (B.pml[1] && x <= npml) take(1, 0, d0 * std::fabs((wp)(x - (1 + npml)) / (wp)npml));
+  if (B.pml[2] && x >= nx - npml + 1) take(2, 0, d0 * std::fabs((wp)(x - (nx - npml)) / (wp)npml));
+  if (B.pml[3] && y <= npml) take(3, 1, d0 * std::fabs((wp)(y - (1 + npml)) / (wp)npml));
+  if (B.pml[4] && y >= ny - npml + 1) take(4, 1, d0 * std::fabs((wp)(y - (ny - npml)) / (wp)npml));
+  if (B.pml[5] && z <= npml) take(5, 2, d0 * std::fabs((wp)(z - npml) / (wp)npml));
+  if (B.pml[6] && z >= nz - npml + 1) take(6, 2, d0 * std::fabs((wp)(z - (nz - npml)) / (wp)npml));
+  const wp dx = dxyz[0], dy = dxyz[1], dz = dxyz[2];
+  const bool in_pml = (B.pml[1] && x <= npml) || (B.pml[2] && x >= nx - npml + 1) || (B.pml[3] && y <= npml) ||
+                      (B.pml[4] && y >= ny - npml + 1) || (B.pml[5] && z <= npml) || (B.pml[6] && z >= nz - npml + 1);
+  wp e[6], tr;
+  if (in_pml) {
+    e[0] = Ux[0] - dx * Qv[0][3];
+    e[1] = Uy[1] - dy * Qv[1][4];
+    e[2] = Uz[2] - dz * Qv[2][5];
+    tr = e[0] + e[1] + e[2];
+    e[3] = (Uy[0] + Ux[1]) - dx * Qv[0][6] - dy * Qv[1][6];
+    e[4] = (Uz[0] + Ux[2]) - dx * Qv[0][7] - dz * Qv[2][7];
+    e[5] = (Uz[1] + Uy[2]) - dy * Qv[1][8] - dz * Qv[2][8];
+  } else {
+    e[0] = Ux[0];
+    e[1] = Uy[1];
+    e[2] = Uz[2];
+    tr = Ux[0] + Uy[1] + Uz[2];
+    e[3] = Uy[0] + Ux[1];
+    e[4] = Uz[0] + Ux[2];
+    e[5] = Uz[1] + Uy[2];
+  }
+  wp* Dp[6] = {D0, D1, D2, D3, D4, D5};
+  for (int c = 0; c < 6; ++c)
+    *Dp[c] = *Dp[c] - (B.eta[c][0][p] + B.eta[c][1][p] + B.eta[c][2][p] + B.eta[c][3][p]);
+  const wp lam = B.M[0][p], mu = B.M[1][p], Qs = B.Qs_inv[p], Qp = B.Qp_inv[p];
+  for (int i = 0; i < 4; ++i) {
+    const wp wi = B.weight[i];
+    for (int c = 0; c < 3; ++c)
+      B.Deta[c][i][p] = B.Deta[c][i][p] + (((wi * 2.0 * mu * Qs) * e[c] +
+                                            (wi * ((lam + 2.0 * mu) * Qp - 2.0 * mu * Qs)) * tr) -
+                                           B.eta[c][i][p]) / B.tau[i];
+    for (int c = 3; c < 6; ++c)
+      B.Deta[c][i][p] = B.Deta[c][i][p] + ((wi * mu * Qs * e[c] - B.eta[c][i][p]) / B.tau[i]);
+  }
+}
+
 void interior_limits(const RBlock& B, int& ix, int& iy, int& iz, int& fx, int& fy, int& fz) {
   ix = iy = iz = fx = fy = fz = 6;  // JU:16211-16226
   if (B.pml[5]) iz = std::max(B.npml, 6);
@@ -1382,6 +1495,9 @@ void rhs_interior(RBlock& B, bool cart) {
         B.DF[6][p] = B.DF[6][p] + a4 * (DFy[0] + DFx[1]);
         B.DF[7][p] = B.DF[7][p] + a4 * (DFz[0] + DFx[2]);
         B.DF[8][p] = B.DF[8][p] + a4 * (DFz[1] + DFy[2]);
+        if (B.anelastic)
+          anelastic_point(B, p, x, y, z, DFx, DFy, DFz, &B.DF[3][p], &B.DF[4][p], &B.DF[5][p], &B.DF[6][p],
+                          &B.DF[7][p], &B.DF[8][p]);
       }
 }
 
@@ -1446,6 +1562,9 @@ void rhs_interior_upwind(RBlock& B, bool cart) {
         B.DF[6][p] = B.DF[6][p] + a4 * (DFy[0] + DFx[1]);
         B.DF[7][p] = B.DF[7][p] + a4 * (DFz[0] + DFx[2]);
         B.DF[8][p] = B.DF[8][p] + a4 * (DFz[1] + DFy[2]);
+        if (B.anelastic)
+          anelastic_point(B, p, x, y, z, DFx, DFy, DFz, &B.DF[3][p], &B.DF[4][p], &B.DF[5][p], &B.DF[6][p],
+                          &B.DF[7][p], &B.DF[8][p]);
       }
 }
 
@@ -1484,6 +1603,7 @@ void rhs_near_boundaries(RBlock& B) {
         DU[6] = B.M[1][p] * (Uy[0] + Ux[1]);
         DU[7] = B.M[1][p] * (Uz[0] + Ux[2]);
         DU[8] = B.M[1][p] * (Uz[1] + Uy[2]);
+        if (B.anelastic) anelastic_point(B, p, x, y, z, Ux, Uy, Uz, &DU[3], &DU[4], &DU[5], &DU[6], &DU[7], &DU[8]);
         pml_point(B, DU, Ux, Uy, Uz, x, y, z, rhoJ_inv, lambda2mu);
         for (int c = 0; c < 9; ++c) B.DF[c][p] = B.DF[c][p] + DU[c];
       }
@@ -2056,6 +2176,10 @@ void time_step(Domain& D) {
       for (int c = 0; c < 4; ++c)
         for (auto& v : D.If[b].DS[c]) v = A * v;
       for (auto& v : D.If[b].DW) v = A * v;
+      if (B.anelastic)  // src/fields.f90:61-68
+        for (int c = 0; c < 6; ++c)
+          for (int i = 0; i < 4; ++i)
+            for (auto& v : B.Deta[c][i]) v = A * v;
     }
     // set_rates
     for (int b = 0; b < 2; ++b) {
@@ -2096,6 +2220,10 @@ void time_step(Domain& D) {
       for (int c = 0; c < 4; ++c)
         for (size_t f = 0; f < I.S[c].size(); ++f) I.S[c][f] = I.S[c][f] + Bdt * I.DS[c][f];
       for (size_t f = 0; f < I.W.size(); ++f) I.W[f] = I.W[f] + Bdt * I.DW[f];
+      if (B.anelastic)  // src/fields.f90:122-129
+        for (int c = 0; c < 6; ++c)
+          for (int i = 0; i < 4; ++i)
+            for (size_t p = 0; p < B.np; ++p) B.eta[c][i][p] = B.eta[c][i][p] + Bdt * B.Deta[c][i][p];
     }
     if (stage == 5)
       for (int b = 0; b < 2; ++b) plasticity(D, D.Bk[b]);
@@ -2234,6 +2362,13 @@ static void* create_domain(Domain* D, const Media& md) {
       delete D;
       return nullptr;
     }
+  }
+  if (D->P.response == "anelastic" &&
+      !(D->P.anel.weight_exp < 0.01 || (D->P.anel.weight_exp > 0.59 && D->P.anel.weight_exp < 0.61))) {
+    // src/material.f90:85-115 sets the relaxation times only for these
+    std::snprintf(g_err, sizeof(g_err), "anelastic weight_exp must be 0 or 0.6");
+    delete D;
+    return nullptr;
   }
   if (D->plastic && !D->scec) {
     std::snprintf(g_err, sizeof(g_err), "only plastic_model='scec' is restated");

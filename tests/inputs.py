@@ -85,6 +85,12 @@ def case_text(name):
         return problem("TPV101", "rate-and-state_friction", "curvilinear") + block_list()
     if name == "locked":
         return problem("TPV5", "locked") + block_list()
+    if name.startswith(("an_", "an0_")):
+        # anelastic response (GSLS memory variables, src/material.f90:11-142)
+        c, wexp = ("2.0d0", "0.6d0") if not name.startswith("an0_") else ("5.0d0", "0d0")
+        base = case_text(name.split("_", 1)[1])
+        base = base.replace(" w_stride = 1,", " w_stride = 1,\n response = 'anelastic',", 1)
+        return base + f"&anelastic_list\n c = {c},\n weight_exp = {wexp},\n fref = 1d0 /\n"
     if name.startswith("up_"):
         # the upwind operators of order 6 (fd_type = 'upwind')
         return case_text(name[3:]).replace(" w_stride = 1,", " w_stride = 1,\n fd_type = 'upwind',\n order = 6,", 1)

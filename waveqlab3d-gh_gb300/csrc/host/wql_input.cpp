@@ -415,6 +415,14 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
       else if (it.key == "tv") P.plast.Tv = v;
     }
   }
+  if (groups.count("anelastic_list")) {
+    for (auto& it : items_of("anelastic_list")) {
+      double v = it.values.empty() ? 0.0 : to_double(it.values[0]);
+      if (it.key == "c") P.anel.c = v;
+      else if (it.key == "weight_exp") P.anel.weight_exp = v;
+      else if (it.key == "fref") P.anel.fref = v;
+    }
+  }
   P.stationsU = marker_block(text, "station_listU");
   P.stationsV = marker_block(text, "station_listV");
   P.stations = marker_block(text, "station_list");

@@ -60,6 +60,13 @@ struct PlasticExt {
   double cohesion = 1.36, friction = 0.1934, Tv = 0.03;   // src/plastic.f90:174-176
 };
 
+// &anelastic_list (src/material.f90:28-41): quality factor scale c
+// (Qs = c * vs), the weight-set selector weight_exp (0 or 0.6) and the
+// reference frequency fref (Hz) of the unrelaxed moduli.
+struct AnelasticParams {
+  double c = 1.0, weight_exp = 0.0, fref = 1.0;
+};
+
 // One moment-tensor point source, a line of a tensor list
 // (src/moment_tensor.f90:232-246): source_type duration t_init
 // mXX mYY mZZ mXY mXZ mYZ x y z alpha.
@@ -85,6 +92,7 @@ struct Problem {
   bool w_fault = true, interpol = false, use_topography = false,
        mollify_source = false;
   BlockParams btp[2];
+  AnelasticParams anel;  // response = 'anelastic'
   // &moment_list (src/block.f90:63)
   bool use_moment_tensor = false;
   int mt_order = 2;

@@ -124,6 +124,9 @@ struct wql_scn {
     void* DQ[6] = {};
     long long slab_np[6] = {};
     void* G = nullptr;  // PML velocity gradient hand-off (FP32C with PML)
+    void* eta = nullptr;   // anelastic memory variables (24 x np)
+    void* Deta = nullptr;  // and their rates
+    void* qs = nullptr;    // 1/Qs per point
     void* y = nullptr;
     double cart_metric[3] = {1, 1, 1};
     double tau_h[3] = {};
@@ -146,6 +149,8 @@ struct wql_scn {
   int stage_launches = 0;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
   int fd = 0;              // 0: traditional SBP-6; 1: upwind SBP-6
+  bool anel = false;       // response = 'anelastic'
+  double an_tau[4] = {}, an_w[4] = {};
   int schunk = 0;          // planes per CTA along s (0: default)
   bool plastic = false;
   double pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
@@ -454,6 +459,25 @@ int setup_block(wql_scn* S, int b) {
       CK(cudaStreamSynchronize(S->stream));
     }
   }
+  // anelastic response: Q and the unrelaxed moduli before anything reads
+  // the material (src/block.f90:150-151)
+  if (S->anel) {
+    double* qsd = nullptr;
+    if ((rc = S->alloc((void**)&qsd, np * sizeof(double), false))) return rc;
+    const double wref = 2.0 * 3.141592653589793 * S->P.anel.fref;
+    double den[4];
+    for (int l = 0; l < 4; ++l) den[l] = (wref * wref) * (S->an_tau[l] * S->an_tau[l]) + 1.0;
+    launch_anelastic_material(np, S->P.anel.c, den, S->an_w, mat, mat + np, mat + 2 * np, qsd, S->stream);
+    CK(cudaGetLastError());
+    if ((rc = S->alloc(&B.qs, B.np * S->esz))) return rc;
+    if ((rc = S->alloc(&B.eta, 24 * B.np * S->esz))) return rc;
+    if ((rc = S->alloc(&B.Deta, 24 * B.np * S->esz))) return rc;
+    if (S->prec == WQL_FP64)
+      pad_rows<double><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(qsd, (double*)B.qs, B.nq, B.pq, np);
+    else
+      pad_rows<float><<<(unsigned)((np + 255) / 256), 256, 0, S->stream>>>(qsd, (float*)B.qs, B.nq, B.pq, np);
+    CK(cudaGetLastError());
+  }
   // faces
   for (int s = 0; s < 6; ++s) {
     const int axis = s / 2;
@@ -678,7 +702,22 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   else if (Pr.fd_type != "traditional")
     return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' with order " + std::to_string(Pr.order) +
                                  " is not supported (traditional SBP-6, or upwind with order = 6)");
-  if (Pr.response == "anelastic") return fail(WQL_E_INPUT, "response='anelastic' is not supported");
+  if (Pr.response == "anelastic") {
+    // init_anelastic_properties (src/material.f90:85-115): relaxation times
+    // and weights exist for weight_exp 0 and 0.6 only
+    const double we = Pr.anel.weight_exp;
+    const bool w0 = we < 0.01, w6 = we > 0.59 && we < 0.61;
+    if (!w0 && !w6) return fail(WQL_E_INPUT, "anelastic weight_exp must be 0 or 0.6");
+    const double pi = 3.141592653589793, FAC = 1.0;
+    const double taumin = 1.0 / (2.0 * pi * 15.0) * 1.0 * FAC;
+    const double taumax = 1.0 / (2.0 * pi * 0.08) * 200.0 * FAC;
+    const double wa[4] = {1.6126, 0.6255, 0.6382, 1.5969}, wb[4] = {0.0336, 0.6873, 0.8767, 1.5202};
+    for (int k = 1; k <= 4; ++k) {
+      S->an_tau[k - 1] = std::exp(std::log(taumin) + (2.0 * k - 1.0) / 16.0 * (std::log(taumax) - std::log(taumin)));
+      S->an_w[k - 1] = w0 ? wa[k - 1] : wb[k - 1];
+    }
+    S->anel = true;
+  }
   if (Pr.use_moment_tensor) {
     if (Pr.mt_order != 2 && Pr.mt_order != 4) return fail(WQL_E_INPUT, "moment_list order must be 2 or 4");
     for (const auto* L : {&Pr.tensors, &Pr.tensorsU, &Pr.tensorsV}) {
@@ -898,6 +937,14 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.pl_sin = std::sin(std::atan(S->pl_nu));
   a.pl_decay = std::exp(-S->dt / S->pl_Tv);
   a.err = S->err_dev;
+  a.anel = S->anel ? 1 : 0;
+  a.eta = (T*)B.eta;
+  a.Deta = (T*)B.Deta;
+  a.qsinv = (const T*)B.qs;
+  for (int m = 0; m < 4; ++m) {
+    a.an_tau[m] = S->an_tau[m];
+    a.an_w[m] = S->an_w[m];
+  }
   a.pml_d0 = 6.0 / (2.0 * 1.0) * std::log(1.0 / 1.0e-3);
   B.maps.cur = S->cur;
   a.tma = &B.maps;
@@ -1823,6 +1870,7 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
     for (int s2 = 0; s2 < 3; ++s2) any_pml = any_pml || bp.pml_lqrs[s2] || bp.pml_rqrs[s2];
     if (any_pml && bp.npml > 0 && precision == WQL_FP32C) res += al(9 * np * esz);
     if (P.response == "plastic") res += al(np * esz);
+    if (P.response == "anelastic") res += 2 * al(24 * np * esz) + al(np * esz) + al(npd * 8);
     // set-up arrays of one block: x, metric, J, material (FP64)
     transient = std::max(transient, al(3 * npd * 8) + al(9 * npd * 8) + al(npd * 8) + al(3 * npd * 8));
   }

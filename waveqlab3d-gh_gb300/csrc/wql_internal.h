@@ -72,6 +72,15 @@ struct VolumeArgs {
   const T* __restrict__ ycoord;  // depth coordinate for the initial stress
   double pl_c, pl_nu, pl_Tv, dt;
   double pl_ccos, pl_sin, pl_decay;  // c*cos(atan nu), sin(atan nu), exp(-dt/Tv)
+  // anelastic response (src/RHS_Interior.f90:2390-2509): memory variables
+  // eta and their rates Deta (24 x np each, component c*4 + i for stress
+  // component 4+c and mechanism i), 1/Qs per point (1/Qp = 1/(2 Qs)), the
+  // relaxation times and weights; anel = 0 without
+  int anel;
+  T* eta;
+  T* Deta;
+  const T* qsinv;
+  double an_tau[4], an_w[4];
   int* err;                      // device error word (pipeline wait timeouts)
   double pml_d0;                 // PML damping scale 3 ln(1000)
   const void* tma;               // host pointer to the block's StencilMaps (FP32 only)
@@ -188,6 +197,11 @@ void launch_source(const VolumeArgs<T>& a, const int lo[3], const int dim[3], co
 void launch_interface(const InterfaceArgs& a, void* stream);
 void launch_metrics(int nq, int nr, int ns, const double* x, double* metric, double* J,
                     void* stream);
+// Anelastic set-up on the dense FP64 material arrays (src/material.f90:
+// 69-140): qsinv = 1/(c vs) from the relaxed moduli, then mu and lambda
+// replaced by their unrelaxed values; den[l] = (2 pi fref)^2 tau_l^2 + 1.
+void launch_anelastic_material(long long n, double c, const double den[4], const double w[4], double* lam,
+                               double* mu, const double* rho, double* qsinv, void* stream);
 void launch_faces(int nq, int nr, int ns, const double* metric, const double* lam,
                   const double* mu, const double* rho, double* const face[6], void* stream);
 template <typename T>

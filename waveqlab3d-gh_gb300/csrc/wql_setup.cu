@@ -178,6 +178,52 @@ void launch_coef(int nq, int nr, int ns, int pq, bool curv, const double* metric
                                                                    lam, mu, rho, coef);
 }
 
+// Anelastic set-up, one thread per point (src/material.f90:69-74, 117-140):
+// the quality factors from the relaxed shear speed, then the moduli that
+// make the relaxed speeds the unrelaxed ones at the reference frequency.
+struct AnelMat {
+  double c, den[4], w[4];
+};
+
+__global__ void anelastic_material_kernel(long long n, AnelMat m, double* __restrict__ lam, double* __restrict__ mu,
+                                          const double* __restrict__ rho, double* __restrict__ qsinv) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const double r = rho[p];
+  const double qs = 1.0 / (m.c * sqrt(mu[p] / r));
+  const double qp = 0.5 * qs;
+  double val_S = 0.0, val_P = 0.0;
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const double denom_S = m.den[l] * (1.0 / qs) * 1.0;
+    const double denom_P = m.den[l] * (1.0 / qp) * 1.0;
+    val_S = val_S + m.w[l] / denom_S;
+    val_P = val_P + m.w[l] / denom_P;
+  }
+  double vs = sqrt(mu[p] / r);
+  double vp = sqrt((lam[p] + 2.0 * mu[p]) / r);
+  const double mu_S = r * (vs * vs) / (1.0 - val_S);
+  const double mu_P = r * (vp * vp) / (1.0 - val_P);
+  vs = sqrt(mu_S / r);
+  vp = sqrt(mu_P / r);
+  const double mu_new = (vs * vs) * r;
+  mu[p] = mu_new;
+  lam[p] = (vp * vp) * r - 2.0 * mu_new;
+  qsinv[p] = qs;
+}
+
+void launch_anelastic_material(long long n, double c, const double den[4], const double w[4], double* lam,
+                               double* mu, const double* rho, double* qsinv, void* stream) {
+  AnelMat m;
+  m.c = c;
+  for (int l = 0; l < 4; ++l) {
+    m.den[l] = den[l];
+    m.w[l] = w[l];
+  }
+  anelastic_material_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(n, m, lam, mu, rho,
+                                                                                            qsinv);
+}
+
 template void launch_coef<double>(int, int, int, int, bool, const double*, const double*, const double*,
                                   const double*, const double*, double*, void*);
 template void launch_coef<float>(int, int, int, int, bool, const double*, const double*, const double*,

@@ -781,6 +781,125 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 }
 
 // ---------------------------------------------------------------------------
+// Anelastic kernel (response = 'anelastic'; src/RHS_Interior.f90:2390-2509,
+// the interior terms of src/JU_xJU_yJU_z6.f90:16316-16346, src/fields.f90:
+// 61-68 and 122-129), one thread per point: the stress rates lose the sum
+// of the point's four memory variables, each memory variable's rate is
+//   Deta <- A*Deta + (relaxed strain-rate forcing - eta) / tau
+// and eta <- eta + B*dt*Deta.  Inside a PML slab the strain rates lose the
+// damped auxiliary fields (pml_damping_and_q, src/RHS_Interior.f90:
+// 2287-2387), so this kernel runs before the PML kernel advances Q.  The
+// velocity gradient is formed here with the block's operator.
+template <typename T, bool CURV, bool KAHAN, int FD>
+__global__ void __launch_bounds__(256) anelastic_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  const int nq = a.nq, nr = a.nr, ns = a.ns, npml = a.npml;
+  if (i >= nq || j >= nr) return;
+  const long long np = a.np;
+  const long long p = i + (long long)a.pq * (j + (long long)nr * k);
+  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
+  const long long st[3] = {1, a.pq, (long long)a.pq * nr};
+  const T* __restrict__ F = a.Fin;
+  const T* __restrict__ coef = a.coef;
+  const T Jinv = CURV ? coef[9 * np + p] : T(1);
+  T g[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    T o[3];
+    if (FD) diff_v_up<T>(F, np, p, idx[d], nn[d], st[d], o);
+    else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
+    const T rh = a.rh[d];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (CURV) {
+#pragma unroll
+        for (int jj = 0; jj < 3; ++jj) {
+          const T m = coef[(d * 3 + jj) * np + p] * Jinv;
+          g[c][jj] = d == 0 ? m * (rh * o[c]) : g[c][jj] + m * (rh * o[c]);
+        }
+      } else {
+        g[c][d] = a.cart_metric[d] * rh * o[c];
+      }
+    }
+  }
+  // strain rates: exx, eyy, ezz, gxy, gxz, gyz and the trace
+  T e[6];
+  e[0] = g[0][0];
+  e[1] = g[1][1];
+  e[2] = g[2][2];
+  e[3] = g[0][1] + g[1][0];
+  e[4] = g[0][2] + g[2][0];
+  e[5] = g[1][2] + g[2][1];
+  bool in_pml = false;
+#pragma unroll
+  for (int side = 0; side < 6; ++side) {
+    const int ax = side >> 1;
+    if (a.pml[side] && ((side & 1) ? idx[ax] >= nn[ax] - npml : idx[ax] < npml)) in_pml = true;
+  }
+  if (in_pml) {
+    // d * Q terms per axis (damping profile and slab indexing as the PML kernel)
+    T dq[3][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
+#pragma unroll
+    for (int side = 0; side < 6; ++side) {
+      if (!a.pml[side]) continue;
+      const int axis = side >> 1;
+      const bool hi = side & 1;
+      const int ii = idx[axis], n = nn[axis];
+      if (!(hi ? (ii >= n - npml) : (ii < npml))) continue;
+      const int off = hi ? ii + 1 - (n - npml) : (axis == 2 ? ii + 1 - npml : ii - npml);
+      const T damp = (T)a.pml_d0 * (fabs((T)off / (T)npml));
+      long long sp;
+      if (axis == 0) sp = (hi ? ii - (n - npml) : ii) + (long long)npml * (j + (long long)nr * k);
+      else if (axis == 1) sp = i + (long long)nq * ((hi ? ii - (n - npml) : ii) + (long long)npml * k);
+      else sp = i + (long long)nq * (j + (long long)nr * (hi ? ii - (n - npml) : ii));
+      const long long snp = a.slab_np[side];
+      const T* Q = a.Q[side];
+      // Q components of the normal strain and the two shear strains of this axis
+      const int cn = 3 + axis;
+      const int c1 = axis == 0 ? 6 : (axis == 1 ? 6 : 7);
+      const int c2 = axis == 0 ? 7 : 8;
+      dq[axis][0] = damp * Q[cn * snp + sp];
+      dq[axis][1] = damp * Q[c1 * snp + sp];
+      dq[axis][2] = damp * Q[c2 * snp + sp];
+    }
+    e[0] = e[0] - dq[0][0];
+    e[1] = e[1] - dq[1][0];
+    e[2] = e[2] - dq[2][0];
+    e[3] = e[3] - dq[0][1] - dq[1][1];  // gxy: Qx(7), Qy(7)
+    e[4] = e[4] - dq[0][2] - dq[2][1];  // gxz: Qx(8), Qz(8)
+    e[5] = e[5] - dq[1][2] - dq[2][2];  // gyz: Qy(9), Qz(9)
+  }
+  const T tr = e[0] + e[1] + e[2];
+  const T lam = CURV ? coef[10 * np + p] : coef[0 * np + p];
+  const T mu = CURV ? coef[11 * np + p] : coef[1 * np + p];
+  const T qs = a.qsinv[p];
+  const T qp = T(0.5) * qs;
+  T corr[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) corr[c] = T(0);
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    T ev[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) ev[m] = a.eta[(c * 4 + m) * np + p];
+    corr[3 + c] = -(ev[0] + ev[1] + ev[2] + ev[3]);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const T w = (T)a.an_w[m];
+      const T force = c < 3 ? (w * T(2) * mu * qs) * e[c] + (w * ((lam + T(2) * mu) * qp - T(2) * mu * qs)) * tr
+                            : w * mu * qs * e[c];
+      const long long q = (c * 4 + m) * np + p;
+      const T de = a.A * a.Deta[q] + (force - ev[m]) / (T)a.an_tau[m];
+      a.Deta[q] = de;
+      a.eta[q] = ev[m] + a.Bdt * de;
+    }
+  }
+  add_correction<T, KAHAN>(a, p, corr);
+}
+
+// ---------------------------------------------------------------------------
 // Face kernel: outer-boundary SAT (src/RHS_Interior.f90:1516-1703 with
 // src/BoundaryConditions.f90:777-918 + structure(), or the weighted form of
 // src/BoundaryConditions3.f90:777-903) and the fault SAT computed by the
@@ -1016,6 +1135,11 @@ template <typename T, bool CURV, bool KAHAN>
 int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
   int n = 0;
   dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
+  if (a.anel) {  // before the PML kernel: it reads Q of the stage's input
+    if (a.fd) anelastic_kernel<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a);
+    else anelastic_kernel<T, CURV, KAHAN, 0><<<grd, blk, 0, s>>>(a);
+    ++n;
+  }
   if (a.npml > 0) {
     const PmlBoxes bx = pml_boxes(a);
     const unsigned nblk = (unsigned)((bx.start[bx.n] + 255) / 256);
