@@ -129,8 +129,8 @@ def workload(args):
     import wql_configs
     if args.workload == "config2":
         text, media = wql_configs.config2(steps=10 ** 6, seed=args.seed)
-    elif args.workload == "upwind":
-        text, media = wql_configs.upwind_pml12(steps=10 ** 6)
+    elif args.workload in ("upwind", "upwind_anelastic"):
+        text, media = wql_configs.upwind_pml12(steps=10 ** 6, anelastic=args.workload == "upwind_anelastic")
     else:
         text, media = wql_configs.config1(n=args.n, steps=10 ** 6, seed=args.seed)
     return text, media, wql_configs.updates_per_step(text)
@@ -406,10 +406,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
                     help="step: config 1 (default); batch: config 3 ensemble in one batch; serve: config 4 stream")
-    ap.add_argument("--workload", default="config1", choices=["config1", "config2", "upwind"],
+    ap.add_argument("--workload", default="config1", choices=["config1", "config2", "upwind", "upwind_anelastic"],
                     help="step mode: config1 (2 x n^3 curvilinear, rate and state), config2 (2 x 401x201x201, "
-                         "PML, von Karman, plasticity) or upwind (2 x 76x101x151 Cartesian, upwind SBP-6, PML, "
-                         "point source)")
+                         "PML, von Karman, plasticity), upwind (2 x 76x101x151 Cartesian, upwind SBP-6, PML, "
+                         "point source) or upwind_anelastic (the same with the anelastic response)")
     ap.add_argument("--members", type=int, default=64, help="batch mode: ensemble size")
     ap.add_argument("--requests", type=int, default=32, help="serve mode: number of requests")
     ap.add_argument("--rate", type=float, default=4.0, help="serve mode: Poisson arrival rate (requests/s)")
@@ -424,9 +424,11 @@ def main():
     if args.workload == "config2":
         wl = (f"config2: 2 x 401x201x201 curvilinear blocks, 20-point PML on 5 sides, von Karman medium, "
               f"scec viscoplasticity, TPV26 stress, slip weakening, {ups // 5} grid points")
-    if args.workload == "upwind":
-        wl = (f"upwind: 2 x 76x101x151 Cartesian blocks, upwind SBP-6 operators, 12-point PML on 5 sides, "
-              f"locked interface, one moment-tensor source, {ups // 5} grid points")
+    if args.workload in ("upwind", "upwind_anelastic"):
+        wl = (f"{args.workload}: 2 x 76x101x151 Cartesian blocks, upwind SBP-6 operators, 12-point PML on 5 sides, "
+              f"locked interface, one moment-tensor source, "
+              f"{'anelastic response (4 mechanisms, c = 2, weight_exp = 0.6), ' if 'anelastic' in args.workload else ''}"
+              f"{ups // 5} grid points")
 
     if args.impl == "reference":
         if rank != 0:
@@ -488,7 +490,7 @@ def main():
     # per-point launch per block)
     kernel_name = "stencil_kernel_tma2<float,curv,kahan>"
     mesh = "curv"
-    if args.workload == "upwind":
+    if args.workload in ("upwind", "upwind_anelastic"):
         kernel_name, mesh = "stencil_kernel_tma2<float,cart,kahan,upwind>", "cart"
     pts_per_launch = ups * main_r["kt"]["prof_steps"] / vol_n if vol_n else 0
     algo = BYTES_PER_UPDATE[(mesh, "fp32c")] * pts_per_launch
@@ -523,7 +525,8 @@ def main():
         "dtype": "f32 fields, Kahan-compensated RK update, f64 fault solve",
         "data": {"config1": "synthetic (seeded topography, fault roughness)",
                  "config2": "synthetic (seeded von Karman medium)",
-                 "upwind": "synthetic (uniform medium, one point source)"}[args.workload],
+                 "upwind": "synthetic (uniform medium, one point source)",
+                 "upwind_anelastic": "synthetic (uniform medium, one point source)"}[args.workload],
         "config": {"workload": wl, "precision": "fp32c", "steps_timed": args.steps,
                    "l2": f"inputs larger than L2: {ws_bytes / 2**20:.0f} MiB resident per GPU vs 129 MiB L2",
                    "parallelism": f"{world} independent replica(s), no collective"},

@@ -53,3 +53,18 @@ def test_anelastic_unsupported_weight_set(ctx, wqlmod, tmp_path):
     p = write(tmp_path, "w.in", case_text("an_mt4").replace("weight_exp = 0.6d0", "weight_exp = 0.3d0"))
     with pytest.raises(Exception, match="weight_exp"):
         wqlmod.Scenario(ctx, p)
+
+
+@pytest.mark.parametrize("case,steps", [("an_pml_curv", 20), ("an_up_mt4", 30)])
+def test_anelastic_gradient_handoff(ctx, wqlmod, tmp_path, case, steps):
+    """FP32C: the anelastic kernel fed the TMA stencil's velocity gradient
+    against the per-point stencil run, where it forms the gradient itself."""
+    p = write(tmp_path, case + ".in", case_text(case))
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    g = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    g.set_tuning(1, 0)
+    f.step(steps)
+    g.step(steps)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), g.fields(b)) < 1e-6

@@ -532,8 +532,11 @@ int setup_block(wql_scn* S, int b) {
       if ((rc = S->alloc(&B.Q[s], 9 * slab * S->esz))) return rc;
       if ((rc = S->alloc(&B.DQ[s], 9 * slab * S->esz))) return rc;
     }
-    if (S->prec == WQL_FP32C && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
+    if (S->prec == WQL_FP32C && !S->anel && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   }
+  // anelastic: the TMA stencil hands the velocity gradient of every point
+  // to the anelastic kernel
+  if (S->prec == WQL_FP32C && S->anel && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   // src/block.f90:189-214
   const double tau0 = S->fd ? kTau0Upwind6 : 1.0 / (0.315949074074074);
   const int dims[3] = {B.nq, B.nr, B.ns};
@@ -1870,7 +1873,10 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
     for (int s2 = 0; s2 < 3; ++s2) any_pml = any_pml || bp.pml_lqrs[s2] || bp.pml_rqrs[s2];
     if (any_pml && bp.npml > 0 && precision == WQL_FP32C) res += al(9 * np * esz);
     if (P.response == "plastic") res += al(np * esz);
-    if (P.response == "anelastic") res += 2 * al(24 * np * esz) + al(np * esz) + al(npd * 8);
+    if (P.response == "anelastic") {
+      res += 2 * al(24 * np * esz) + al(np * esz) + al(npd * 8);
+      if (precision == WQL_FP32C && !(any_pml && bp.npml > 0)) res += al(9 * np * esz);
+    }
     // set-up arrays of one block: x, metric, J, material (FP64)
     transient = std::max(transient, al(3 * npd * 8) + al(9 * npd * 8) + al(npd * 8) + al(3 * npd * 8));
   }

@@ -243,7 +243,8 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
   const int q = q0 + tx, r = r0 + ty;
   const bool own = q < nq && r >= spr.own_lo && r < spr.own_hi;
   const int kq = sbp_kind(q, nq), kr = sbp_kind(r, nr);
-  // PML points hand their velocity gradient to the PML kernel (a.G)
+  // PML points (every point with the anelastic response) hand their
+  // velocity gradient to the correction kernels (a.G)
   const int npml = a.npml;
   const bool pml_qr = a.G != nullptr && ((a.pml[0] && q < npml) || (a.pml[1] && q >= nq - npml) ||
                                          (a.pml[2] && r < npml) || (a.pml[3] && r >= nr - npml));
@@ -491,7 +492,7 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
           }
         }
       }
-      if (a.G != nullptr && (pml_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))) {
+      if (a.G != nullptr && (a.anel || pml_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))) {
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll

@@ -789,7 +789,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 // and eta <- eta + B*dt*Deta.  Inside a PML slab the strain rates lose the
 // damped auxiliary fields (pml_damping_and_q, src/RHS_Interior.f90:
 // 2287-2387), so this kernel runs before the PML kernel advances Q.  The
-// velocity gradient is formed here with the block's operator.
+// velocity gradient comes from the TMA stencil (FP32C) or is formed here
+// with the block's operator.
 template <typename T, bool CURV, bool KAHAN, int FD>
 __global__ void __launch_bounds__(256) anelastic_kernel(const __grid_constant__ VolumeArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -805,22 +806,32 @@ __global__ void __launch_bounds__(256) anelastic_kernel(const __grid_constant__ 
   const T* __restrict__ coef = a.coef;
   const T Jinv = CURV ? coef[9 * np + p] : T(1);
   T g[3][3];
+  // the velocity gradient: from the TMA stencil of this stage (a.G), else
+  // formed here
+  if (a.G != nullptr) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    T o[3];
-    if (FD) diff_v_up<T>(F, np, p, idx[d], nn[d], st[d], o);
-    else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
-    const T rh = a.rh[d];
+    for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      if (CURV) {
+      for (int jj = 0; jj < 3; ++jj) g[c][jj] = a.G[(c * 3 + jj) * np + p];
+  }
+  if (a.G == nullptr) {
 #pragma unroll
-        for (int jj = 0; jj < 3; ++jj) {
-          const T m = coef[(d * 3 + jj) * np + p] * Jinv;
-          g[c][jj] = d == 0 ? m * (rh * o[c]) : g[c][jj] + m * (rh * o[c]);
+    for (int d = 0; d < 3; ++d) {
+      T o[3];
+      if (FD) diff_v_up<T>(F, np, p, idx[d], nn[d], st[d], o);
+      else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
+      const T rh = a.rh[d];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (CURV) {
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            const T m = coef[(d * 3 + jj) * np + p] * Jinv;
+            g[c][jj] = d == 0 ? m * (rh * o[c]) : g[c][jj] + m * (rh * o[c]);
+          }
+        } else {
+          g[c][d] = a.cart_metric[d] * rh * o[c];
         }
-      } else {
-        g[c][d] = a.cart_metric[d] * rh * o[c];
       }
     }
   }

@@ -13,7 +13,8 @@ arrays for wql_scenario_create_ex:
             Drucker-Prager viscoplasticity, depth-dependent stress, slip weakening
   upwind    2 x 76x101x151 Cartesian, upwind SBP-6, 12-point PML, locked
             interface, one moment-tensor point source (the block shapes of the
-            reference's PML study with the upwind operators)
+            reference's PML study with the upwind operators), optionally with
+            the anelastic response
 """
 import math
 
@@ -176,15 +177,16 @@ def config2(nq=401, nrs=201, steps=3000, seed=2239, npml=20):
     return text, media
 
 
-def upwind_pml12(steps=2000, nq=76, nr=101, ns=151):
+def upwind_pml12(steps=2000, nq=76, nr=101, ns=151, anelastic=False):
     """2 x nq x nr x ns Cartesian blocks, (0,0,0)-(15,20,30) and (15,0,0)-(30,20,30)
     km, the upwind SBP operators of order 6, a 12-point PML on every outer side
     but the y = 0 free surface, a locked interface at x = 15 km and one
     Cos-Bell moment-tensor source (M_xz = -10) at (5, 1.8, 5) km, order-4
-    discrete delta."""
+    discrete delta.  anelastic: response = 'anelastic' with c = 2, weight_exp =
+    0.6, fref = 1 Hz (the reference's PML study with attenuation)."""
     ext = (15.0, 20.0, 30.0)
     dt = dt_of((nq, nr, ns), ext)
-    extra = ",\n fd_type = 'upwind',\n order = 6"
+    extra = ",\n fd_type = 'upwind',\n order = 6" + (",\n response = 'anelastic'" if anelastic else "")
     text = _problem("upwind_pml12", "TPV5", "locked", "cartesian", (steps + 0.5) * dt, extra)
     n = (nq, nr, ns)
     text += "&block_list\n" + _block(1, n, (0.0, 0.0, 0.0), (15.0, 20.0, 30.0), (1, 2, 1), (0, 1, 1),
@@ -196,6 +198,8 @@ def upwind_pml12(steps=2000, nq=76, nr=101, ns=151):
              "'Cos-Bell' 0d0 0.2d0 0d0 0d0 0d0 0d0 -10d0 0d0 5d0 1.8d0 5d0 0\n"
              "!---end:tensor_listU---\n"
              "!---begin:tensor_listV---\n!---end:tensor_listV---\n")
+    if anelastic:
+        text += "&anelastic_list\n c = 2d0,\n weight_exp = 0.6d0,\n fref = 1d0 /\n"
     return text, None
 
 
