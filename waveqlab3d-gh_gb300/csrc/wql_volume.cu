@@ -781,6 +781,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 }
 
 // ---------------------------------------------------------------------------
+// three CTAs per SM: 80 registers, no spills (four would cap it at 64 and
+// spill)
+#ifndef WQL_ANEL_MINB
+#define WQL_ANEL_MINB 3
+#endif
 // Anelastic kernel (response = 'anelastic'; src/RHS_Interior.f90:2390-2509,
 // the interior terms of src/JU_xJU_yJU_z6.f90:16316-16346, src/fields.f90:
 // 61-68 and 122-129), one thread per point: the stress rates lose the sum
@@ -792,7 +797,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 // velocity gradient comes from the TMA stencil (FP32C) or is formed here
 // with the block's operator.
 template <typename T, bool CURV, bool KAHAN, int FD>
-__global__ void __launch_bounds__(256) anelastic_kernel(const __grid_constant__ VolumeArgs<T> a) {
+__global__ void __launch_bounds__(256, WQL_ANEL_MINB) anelastic_kernel(const __grid_constant__ VolumeArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
@@ -890,21 +895,28 @@ __global__ void __launch_bounds__(256) anelastic_kernel(const __grid_constant__ 
   T corr[9];
 #pragma unroll
   for (int c = 0; c < 9; ++c) corr[c] = T(0);
+  // the memory-variable streams do not overlap (restrict): a component's
+  // loads need not wait for the previous component's stores
+  T* __restrict__ eta = a.eta;
+  T* __restrict__ deta = a.Deta;
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
-    T ev[4];
+    T ev[1][4], dv[1][4];  // this component's four mechanisms
 #pragma unroll
-    for (int m = 0; m < 4; ++m) ev[m] = a.eta[(c * 4 + m) * np + p];
-    corr[3 + c] = -(ev[0] + ev[1] + ev[2] + ev[3]);
+    for (int m = 0; m < 4; ++m) {
+      ev[0][m] = eta[(c * 4 + m) * np + p];
+      dv[0][m] = deta[(c * 4 + m) * np + p];
+    }
+    corr[3 + c] = -(ev[0][0] + ev[0][1] + ev[0][2] + ev[0][3]);
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       const T w = (T)a.an_w[m];
       const T force = c < 3 ? (w * T(2) * mu * qs) * e[c] + (w * ((lam + T(2) * mu) * qp - T(2) * mu * qs)) * tr
                             : w * mu * qs * e[c];
       const long long q = (c * 4 + m) * np + p;
-      const T de = a.A * a.Deta[q] + (force - ev[m]) / (T)a.an_tau[m];
-      a.Deta[q] = de;
-      a.eta[q] = ev[m] + a.Bdt * de;
+      const T de = a.A * dv[0][m] + (force - ev[0][m]) / (T)a.an_tau[m];
+      deta[q] = de;
+      eta[q] = ev[0][m] + a.Bdt * de;
     }
   }
   add_correction<T, KAHAN>(a, p, corr);
