@@ -186,18 +186,23 @@ __device__ void boundary_sat(const R u[9], const double* __restrict__ face, long
 template <typename T, bool KAHAN>
 __device__ __forceinline__ void add_correction(const VolumeArgs<T>& a, long long p, const T (&corr)[9]) {
   const long long np = a.np;
+  // DF, F_out and C are distinct arrays: a component's loads need not wait
+  // for the previous component's stores
+  T* __restrict__ DF = a.DF;
+  T* __restrict__ Fo = a.Fout;
+  T* __restrict__ Ck = a.C;
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
     if (corr[c] == T(0)) continue;
-    a.DF[c * np + p] += corr[c];
-    const T f0 = a.Fout[c * np + p];
+    DF[c * np + p] += corr[c];
+    const T f0 = Fo[c * np + p];
     if (KAHAN) {
-      const T y = a.Bdt * corr[c] - a.C[c * np + p];
+      const T y = a.Bdt * corr[c] - Ck[c * np + p];
       const T t = f0 + y;
-      a.C[c * np + p] = (t - f0) - y;
-      a.Fout[c * np + p] = t;
+      Ck[c * np + p] = (t - f0) - y;
+      Fo[c * np + p] = t;
     } else {
-      a.Fout[c * np + p] = f0 + a.Bdt * corr[c];
+      Fo[c * np + p] = f0 + a.Bdt * corr[c];
     }
   }
 }

@@ -721,8 +721,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
     else if (axis == 1) sp = i + (long long)nq * ((hi ? ii - (n - npml) : ii) + (long long)npml * k);
     else sp = i + (long long)nq * (j + (long long)nr * (hi ? ii - (n - npml) : ii));
     const long long snp = a.slab_np[side];
-    T* Q = a.Q[side];
-    T* DQ = a.DQ[side];
+    T* __restrict__ Q = a.Q[side];
+    T* __restrict__ DQ = a.DQ[side];
     T qv[9];
     for (int c = 0; c < 9; ++c) qv[c] = Q[c * snp + sp];
     // per-axis split of the stress divergence along physical axis `axis`
