@@ -68,3 +68,21 @@ def test_anelastic_gradient_handoff(ctx, wqlmod, tmp_path, case, steps):
     f.sync(check_nan=True)
     for b in range(2):
         assert rel_l2(f.fields(b), g.fields(b)) < 1e-6
+
+
+def test_anelastic_in_batch_equals_alone(ctx, wqlmod, tmp_path):
+    """An anelastic scenario stepped in a packed batch (the batched TMA
+    stencil also hands it the gradient) gives the fields it gives alone."""
+    p = write(tmp_path, "a.in", case_text("an_pml_curv"))
+    q = write(tmp_path, "b.in", case_text("pml_curv"))
+    alone = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    alone.step(10)
+    a = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    b = wqlmod.Scenario(ctx, q, precision=wqlmod.FP32C)
+    bt = wqlmod.Batch(ctx)
+    bt.add(a)
+    bt.add(b)
+    bt.step(10)
+    for k in range(2):
+        assert np.array_equal(a.fields(k), alone.fields(k))
+    bt.close()

@@ -77,6 +77,21 @@ def test_footprint_estimate_host(wqlmod):
     assert wqlmod.estimate_device_bytes(pml, wqlmod.FP32C)[0] > r32
 
 
+def test_footprint_estimate_anelastic(wqlmod):
+    """The anelastic response adds its 48 memory-variable arrays and 1/Q per
+    block (and the FP32C gradient hand-off array when no PML holds one)."""
+    text = golden_in("test_rup_cart_fric")
+    an = text.replace("response = 'elastic'", "response = 'anelastic'") \
+        if "response = 'elastic'" in text else text.replace(" coupling", " response = 'anelastic',\n coupling", 1)
+    r32 = wqlmod.estimate_device_bytes(text, wqlmod.FP32C)[0]
+    a32 = wqlmod.estimate_device_bytes(an, wqlmod.FP32C)[0]
+    np_pts = 2 * 24 * 21 * 21  # two blocks, pitch 24 floats, 21 x 21 rows
+    assert a32 - r32 >= (2 * 24 + 1 + 9) * 4 * np_pts
+    r64 = wqlmod.estimate_device_bytes(text, wqlmod.FP64)[0]
+    a64 = wqlmod.estimate_device_bytes(an, wqlmod.FP64)[0]
+    assert a64 - r64 >= (2 * 24 + 1) * 8 * 2 * 22 * 21 * 21
+
+
 def _fractal_case(tmp_path, n=21):
     """The truth/2 curvilinear input with profile_type
     'read_from_memomry_fractal': a fault surface file of n*n rows (x, y, z),
