@@ -69,7 +69,7 @@ int wql_ctx_destroy(wql_ctx* ctx);
  * boundary codes, PML slabs, interface state (src/Interface_Condition.f90:
  * 2722-2850).  precision is WQL_FP64 or WQL_FP32C.  The difference operator
  * follows &problem_list fd_type (src/RHS_Interior.f90:31-125): 'traditional'
- * (SBP-6) or 'upwind' with order = 6; other operators return WQL_E_INPUT.
+ * (SBP-6) or 'upwind' with order = 5 or 6; other operators return WQL_E_INPUT.
  * response: 'elastic', 'plastic' (plastic_model = 'scec') or 'anelastic'
  * (&anelastic_list c, weight_exp 0 or 0.6, fref; src/material.f90:11-142). */
 int wql_scenario_create_from_in(wql_ctx* ctx, const char* in_path, int precision, wql_scn** out);

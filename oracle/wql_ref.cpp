@@ -407,26 +407,54 @@ const URow UMROW[6] = {  // D- (the same lines, stress parts)
 const wp UP_CF[7] = {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0};
 const wp UP_CB[7] = {1.0 / 60.0, -2.0 / 15.0, 1.0 / 2.0, -4.0 / 3.0, 7.0 / 12.0, 2.0 / 5.0, -1.0 / 30.0};
 
-// Row of D+ (plus = true) or D- at 1-based index i of n points.
-int stencil_up(bool plus, int i, int n, int* pt, wp* c) {
-  if (i >= 7 && i <= n - 6) {
-    const wp* cc = plus ? UP_CF : UP_CB;
-    const int o0 = plus ? -2 : -4;
-    for (int k = 0; k < 7; ++k) {
+// Order 5 (src/JU_xJU_yJU_z6.f90:2049-2677, 17364-17671): four closure
+// rows; interior D+ on points i-2..i+3, D- on i-3..i+2.
+const URow UP5ROW[4] = {  // D+ (velocity parts)
+    {4, {4, 3, 2, 1}, {-0.041832669322709, -0.374501992031873, 1.874501992031873, -1.458167330677291}},
+    {5, {5, 4, 3, 2, 1}, {0.026755852842809, -0.0958751393534, 0.627090301003345, -0.073578595317726, -0.484392419175028}},
+    {6, {6, 5, 4, 3, 2, 1}, {0.037914691943128, -0.28436018957346, 1.033965244865719, -0.274881516587678, -0.604265402843602, 0.091627172195893}},
+    {7, {7, 6, 5, 4, 3, 2, 1}, {0.032476319350474, -0.243572395128552, 0.974289580514208, -0.316644113667118, -0.44722598105548, -0.029769959404601, 0.030446549391069}},
+};
+const URow UM5ROW[4] = {  // D- (stress parts)
+    {4, {4, 3, 2, 1}, {-0.089641434262948, -0.231075697211155, 1.731075697211155, -1.410358565737052}},
+    {4, {4, 3, 2, 1}, {0.024526198439242, 0.426421404682274, 0.073578595317726, -0.524526198439242}},
+    {5, {5, 4, 3, 2, 1}, {-0.056872037914692, 0.522116903633491, 0.274881516587678, -0.888625592417062, 0.148499210110585}},
+    {6, {6, 5, 4, 3, 2, 1}, {-0.04871447902571, 0.487144790257104, 0.316644113667118, -0.885656292286874, 0.11637347767253, 0.014208389715832}},
+};
+const wp UP5_CF[6] = {0.05, -0.5, -1.0 / 3.00, 1.0, -0.25, 1.0 / 30.0};
+const wp UP5_CB[6] = {-1.0 / 30.0, 0.25, -1.0, 1.0 / 3.0, 0.5, -0.05};
+
+// Closure rows per end and interior-row limit of the upwind operator of an order.
+int up_rows(int order) { return order == 5 ? 4 : 6; }
+
+// Row of D+ (plus = true) or D- of the given order (5 or 6) at 1-based
+// index i of n points along axis ax (0..2).  Reference quirk, kept: on the
+// s axis the order-5 D+ row 4 weights point 7 with a default-real (single
+// precision) literal (src/JU_xJU_yJU_z6.f90:2558).
+int stencil_up(int order, bool plus, int i, int n, int* pt, wp* c, int ax = 0) {
+  const int R = up_rows(order);
+  if (i >= R + 1 && i <= n - R) {
+    const int m = order == 5 ? 6 : 7;
+    const wp* cc = order == 5 ? (plus ? UP5_CF : UP5_CB) : (plus ? UP_CF : UP_CB);
+    const int o0 = plus ? -2 : (order == 5 ? -3 : -4);
+    for (int k = 0; k < m; ++k) {
       pt[k] = i + o0 + k;
       c[k] = cc[k];
     }
-    return 7;
+    return m;
   }
-  if (i <= 6) {
-    const URow& r = (plus ? UPROW : UMROW)[i - 1];
+  const URow* PR = order == 5 ? UP5ROW : UPROW;
+  const URow* MR = order == 5 ? UM5ROW : UMROW;
+  if (i <= R) {
+    const URow& r = (plus ? PR : MR)[i - 1];
     for (int k = 0; k < r.n; ++k) {
       pt[k] = r.pt[k];
       c[k] = r.c[k];
     }
+    if (order == 5 && plus && ax == 2 && i == 4) c[0] = (wp)(float)0.032476319350474;
     return r.n;
   }
-  const URow& r = (plus ? UMROW : UPROW)[n - i];
+  const URow& r = (plus ? MR : PR)[n - i];
   for (int k = 0; k < r.n; ++k) {
     pt[k] = n + 1 - r.pt[k];
     c[k] = -r.c[k];
@@ -454,7 +482,8 @@ struct RBlock {
   int npml = 0;
   vector<wp> Q[7][9], DQ[7][9];    // full-size per active side
   wp tau0 = 0;
-  bool upwind = false;  // fd_type 'upwind', order 6
+  bool upwind = false;  // fd_type 'upwind', order 5 or 6
+  int up_order = 0;
   // response = 'anelastic' (src/datatypes.f90:38-50): four relaxation
   // mechanisms per stress component 4..9
   bool anelastic = false;
@@ -1216,7 +1245,8 @@ int init_block(Domain& D, int b, const Media& md) {
       }
   // src/block.f90:189-214
   B.upwind = D.P.fd_type == "upwind";
-  B.tau0 = B.upwind ? 42300.0 / 13613.0 : 1.0 / (0.315949074074074);
+  B.up_order = B.upwind ? D.P.order : 0;
+  B.tau0 = !B.upwind ? 1.0 / (0.315949074074074) : (B.up_order == 5 ? 720.0 / 251.0 : 42300.0 / 13613.0);
   return 0;
 }
 
@@ -1260,8 +1290,8 @@ void jju_x6_upwind(const RBlock& B, int x, int y, int z, const vector<wp>* Xm, w
   const int pos[3] = {x, y, z};
   wp* out[3] = {Jq, Jr, Js};
   for (int ax = 0; ax < 3; ++ax) {
-    const int mp = stencil_up(true, pos[ax], dims[ax], ptp, cp);
-    const int mm = stencil_up(false, pos[ax], dims[ax], ptm, cm);
+    const int mp = stencil_up(B.up_order, true, pos[ax], dims[ax], ptp, cp, ax);
+    const int mm = stencil_up(B.up_order, false, pos[ax], dims[ax], ptm, cm, ax);
     const vector<wp>& Xa = Xm[ax];
     const wp centre = Xa[B.id(x, y, z)];
     for (int comp = 0; comp < 9; ++comp) {
@@ -1407,13 +1437,16 @@ void anelastic_point(RBlock& B, size_t p, int x, int y, int z, const wp Ux[9], c
 }
 
 void interior_limits(const RBlock& B, int& ix, int& iy, int& iz, int& fx, int& fy, int& fz) {
-  ix = iy = iz = fx = fy = fz = 6;  // JU:16211-16226
-  if (B.pml[5]) iz = std::max(B.npml, 6);
-  if (B.pml[6]) fz = std::max(B.npml, 6);
-  if (B.pml[3]) iy = std::max(B.npml, 6);
-  if (B.pml[4]) fy = std::max(B.npml, 6);
-  if (B.pml[1]) ix = std::max(B.npml, 6);
-  if (B.pml[2]) fx = std::max(B.npml, 6);
+  // JU:16211-16226; 4 for the order-5 upwind operators (JU:17434-17446,
+  // src/RHS_Interior.f90:517-530)
+  const int L = B.up_order == 5 ? 4 : 6;
+  ix = iy = iz = fx = fy = fz = L;
+  if (B.pml[5]) iz = std::max(B.npml, L);
+  if (B.pml[6]) fz = std::max(B.npml, L);
+  if (B.pml[3]) iy = std::max(B.npml, L);
+  if (B.pml[4]) fy = std::max(B.npml, L);
+  if (B.pml[1]) ix = std::max(B.npml, L);
+  if (B.pml[2]) fx = std::max(B.npml, L);
 }
 
 // JJU_x6_interior: src/JU_xJU_yJU_z6.f90:16141-16449 (elastic, no anelastic terms)
@@ -1505,10 +1538,16 @@ void rhs_interior(RBlock& B, bool cart) {
 void rhs_interior_upwind(RBlock& B, bool cart) {
   int ix, iy, iz, fx, fy, fz;
   interior_limits(B, ix, iy, iz, fx, fy, fz);
+  // order 6: s = -2..4, stresses at s-2; order 5 (JU:17364-17671): s = -2..3,
+  // stresses at s-1
+  const bool o5 = B.up_order == 5;
+  const int shi = o5 ? 3 : 4, bsh = o5 ? 1 : 2;
+  const wp* CF = o5 ? UP5_CF : UP_CF;
+  const wp* CB = o5 ? UP5_CB : UP_CB;
   wp cfx[7], cfy[7], cfz[7], cbx[7], cby[7], cbz[7];
-  for (int k = 0; k < 7; ++k) {
-    cfx[k] = UP_CF[k] / B.hq; cfy[k] = UP_CF[k] / B.hr; cfz[k] = UP_CF[k] / B.hs;
-    cbx[k] = UP_CB[k] / B.hq; cby[k] = UP_CB[k] / B.hr; cbz[k] = UP_CB[k] / B.hs;
+  for (int k = 0; k <= shi + 2; ++k) {
+    cfx[k] = CF[k] / B.hq; cfy[k] = CF[k] / B.hr; cfz[k] = CF[k] / B.hs;
+    cbx[k] = CB[k] / B.hq; cby[k] = CB[k] / B.hr; cbz[k] = CB[k] / B.hs;
   }
   const int nx = B.nq, ny = B.nr, nz = B.ns;
 #pragma omp parallel for schedule(static)
@@ -1519,10 +1558,10 @@ void rhs_interior_upwind(RBlock& B, bool cart) {
           continue;
         const size_t p = B.id(x, y, z);
         wp DFx[9] = {0}, DFy[9] = {0}, DFz[9] = {0};
-        for (int s = -2; s <= 4; ++s) {
+        for (int s = -2; s <= shi; ++s) {
           const int k = s + 2;
           const size_t xf = B.id(x + s, y, z), yf = B.id(x, y + s, z), zf = B.id(x, y, z + s);
-          const size_t xb = B.id(x + s - 2, y, z), yb = B.id(x, y + s - 2, z), zb = B.id(x, y, z + s - 2);
+          const size_t xb = B.id(x + s - bsh, y, z), yb = B.id(x, y + s - bsh, z), zb = B.id(x, y, z + s - bsh);
           if (!cart) {
             const vector<wp>* Ms[3] = {B.mx, B.my, B.mz};
             wp* Ds[3] = {DFx, DFy, DFz};
@@ -2283,7 +2322,7 @@ int wqlref_fd_matrix(int fd, int plus, int n, double* D) {
   wp c[10];
   for (size_t k = 0; k < (size_t)n * n; ++k) D[k] = 0.0;
   for (int i = 1; i <= n; ++i) {
-    const int m = fd ? stencil_up(plus != 0, i, n, pt, c) : stencil(i, n, pt, c);
+    const int m = fd ? stencil_up(fd == 2 ? 5 : 6, plus != 0, i, n, pt, c) : stencil(i, n, pt, c);
     for (int t = 0; t < m; ++t) D[(size_t)(i - 1) * n + (pt[t] - 1)] += c[t];
   }
   return 0;
@@ -2337,7 +2376,7 @@ static void* create_domain(Domain* D, const Media& md) {
   // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator, or the
   // upwind operators of order 6 (the other orders and the DRP variants are
   // not restated)
-  if (!(D->P.fd_type == "traditional" || (D->P.fd_type == "upwind" && D->P.order == 6))) {
+  if (!(D->P.fd_type == "traditional" || (D->P.fd_type == "upwind" && (D->P.order == 5 || D->P.order == 6)))) {
     std::snprintf(g_err, sizeof(g_err), "fd_type %s with order %d is not restated", D->P.fd_type.c_str(), D->P.order);
     delete D;
     return nullptr;

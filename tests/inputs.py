@@ -91,9 +91,11 @@ def case_text(name):
         base = case_text(name.split("_", 1)[1])
         base = base.replace(" w_stride = 1,", " w_stride = 1,\n response = 'anelastic',", 1)
         return base + f"&anelastic_list\n c = {c},\n weight_exp = {wexp},\n fref = 1d0 /\n"
-    if name.startswith("up_"):
-        # the upwind operators of order 6 (fd_type = 'upwind')
-        return case_text(name[3:]).replace(" w_stride = 1,", " w_stride = 1,\n fd_type = 'upwind',\n order = 6,", 1)
+    if name.startswith(("up_", "up5_")):
+        # the upwind operators of order 6 or 5 (fd_type = 'upwind')
+        order = 5 if name.startswith("up5_") else 6
+        return case_text(name.split("_", 1)[1]).replace(
+            " w_stride = 1,", f" w_stride = 1,\n fd_type = 'upwind',\n order = {order},", 1)
     if name in MT_CASES:
         mesh, order, mollify, lists = MT_CASES[name]
         extra = ",\n mollify_source = T" if mollify else ""

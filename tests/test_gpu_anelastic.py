@@ -29,7 +29,8 @@ def wqlmod():
 
 
 @pytest.mark.parametrize("case,steps", [("an_pml", 30), ("an_pml_curv", 20), ("an_mt4", 30),
-                                        ("an0_mt4_curv", 20), ("an_up_pml", 30), ("an_up_mt4_curv", 20)])
+                                        ("an0_mt4_curv", 20), ("an_up_pml", 30), ("an_up_mt4_curv", 20),
+                                        ("an_up5_pml", 30)])
 def test_anelastic_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, steps):
     p = write(tmp_path, case + ".in", case_text(case))
     s, o = run_pair(wqlmod, oracle_lib, ctx, p, steps)

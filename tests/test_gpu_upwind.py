@@ -1,4 +1,4 @@
-"""The upwind SBP operators of order 6 (fd_type = 'upwind', order = 6) on the
+"""The upwind SBP operators of orders 6 and 5 (fd_type = 'upwind') on the
 GPU against the oracle: FP64 fields to 1e-11 relative L2 (rate and state to
 its solver tolerance), and the FP32-compensated mode against FP64 to 1e-5."""
 import numpy as np
@@ -28,23 +28,25 @@ def wqlmod():
 
 
 @pytest.mark.parametrize("case,steps", [("up_pml", 40), ("up_pml_curv", 20), ("up_plastic", 46),
-                                        ("up_rs_curv", 20), ("up_mt4", 30), ("up_mt4_curv", 20)])
+                                        ("up_rs_curv", 20), ("up_mt4", 30), ("up_mt4_curv", 20),
+                                        ("up5_pml", 40), ("up5_pml_curv", 20), ("up5_mt4_curv", 20)])
 def test_upwind_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, steps):
     p = write(tmp_path, case + ".in", case_text(case))
     s, o = run_pair(wqlmod, oracle_lib, ctx, p, steps)
     errs = field_errors(s, o)
-    if case.startswith("up_rs"):
+    if "_rs" in case:
         for b in range(2):
             assert rs_close(s.fields(b), o.fields(b)), errs
     else:
         assert max(errs) < TOL, errs
     # and the run differs from the traditional operator's
-    t = wqlmod.Scenario(ctx, write(tmp_path, "t.in", case_text(case[3:])))
+    t = wqlmod.Scenario(ctx, write(tmp_path, "t.in", case_text(case.split("_", 1)[1])))
     t.step(steps)
     assert rel_l2(t.fields(0), s.fields(0)) > 1e-6
 
 
-@pytest.mark.parametrize("case,steps", [("up_pml", 40), ("up_pml_curv", 20), ("up_mt4_curv", 20)])
+@pytest.mark.parametrize("case,steps", [("up_pml", 40), ("up_pml_curv", 20), ("up_mt4_curv", 20),
+                                        ("up5_pml_curv", 20)])
 def test_upwind_fp32c_vs_fp64(ctx, wqlmod, tmp_path, case, steps):
     p = write(tmp_path, case + ".in", case_text(case))
     d = wqlmod.Scenario(ctx, p, precision=wqlmod.FP64)
@@ -105,6 +107,6 @@ def test_upwind_in_batch_equals_alone(ctx, wqlmod, tmp_path):
 
 
 def test_upwind_other_orders_rejected(ctx, wqlmod, tmp_path):
-    p = write(tmp_path, "u5.in", case_text("up_pml").replace("order = 6", "order = 5"))
-    with pytest.raises(Exception, match="order = 6"):
+    p = write(tmp_path, "u4.in", case_text("up_pml").replace("order = 6", "order = 4"))
+    with pytest.raises(Exception, match="order = 5 or 6"):
         wqlmod.Scenario(ctx, p)

@@ -1,5 +1,5 @@
-"""The oracle's upwind SBP operators of order 6 (fd_type = 'upwind',
-src/JU_xJU_yJU_z6.f90:2680-3706, 17675-17983).  The reference holds no
+"""The oracle's upwind SBP operators of orders 6 and 5 (fd_type = 'upwind',
+src/JU_xJU_yJU_z6.f90:2680-3706, 17675-17983; 2049-2677, 17364-17671).  The reference holds no
 output of an upwind run, so the transcribed closure rows are pinned by the
 properties that define the operators: the upwind summation-by-parts
 identity H D+ + (H D-)^T = diag(-1, 0, ..., 0, 1) with a positive diagonal
@@ -81,6 +81,31 @@ def test_upwind_run_near_traditional(oracle_lib):
 
 
 def test_upwind_other_orders_rejected(oracle_lib):
-    text = case_text("up_pml").replace("order = 6", "order = 5")
+    text = case_text("up_pml").replace("order = 6", "order = 4")
     with pytest.raises(Exception, match="not restated"):
         oracle_lib.Oracle(text=text)
+
+
+@pytest.mark.parametrize("n", [12, 30])
+def test_upwind5_summation_by_parts(oracle_lib, n):
+    """Order 5: the same identity with h11 = 251/720 = 1/tau0, exactness of
+    degree 2 at the closures and 5 inside, one-sided reach of 3 points."""
+    Dp = oracle_lib.fd_matrix(2, True, n)
+    Dm = oracle_lib.fd_matrix(2, False, n)
+    h, res = _norm(Dp, Dm)
+    assert res < 1e-13 and (h > 0).all()
+    assert abs(h[0] - 251.0 / 720.0) < 1e-12
+    x = np.arange(n, dtype=np.float64)
+    for D in (Dp, Dm):
+        for deg in range(6):
+            f = x ** deg
+            df = deg * x ** (deg - 1) if deg else np.zeros(n)
+            err = np.abs(D @ f - df)
+            scale = max(1.0, np.abs(df).max())
+            assert err[4:-4].max() < 1e-11 * scale
+            if deg <= 2:
+                assert err.max() < 1e-11 * scale
+    nz = np.nonzero(Dp[n // 2])[0] - n // 2
+    assert (nz.min(), nz.max()) == (-2, 3)
+    nz = np.nonzero(Dm[n // 2])[0] - n // 2
+    assert (nz.min(), nz.max()) == (-3, 2)

@@ -148,7 +148,7 @@ struct wql_scn {
   double stage_t0 = 0.0;
   int stage_launches = 0;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
-  int fd = 0;              // 0: traditional SBP-6; 1: upwind SBP-6
+  int fd = 0;              // 0: traditional SBP-6; 1: upwind order 6; 2: upwind order 5
   bool anel = false;       // response = 'anelastic'
   double an_tau[4] = {}, an_w[4] = {};
   int schunk = 0;          // planes per CTA along s (0: default)
@@ -538,7 +538,7 @@ int setup_block(wql_scn* S, int b) {
   // to the anelastic kernel
   if (S->prec == WQL_FP32C && S->anel && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   // src/block.f90:189-214
-  const double tau0 = S->fd ? kTau0Upwind6 : 1.0 / (0.315949074074074);
+  const double tau0 = S->fd == 1 ? kTau0Upwind6 : (S->fd == 2 ? kTau0Upwind5 : 1.0 / (0.315949074074074));
   const int dims[3] = {B.nq, B.nr, B.ns};
   for (int d = 0; d < 3; ++d) B.tau_h[d] = tau0 / (1.0 / (double)(dims[d] - 1));
   // depth coordinate for the plastic update
@@ -702,9 +702,10 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator or the
   // upwind operators of order 6
   if (Pr.fd_type == "upwind" && Pr.order == 6) S->fd = 1;
+  else if (Pr.fd_type == "upwind" && Pr.order == 5) S->fd = 2;
   else if (Pr.fd_type != "traditional")
     return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' with order " + std::to_string(Pr.order) +
-                                 " is not supported (traditional SBP-6, or upwind with order = 6)");
+                                 " is not supported (traditional SBP-6, or upwind with order = 5 or 6)");
   if (Pr.response == "anelastic") {
     // init_anelastic_properties (src/material.f90:85-115): relaxation times
     // and weights exist for weight_exp 0 and 0.6 only

@@ -60,7 +60,7 @@ struct VolumeArgs {
   // written by the TMA stencil kernel and read by the PML kernel of the same
   // stage; nullptr where the PML kernel forms it itself
   T* G;
-  int fd;             // difference operator: 0 SBP-6 central, 1 upwind SBP-6 (D+ on v, D- on fluxes)
+  int fd;             // difference operator: 0 SBP-6 central; upwind pair (D+ on v, D- on fluxes) of order 6 (1) or 5 (2)
   int kernel;         // stencil variant: 0 default, 1 per-point, 2..4 tiled
   int schunk;         // planes per CTA along s for the tiled kernel (0: default)
   // RK

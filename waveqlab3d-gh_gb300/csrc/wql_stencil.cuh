@@ -85,6 +85,54 @@ __device__ __forceinline__ void up_entry(int kind, int t, T& wv, T& wf, int& off
 // Interior weights of D+ on offsets -2..4 (D- at offset o is -UP_CF[2-o]).
 #define WQL_UP_CF {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0}
 
+// The upwind pair of a kernel's operator FD (1: order 6, 2: order 5):
+// closure rows R per end, closure columns NCOL, interior D+ offsets
+// -2..PHI (D- offsets -PHI..2).
+__constant__ double c_up5_d[2][4][7] = WQL_UP5_TABLE;
+__constant__ float c_up5_f[2][4][7] = WQL_UP5_TABLE;
+template <int FD>
+struct UpOp {
+  static constexpr int R = FD == 2 ? 4 : 6, NCOL = FD == 2 ? 7 : 10, PHI = FD == 2 ? 3 : 4;
+};
+template <int FD>
+__device__ __forceinline__ int up_kind(int i, int n) {
+  constexpr int R = UpOp<FD>::R;
+  if (i < R) return -(i + 1);
+  if (i >= n - R) return n - i;
+  return 0;
+}
+template <typename T, int FD>
+__device__ __forceinline__ T upw(int op, int row, int col) {
+  if (FD == 2) return sizeof(T) == 8 ? (T)c_up5_d[op][row][col] : (T)c_up5_f[op][row][col];
+  return up_w<T>(op, row, col);
+}
+// Interior D+ weight at offset o (-2..PHI).
+template <typename T, int FD>
+__device__ __forceinline__ T up_cf(int o) {
+  if (FD == 2) {
+    const T cf[6] = WQL_UP5_CF;
+    return cf[o + 2];
+  }
+  const T cf[7] = WQL_UP_CF;
+  return cf[o + 2];
+}
+// Closure entry t (0..NCOL-1) of operator FD on axis ax, as up_entry.
+template <typename T, int FD>
+__device__ __forceinline__ void upx_entry(int kind, int t, int ax, T& wv, T& wf, int& off) {
+  if (kind < 0) {
+    const int i = -kind - 1;
+    wv = upw<T, FD>(0, i, t);
+    wf = upw<T, FD>(1, i, t);
+    off = t - i;
+    if (FD == 2 && ax == 2 && i == 3 && t == 6) wv = (T)WQL_UP5_S_ROW4_P7;
+  } else {
+    const int k = kind - 1;
+    wv = -upw<T, FD>(1, k, t);
+    wf = -upw<T, FD>(0, k, t);
+    off = k - t;
+  }
+}
+
 struct TileSpan {
   int origin, own_lo, own_hi;
 };

@@ -171,45 +171,33 @@ __device__ void diff_pml_flux(const T* __restrict__ F, const T* __restrict__ coe
 // the velocities, D- on the fluxes.  Interior D+ weights on offsets -2..4
 // and D- weights on offsets -4..2; the closure rows of both operators cover
 // the same columns, so one load per column serves both.
-template <typename T, bool CURV>
+template <typename T, bool CURV, int FD>
 __device__ __forceinline__ void diff6_up(const T* __restrict__ F, const T* __restrict__ coef, long long np,
                                          long long p, int i, int n, long long st, int d, T r[6]) {
+  constexpr int PHI = UpOp<FD>::PHI, NCOL = UpOp<FD>::NCOL;
   T t[6];
 #pragma unroll
   for (int c = 0; c < 6; ++c) r[c] = T(0);
-  const int kind = sbp_kind(i, n);
+  const int kind = up_kind<FD>(i, n);
   if (kind == 0) {
-    const T cf[7] = WQL_UP_CF;
 #pragma unroll
-    for (int o = -4; o <= 4; ++o) {
+    for (int o = -PHI; o <= PHI; ++o) {
       load6<T, CURV>(F, coef, np, p + o * st, d, t);
       if (o >= -2)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) r[c] += cf[o + 2] * t[c];
+        for (int c = 0; c < 3; ++c) r[c] += up_cf<T, FD>(o) * t[c];
       if (o <= 2)
 #pragma unroll
-        for (int c = 3; c < 6; ++c) r[c] -= cf[2 - o] * t[c];
-    }
-  } else if (kind < 0) {
-    const int row = -kind - 1;
-    const long long p0 = p - (long long)i * st;
-    for (int col = 0; col < 10; ++col) {
-      const T wv = up_w<T>(0, row, col), wf = up_w<T>(1, row, col);
-      if (wv != T(0) || wf != T(0)) {
-        load6<T, CURV>(F, coef, np, p0 + col * st, d, t);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) r[c] += wv * t[c];
-#pragma unroll
-        for (int c = 3; c < 6; ++c) r[c] += wf * t[c];
-      }
+        for (int c = 3; c < 6; ++c) r[c] -= up_cf<T, FD>(-o) * t[c];
     }
   } else {
-    const int row = kind - 1;
-    const long long pn = p + (long long)(n - 1 - i) * st;
-    for (int col = 0; col < 10; ++col) {
-      const T wv = -up_w<T>(1, row, col), wf = -up_w<T>(0, row, col);
+    const long long base = kind < 0 ? p - (long long)i * st : p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < NCOL; ++col) {
+      T wv, wf;
+      int off;
+      upx_entry<T, FD>(kind, col, d, wv, wf, off);
       if (wv != T(0) || wf != T(0)) {
-        load6<T, CURV>(F, coef, np, pn - col * st, d, t);
+        load6<T, CURV>(F, coef, np, base + (kind < 0 ? col : -col) * st, d, t);
 #pragma unroll
         for (int c = 0; c < 3; ++c) r[c] += wv * t[c];
 #pragma unroll
@@ -219,67 +207,54 @@ __device__ __forceinline__ void diff6_up(const T* __restrict__ F, const T* __res
   }
 }
 
-// D+ of the three velocities only.
-template <typename T>
+// D+ of the three velocities only, along axis d.
+template <typename T, int FD>
 __device__ __forceinline__ void diff_v_up(const T* __restrict__ F, long long np, long long p, int i, int n,
-                                          long long st, T r[3]) {
+                                          long long st, int d, T r[3]) {
+  constexpr int PHI = UpOp<FD>::PHI, NCOL = UpOp<FD>::NCOL;
   r[0] = r[1] = r[2] = T(0);
-  const int kind = sbp_kind(i, n);
+  const int kind = up_kind<FD>(i, n);
   if (kind == 0) {
-    const T cf[7] = WQL_UP_CF;
 #pragma unroll
-    for (int o = -2; o <= 4; ++o)
+    for (int o = -2; o <= PHI; ++o)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) r[c] += cf[o + 2] * F[c * np + p + o * st];
-  } else if (kind < 0) {
-    const int row = -kind - 1;
-    const long long p0 = p - (long long)i * st;
-    for (int col = 0; col < 10; ++col) {
-      const T w = up_w<T>(0, row, col);
-      if (w != T(0))
-#pragma unroll
-        for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + p0 + col * st];
-    }
+      for (int c = 0; c < 3; ++c) r[c] += up_cf<T, FD>(o) * F[c * np + p + o * st];
   } else {
-    const int row = kind - 1;
-    const long long pn = p + (long long)(n - 1 - i) * st;
-    for (int col = 0; col < 10; ++col) {
-      const T w = -up_w<T>(1, row, col);
-      if (w != T(0))
+    const long long base = kind < 0 ? p - (long long)i * st : p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < NCOL; ++col) {
+      T wv, wf;
+      int off;
+      upx_entry<T, FD>(kind, col, d, wv, wf, off);
+      if (wv != T(0))
 #pragma unroll
-        for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + pn - col * st];
+        for (int c = 0; c < 3; ++c) r[c] += wv * F[c * np + base + (kind < 0 ? col : -col) * st];
     }
   }
 }
 
 // D- of the three fluxes J*metric_j(d)*sigma_{c,j} (PML split, as
 // diff_pml_flux).
-template <typename T>
+template <typename T, int FD>
 __device__ void diff_pml_flux_up(const T* __restrict__ F, const T* __restrict__ coef, long long np, long long p,
                                  int i, int n, long long st, int d, int j, T r[3]) {
+  constexpr int PHI = UpOp<FD>::PHI, NCOL = UpOp<FD>::NCOL;
   r[0] = r[1] = r[2] = T(0);
-  const int kind = sbp_kind(i, n);
+  const int kind = up_kind<FD>(i, n);
   auto acc = [&](long long q, T w) {
     const T a = coef[(d * 3 + j) * np + q];
 #pragma unroll
     for (int c = 0; c < 3; ++c) r[c] += w * (a * F[sig(c, j) * np + q]);
   };
   if (kind == 0) {
-    const T cf[7] = WQL_UP_CF;
-    for (int o = -4; o <= 2; ++o) acc(p + o * st, -cf[2 - o]);
-  } else if (kind < 0) {
-    const int row = -kind - 1;
-    const long long p0 = p - (long long)i * st;
-    for (int col = 0; col < 10; ++col) {
-      const T w = up_w<T>(1, row, col);
-      if (w != T(0)) acc(p0 + col * st, w);
-    }
+#pragma unroll
+    for (int o = -PHI; o <= 2; ++o) acc(p + o * st, -up_cf<T, FD>(-o));
   } else {
-    const int row = kind - 1;
-    const long long pn = p + (long long)(n - 1 - i) * st;
-    for (int col = 0; col < 10; ++col) {
-      const T w = -up_w<T>(0, row, col);
-      if (w != T(0)) acc(pn - col * st, w);
+    const long long base = kind < 0 ? p - (long long)i * st : p + (long long)(n - 1 - i) * st;
+    for (int col = 0; col < NCOL; ++col) {
+      T wv, wf;
+      int off;
+      upx_entry<T, FD>(kind, col, d, wv, wf, off);
+      if (wf != T(0)) acc(base + (kind < 0 ? col : -col) * st, wf);
     }
   }
 }
@@ -288,7 +263,7 @@ __device__ void diff_pml_flux_up(const T* __restrict__ F, const T* __restrict__ 
 template <typename T, bool CURV, int FD>
 __device__ __forceinline__ void diff6_op(const T* __restrict__ F, const T* __restrict__ coef, long long np,
                                          long long p, int i, int n, long long st, int d, T r[6]) {
-  if (FD) diff6_up<T, CURV>(F, coef, np, p, i, n, st, d, r);
+  if (FD) diff6_up<T, CURV, FD ? FD : 1>(F, coef, np, p, i, n, st, d, r);
   else diff6<T, CURV>(F, coef, np, p, i, n, st, d, r);
 }
 
@@ -678,7 +653,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T o[3];
-      if (FD) diff_v_up<T>(F, np, p, idx[d], nn[d], st[d], o);
+      if (FD) diff_v_up<T, FD ? FD : 1>(F, np, p, idx[d], nn[d], st[d], d, o);
       else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
       const T rh = a.rh[d];
       for (int c = 0; c < 3; ++c) {
@@ -732,7 +707,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         T r3[3];
-        if (FD) diff_pml_flux_up<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
+        if (FD) diff_pml_flux_up<T, FD ? FD : 1>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
         else diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
         for (int c = 0; c < 3; ++c) acc3[c] += a.rh[d] * r3[c];
       }
@@ -823,7 +798,7 @@ __global__ void __launch_bounds__(256, WQL_ANEL_MINB) anelastic_kernel(const __g
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T o[3];
-      if (FD) diff_v_up<T>(F, np, p, idx[d], nn[d], st[d], o);
+      if (FD) diff_v_up<T, FD ? FD : 1>(F, np, p, idx[d], nn[d], st[d], d, o);
       else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
       const T rh = a.rh[d];
 #pragma unroll
@@ -1111,8 +1086,9 @@ int effective_variant(const VolumeArgs<T>& a) {
   int v = a.kernel != 0 ? a.kernel : (f32 ? 5 : 2);
   if ((v == 5 || v == 6) && !f32) v = 2;
   if (a.fd) {
-    // the upwind pair: the TMA kernel (compensated FP32) or per point
-    if (!(v == 5 || v == 6) || a.C == nullptr || !tiles_ok_up(a.nr, kTmaTR)) v = 1;
+    // the order-6 upwind pair: the TMA kernel (compensated FP32) or per
+    // point; order 5 per point
+    if (a.fd != 1 || !(v == 5 || v == 6) || a.C == nullptr || !tiles_ok_up(a.nr, kTmaTR)) v = 1;
     return v;
   }
   if ((v == 5 || v == 6) && !tiles_ok(a.nr, kTmaTR)) v = 1;
@@ -1137,7 +1113,8 @@ void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
   switch (v) {
     case 1: {
       dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
-      if (a.fd) stencil_kernel_pointwise<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a, 0);
+      if (a.fd == 1) stencil_kernel_pointwise<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a, 0);
+      else if (a.fd == 2) stencil_kernel_pointwise<T, CURV, KAHAN, 2><<<grd, blk, 0, s>>>(a, 0);
       else stencil_kernel_pointwise<T, CURV, KAHAN, 0><<<grd, blk, 0, s>>>(a, 0);
       return;
     }
@@ -1159,7 +1136,8 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
   int n = 0;
   dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
   if (a.anel) {  // before the PML kernel: it reads Q of the stage's input
-    if (a.fd) anelastic_kernel<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a);
+    if (a.fd == 1) anelastic_kernel<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a);
+    else if (a.fd == 2) anelastic_kernel<T, CURV, KAHAN, 2><<<grd, blk, 0, s>>>(a);
     else anelastic_kernel<T, CURV, KAHAN, 0><<<grd, blk, 0, s>>>(a);
     ++n;
   }
@@ -1167,7 +1145,8 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
     const PmlBoxes bx = pml_boxes(a);
     const unsigned nblk = (unsigned)((bx.start[bx.n] + 255) / 256);
     if (bx.start[bx.n] > 0) {
-      if (a.fd) pml_kernel<T, CURV, KAHAN, 1><<<nblk, 256, 0, s>>>(a, bx);
+      if (a.fd == 1) pml_kernel<T, CURV, KAHAN, 1><<<nblk, 256, 0, s>>>(a, bx);
+      else if (a.fd == 2) pml_kernel<T, CURV, KAHAN, 2><<<nblk, 256, 0, s>>>(a, bx);
       else pml_kernel<T, CURV, KAHAN, 0><<<nblk, 256, 0, s>>>(a, bx);
     }
     ++n;
