@@ -123,3 +123,62 @@ def test_fault_profile_file(wqlmod, tmp_path):
     (tmp_path / "fault.dat").write_text("1 2 3\n")
     with pytest.raises(wqlmod.WqlError):
         wqlmod.write_block_grids(text, out, base_dir=tmp_path)
+
+
+_TABLE_PROBE = r"""
+#include <cstdio>
+#include "wql_sbp.cuh"
+// Dense n x n matrices of the library's upwind pair of one order from its
+// tables: left closure rows, right rows as the negated mirror images of the
+// other operator's left rows, interior rows from the interior weights.
+int main() {
+  const double t6[2][6][10] = WQL_UP_TABLE;
+  const double t5[2][4][7] = WQL_UP5_TABLE;
+  const double c6[7] = WQL_UP_CF, c5[6] = WQL_UP5_CF;
+  const int n = 30;
+  for (int order = 6; order >= 5; --order) {
+    const int R = order == 6 ? 6 : 4, NC = order == 6 ? 10 : 7, PHI = order == 6 ? 4 : 3;
+    for (int op = 0; op < 2; ++op) {
+      static double D[30][30];
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) D[i][j] = 0.0;
+      for (int i = 0; i < n; ++i) {
+        if (i < R) {
+          for (int c = 0; c < NC; ++c) D[i][c] = order == 6 ? t6[op][i][c] : t5[op][i][c];
+        } else if (i >= n - R) {
+          const int k = n - 1 - i;
+          for (int c = 0; c < NC; ++c) D[i][n - 1 - c] = -(order == 6 ? t6[1 - op][k][c] : t5[1 - op][k][c]);
+        } else {
+          for (int o = -PHI; o <= PHI; ++o) {
+            const double* cf = order == 6 ? c6 : c5;
+            if (op == 0 && o >= -2) D[i][i + o] = cf[o + 2];
+            if (op == 1 && o <= 2) D[i][i + o] = -cf[2 - o];
+          }
+        }
+      }
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) std::printf("%.17g\n", D[i][j]);
+    }
+  }
+  return 0;
+}
+"""
+
+
+def test_library_upwind_tables_match_oracle(oracle_lib, tmp_path):
+    """The library's transcription of the upwind tables (wql_sbp.cuh, read by
+    the kernels) against the oracle's, row by row, for orders 6 and 5."""
+    import os
+    import subprocess
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "waveqlab3d-gh_gb300", "csrc")
+    src = tmp_path / "probe.cpp"
+    src.write_text(_TABLE_PROBE)
+    exe = tmp_path / "probe"
+    subprocess.run(["g++", "-std=c++17", "-O0", "-I" + csrc, str(src), "-o", str(exe)], check=True)
+    vals = np.array([float(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.split()])
+    mats = vals.reshape(4, 30, 30)
+    ref = [oracle_lib.fd_matrix(1, True, 30), oracle_lib.fd_matrix(1, False, 30),
+           oracle_lib.fd_matrix(2, True, 30), oracle_lib.fd_matrix(2, False, 30)]
+    for got, want in zip(mats, ref):
+        assert np.abs(got - want).max() < 1e-15

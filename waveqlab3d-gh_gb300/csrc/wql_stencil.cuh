@@ -82,8 +82,6 @@ __device__ __forceinline__ void up_entry(int kind, int t, T& wv, T& wf, int& off
   }
 }
 
-// Interior weights of D+ on offsets -2..4 (D- at offset o is -UP_CF[2-o]).
-#define WQL_UP_CF {1.0 / 30.0, -2.0 / 5.0, -7.0 / 12.0, 4.0 / 3.0, -1.0 / 2.0, 2.0 / 15.0, -1.0 / 60.0}
 
 // The upwind pair of a kernel's operator FD (1: order 6, 2: order 5):
 // closure rows R per end, closure columns NCOL, interior D+ offsets
