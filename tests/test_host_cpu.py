@@ -127,6 +127,7 @@ def test_fault_profile_file(wqlmod, tmp_path):
 
 _TABLE_PROBE = r"""
 #include <cstdio>
+#include <cstdlib>
 #include "wql_sbp.cuh"
 // Dense n x n matrices of the library's upwind pair of one order from its
 // tables: left closure rows, right rows as the negated mirror images of the
@@ -160,14 +161,27 @@ int main() {
         for (int j = 0; j < n; ++j) std::printf("%.17g\n", D[i][j]);
     }
   }
+  // the central SBP-6 operator: closure rows, right rows as their negated
+  // mirror images, interior (kC1, kC2, kC3)
+  const double ts[6][9] = WQL_SBP_TABLE;
+  const double cc[3] = {wql::kC1, wql::kC2, wql::kC3};
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double w = 0.0;
+      if (i < 6) w = j < 9 ? ts[i][j] : 0.0;
+      else if (i >= n - 6) w = (n - 1 - j) < 9 ? -ts[n - 1 - i][n - 1 - j] : 0.0;
+      else if (j != i && std::abs(j - i) <= 3) w = (j > i ? 1.0 : -1.0) * cc[std::abs(j - i) - 1];
+      std::printf("%.17g\n", w);
+    }
   return 0;
 }
 """
 
 
 def test_library_upwind_tables_match_oracle(oracle_lib, tmp_path):
-    """The library's transcription of the upwind tables (wql_sbp.cuh, read by
-    the kernels) against the oracle's, row by row, for orders 6 and 5."""
+    """The library's transcription of the operator tables (wql_sbp.cuh, read
+    by the kernels) against the oracle's, row by row: the upwind pairs of
+    orders 6 and 5 and the central SBP-6 operator."""
     import os
     import subprocess
     csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "waveqlab3d-gh_gb300", "csrc")
@@ -177,8 +191,9 @@ def test_library_upwind_tables_match_oracle(oracle_lib, tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O0", "-I" + csrc, str(src), "-o", str(exe)], check=True)
     vals = np.array([float(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
                                                        text=True).stdout.split()])
-    mats = vals.reshape(4, 30, 30)
+    mats = vals.reshape(5, 30, 30)
     ref = [oracle_lib.fd_matrix(1, True, 30), oracle_lib.fd_matrix(1, False, 30),
-           oracle_lib.fd_matrix(2, True, 30), oracle_lib.fd_matrix(2, False, 30)]
+           oracle_lib.fd_matrix(2, True, 30), oracle_lib.fd_matrix(2, False, 30),
+           oracle_lib.fd_matrix(0, True, 30)]
     for got, want in zip(mats, ref):
         assert np.abs(got - want).max() < 1e-15
