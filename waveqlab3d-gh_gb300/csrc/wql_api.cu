@@ -123,7 +123,7 @@ struct wql_scn {
     void* Q[6] = {};
     void* DQ[6] = {};
     long long slab_np[6] = {};
-    void* G = nullptr;  // PML velocity gradient hand-off (FP32C with PML)
+    void* G = nullptr;  // velocity gradient hand-off (FP32C with PML or attenuation)
     void* eta = nullptr;   // anelastic memory variables (24 x np)
     void* Deta = nullptr;  // and their rates
     void* qs = nullptr;    // 1/Qs per point

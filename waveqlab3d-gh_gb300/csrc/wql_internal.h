@@ -13,6 +13,9 @@
 //   face  : per side 15 x nface (FP64): n(3), m(3), l(3), grad(3) of the
 //           face-normal coordinate, lambda, mu, rho
 //   Q/DQ  : PML auxiliary fields on slabs of npml layers per active side
+//   G     : 9 x np velocity gradient hand-off (FP32C with PML or attenuation)
+//   eta/Deta, qs : 24 x np memory variables and their rates, 1/Qs per point
+//           (anelastic response only)
 #pragma once
 #include <cuda.h>
 
@@ -56,9 +59,10 @@ struct VolumeArgs {
   T* Q[6];
   T* DQ[6];
   long long slab_np[6];
-  // velocity gradient g[c][j] (component c*3+j, stride np) of the PML points,
-  // written by the TMA stencil kernel and read by the PML kernel of the same
-  // stage; nullptr where the PML kernel forms it itself
+  // velocity gradient g[c][j] (component c*3+j, stride np) of the PML points
+  // (of every point with the anelastic response), written by the TMA stencil
+  // kernel and read by the PML and anelastic kernels of the same stage;
+  // nullptr where those kernels form it themselves
   T* G;
   int fd;             // difference operator: 0 SBP-6 central; upwind pair (D+ on v, D- on fluxes) of order 6 (1) or 5 (2)
   int kernel;         // stencil variant: 0 default, 1 per-point, 2..4 tiled
