@@ -31,8 +31,12 @@
 //   material ....................... src/material.f90:146-190
 //   fault output frames ............ src/domain.f90:715-806, src/fault_output.f90
 //
-// Pinned by the reference's own regression outputs
-// (test_problems/truth/1 and truth/2, checked by tests/test_oracle_truth.py).
+// Pinned by the reference's own regression outputs, checked by
+// tests/test_oracle_truth.py: test_problems/truth/1 (Cartesian) and
+// test_problems/truth/2 (curvilinear bump fault) are both reproduced to
+// float32 rounding in every frame of every fault stream.  truth/2 needs the
+// TPV28 stress tensor with szz = -60 MPa (tpv28_prestress = 'benchmark'); the
+// reference's current source has +60, with which frame 0 already differs.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -89,8 +93,12 @@ wp smooth_boxcar(wp x, wp w, wp wr) {
   return 0.0;
 }
 
-// src/initial_stress_condition.f90:8-254 (subset with the presets below)
-bool initial_stress_tensor(wp s0[6], const wp x[3], const std::string& problem) {
+// src/initial_stress_condition.f90:8-254 (subset with the presets below).
+// tpv28_bench: TPV28 with szz = -60 MPa (the SCEC benchmark value) instead of
+// the +60 at src/initial_stress_condition.f90:80; the reference's truth/2
+// fixture was produced with it (&gb300_list tpv28_prestress = 'benchmark').
+bool initial_stress_tensor(wp s0[6], const wp x[3], const std::string& problem,
+                           bool tpv28_bench = false) {
   if (problem == "TPV26" || problem == "TPV27") {
     wp Omega = 0;
     if (x[1] <= 15.0) Omega = 1.0;
@@ -108,7 +116,8 @@ bool initial_stress_tensor(wp s0[6], const wp x[3], const std::string& problem) 
     return true;
   }
   if (problem == "TPV28") {
-    s0[0] = -60.0; s0[1] = 0.0; s0[2] = 60.0; s0[3] = 0.0; s0[4] = 29.38; s0[5] = 0.0;
+    s0[0] = -60.0; s0[1] = 0.0; s0[2] = tpv28_bench ? -60.0 : 60.0;
+    s0[3] = 0.0; s0[4] = 29.38; s0[5] = 0.0;
     return true;
   }
   if (problem == "TPV29" || problem == "TPV30") {
@@ -158,6 +167,7 @@ void traction_nml(const wp s0[6], const wp n[3], const wp m[3], const wp l[3],
 struct Presets {
   std::string problem;
   const wql::FrictionExt* fx = nullptr;
+  bool tpv28_bench = false;
 };
 
 // prestress: src/Interface_Condition.f90:1802-2435
@@ -180,7 +190,7 @@ void prestress(wp& T0n, wp& T0m, wp& T0l, const wp x[3], wp t, const Presets& P,
       // reference only through Tau_strength (forced rupture); no extra load here
     }
   } else if (pb == "TPV28") {
-    initial_stress_tensor(s0, x, pb);
+    initial_stress_tensor(s0, x, pb, P.tpv28_bench);
     traction_nml(s0, n, m, l, T0n, T0m, T0l);
     wp r = std::sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
     wp tau_nuke;
@@ -1782,10 +1792,12 @@ void impose_bc(RBlock& B, bool weighted) {
 wp f_rs(wp V, wp Phi, wp eta, wp sigma_n, wp psi, wp V0, wp a) {
   return V + a * sigma_n / eta * std::asinh(0.5 * V / V0 * std::exp(psi / a)) - Phi / eta;
 }
-void regula_falsi(wp& V, wp Phi, wp eta, wp sigma_n, wp psi, wp V0, wp a) {
-  wp err = 1.0, tol = 1.0e-12;
+// tol and maxit: 1e-12 and 5000 in the reference (:1188, :1194); the input
+// may override both (&gb300_list rs_tol, rs_maxit).
+void regula_falsi(wp& V, wp Phi, wp eta, wp sigma_n, wp psi, wp V0, wp a, wp tol, int maxit) {
+  wp err = 1.0;
   wp Vl = 0.0, Vr = Phi / eta;
-  int k = 1, maxit = 5000;
+  int k = 1;
   wp fv = f_rs(V, Phi, eta, sigma_n, psi, V0, a);
   wp fl = f_rs(Vl, Phi, eta, sigma_n, psi, V0, a);
   wp fr = f_rs(Vr, Phi, eta, sigma_n, psi, V0, a);
@@ -1886,7 +1898,7 @@ void interface_point(const Domain& D, const wp U[6], const wp V[6], wp Z1s, wp Z
     wp Phi = std::sqrt(phi_1 * phi_1 + phi_2 * phi_2);
     wp Vv = std::sqrt(vv_m * vv_m + vv_l * vv_l);
     if (Vv > Phi) Vv = 0.5 * Phi / eta_s;
-    regula_falsi(Vv, Phi, eta_s, sigma_n, psi, rsp->V0, rsp->a);
+    regula_falsi(Vv, Phi, eta_s, sigma_n, psi, rsp->V0, rsp->a, D.P.rs_tol, D.P.rs_maxit);
     Vel = Vv;
     wp fv = sigma_n * rsp->a * std::asinh(0.5 * Vv / rsp->V0 * std::exp(psi / rsp->a));
     vv_m = phi_1 / (eta_s + fv / Vv);
@@ -2134,7 +2146,7 @@ void plasticity(Domain& D, RBlock& B) {
         wp x[3] = {B.X[0][p], B.X[1][p], B.X[2][p]}, s0[6];
         const bool param = D.P.problem == "sw_param" || D.P.problem == "rs_param";
         const std::string& prof = param ? D.P.fric.stress_profile : D.P.problem;
-        if (!initial_stress_tensor(s0, x, prof)) {
+        if (!initial_stress_tensor(s0, x, prof, D.pre.tpv28_bench)) {
           for (int t = 0; t < 6; ++t) s0[t] = param ? D.P.fric.s0[t] : 0.0;
         }
         wp s[6], sa[6];
@@ -2367,6 +2379,7 @@ void* wqlref_create_ex(const char* in_text, const double* fault_offset, const do
 static void* create_domain(Domain* D, const Media& md) {
   D->pre.problem = D->P.problem;
   D->pre.fx = &D->P.fric;
+  D->pre.tpv28_bench = D->P.tpv28_prestress == "benchmark";
   D->rk = rk54();
   const std::string& cp = D->P.coupling;
   D->sw = cp == "slip-weakening_friction";
@@ -2533,6 +2546,18 @@ int wqlref_get_geom(void* h, int block, int what, double* out) {
   else if (what == 12) src = &B.J;
   if (!src) return 1;
   std::memcpy(out, src->data(), B.np * sizeof(double));
+  return 0;
+}
+
+// Unit vectors of face `side` (1..6) of block `block`
+// (local_orth_vectors_*, src/unit_normals.f90:8-160): what 0..2 the normal n,
+// 3..5 m, 6..8 l, each on the face's points (first face index fastest).
+int wqlref_get_face(void* h, int block, int side, int what, double* out) {
+  Domain* D = (Domain*)h;
+  if (block < 0 || block > 1 || side < 1 || side > 6 || what < 0 || what > 8) return 1;
+  const Face& F = D->Bk[block].B[side];
+  const vector<wp>& v = what < 3 ? F.n_n[what] : what < 6 ? F.n_m[what - 3] : F.n_l[what - 6];
+  std::memcpy(out, v.data(), v.size() * sizeof(double));
   return 0;
 }
 

@@ -4,8 +4,10 @@ The reference's regression suite (src/CMakeLists.txt:104-165,
 cmake/run_mpi_test.cmake) runs two 2x21^3 rupture problems and compares six
 float32 fault streams against `test_problems/truth/{1,2}` with
 python/read_binary.py (max |diff| <= 1e-3).  This script copies the inputs and
-those truth streams (plus trup, state and the two station seismograms) into
-compressed fixtures so the parity tests run without the reference present.
+those truth streams (plus trup, state, the two station seismograms and, for
+the curvilinear case, the fault coordinates and unit vectors shipped beside
+the truth) into compressed fixtures so the parity tests run without the
+reference present.
 
 Usage:  python tests/golden/make_golden.py /path/to/reference
 """
@@ -21,6 +23,10 @@ CASES = {
 STREAMS = {"S": 4, "Svel": 3, "Uface": 9, "Vface": 9, "Uhat": 6, "Vhat": 6,
            "trup": 1, "state": 1}
 NGRID, NTIME = 21, 46
+GEOMETRY = {"fault_xyz": "fault_topography_AX",
+            "fault_normal": "unit_normal_vector_fractal_fault",
+            "fault_strike": "unit_strike_vector_fractal_fault",
+            "fault_dip": "unit_dip_vector_fractal_fault"}
 
 
 def main(ref):
@@ -40,9 +46,17 @@ def main(ref):
         for st in ("1_11_11", "21_11_11"):
             path = os.path.join(ref, "test_problems", "truth", d, f"{prefix}_{st}.dat")
             arrays["station_" + st] = np.loadtxt(path).astype(np.float64)
+        # the fault geometry shipped with the curvilinear truth: x y z and the
+        # unit normal, strike and dip vectors per fault point (rows r fastest)
+        for key, suffix in GEOMETRY.items():
+            path = os.path.join(ref, "test_problems", "truth", d, f"{prefix}_{suffix}.dat")
+            if os.path.exists(path):
+                arrays[key] = np.loadtxt(path).astype(np.float64)
         np.savez_compressed(os.path.join(here, f"truth_{tag}.npz"), **arrays)
         print(tag, {k: v.shape for k, v in arrays.items()})
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    main(sys.argv[1])

@@ -96,6 +96,11 @@ def case_text(name):
         order = 5 if name.startswith("up5_") else 6
         return case_text(name.split("_", 1)[1]).replace(
             " w_stride = 1,", f" w_stride = 1,\n fd_type = 'upwind',\n order = {order},", 1)
+    if name.startswith("linear_"):
+        # linear friction coupling, tau = alpha v with alpha = 1e14
+        # (src/Interface_Condition.f90:639-742, called at :366), around the
+        # point sources of the moment-tensor cases
+        return case_text(name.split("_", 1)[1]).replace("coupling = 'locked'", "coupling = 'linear_friction'", 1)
     if name in MT_CASES:
         mesh, order, mollify, lists = MT_CASES[name]
         extra = ",\n mollify_source = T" if mollify else ""

@@ -27,6 +27,7 @@ def lib():
         L.wqlref_set_field.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_get_geom.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_get_iface.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_get_face.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_info.argtypes = [vp, vp, vp, vp, vp, vp]
         L.wqlref_create_ex.restype = ctypes.c_void_p
         L.wqlref_create_ex.argtypes = [ctypes.c_char_p] + [vp] * 9
@@ -98,6 +99,15 @@ class Oracle:
         out = np.empty(nq * nr * ns, np.float64)
         lib().wqlref_get_geom(self.h, block, what, out.ctypes.data)
         return out.reshape(ns, nr, nq)
+
+    def face_vectors(self, block, side):
+        """(n, m, l) unit vectors of face `side` (1..6) of `block`, each (3, nb, na)."""
+        nq, nr, ns = self.dims[block]
+        na, nb = {1: (nr, ns), 2: (nq, ns), 3: (nq, nr)}[(side + 1) // 2]
+        out = np.empty((9, nb, na), np.float64)
+        for w in range(9):
+            assert lib().wqlref_get_face(self.h, block, side, w, out[w].ctypes.data) == 0
+        return out[0:3], out[3:6], out[6:9]
 
     def iface(self, block, what):
         nr, ns = self.dims[0][1], self.dims[0][2]

@@ -1,5 +1,5 @@
 """FP64 parity of the CUDA path against the oracle (and the reference's
-truth/1 fixture).  Bar: 1e-11 relative L2 in the fields; fault streams to
+truth/1 and truth/2 fixtures).  Bar: 1e-11 relative L2 in the fields; fault streams to
 float32 rounding of the fixture."""
 import os
 
@@ -53,6 +53,31 @@ def test_truth1_fault_streams(ctx, wqlmod, oracle_lib, tmp_path):
         assert idx.tolist() == oidx.tolist()
         assert rec.shape == orec.shape == (46, 1, 4)
         assert np.abs(rec - orec).max() <= 1e-11 * max(np.abs(orec).max(), 1.0)
+        assert np.abs(rec[:, 0, :] - truth[name]).max() <= 5.1e-7
+
+
+def test_truth2_fault_streams(ctx, wqlmod, oracle_lib, tmp_path):
+    """The GPU FP64 path reproduces test_problems/truth/2 (TPV28 on the
+    curvilinear bump fault; the fixture's TPV28 tensor has szz = -60 MPa)
+    in every frame of the eight fault streams, and the stations placed on
+    the bump's crest match truth/2's station files."""
+    text = with_groups(golden_in("test_rup_curv_fric"),
+                       "&gb300_list\n bc_penalty = 'weighted', tpv28_prestress = 'benchmark' /")
+    text = text.replace(" -0d0 7.5d0 0d0", " 0.1d0 7.5d0 0d0").replace(" 0d0 7.5d0 0d0", " 0.1d0 7.5d0 0d0")
+    p = write(tmp_path, "curv.in", text)
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, 46)
+    truth = np.load(os.path.join(GOLDEN, "truth_curv.npz"))
+    for name in ["S", "Svel", "Uface", "Vface", "Uhat", "Vhat", "trup", "state"]:
+        got = s.frames(name).astype(np.float64)
+        ref = truth[name]
+        assert got.shape == ref.shape
+        scale = max(np.abs(ref).max(), 1.0)
+        assert np.abs(got - ref).max() <= 1e-9 * scale, name
+    for e in field_errors(s, o):
+        assert e < TOL
+    for block, name in ((0, "station_21_11_11"), (1, "station_1_11_11")):
+        idx, rec = s.stations(block)
+        assert rec.shape == (46, 1, 4)
         assert np.abs(rec[:, 0, :] - truth[name]).max() <= 5.1e-7
 
 

@@ -1,9 +1,10 @@
 """Pin the oracle against the reference's own regression fixtures.
 
 The reference's ctest (src/CMakeLists.txt:104-165, cmake/run_mpi_test.cmake)
-runs test_problems/test_rup_cart_fric.in and compares six float32 fault
-streams with python/read_binary.py at max |diff| <= 1e-3.  These tests apply
-the same comparison to the oracle, plus much tighter checks.
+runs test_problems/test_rup_cart_fric.in and test_rup_curv_fric.in and
+compares six float32 fault streams with python/read_binary.py at
+max |diff| <= 1e-3 against test_problems/truth/1 and truth/2.  These tests
+apply the same comparison to the oracle, plus much tighter checks.
 """
 import numpy as np
 import pytest
@@ -91,6 +92,90 @@ def test_compiled_bc_form_differs_from_fixture(oracle_lib, tmp_path, truth_cart)
     uf = o.frames("Uface").astype(np.float64)
     assert np.abs(uf[0] - truth_cart["Uface"][0]).max() == 0.0
     assert np.abs(uf - truth_cart["Uface"]).max() > 1e-2
+
+
+CURV_FIXTURE = "&gb300_list\n bc_penalty = 'weighted', tpv28_prestress = 'benchmark' /"
+
+
+@pytest.fixture(scope="module")
+def truth_curv():
+    import os
+    from inputs import GOLDEN
+    return np.load(os.path.join(GOLDEN, "truth_curv.npz"))
+
+
+def test_curvilinear_truth_bitwise(oracle_lib, tmp_path, truth_curv):
+    """truth/2 (TPV28 on the analytical bump fault, curvilinear, 2 x 21^3) is
+    reproduced to float32 rounding in all 46 frames of all eight streams and
+    both station files, with the weighted SAT form and the TPV28 stress
+    tensor with szz = -60 MPa (the SCEC benchmark value)."""
+    p = write(tmp_path, "curv.in", with_groups(golden_in("test_rup_curv_fric"), CURV_FIXTURE))
+    o = run(oracle_lib, p)
+    for name in READ_BINARY_STREAMS + ["trup", "state"]:
+        got = o.frames(name).astype(np.float64)
+        ref = truth_curv[name]
+        assert got.shape == ref.shape
+        diff = np.abs(got - ref).max()
+        assert diff <= 1e-3, name
+        assert diff <= 1e-10 * max(np.abs(ref).max(), 1.0), (name, diff)
+    # The deck's stations sit at x = 0, 0.1 km behind the bump's crest, so the
+    # station rule of src/seismogram.f90:531-650 places block 1's at grid
+    # point (20,11,11).  The truth files hold the fault points (21,11,11) of
+    # block 1 and (1,11,11) of block 2, as their names say.
+    assert o.stations(0)[0].tolist() == [[20, 11, 11]]
+    assert o.stations(1)[0].tolist() == [[1, 11, 11]]
+
+
+def test_curvilinear_truth_stations(oracle_lib, tmp_path, truth_curv):
+    """Stations on the bump's crest (x = 0.1 km, y = 7.5, z = 0) resolve to
+    the fault points named by truth/2's station files and match their
+    records (printed to 6 decimals)."""
+    text = with_groups(golden_in("test_rup_curv_fric"), CURV_FIXTURE)
+    text = text.replace(" -0d0 7.5d0 0d0", " 0.1d0 7.5d0 0d0").replace(" 0d0 7.5d0 0d0", " 0.1d0 7.5d0 0d0")
+    o = run(oracle_lib, write(tmp_path, "crest.in", text))
+    for block, name, ijk in ((0, "station_21_11_11", (21, 11, 11)), (1, "station_1_11_11", (1, 11, 11))):
+        idx, rec = o.stations(block)
+        assert idx.tolist() == [list(ijk)]
+        assert rec.shape == (46, 1, 4)
+        assert np.abs(rec[:, 0, :] - truth_curv[name]).max() <= 5.1e-7, name
+
+
+def test_curvilinear_fault_geometry_matches_truth(oracle_lib, truth_curv):
+    """The fault surface and its unit vectors computed through the SBP
+    metrics (src/grid.f90:794-826, src/metrics.f90, src/unit_normals.f90)
+    match the coordinates and normal/dip/strike vectors shipped beside
+    truth/2, for both blocks' fault faces."""
+    from inputs import GOLDEN
+    import os
+    o = oracle_lib.Oracle(os.path.join(GOLDEN, "test_rup_curv_fric.in"))
+    for block, side, iq in ((0, 2, 20), (1, 1, 0)):
+        xyz = np.stack([o.geom(block, c)[:, :, iq] for c in range(3)], -1).reshape(-1, 3)
+        assert np.abs(xyz - truth_curv["fault_xyz"]).max() < 1e-13
+        n, m, l = (v.reshape(3, -1).T for v in o.face_vectors(block, side))
+        assert np.abs(n - truth_curv["fault_normal"]).max() < 1e-13
+        assert np.abs(m - truth_curv["fault_dip"]).max() < 1e-13
+        assert np.abs(l - truth_curv["fault_strike"]).max() < 1e-13
+    # the bump tilts the normal by up to about 22 degrees
+    assert np.abs(truth_curv["fault_normal"][:, 2]).max() > 0.3
+
+
+def test_tpv28_source_tensor_differs_from_truth(oracle_lib, tmp_path, truth_curv):
+    """With the TPV28 tensor of the reference's current source (szz = +60 MPa,
+    src/initial_stress_condition.f90:78-83) frame 0 already departs from
+    truth/2 wherever the fault normal tilts out of the x-y plane, although
+    the geometry is the same: the fixture predates that tensor.  With
+    szz = -60 MPa frame 0 agrees everywhere."""
+    text = with_groups(golden_in("test_rup_curv_fric"), "&gb300_list\n bc_penalty = 'weighted' /")
+    o = oracle_lib.Oracle(write(tmp_path, "src.in", text))
+    o.step(1)
+    d = np.abs(o.frames("Uhat")[0].astype(np.float64) - truth_curv["Uhat"][0]).max(axis=0)
+    tilt = np.abs(truth_curv["fault_normal"][:, 2].reshape(21, 21))
+    assert (d > 1e-3).sum() > 300 and d.max() > 10.0
+    assert d[tilt < 1e-12].max() < 1e-6          # where n_z = 0 the two tensors agree
+    ob = oracle_lib.Oracle(write(tmp_path, "bench.in", with_groups(golden_in("test_rup_curv_fric"),
+                                                                    CURV_FIXTURE)))
+    ob.step(1)
+    assert np.abs(ob.frames("Uhat")[0].astype(np.float64) - truth_curv["Uhat"][0]).max() < 1e-10
 
 
 def test_seeded_generators_statistics():

@@ -374,9 +374,20 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
   for (auto& it : items_of("gb300_list")) {
     auto s = it.values.empty() ? std::string() : it.values[0];
     if (it.key == "bc_penalty") P.bc_penalty = s;
+    else if (it.key == "tpv28_prestress") P.tpv28_prestress = s;
+    else if (it.key == "rs_tol") P.rs_tol = to_double(s);
+    else if (it.key == "rs_maxit") P.rs_maxit = (int)to_double(s);
   }
   if (P.bc_penalty != "characteristic" && P.bc_penalty != "weighted") {
     err = "bc_penalty must be 'characteristic' or 'weighted'";
+    return 1;
+  }
+  if (P.tpv28_prestress != "source" && P.tpv28_prestress != "benchmark") {
+    err = "tpv28_prestress must be 'source' or 'benchmark'";
+    return 1;
+  }
+  if (!(P.rs_tol > 0.0) || P.rs_maxit < 1 || P.rs_maxit > 1000000) {
+    err = "rs_tol must be positive and rs_maxit in 1..1000000";
     return 1;
   }
   if (groups.count("fault_list")) {

@@ -118,6 +118,18 @@ struct Problem {
   // alpha/theta form of src/BoundaryConditions3.f90:777-903, which the
   // reference's regression fixtures (test_problems/truth/1) were produced with.
   std::string bc_penalty = "characteristic";
+  // &gb300_list tpv28_prestress: 'source' is the TPV28 stress tensor of
+  // src/initial_stress_condition.f90:78-83 (szz = +60 MPa); 'benchmark' has
+  // szz = -60 MPa, the SCEC TPV28 value.  The reference's curvilinear
+  // regression fixture (test_problems/truth/2) was produced with 'benchmark'.
+  std::string tpv28_prestress = "source";
+  // &gb300_list rs_tol, rs_maxit: tolerance and iteration cap of the FP64
+  // rate-and-state regula falsi (src/Interface_Condition.f90:1188, :1194).
+  // The defaults are the reference's; a tolerance of 1e-300 iterates to a
+  // floating-point fixed point, which lets two implementations of the solve
+  // be compared to rounding.
+  double rs_tol = 1.0e-12;
+  int rs_maxit = 5000;
   FrictionExt fric;
   PlasticExt plast;
   // raw groups for anything not mapped above

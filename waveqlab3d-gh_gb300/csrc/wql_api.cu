@@ -141,6 +141,8 @@ struct wql_scn {
   int* err_dev = nullptr;  // kernel error word (bounded pipeline waits that ran out)
   FaultParams fp{};
   int bc_form = BC_CHARACTERISTIC;
+  double rs_tol = 1.0e-12;  // FP64 regula falsi tolerance and iteration cap
+  int rs_maxit = 5000;
   // a step advanced stage by stage (wql_stage): the next stage to run (1:
   // no step in progress) and the step's context
   int next_stage = 1;
@@ -739,6 +741,8 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   }
   S->curv = Pr.type_of_mesh == "curvilinear";
   S->bc_form = Pr.bc_penalty == "weighted" ? BC_WEIGHTED : BC_CHARACTERISTIC;
+  S->rs_tol = Pr.rs_tol;
+  S->rs_maxit = Pr.rs_maxit;
   S->plastic = Pr.response == "plastic";
   if (S->plastic && Pr.plastic_model != "scec")
     return fail(WQL_E_INPUT, "only plastic_model='scec' is supported");
@@ -759,8 +763,9 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   else if (cp == "rate-and-state_friction") fp.coupling = CPL_RS;
   else return fail(WQL_E_INPUT, "invalid coupling condition '" + cp + "'");
   fp.preset = preset_of(Pr.problem);
+  if (fp.preset == PRE_TPV28 && Pr.tpv28_prestress == "benchmark") fp.preset = PRE_TPV28_BENCH;
   const bool sw_ok = fp.preset == PRE_TPV5 || fp.preset == PRE_TPV26 || fp.preset == PRE_TPV27 ||
-                     fp.preset == PRE_TPV28 || fp.preset == PRE_TPV29 || fp.preset == PRE_TPV30 ||
+                     fp.preset == PRE_TPV28 || fp.preset == PRE_TPV28_BENCH || fp.preset == PRE_TPV29 || fp.preset == PRE_TPV30 ||
                      fp.preset == PRE_TPV10 || fp.preset == PRE_SW_PARAM;
   const bool rs_ok = fp.preset == PRE_TPV101 || fp.preset == PRE_TPV102 || fp.preset == PRE_RS_PARAM;
   if ((fp.coupling == CPL_SW && !sw_ok) || (fp.coupling == CPL_RS && !rs_ok))
@@ -1016,6 +1021,8 @@ void stage_head(wql_scn* S, StepCtx& c, int stage) {
     ia.rs_bL = r0.b / r0.L0;
     ia.rs_binv = 1.0 / r0.b;
   }
+  ia.rs_tol = S->rs_tol;
+  ia.rs_maxit = S->rs_maxit;
   ia.fp = S->fp;
   ia.frame = (c.want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
   ia.solver_fail = S->solver_fail;

@@ -24,14 +24,14 @@ namespace {
 
 // Regula falsi for V + a*sigma_n/eta*asinh(V/(2V0)*exp(psi/a)) = Phi/eta on
 // [0, Phi/eta] (src/Interface_Condition.f90:1170-1265), including the
-// reference's acceptance test `fv*fl > tol`.  Returns false when the
-// iteration budget (5000) is exhausted.  exp(psi/a) is evaluated once; the
+// reference's acceptance test `fv*fl > tol`.  tol and maxit are the
+// reference's 1e-12 and 5000 unless the input overrides them.  Returns false
+// when the iteration budget is exhausted.  exp(psi/a) is evaluated once; the
 // residual is otherwise formed exactly as the reference forms it.
 __device__ bool regula_falsi(double& V, double Phi, double eta, double sn, double psi, double V0,
-                             double a) {
+                             double a, double tol, int maxit) {
   const double ek = exp(psi / a);
   auto f = [&](double v) { return v + a * sn / eta * asinh(0.5 * v / V0 * ek) - Phi / eta; };
-  const double tol = 1.0e-12;
   double Vl = 0.0, Vr = Phi / eta;
   double fv = f(V), fl = f(Vl), fr = f(Vr);
   if (fabs(fv) <= tol) return true;
@@ -39,7 +39,7 @@ __device__ bool regula_falsi(double& V, double Phi, double eta, double sn, doubl
   if (fabs(fr) <= tol) { V = Vr; return true; }
   double err = 1.0;
   int k = 1;
-  while (k <= 5000 && err >= tol) {
+  while (k <= maxit && err >= tol) {
     const double V1 = V;
     if (fv * fl > tol) {
       Vl = V;
@@ -54,7 +54,7 @@ __device__ bool regula_falsi(double& V, double Phi, double eta, double sn, doubl
     err = fabs(V - V1);
     ++k;
   }
-  return !(k >= 5000);
+  return !(k >= maxit);
 }
 
 // The same equation for FP32 fields, by Newton's method in u = ln V.  With
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(
       const double d1 = (double)vr[1] - (double)ur[1], d2 = (double)vr[2] - (double)ur[2];
       double V = sqrt(d1 * d1 + d2 * d2);
       if (V > Phi) V = 0.5 * Phi / es;
-      const bool ok = F64 ? regula_falsi(V, Phi, es, sn, psi, rs.V0, rs.a)
+      const bool ok = F64 ? regula_falsi(V, Phi, es, sn, psi, rs.V0, rs.a, a.rs_tol, a.rs_maxit)
                           : newton_mixed(V, Phi, es, sn, psi, rs.V0, rs.a, a.lnV0h);
       if (!ok && a.solver_fail) atomicAdd(a.solver_fail, 1u);
       if (F64) {

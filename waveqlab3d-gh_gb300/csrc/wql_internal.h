@@ -111,6 +111,8 @@ struct InterfaceArgs {
   double ramp;              // nucleation ramp at this stage's time
   double lnV0h;             // ln(1/(2 V0)) of the rate-and-state law
   double rs_bL, rs_binv;    // b/L and 1/b of the aging law (uniform along the fault)
+  double rs_tol;            // FP64 regula falsi: tolerance and iteration cap
+  int rs_maxit;
   double tau_h[2];
   double A, Bdt, t;
   int stage;

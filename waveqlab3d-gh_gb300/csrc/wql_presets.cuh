@@ -26,6 +26,9 @@ enum Preset : int {
   PRE_TPV102 = 9,
   PRE_SW_PARAM = 10,
   PRE_RS_PARAM = 11,
+  // TPV28 with the SCEC benchmark's szz = -60 MPa in place of the +60 of
+  // src/initial_stress_condition.f90:80 (&gb300_list tpv28_prestress = 'benchmark')
+  PRE_TPV28_BENCH = 12,
 };
 
 enum Coupling : int { CPL_LOCKED = 0, CPL_LINEAR = 1, CPL_SW = 2, CPL_RS = 3 };
@@ -79,7 +82,9 @@ WQL_HD bool initial_stress(int preset, const double x[3], double s0[6]) {
       return true;
     }
     case PRE_TPV28:
-      s0[0] = -60.0; s0[1] = 0.0; s0[2] = 60.0; s0[3] = 0.0; s0[4] = 29.38; s0[5] = 0.0;
+    case PRE_TPV28_BENCH:
+      s0[0] = -60.0; s0[1] = 0.0; s0[2] = preset == PRE_TPV28 ? 60.0 : -60.0;
+      s0[3] = 0.0; s0[4] = 29.38; s0[5] = 0.0;
       return true;
     case PRE_TPV101:
     case PRE_TPV102:
@@ -123,7 +128,9 @@ WQL_HD bool initial_stress_y(int preset, R y, R s0[6]) {
       return true;
     }
     case PRE_TPV28:
-      s0[0] = R(-60.0); s0[1] = R(0.0); s0[2] = R(60.0); s0[3] = R(0.0); s0[4] = R(29.38); s0[5] = R(0.0);
+    case PRE_TPV28_BENCH:
+      s0[0] = R(-60.0); s0[1] = R(0.0); s0[2] = preset == PRE_TPV28 ? R(60.0) : R(-60.0);
+      s0[3] = R(0.0); s0[4] = R(29.38); s0[5] = R(0.0);
       return true;
     case PRE_TPV101:
     case PRE_TPV102:
@@ -183,7 +190,8 @@ WQL_HD void prestress_static(const FaultParams& fp, const double x[3], const dou
       initial_stress(fp.preset, x, s0);
       tensor_traction(s0, n, m, l, Tn, Tm, Tl);
       return;
-    case PRE_TPV28: {
+    case PRE_TPV28:
+    case PRE_TPV28_BENCH: {
       initial_stress(fp.preset, x, s0);
       tensor_traction(s0, n, m, l, Tn, Tm, Tl);
       const double r = sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
@@ -270,7 +278,8 @@ WQL_HD double tau_strength(const FaultParams& fp, double sigma_n, double D, cons
       const double fd = 0.525, Dc = 0.4;
       return sigma_n * (fs - (fs - fd) * fmin(D, Dc) / Dc);
     }
-    case PRE_TPV28: {
+    case PRE_TPV28:
+    case PRE_TPV28_BENCH: {
       double fs = 0.677 + 1.0e10 * (1.0 - boxcar(x[1], 15.0) * boxcar(x[2], 18.0));
       const double fd = 0.373, Dc = 0.4;
       return sigma_n * (fs - (fs - fd) * fmin(D, Dc) / Dc);
