@@ -125,12 +125,21 @@ int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in);
  * exceeds 1048576 points returns WQL_E_INPUT.  The first call on a device
  * resolves the array's address and must not happen during stream capture.
  * The array is shared by all calls on a device: calls that overlap in time
- * race.  No counterpart in the reference. */
+ * race.  The calling thread's current device is the same after the call as
+ * before.  No counterpart in the reference. */
 int wql_get_field_noalloc(wql_scn* scn, int block, int comp, double* host_out);
 
 /* Interface state of block copy (0/1): what 0..3 = S(1..4), 4 = W, 5 = trup;
  * nr*ns values (src/iface.f90:13-49). */
 int wql_get_iface(wql_scn* scn, int copy, int what, double* host_out);
+
+/* Manufactured-solution error of one block at the current time (needs
+ * &mms_list use_mms = T).  The reference's MMS module (src/mms.f90:77-232)
+ * is never called and its norm routine returns |F| rather than the error
+ * (src/fields.f90:194-218); this gives, per field component c (0..8), the
+ * sums over the block's grid points of (F_c - u_exact_c)^2 in err2[c] and of
+ * u_exact_c^2 in ref2[c]. */
+int wql_mms_norms(wql_scn* scn, int block, double* err2, double* ref2);
 
 /* Fault output frames in the reference's file layout
  * (src/fault_output.f90:13-122, src/mpi3dio.f90:327-364): frame-major, then

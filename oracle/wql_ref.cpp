@@ -30,6 +30,10 @@
 //                                    src/unit_normals.f90:8-282
 //   material ....................... src/material.f90:146-190
 //   fault output frames ............ src/domain.f90:715-806, src/fault_output.f90
+//   manufactured solution .......... src/mms.f90:77-232 (forcing added at every
+//                                    stage), exact data in the outer SAT
+//                                    (src/BoundaryConditions.f90:86-92, 126) and
+//                                    the interface (src/CouplingForcing.f90:147-185)
 //
 // Pinned by the reference's own regression outputs, checked by
 // tests/test_oracle_truth.py: test_problems/truth/1 (Cartesian) and
@@ -1739,7 +1743,64 @@ void structure(wp Ux[9], const wp Uq[9], wp rho, wp mu, wp lam) {
 // impose_boundary_condition: src/RHS_Interior.f90:1516-1703 with BC_Lx..BC_Rz.
 // The reference computes every face's forcing array before adding it; the
 // forcing depends only on F, so computing point by point is identical.
-void impose_bc(RBlock& B, bool weighted) {
+// ------------------------------------------------------------- MMS ----
+// Manufactured solution (evaluate_mms and its derivatives,
+// src/mms.f90:136-232): velocities cos(nt pi t) sin(nx pi x) sin(ny pi y)
+// sin(nz pi z), stresses cos(nt pi t) cos(nx pi x) cos(ny pi y) cos(nz pi z).
+void mms_eval(const wql::Problem& P, wp t, const wp x[3], wp u[9]) {
+  wp T = std::cos(P.mms_nt * PI * t);
+  wp v = T * std::sin(P.mms_nx * PI * x[0]) * std::sin(P.mms_ny * PI * x[1]) * std::sin(P.mms_nz * PI * x[2]);
+  wp s = T * std::cos(P.mms_nx * PI * x[0]) * std::cos(P.mms_ny * PI * x[1]) * std::cos(P.mms_nz * PI * x[2]);
+  for (int c = 0; c < 3; ++c) u[c] = v;
+  for (int c = 3; c < 9; ++c) u[c] = s;
+}
+
+// mms_forcing (src/mms.f90:77-133): f = A u_x + B u_y + C u_z - u_t at one
+// point with (lambda, mu, rho); the rates receive DU - f.  The reference
+// never calls it; here every grid point of both blocks gets it at each
+// stage's time.
+void mms_forcing_point(const wql::Problem& P, wp t, const wp x[3], wp lam, wp mu, wp rho, wp f[9]) {
+  const wp ct = std::cos(P.mms_nt * PI * t), st = std::sin(P.mms_nt * PI * t);
+  const wp kx = P.mms_nx * PI, ky = P.mms_ny * PI, kz = P.mms_nz * PI;
+  const wp sx = std::sin(kx * x[0]), sy = std::sin(ky * x[1]), sz = std::sin(kz * x[2]);
+  const wp cx = std::cos(kx * x[0]), cy = std::cos(ky * x[1]), cz = std::cos(kz * x[2]);
+  wp ut[9], ux[9], uy[9], uz[9];
+  for (int c = 0; c < 3; ++c) {
+    ut[c] = -P.mms_nt * PI * st * sx * sy * sz;
+    ux[c] = kx * ct * cx * sy * sz;
+    uy[c] = ky * ct * sx * cy * sz;
+    uz[c] = kz * ct * sx * sy * cz;
+  }
+  for (int c = 3; c < 9; ++c) {
+    ut[c] = -P.mms_nt * PI * st * cx * cy * cz;
+    ux[c] = -kx * ct * sx * cy * cz;
+    uy[c] = -ky * ct * cx * sy * cz;
+    uz[c] = -kz * ct * cx * cy * sz;
+  }
+  f[0] = (1.0 / rho) * (ux[3] + uy[6] + uz[7]);
+  f[1] = (1.0 / rho) * (ux[6] + uy[4] + uz[8]);
+  f[2] = (1.0 / rho) * (ux[7] + uy[8] + uz[5]);
+  f[3] = (2.0 * mu + lam) * ux[0] + lam * uy[1] + lam * uz[2];
+  f[4] = lam * ux[0] + (2.0 * mu + lam) * uy[1] + lam * uz[2];
+  f[5] = lam * ux[0] + lam * uy[1] + (2.0 * mu + lam) * uz[2];
+  f[6] = mu * (uy[0] + ux[1]);
+  f[7] = mu * (uz[0] + ux[2]);
+  f[8] = mu * (uz[1] + uy[2]);
+  for (int c = 0; c < 9; ++c) f[c] = f[c] - ut[c];
+}
+
+void mms_forcing(const wql::Problem& P, RBlock& B, wp t) {
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < (long long)B.np; ++p) {
+    wp x[3] = {B.X[0][p], B.X[1][p], B.X[2][p]}, f[9];
+    mms_forcing_point(P, t, x, B.M[0][p], B.M[1][p], B.M[2][p], f);
+    for (int c = 0; c < 9; ++c) B.DF[c][p] = B.DF[c][p] - f[c];
+  }
+}
+
+// mms: the manufactured problem (or nullptr); t: the stage's time.  With
+// it the penalty acts on F - u_exact (src/BoundaryConditions.f90:86-92, 126).
+void impose_bc(RBlock& B, bool weighted, const wql::Problem* mms = nullptr, wp t = 0.0) {
   const int codes[7] = {0, B.Lx, B.Rx, B.Ly, B.Ry, B.Lz, B.Rz};
   const wp hs_[3] = {B.hq, B.hr, B.hs};
   for (int side = 1; side <= 6; ++side) {
@@ -1775,6 +1836,11 @@ void impose_bc(RBlock& B, bool weighted) {
           n[c] = B.B[side].n_n[c][f];
         }
         for (int c = 0; c < 9; ++c) u[c] = B.F[c][p];
+        if (mms) {
+          wp fu[9], xp[3] = {B.X[0][p], B.X[1][p], B.X[2][p]};
+          mms_eval(*mms, t, xp, fu);
+          for (int c = 0; c < 9; ++c) u[c] = u[c] - fu[c];
+        }
         bc_char(ubc, u, l, m, n, norm, Zs, Zp, r, hi, weighted, alpha, theta, rho, mu, lam);
         if (weighted)
           for (int c = 0; c < 9; ++c) Ux[c] = ubc[c];
@@ -1944,6 +2010,19 @@ void impose_interface(Domain& D, int b, int stage, bool write_frame) {
       for (int c = 0; c < 9; ++c) {
         u[c] = B1.F[c][pu];
         v[c] = B2.F[c][pv];
+      }
+      if (D.P.use_mms) {
+        // src/CouplingForcing.f90:147-185: both sides' velocities and
+        // tractions less the exact solution at their own fault points (the
+        // fu/fv evaluation left as a TODO at :149-151)
+        wp fu[9], fv[9];
+        wp xu[3] = {B1.X[0][pu], B1.X[1][pu], B1.X[2][pu]}, xv[3] = {B2.X[0][pv], B2.X[1][pv], B2.X[2][pv]};
+        mms_eval(D.P, D.t, xu, fu);
+        mms_eval(D.P, D.t, xv, fv);
+        for (int c = 0; c < 9; ++c) {
+          u[c] = u[c] - fu[c];
+          v[c] = v[c] - fv[c];
+        }
       }
       // tractions and velocities in x,y,z (CouplingForcing.f90:115-168)
       wp ur[6], vr[6];
@@ -2238,12 +2317,13 @@ void time_step(Domain& D) {
       else rhs_interior(D.Bk[b], D.cart);
       rhs_near_boundaries(D.Bk[b]);
       if (D.P.use_moment_tensor) apply_sources(D, b, D.t);
+      if (D.P.use_mms) mms_forcing(D.P, D.Bk[b], D.t);
     }
     // enforce_bound_iface_conditions (block 1 then block 2)
     bool frame = want_frame && stage == 1;
     if (frame) grow_frames(D);
     for (int b = 0; b < 2; ++b) {
-      impose_bc(D.Bk[b], D.weighted_bc);
+      impose_bc(D.Bk[b], D.weighted_bc, D.P.use_mms ? &D.P : nullptr, D.t);
       impose_interface(D, b, stage, frame && b == 0);
     }
     if (frame) {
@@ -2422,6 +2502,18 @@ static void* create_domain(Domain* D, const Media& md) {
     delete D;
     return nullptr;
   }
+  if (D->P.use_mms) {
+    // the manufactured solution is smooth across the fault: it needs a
+    // locked interface, an elastic medium, no PML and no point sources
+    bool pml = false;
+    for (int b = 0; b < 2; ++b)
+      for (int d = 0; d < 3; ++d) pml = pml || D->P.btp[b].pml_lqrs[d] || D->P.btp[b].pml_rqrs[d];
+    if (!D->locked || D->P.response != "elastic" || pml || D->P.use_moment_tensor) {
+      std::snprintf(g_err, sizeof(g_err), "use_mms needs coupling='locked', response='elastic', no PML and no sources");
+      delete D;
+      return nullptr;
+    }
+  }
   if (D->plastic && !D->scec) {
     std::snprintf(g_err, sizeof(g_err), "only plastic_model='scec' is restated");
     delete D;
@@ -2467,6 +2559,15 @@ static void* create_domain(Domain* D, const Media& md) {
   }
   D->fr.nr = nr;
   D->fr.ns = ns;
+  if (D->P.use_mms)  // initial state: the exact solution at t = 0
+    for (int b = 0; b < 2; ++b) {
+      RBlock& B = D->Bk[b];
+      for (size_t p = 0; p < B.np; ++p) {
+        wp x[3] = {B.X[0][p], B.X[1][p], B.X[2][p]}, u[9];
+        mms_eval(D->P, 0.0, x, u);
+        for (int c = 0; c < 9; ++c) B.F[c][p] = u[c];
+      }
+    }
   if (D->P.use_moment_tensor) {
     const wql::Problem& P = D->P;
     std::string bad;
@@ -2558,6 +2659,26 @@ int wqlref_get_face(void* h, int block, int side, int what, double* out) {
   const Face& F = D->Bk[block].B[side];
   const vector<wp>& v = what < 3 ? F.n_n[what] : what < 6 ? F.n_m[what - 3] : F.n_l[what - 6];
   std::memcpy(out, v.data(), v.size() * sizeof(double));
+  return 0;
+}
+
+// Manufactured-solution error of block `block` at the current time: per
+// field component, err2 = sum over grid points of (F - u_exact)^2 and
+// ref2 = sum of u_exact^2.
+int wqlref_mms_norms(void* h, int block, double* err2, double* ref2) {
+  Domain* D = (Domain*)h;
+  if (block < 0 || block > 1 || !D->P.use_mms) return 1;
+  const RBlock& B = D->Bk[block];
+  for (int c = 0; c < 9; ++c) err2[c] = ref2[c] = 0.0;
+  for (size_t p = 0; p < B.np; ++p) {
+    wp x[3] = {B.X[0][p], B.X[1][p], B.X[2][p]}, u[9];
+    mms_eval(D->P, D->t, x, u);
+    for (int c = 0; c < 9; ++c) {
+      const wp e = B.F[c][p] - u[c];
+      err2[c] += e * e;
+      ref2[c] += u[c] * u[c];
+    }
+  }
   return 0;
 }
 

@@ -28,6 +28,7 @@ def lib():
         L.wqlref_get_geom.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_get_iface.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
         L.wqlref_get_face.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_mms_norms.argtypes = [vp, ctypes.c_int, vp, vp]
         L.wqlref_info.argtypes = [vp, vp, vp, vp, vp, vp]
         L.wqlref_create_ex.restype = ctypes.c_void_p
         L.wqlref_create_ex.argtypes = [ctypes.c_char_p] + [vp] * 9
@@ -108,6 +109,12 @@ class Oracle:
         for w in range(9):
             assert lib().wqlref_get_face(self.h, block, side, w, out[w].ctypes.data) == 0
         return out[0:3], out[3:6], out[6:9]
+
+    def mms_norms(self, block):
+        """Per component: sum of (F - u_exact)^2 and of u_exact^2 over the block."""
+        e, r = np.empty(9), np.empty(9)
+        assert lib().wqlref_mms_norms(self.h, block, e.ctypes.data, r.ctypes.data) == 0
+        return e, r
 
     def iface(self, block, what):
         nr, ns = self.dims[0][1], self.dims[0][2]

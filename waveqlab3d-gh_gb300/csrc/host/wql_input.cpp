@@ -355,6 +355,14 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
       set_block_field(P.btp[blk], field, it.values);
   }
 
+  for (auto& it : items_of("mms_list")) {
+    auto s = it.values.empty() ? std::string() : it.values[0];
+    if (it.key == "use_mms") P.use_mms = to_bool(s);
+    else if (it.key == "nt") P.mms_nt = to_double(s);
+    else if (it.key == "nx") P.mms_nx = to_double(s);
+    else if (it.key == "ny") P.mms_ny = to_double(s);
+    else if (it.key == "nz") P.mms_nz = to_double(s);
+  }
   for (auto& it : items_of("moment_list")) {
     auto s = it.values.empty() ? std::string() : it.values[0];
     if (it.key == "use_moment_tensor") P.use_moment_tensor = to_bool(s);

@@ -101,6 +101,11 @@ struct Problem {
   // '!---begin:tensor_list---' for both blocks, else tensor_listU / tensor_listV
   bool mt_unified = false;
   std::vector<MomentSource> tensors, tensorsU, tensorsV;
+  // &mms_list (src/mms.f90:17-49): the manufactured solution
+  // u = cos(nt pi t) * (sin sin sin for velocities, cos cos cos for stresses)
+  // of (nx pi x, ny pi y, nz pi z), defaults nt = 2, nx = ny = nz = 1
+  bool use_mms = false;
+  double mms_nt = 2.0, mms_nx = 1.0, mms_ny = 1.0, mms_nz = 1.0;
   // &output_list (src/seismogram.f90:58-82): seismograms on/off, the station
   // file directory (default 'seismogram') and the file naming by physical
   // position instead of grid index

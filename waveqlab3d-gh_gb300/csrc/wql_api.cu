@@ -128,6 +128,8 @@ struct wql_scn {
     void* Deta = nullptr;  // and their rates
     void* qs = nullptr;    // 1/Qs per point
     void* y = nullptr;
+    void* ms = nullptr;    // manufactured-solution shapes (2 x np) and
+    void* mp = nullptr;    // forcing shapes (9 x np), use_mms only
     double cart_metric[3] = {1, 1, 1};
     double tau_h[3] = {};
     StencilMaps maps{};  // TMA tensor maps (FP32 fields)
@@ -143,6 +145,11 @@ struct wql_scn {
   int bc_form = BC_CHARACTERISTIC;
   double rs_tol = 1.0e-12;  // FP64 regula falsi tolerance and iteration cap
   int rs_maxit = 5000;
+  // manufactured solution (&mms_list use_mms): T(t) = cos(kt t) and T'(t)
+  // at the current stage's time, and an 18-double accumulator for the norms
+  bool mms = false;
+  double mms_kt = 0.0, mms_T = 1.0, mms_Tp = 0.0;
+  double* mms_acc = nullptr;
   // a step advanced stage by stage (wql_stage): the next stage to run (1:
   // no step in progress) and the step's context
   int next_stage = 1;
@@ -543,6 +550,16 @@ int setup_block(wql_scn* S, int b) {
   const double tau0 = S->fd == 1 ? kTau0Upwind6 : (S->fd == 2 ? kTau0Upwind5 : 1.0 / (0.315949074074074));
   const int dims[3] = {B.nq, B.nr, B.ns};
   for (int d = 0; d < 3; ++d) B.tau_h[d] = tau0 / (1.0 / (double)(dims[d] - 1));
+  // manufactured solution: shapes, forcing shapes and the initial fields
+  if (S->mms) {
+    if ((rc = S->alloc(&B.ms, 2 * B.np * S->esz))) return rc;
+    if ((rc = S->alloc(&B.mp, 9 * B.np * S->esz))) return rc;
+    const double pi = 3.141592653589793;
+    const MmsWave w{S->P.mms_nx * pi, S->P.mms_ny * pi, S->P.mms_nz * pi};
+    launch_mms_setup(B.nq, B.nr, B.ns, B.pq, w, x, mat, mat + np, mat + 2 * np, S->prec == WQL_FP64, B.ms, B.mp,
+                     B.F[S->cur], S->stream);
+    CK(cudaGetLastError());
+  }
   // depth coordinate for the plastic update
   if (S->plastic) {
     if ((rc = S->alloc(&B.y, B.np * S->esz))) return rc;
@@ -743,6 +760,17 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   S->bc_form = Pr.bc_penalty == "weighted" ? BC_WEIGHTED : BC_CHARACTERISTIC;
   S->rs_tol = Pr.rs_tol;
   S->rs_maxit = Pr.rs_maxit;
+  S->mms = Pr.use_mms;
+  if (S->mms) {
+    // the manufactured solution is smooth across the fault: a locked
+    // interface, an elastic medium, no PML and no point sources
+    bool pml = false;
+    for (int b = 0; b < 2; ++b)
+      for (int d = 0; d < 3; ++d) pml = pml || Pr.btp[b].pml_lqrs[d] || Pr.btp[b].pml_rqrs[d];
+    if (Pr.coupling != "locked" || Pr.response != "elastic" || pml || Pr.use_moment_tensor)
+      return fail(WQL_E_INPUT, "use_mms needs coupling='locked', response='elastic', no PML and no sources");
+    S->mms_kt = Pr.mms_nt * 3.141592653589793;
+  }
   S->plastic = Pr.response == "plastic";
   if (S->plastic && Pr.plastic_model != "scec")
     return fail(WQL_E_INPUT, "only plastic_model='scec' is supported");
@@ -843,6 +871,7 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   if ((rc = S->alloc(&S->sat, 2 * 9 * nf * S->esz))) return rc;
   if ((rc = S->alloc((void**)&S->solver_fail, sizeof(unsigned int)))) return rc;
   if ((rc = S->alloc((void**)&S->err_dev, sizeof(int)))) return rc;
+  if (S->mms && (rc = S->alloc((void**)&S->mms_acc, 18 * sizeof(double)))) return rc;
   if (fp.coupling == CPL_SW || fp.coupling == CPL_RS)
     if ((rc = precompute_fault(S.get()))) return rc;
   if (fp.coupling == CPL_RS)
@@ -955,6 +984,10 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
     a.an_w[m] = S->an_w[m];
   }
   a.pml_d0 = 6.0 / (2.0 * 1.0) * std::log(1.0 / 1.0e-3);
+  a.ms = (const T*)B.ms;
+  a.mp = (const T*)B.mp;
+  a.mms_T = (T)S->mms_T;
+  a.mms_Tp = (T)S->mms_Tp;
   B.maps.cur = S->cur;
   a.tma = &B.maps;
   return a;
@@ -1023,6 +1056,15 @@ void stage_head(wql_scn* S, StepCtx& c, int stage) {
   }
   ia.rs_tol = S->rs_tol;
   ia.rs_maxit = S->rs_maxit;
+  if (S->mms) {
+    // T(t) and T'(t) of the manufactured solution at this stage's time, for
+    // the interface here and the block phases of the same stage
+    S->mms_T = std::cos(S->mms_kt * ts);
+    S->mms_Tp = -S->mms_kt * std::sin(S->mms_kt * ts);
+    ia.ms0 = S->B[0].ms;
+    ia.ms1 = S->B[1].ms;
+    ia.mms_T = S->mms_T;
+  }
   ia.fp = S->fp;
   ia.frame = (c.want_frame && stage == 1) ? S->frame_dev + (size_t)S->frame_fill * kFrameWords * nf : nullptr;
   ia.solver_fail = S->solver_fail;
@@ -1526,11 +1568,22 @@ int wql_get_field_noalloc(wql_scn* scn, int block, int comp, double* host_out) {
     return fail(WQL_E_INPUT, "bad argument");
   auto& B = scn->B[block];
   const int dev = scn->ctx->device;
+  // the caller's current device is restored on every return
+  struct DeviceGuard {
+    int prev = -1;
+    ~DeviceGuard() {
+      if (prev >= 0) cudaSetDevice(prev);
+    }
+  } guard;
+  CK(cudaGetDevice(&guard.prev));
   CK(cudaSetDevice(dev));
   CK(cudaStreamSynchronize(scn->stream));
   if (scn->prec == WQL_FP64) {
-    CK(cudaMemcpy2D(host_out, B.nq * sizeof(double), (const double*)B.F[scn->cur] + comp * B.np,
-                    B.pq * sizeof(double), B.nq * sizeof(double), (size_t)B.nr * B.ns, cudaMemcpyDeviceToHost));
+    // ordered on the scenario's stream only (no legacy-stream synchronisation)
+    CK(cudaMemcpy2DAsync(host_out, B.nq * sizeof(double), (const double*)B.F[scn->cur] + comp * B.np,
+                         B.pq * sizeof(double), B.nq * sizeof(double), (size_t)B.nr * B.ns, cudaMemcpyDeviceToHost,
+                         scn->stream));
+    CK(cudaStreamSynchronize(scn->stream));
     return WQL_OK;
   }
   const long long plane = (long long)B.pq * B.nr;
@@ -1583,6 +1636,30 @@ int wql_get_iface(wql_scn* scn, int copy, int what, double* host_out) {
   else src = scn->trup + (long long)copy * nf;
   CK(cudaStreamSynchronize(scn->stream));
   CK(cudaMemcpy(host_out, src, nf * sizeof(double), cudaMemcpyDeviceToHost));
+  return WQL_OK;
+}
+
+int wql_mms_norms(wql_scn* scn, int block, double* err2, double* ref2) {
+  if (!scn || !err2 || !ref2 || block < 0 || block > 1) return fail(WQL_E_INPUT, "bad argument");
+  if (!scn->mms) return fail(WQL_E_INPUT, "the scenario has no manufactured solution (&mms_list use_mms)");
+  if (scn->next_stage != 1) return fail(WQL_E_INPUT, "a step is in progress (wql_stage)");
+  const auto& B = scn->B[block];
+  const double Tt = std::cos(scn->mms_kt * scn->t);
+  double acc[18];
+  CK(cudaMemsetAsync(scn->mms_acc, 0, sizeof(acc), scn->stream));
+  if (scn->prec == WQL_FP64)
+    launch_mms_norms<double>(B.nq, B.nr, B.ns, B.pq, (const double*)B.F[scn->cur], (const double*)B.ms, Tt,
+                             scn->mms_acc, scn->stream);
+  else
+    launch_mms_norms<float>(B.nq, B.nr, B.ns, B.pq, (const float*)B.F[scn->cur], (const float*)B.ms, Tt,
+                            scn->mms_acc, scn->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(acc, scn->mms_acc, sizeof(acc), cudaMemcpyDeviceToHost, scn->stream));
+  CK(cudaStreamSynchronize(scn->stream));
+  for (int c = 0; c < 9; ++c) {
+    err2[c] = acc[c];
+    ref2[c] = acc[9 + c];
+  }
   return WQL_OK;
 }
 

@@ -154,8 +154,24 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(
   const int j = (int)(f % a.nr), k = (int)(f / a.nr);
   // fields on both faces: block 0 at q = nq0-1, block 1 at q = 0
   R u[9], v[9];
-  load_face<T>(a.F0, a.np0, (a.nq0 - 1) + (long long)a.pq0 * (j + (long long)a.nr * k), u);
-  load_face<T>(a.F1, a.np1, (long long)a.pq1 * (j + (long long)a.nr * k), v);
+  const long long pu = (a.nq0 - 1) + (long long)a.pq0 * (j + (long long)a.nr * k);
+  const long long pv = (long long)a.pq1 * (j + (long long)a.nr * k);
+  load_face<T>(a.F0, a.np0, pu, u);
+  load_face<T>(a.F1, a.np1, pv, v);
+  if (a.ms0) {
+    // manufactured solution: both sides' velocities and tractions less the
+    // exact solution at their own fault points (src/CouplingForcing.f90:147-185)
+    const T* s0 = (const T*)a.ms0;
+    const T* s1 = (const T*)a.ms1;
+    const R Tt = (R)a.mms_T;
+    const R u_v = Tt * s0[pu], u_s = Tt * s0[a.np0 + pu];
+    const R v_v = Tt * s1[pv], v_s = Tt * s1[a.np1 + pv];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+      u[c] -= c < 3 ? u_v : u_s;
+      v[c] -= c < 3 ? v_v : v_s;
+    }
+  }
   const double* face = b == 0 ? a.face0 : a.face1;
   R n[3], m[3], l[3];
 #pragma unroll
@@ -315,8 +331,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(
       float* fr = a.frame;
 #pragma unroll
       for (int c = 0; c < 9; ++c) {
-        fr[(FR_UFACE + c) * nf + f] = (float)u[c];
-        fr[(FR_VFACE + c) * nf + f] = (float)v[c];
+        fr[(FR_UFACE + c) * nf + f] = (float)((const T*)a.F0)[c * a.np0 + pu];
+        fr[(FR_VFACE + c) * nf + f] = (float)((const T*)a.F1)[c * a.np1 + pv];
       }
 #pragma unroll
       for (int c = 0; c < 4; ++c) fr[(FR_S + c) * nf + f] = (float)S[c * nf + f];

@@ -88,6 +88,14 @@ struct VolumeArgs {
   int* err;                      // device error word (pipeline wait timeouts)
   double pml_d0;                 // PML damping scale 3 ln(1000)
   const void* tma;               // host pointer to the block's StencilMaps (FP32 only)
+  // manufactured solution (&mms_list use_mms): u_exact = T(t) S(x), where S
+  // is sin*sin*sin for the velocities (ms[0..np)) and cos*cos*cos for the
+  // stresses (ms[np..2np)); the forcing is T(t) mp - T'(t) S with mp the
+  // 9 x np operator shapes.  nullptr without; mms_T and mms_Tp are T and T'
+  // at the stage's time.
+  const T* ms;
+  const T* mp;
+  T mms_T, mms_Tp;
 };
 
 struct InterfaceArgs {
@@ -119,6 +127,11 @@ struct InterfaceArgs {
   FaultParams fp;
   float* frame;             // 39 x nf or nullptr
   unsigned int* solver_fail;  // count of non-converged rate-and-state solves
+  // manufactured solution: the two blocks' shapes (2 x np, field type) or
+  // nullptr, and T(t) at the stage's time
+  const void* ms0;
+  const void* ms1;
+  double mms_T;
 };
 
 // Frame record layout (floats per fault point, component-major):
@@ -213,5 +226,18 @@ void launch_faces(int nq, int nr, int ns, const double* metric, const double* la
 template <typename T>
 void launch_coef(int nq, int nr, int ns, int pq, bool curv, const double* metric, const double* J,
                  const double* lam, const double* mu, const double* rho, T* coef, void* stream);
+// Manufactured solution (&mms_list): wavenumbers kx, ky, kz = n pi of the
+// space factors (src/mms.f90:136-150).  The set-up writes the shapes ms
+// (2 x np), the forcing shapes mp (9 x np) and the initial fields F of one
+// block in the field type; the norms kernel adds, per component, the sums
+// of (F - T S)^2 and (T S)^2 into acc[0..18).
+struct MmsWave {
+  double kx, ky, kz;
+};
+void launch_mms_setup(int nq, int nr, int ns, int pq, const MmsWave& w, const double* x, const double* lam,
+                      const double* mu, const double* rho, bool fp64, void* ms, void* mp, void* F, void* stream);
+template <typename T>
+void launch_mms_norms(int nq, int nr, int ns, int pq, const T* F, const T* ms, double Tt, double* acc,
+                      void* stream);
 
 }  // namespace wql

@@ -224,6 +224,109 @@ void launch_anelastic_material(long long n, double c, const double den[4], const
                                                                                             qsinv);
 }
 
+// Manufactured-solution shapes (src/mms.f90:136-232), one thread per point,
+// in FP64 from the dense grid and material: u_exact = T(t) S with
+// S = sin(kx x) sin(ky y) sin(kz z) for the velocities and
+// cos(kx x) cos(ky y) cos(kz z) for the stresses, T = cos(kt t); the operator
+// shapes mp = A S_x + B S_y + C S_z of mms_forcing (src/mms.f90:104-122), so
+// that the forcing f = A u_x + B u_y + C u_z - u_t is T(t) mp - T'(t) S; and
+// the initial fields F = S (T(0) = 1).  Outputs are pitched (row pitch pq).
+__global__ void mms_setup_kernel(long long npd, int nq, int pq, long long np, MmsWave w,
+                                 const double* __restrict__ x, const double* __restrict__ lam,
+                                 const double* __restrict__ mu, const double* __restrict__ rho, int fp64,
+                                 void* ms, void* mp, void* F) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= npd) return;
+  const long long o = p % nq + (long long)pq * (p / nq);
+  const double X = x[p], Y = x[npd + p], Z = x[2 * npd + p];
+  const double sx = sin(w.kx * X), sy = sin(w.ky * Y), sz = sin(w.kz * Z);
+  const double cx = cos(w.kx * X), cy = cos(w.ky * Y), cz = cos(w.kz * Z);
+  const double sv = sx * sy * sz, ss = cx * cy * cz;
+  // space derivatives of the velocity and stress shapes
+  const double vx = w.kx * cx * sy * sz, vy = w.ky * sx * cy * sz, vz = w.kz * sx * sy * cz;
+  const double tx = -w.kx * sx * cy * cz, ty = -w.ky * cx * sy * cz, tz = -w.kz * cx * cy * sz;
+  const double l = lam[p], m = mu[p], r = rho[p];
+  double P[9];
+  P[0] = (1.0 / r) * (tx + ty + tz);
+  P[1] = P[0];
+  P[2] = P[0];
+  P[3] = (2.0 * m + l) * vx + l * vy + l * vz;
+  P[4] = l * vx + (2.0 * m + l) * vy + l * vz;
+  P[5] = l * vx + l * vy + (2.0 * m + l) * vz;
+  P[6] = m * (vy + vx);
+  P[7] = m * (vz + vx);
+  P[8] = m * (vz + vy);
+  if (fp64) {
+    double* s = (double*)ms;
+    double* q = (double*)mp;
+    double* f = (double*)F;
+    s[o] = sv;
+    s[np + o] = ss;
+    for (int c = 0; c < 9; ++c) {
+      q[c * np + o] = P[c];
+      f[c * np + o] = c < 3 ? sv : ss;
+    }
+  } else {
+    float* s = (float*)ms;
+    float* q = (float*)mp;
+    float* f = (float*)F;
+    s[o] = (float)sv;
+    s[np + o] = (float)ss;
+    for (int c = 0; c < 9; ++c) {
+      q[c * np + o] = (float)P[c];
+      f[c * np + o] = (float)(c < 3 ? sv : ss);
+    }
+  }
+}
+
+void launch_mms_setup(int nq, int nr, int ns, int pq, const MmsWave& w, const double* x, const double* lam,
+                      const double* mu, const double* rho, bool fp64, void* ms, void* mp, void* F, void* stream) {
+  const long long npd = (long long)nq * nr * ns, np = (long long)pq * nr * ns;
+  mms_setup_kernel<<<(unsigned)((npd + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      npd, nq, pq, np, w, x, lam, mu, rho, fp64 ? 1 : 0, ms, mp, F);
+}
+
+// Sums over the points of one block, per field component, of
+// (F - T S)^2 and (T S)^2 (acc[0..9) and acc[9..18), accumulated in FP64).
+template <typename T>
+__global__ void mms_norms_kernel(int nq, int nr, int ns, int pq, long long np, const T* __restrict__ F,
+                                 const T* __restrict__ ms, double Tt, double* acc) {
+  const long long npd = (long long)nq * nr * ns;
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double e[9], r[9];
+  for (int c = 0; c < 9; ++c) e[c] = r[c] = 0.0;
+  if (p < npd) {
+    const long long o = p % nq + (long long)pq * (p / nq);
+    const double sv = Tt * (double)ms[o], ss = Tt * (double)ms[np + o];
+    for (int c = 0; c < 9; ++c) {
+      const double u = c < 3 ? sv : ss;
+      const double d = (double)F[c * np + o] - u;
+      e[c] = d * d;
+      r[c] = u * u;
+    }
+  }
+  for (int c = 0; c < 9; ++c)
+    for (int off = 16; off > 0; off >>= 1) {
+      e[c] += __shfl_down_sync(0xffffffffu, e[c], off);
+      r[c] += __shfl_down_sync(0xffffffffu, r[c], off);
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int c = 0; c < 9; ++c) {
+      atomicAdd(acc + c, e[c]);
+      atomicAdd(acc + 9 + c, r[c]);
+    }
+}
+
+template <typename T>
+void launch_mms_norms(int nq, int nr, int ns, int pq, const T* F, const T* ms, double Tt, double* acc,
+                      void* stream) {
+  const long long npd = (long long)nq * nr * ns, np = (long long)pq * nr * ns;
+  mms_norms_kernel<T><<<(unsigned)((npd + 255) / 256), 256, 0, (cudaStream_t)stream>>>(nq, nr, ns, pq, np, F, ms,
+                                                                                       Tt, acc);
+}
+template void launch_mms_norms<double>(int, int, int, int, const double*, const double*, double, double*, void*);
+template void launch_mms_norms<float>(int, int, int, int, const float*, const float*, double, double*, void*);
+
 template void launch_coef<double>(int, int, int, int, bool, const double*, const double*, const double*,
                                   const double*, const double*, double*, void*);
 template void launch_coef<float>(int, int, int, int, bool, const double*, const double*, const double*,

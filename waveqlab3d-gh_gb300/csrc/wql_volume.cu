@@ -898,6 +898,36 @@ __global__ void __launch_bounds__(256, WQL_ANEL_MINB) anelastic_kernel(const __g
 }
 
 // ---------------------------------------------------------------------------
+// With a manufactured solution the boundary penalty acts on the fields less
+// the exact solution at the stage's time (u = F - switch*fu,
+// src/BoundaryConditions.f90:86-92, 126).
+template <typename T>
+__device__ __forceinline__ void mms_deviation(const VolumeArgs<T>& a, long long p, T (&u)[9]) {
+  if (!a.ms) return;
+  const T sv = a.mms_T * a.ms[p], ss = a.mms_T * a.ms[a.np + p];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) u[c] -= c < 3 ? sv : ss;
+}
+
+// Manufactured-solution forcing (mms_forcing, src/mms.f90:77-133, which the
+// reference never calls): DF -= T(t) mp - T'(t) S at every point of the
+// block, with the matching update of F_out.
+template <typename T, bool KAHAN>
+__global__ void __launch_bounds__(256) mms_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= a.nq || j >= a.nr) return;
+  const long long np = a.np;
+  const long long p = i + (long long)a.pq * (j + (long long)a.nr * k);
+  const T sv = a.ms[p], ss = a.ms[np + p];
+  T corr[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) corr[c] = -(a.mms_T * a.mp[c * np + p] - a.mms_Tp * (c < 3 ? sv : ss));
+  add_correction<T, KAHAN>(a, p, corr);
+}
+
+// ---------------------------------------------------------------------------
 // Face kernel: outer-boundary SAT (src/RHS_Interior.f90:1516-1703 with
 // src/BoundaryConditions.f90:777-918 + structure(), or the weighted form of
 // src/BoundaryConditions3.f90:777-903) and the fault SAT computed by the
@@ -930,6 +960,7 @@ __global__ void __launch_bounds__(256) face_kernel(const __grid_constant__ Volum
   const long long p = i + (long long)a.pq * (j + (long long)nr * k);
   T u[9], tot[9], corr[9];
   for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
+  mms_deviation(a, p, u);
   const bool any = face_penalty(a, i, j, k, u, tot);
   for (int c = 0; c < 9; ++c) corr[c] = -tot[c];
   if (any) add_correction<T, KAHAN>(a, p, corr);
@@ -972,6 +1003,7 @@ __global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ V
   T u[9], tot[9];
 #pragma unroll
   for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
+  mms_deviation(a, p, u);
   if (!face_penalty(a, i, j, k, u, tot)) return;
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
@@ -1154,6 +1186,10 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
   if (!stencil_is_tma(a)) {
     const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
     face_kernel<T, KAHAN><<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(a);
+    ++n;
+  }
+  if (a.mp) {
+    mms_kernel<T, KAHAN><<<grd, blk, 0, s>>>(a);
     ++n;
   }
   if (a.plastic) {

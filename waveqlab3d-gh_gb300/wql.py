@@ -28,7 +28,7 @@ EXPORTS = ["wql_last_error", "wql_ctx_create", "wql_ctx_destroy", "wql_scenario_
            "wql_batch_add", "wql_batch_remove", "wql_batch_step", "wql_batch_stream",
            "wql_estimate_device_bytes", "wql_server_create", "wql_server_submit", "wql_server_wait",
            "wql_server_result", "wql_server_release", "wql_server_stats", "wql_server_destroy",
-           "wql_autotune", "wql_write_outputs", "wql_write_block_grids", "wql_stage"]
+           "wql_autotune", "wql_write_outputs", "wql_write_block_grids", "wql_stage", "wql_mms_norms"]
 
 
 class Media(ctypes.Structure):
@@ -98,6 +98,7 @@ def lib():
         L.wql_stage.argtypes = [vp, ci]
         L.wql_write_block_grids.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         L.wql_get_iface.argtypes = [vp, ci, ci, vp]
+        L.wql_mms_norms.argtypes = [vp, ci, vp, vp]
         L.wql_frame_count.argtypes = [vp, ctypes.POINTER(ci)]
         L.wql_get_frames.argtypes = [vp, ci, vp]
         L.wql_scenario_stream.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
@@ -252,6 +253,12 @@ class Scenario:
         out = np.empty(nr * ns, np.float64)
         _check(lib().wql_get_iface(self.h, copy, what, out.ctypes.data))
         return out.reshape(ns, nr)
+
+    def mms_norms(self, block):
+        """Per component: sum of (F - u_exact)^2 and of u_exact^2 over the block."""
+        e, r = np.empty(9), np.empty(9)
+        _check(lib().wql_mms_norms(self.h, block, e.ctypes.data, r.ctypes.data))
+        return e, r
 
     def frame_count(self):
         n = ctypes.c_int()
