@@ -128,7 +128,14 @@ def allsum(world, v):
 def workload(args):
     import wql_configs
     if args.workload == "config2":
-        text, media = wql_configs.config2(steps=10 ** 6, seed=args.seed)
+        # --n scales the blocks to (2n - 1) x n x n (201: the configured 401 x 201 x 201)
+        text, media = wql_configs.config2(nq=2 * args.n - 1, nrs=args.n, steps=10 ** 6, seed=args.seed)
+    elif args.workload == "config3_member":
+        medium = wql_configs.von_karman((2 * 160 - 1, 160, 160), (0.1, 0.1, 0.1), 2.0, 0.2, 0.05, 3131)
+        text, media, _ = wql_configs.config3_scenario(args.member, steps=10 ** 6, medium=medium)
+    elif args.workload == "config4_request":
+        medium = wql_configs.config4_medium(256, h=0.05)
+        text, media, _ = wql_configs.config4_request(args.member, steps=10 ** 6, medium=medium)
     elif args.workload in ("upwind", "upwind_anelastic"):
         text, media = wql_configs.upwind_pml12(steps=10 ** 6, anelastic=args.workload == "upwind_anelastic")
     else:
@@ -246,7 +253,9 @@ def accuracy(wql, ctx, text, media, steps, stride=20):
     """FP32C against FP64 on the same workload after `steps` steps: relative
     L2 of the velocity fields and of the slip, relative error of the peak
     slip rate (over fault frames every `stride` steps) and the largest
-    rupture-time difference in time steps over points that ruptured in both."""
+    rupture-time difference in time steps over points that ruptured in both,
+    with the number of points at each difference; for workloads with
+    stations, the relative L2 of the seismograms."""
     import numpy as np
     text_f = text.replace("w_fault = F", "w_fault = T").replace("w_stride = 1", f"w_stride = {stride}")
     out = {}
@@ -256,7 +265,8 @@ def accuracy(wql, ctx, text, media, steps, stride=20):
         for _ in range(0, steps, 100):
             s.step(min(100, steps - _))
         s.sync(check_nan=True)
-        runs[name] = dict(v=[np.concatenate([s.field(b, c).ravel() for c in range(3)]) for b in range(2)],
+        seis = [s.stations(b)[1] for b in range(2)] if "output_seismograms = T" in text_f else None
+        runs[name] = dict(seis=seis, v=[np.concatenate([s.field(b, c).ravel() for c in range(3)]) for b in range(2)],
                           slip=s.iface(0, 3), trup=s.iface(0, 5),
                           peak=float(np.sqrt((s.frames("Svel")[:, 1:3].astype(np.float64) ** 2).sum(axis=1)).max()),
                           dt=s.info().dt)
@@ -273,6 +283,12 @@ def accuracy(wql, ctx, text, media, steps, stride=20):
     out["ruptured_points_fp64"] = int(rup_d.sum())
     out["ruptured_points_fp32c"] = int(rup_f.sum())
     out["rupture_time_err_dt"] = float(np.abs(f["trup"][both] - d["trup"][both]).max() / d["dt"]) if both.any() else None
+    if both.any():
+        k = np.rint(np.abs(f["trup"][both] - d["trup"][both]) / d["dt"]).astype(int)
+        out["rupture_time_err_points"] = {str(v): int((k == v).sum()) for v in np.unique(k)}
+    if d["seis"] is not None:
+        out["seismogram_rel_l2"] = max(rel(f["seis"][b][..., 1:], d["seis"][b][..., 1:])
+                                       for b in range(2) if d["seis"][b].size)
     return out
 
 
@@ -406,7 +422,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
                     help="step: config 1 (default); batch: config 3 ensemble in one batch; serve: config 4 stream")
-    ap.add_argument("--workload", default="config1", choices=["config1", "config2", "upwind", "upwind_anelastic"],
+    ap.add_argument("--member", type=int, default=0,
+                    help="config3_member / config4_request: which seeded member or request")
+    ap.add_argument("--workload", default="config1",
+                    choices=["config1", "config2", "upwind", "upwind_anelastic", "config3_member", "config4_request"],
                     help="step mode: config1 (2 x n^3 curvilinear, rate and state), config2 (2 x 401x201x201, "
                          "PML, von Karman, plasticity), upwind (2 x 76x101x151 Cartesian, upwind SBP-6, PML, "
                          "point source) or upwind_anelastic (the same with the anelastic response)")
@@ -422,8 +441,13 @@ def main():
     wl = (f"config1: 2 x {args.n}^3 curvilinear blocks, seeded topography + self-similar rough fault, "
           f"aging-law rate-and-state, {ups // 5} grid points")
     if args.workload == "config2":
-        wl = (f"config2: 2 x 401x201x201 curvilinear blocks, 20-point PML on 5 sides, von Karman medium, "
+        wl = (f"config2: 2 x {2 * args.n - 1}x{args.n}x{args.n} curvilinear blocks, 20-point PML on 5 sides, "
+              f"von Karman medium, "
               f"scec viscoplasticity, TPV26 stress, slip weakening, {ups // 5} grid points")
+    if args.workload == "config3_member":
+        wl = f"config3 member {args.member} (seeded, 10-point PML, slip weakening), {ups // 5} grid points"
+    if args.workload == "config4_request":
+        wl = f"config4 request {args.member} (seeded point source, 32 stations), {ups // 5} grid points"
     if args.workload in ("upwind", "upwind_anelastic"):
         wl = (f"{args.workload}: 2 x 76x101x151 Cartesian blocks, upwind SBP-6 operators, 12-point PML on 5 sides, "
               f"locked interface, one moment-tensor source, "
@@ -509,6 +533,12 @@ def main():
         e2e = {"value": total_ups * args.steps / allmax(world, secs), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
                "includes": "scenario setup upload, per-step fault frame D2H, final velocity D2H"}
+        # the FP64 mode through the same public API path (like for like with
+        # the FP64 CPU baseline)
+        f_steps = res["fp64"]["steps"]
+        secs64, h2d64, d2h64 = time_e2e(wql, ctx, text, media, wql.FP64, f_steps)
+        e2e["fp64"] = {"value": total_ups * f_steps / allmax(world, secs64), "unit": UNIT, "steps": f_steps,
+                       "h2d_bytes_per_step": int(h2d64 / f_steps), "d2h_bytes_per_step": int(d2h64 / f_steps)}
     cpu = None
     if rank == 0 and not args.no_cpu:
         secs, cores = cpu_sample(text, media, args.cpu_steps)

@@ -116,7 +116,7 @@ def test_fp32c_error_vs_fp64(ctx, wqlmod, tmp_path, case):
     assert ruptured.any()
     terr = np.abs(tr_f[ruptured] - tr_d[ruptured]).max() / dt
     print(f"{case} FP32C vs FP64: vel relL2 {vel:.2e} slip relL2 {slip:.2e} peak-rate {peak:.2e} trup {terr:.2f} dt")
-    assert vel < 1e-4 and slip < 1e-4 and peak < 1e-4
+    assert vel < 1e-5 and slip < 1e-5 and peak < 1e-5
     assert terr <= 1.0
 
 

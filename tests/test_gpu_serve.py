@@ -51,18 +51,24 @@ def test_footprint_estimate(ctx, wqlmod, medium):
 
 
 def test_served_equals_alone(ctx, wqlmod, medium):
-    """Requests submitted while others run join the running batch; each
-    result equals the request run alone (bitwise)."""
+    """Requests submitted while another runs join the running batch: each is
+    admitted before the first one completes, so their work overlaps on the
+    device; each result equals the request run alone (bitwise)."""
     import wql_configs
-    steps = 24
+    steps = 120
     reqs = [wql_configs.config4_request(i, n_lo=24, n_hi=44, steps=steps, medium=medium) for i in range(4)]
     srv = wqlmod.Server(ctx, hbm_budget_bytes=64 << 30, round_steps=4)
-    ids = []
-    for text, media, _ in reqs:
+    ids = [srv.submit(reqs[0][0], steps, media=reqs[0][1])]
+    t_end = time.time() + 60.0
+    while srv.stats()["active"] < 1 and srv.stats()["completed"] < 1 and time.time() < t_end:
+        time.sleep(0.001)
+    for text, media, _ in reqs[1:]:
         ids.append(srv.submit(text, steps, media=media))
-        time.sleep(0.05)
     for rid in ids:
         assert srv.wait(rid, 300.0) == 1
+    times = [srv.result(rid, 0)[1] for rid in ids]
+    for k in range(1, len(ids)):
+        assert times[k][1] < times[0][2], (k, times[k], times[0])  # admitted while request 0 ran
     for (text, media, _), rid in zip(reqs, ids):
         ref = _alone(wqlmod, ctx, text, media, steps)
         for b in range(2):
