@@ -25,7 +25,7 @@
 //   presets ........................ src/Interface_Condition.f90:1268-2476,
 //                                    2722-2850, src/initial_stress_condition.f90
 //   plasticity ..................... src/plastic.f90:11-352
-//   grid/metrics/normals ........... src/grid.f90:13-469, 471-1068, 2290-2455,
+//   grid/metrics/normals ........... src/grid.f90:13-469, 471-1875, 2290-2500,
 //                                    src/metrics.f90:16-488,
 //                                    src/unit_normals.f90:8-282
 //   material ....................... src/material.f90:146-190
@@ -694,7 +694,236 @@ bool read_profile_rows(const std::string& path, size_t n, vector<wp>& x1, std::s
   return true;
 }
 
-// Gen3_Curve_Mesh src/grid.f90:2290-2416
+// Gen3_Curve_Mesh (src/grid.f90:2290-2416): component `comp` of the block
+// from its six faces; Lf, Rf on (j,k), Tf, Bf on (i,k), Ff, Kf on (i,j).
+void gen3_mesh(RBlock& B, int comp, const vector<wp>& Lf, const vector<wp>& Rf, const vector<wp>& Tf,
+               const vector<wp>& Bf, const vector<wp>& Ff, const vector<wp>& Kf) {
+  const int mx = B.nq, my = B.nr, mz = B.ns;
+  int nq = mx, nr = my, ns = mz;
+  wp hq = 1.0 / (wp)(nq - 1), hr = 1.0 / (wp)(nr - 1), hs = 1.0 / (wp)(ns - 1);
+  auto LK = [&](const vector<wp>& a, int j, int k) { return a[(size_t)(j - 1) + (size_t)my * (k - 1)]; };
+  auto IK = [&](const vector<wp>& a, int i, int k) { return a[(size_t)(i - 1) + (size_t)mx * (k - 1)]; };
+  auto IJ = [&](const vector<wp>& a, int i, int j) { return a[(size_t)(i - 1) + (size_t)mx * (j - 1)]; };
+  for (int k = 1; k <= mz; ++k)
+    for (int j = 1; j <= my; ++j)
+      for (int i = 1; i <= mx; ++i) {
+        wp q = (wp)(i - 1) * hq, r = (wp)(j - 1) * hr, s = (wp)(k - 1) * hs;
+        wp U = (1.0 - q) * LK(Lf, j, k) + q * LK(Rf, j, k);
+        wp V = (1.0 - r) * IK(Tf, i, k) + r * IK(Bf, i, k);
+        wp W = (1.0 - s) * IJ(Ff, i, j) + s * IJ(Kf, i, j);
+        wp UW = (1.0 - q) * ((1.0 - r) * LK(Lf, 1, k) + r * LK(Lf, nr, k)) +
+                q * ((1.0 - r) * LK(Rf, 1, k) + r * LK(Rf, nr, k));
+        wp UV = (1.0 - r) * ((1.0 - s) * IK(Tf, i, 1) + s * IK(Tf, i, ns)) +
+                r * ((1.0 - s) * IK(Bf, i, 1) + s * IK(Bf, i, ns));
+        wp VW = (1.0 - s) * ((1.0 - q) * IJ(Ff, 1, j) + q * IJ(Ff, nq, j)) +
+                s * ((1.0 - q) * IJ(Kf, 1, j) + q * IJ(Kf, nq, j));
+        wp UVW1 = (1.0 - q) * ((1.0 - r) * ((1.0 - s) * IK(Tf, 1, 1) + s * IK(Tf, 1, ns)) +
+                               r * ((1.0 - s) * IK(Bf, 1, 1) + s * IK(Bf, 1, ns)));
+        wp UVW2 = q * ((1.0 - r) * ((1.0 - s) * IK(Tf, nq, 1) + s * IK(Tf, nq, ns)) +
+                       r * ((1.0 - s) * IK(Bf, nq, 1) + s * IK(Bf, nq, ns)));
+        B.X[comp][B.id(i, j, k)] = U + V + W - UV - UW - VW + UVW1 + UVW2;
+      }
+}
+
+// read_2darray (src/grid.f90:2457-2481) of n rows of three columns: A[c][row]
+bool read_rows3(const std::string& path, size_t n, vector<wp> A[3], std::string& err) {
+  std::FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) {
+    err = "cannot open " + path;
+    return false;
+  }
+  for (int c = 0; c < 3; ++c) A[c].assign(n, 0.0);
+  size_t row = 0;
+  char buf[4096];
+  while (row < n && std::fgets(buf, sizeof(buf), f)) {
+    std::string line(buf);
+    for (auto& c : line)
+      if (c == 'd' || c == 'D') c = 'e';
+      else if (c == ',') c = ' ';
+    double a, b, c;
+    if (std::sscanf(line.c_str(), "%lf %lf %lf", &a, &b, &c) == 3) {
+      A[0][row] = a;
+      A[1][row] = b;
+      A[2][row] = c;
+      ++row;
+    }
+  }
+  std::fclose(f);
+  if (row != n) {
+    err = path + ": too few rows";
+    return false;
+  }
+  return true;
+}
+
+// Curve_Grid_3D3 with use_topography = T: src/grid.f90:1349-1875
+bool curve_grid_topo(RBlock& B, const wql::Problem& P, const wql::BlockParams& bp, std::string& err) {
+  int mx = B.nq, my = B.nr, mz = B.ns;
+  wp ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1], az = bp.aqrs[2], bz = bp.bqrs[2];
+  wp lc = bp.lc, rc = bp.rc, topo = P.topo;
+  auto fix = [&](std::string p) {
+    if (!p.empty() && p[0] != '/' && !P.base_dir.empty()) p = P.base_dir + "/" + p;
+    return p;
+  };
+  // top/bottom (i,k): index (i-1) + mx*(k-1)
+  auto IK = [&](int i, int k) { return (size_t)(i - 1) + (size_t)mx * (k - 1); };
+  auto JK = [&](int j, int k) { return (size_t)(j - 1) + (size_t)my * (k - 1); };
+  auto IJ = [&](int i, int j) { return (size_t)(i - 1) + (size_t)mx * (j - 1); };
+  vector<wp> Xt((size_t)mx * mz), Yt((size_t)mx * mz), Zt((size_t)mx * mz), Ybo((size_t)mx * mz);
+  for (int k = 1; k <= mz; ++k)
+    for (int i = 1; i <= mx; ++i) {
+      Ybo[IK(i, k)] = by;
+      Yt[IK(i, k)] = ay;
+    }
+  if (bp.topography_type == "analytical_topography") {  // :1364-1392
+    wp hx = (bx - ax) / (wp)(mx - 1), hz = (bz - az) / (wp)(mz - 1);
+    for (int k = 1; k <= mz; ++k)
+      for (int i = 1; i <= mx; ++i) {
+        Xt[IK(i, k)] = ax + (wp)(i - 1) * hx;
+        Zt[IK(i, k)] = az + (wp)(k - 1) * hz;
+        wp f = 0.0;
+        wp r1 = std::sqrt((Xt[IK(i, k)] - 10.0) * (Xt[IK(i, k)] - 10.0) + (Zt[IK(i, k)] - 10.0) * (Zt[IK(i, k)] - 10.0));
+        if (r1 <= 3.0) f = -0.3 * (1.0 + std::cos(PI * r1 / 3.0));
+        Yt[IK(i, k)] = ay - topo * 1.5 * f;
+      }
+  } else if (bp.topography_type == "read_topo_from_memory") {  // :1394-1425
+    vector<wp> T[3];
+    if (!read_rows3(fix(bp.topography_path), (size_t)mx * mz, T, err)) return false;
+    // reshape_2darray(XT, Topography(:,1), mz, mx): XT(k,i) = row (i-1)*mz + k
+    for (int k = 1; k <= mz; ++k)
+      for (int i = 1; i <= mx; ++i) {
+        size_t row = (size_t)(i - 1) * mz + (size_t)(k - 1);
+        Xt[IK(i, k)] = T[0][row];
+        Yt[IK(i, k)] = ay + topo * T[1][row];
+        Zt[IK(i, k)] = T[2][row];
+      }
+  } else {
+    err = "specify topography profile";
+    return false;
+  }
+  // x-faces (:1440-1518)
+  wp hx = 1.0 / (wp)(mx - 1), hy = 1.0 / (wp)(my - 1), hz = 1.0 / (wp)(mz - 1);
+  vector<wp> Yl, Zl, Yr, Zr;
+  {
+    vector<wp> Y0xT(my), Y0xB(my), Z0xT(my), Z0xB(my), Z0xL(mz), Z0xR(mz), Y0xL(mz), Y0xR(mz);
+    vector<wp> YnxT(my), YnxB(my), ZnxT(my), ZnxB(my), ZnxL(mz), ZnxR(mz), YnxL(mz), YnxR(mz);
+    for (int j = 1; j <= my; ++j) {
+      wp r = (wp)(j - 1) * hy, stretch = r;
+      Y0xT[j - 1] = Yt[IK(1, mz)] + (by - Yt[IK(1, mz)]) * stretch;
+      Y0xB[j - 1] = Yt[IK(1, 1)] + (by - Yt[IK(1, 1)]) * stretch;
+      Z0xT[j - 1] = bz;
+      Z0xB[j - 1] = az;
+    }
+    for (int k = 1; k <= mz; ++k) {
+      wp s = (wp)(k - 1) * hz;
+      Z0xL[k - 1] = az + (bz - az) * s;
+      Z0xR[k - 1] = az + (bz - az) * s;
+      Y0xR[k - 1] = by;
+      Y0xL[k - 1] = Yt[IK(1, k)];
+    }
+    for (int j = 1; j <= my; ++j) {
+      wp r = (wp)(j - 1) * hy, stretch = r;
+      YnxT[j - 1] = Yt[IK(mx, mz)] + (by - Yt[IK(mx, mz)]) * stretch;
+      YnxB[j - 1] = Yt[IK(mx, 1)] + (by - Yt[IK(mx, 1)]) * stretch;
+      ZnxT[j - 1] = bz;
+      ZnxB[j - 1] = az;
+    }
+    for (int k = 1; k <= mz; ++k) {
+      wp s = (wp)(k - 1) * hz;
+      ZnxL[k - 1] = az + (bz - az) * s;
+      ZnxR[k - 1] = az + (bz - az) * s;
+      YnxR[k - 1] = by;
+      YnxL[k - 1] = Yt[IK(mx, k)];
+    }
+    surf_mesh(my, mz, Y0xL, Y0xR, Y0xB, Y0xT, Z0xL, Z0xR, Z0xB, Z0xT, Yl, Zl);
+    surf_mesh(my, mz, YnxL, YnxR, YnxB, YnxT, ZnxL, ZnxR, ZnxB, ZnxT, Yr, Zr);
+  }
+  vector<wp> Xl((size_t)my * mz, ax), Xr((size_t)my * mz, bx);
+  const std::string& pt = bp.profile_type;
+  if (pt == "read_from_memomry_fractal") {  // :1538-1676
+    vector<wp> Fg[3];
+    if (!read_rows3(fix(bp.profile_path), (size_t)my * mz, Fg, err)) return false;
+    for (int k = 1; k <= mz; ++k)
+      for (int j = 1; j <= my; ++j) {
+        size_t p = JK(j, k);  // reshape_2darray(X1, ..., ny, nz): X1(j,k) = row (k-1)*ny + j
+        Xl[p] = ax;
+        Xr[p] = bx;
+        if (rc != 0.0) {
+          Xl[p] = ax + Fg[0][p];
+          Yl[p] = Fg[1][p];
+          Zl[p] = Fg[2][p];
+        }
+        if (lc != 0.0) {
+          Xr[p] = bx + Fg[0][p];
+          Yr[p] = Fg[1][p];
+          Zr[p] = Fg[2][p];
+        }
+      }
+  } else if (pt != "no_path") {
+    err = "specify fault profile";
+    return false;
+  }
+  // z-faces (:1695-1805)
+  vector<wp> Xf, Yf, Xbk, Ybk;
+  {
+    vector<wp> X0zT(mx), Y0zT(mx), X0zB(mx), Y0zB(mx), X0zL(my), X0zR(my), Y0zL(my), Y0zR(my);
+    for (int i = 1; i <= mx; ++i) {
+      wp q = (wp)(i - 1) * hx, stretch = q;
+      X0zT[i - 1] = Xl[JK(my, 1)] + (Xr[JK(my, 1)] - Xl[JK(my, 1)]) * stretch;
+      Y0zT[i - 1] = Ybo[IK(i, 1)];
+      X0zB[i - 1] = Xt[IK(i, 1)];
+      Y0zB[i - 1] = Yt[IK(i, 1)];
+    }
+    for (int j = 1; j <= my; ++j) {
+      X0zL[j - 1] = Xl[JK(j, 1)];
+      X0zR[j - 1] = Xr[JK(j, 1)];
+      Y0zL[j - 1] = Yl[JK(j, 1)];
+      Y0zR[j - 1] = Yr[JK(j, 1)];
+    }
+    vector<wp> XnzT(mx), YnzT(mx), XnzB(mx), YnzB(mx), XnzL(my), XnzR(my), YnzL(my), YnzR(my);
+    for (int i = 1; i <= mx; ++i) {
+      wp q = (wp)(i - 1) * hx, stretch = q;
+      XnzT[i - 1] = Xl[JK(my, mz)] + (Xr[JK(my, mz)] - Xl[JK(my, mz)]) * stretch;
+      YnzT[i - 1] = Ybo[IK(i, mz)];
+      XnzB[i - 1] = Xt[IK(i, mz)];
+      YnzB[i - 1] = Yt[IK(i, mz)];
+    }
+    for (int j = 1; j <= my; ++j) {
+      XnzL[j - 1] = Xl[JK(j, mz)];
+      XnzR[j - 1] = Xr[JK(j, mz)];
+      YnzL[j - 1] = Yl[JK(j, mz)];
+      YnzR[j - 1] = Yr[JK(j, mz)];
+    }
+    surf_mesh(mx, my, X0zL, X0zR, X0zB, X0zT, Y0zL, Y0zR, Y0zB, Y0zT, Xf, Yf);
+    surf_mesh(mx, my, XnzL, XnzR, XnzB, XnzT, YnzL, YnzR, YnzB, YnzT, Xbk, Ybk);
+  }
+  vector<wp> Zf((size_t)mx * my, az), Zbk((size_t)mx * my, bz);
+  // bottom face (:1826-1858)
+  vector<wp> Xbo, Zbo;
+  {
+    vector<wp> XnyT(mx), XnyB(mx), ZnyT(mx), ZnyB(mx), XnyL(mz), XnyR(mz), ZnyL(mz), ZnyR(mz);
+    for (int i = 1; i <= mx; ++i) {
+      XnyT[i - 1] = Xbk[IJ(i, my)];
+      XnyB[i - 1] = Xf[IJ(i, my)];
+      ZnyT[i - 1] = Zbk[IJ(i, my)];
+      ZnyB[i - 1] = Zf[IJ(i, my)];
+    }
+    for (int k = 1; k <= mz; ++k) {
+      XnyL[k - 1] = Xl[JK(my, k)];
+      XnyR[k - 1] = Xr[JK(my, k)];
+      ZnyL[k - 1] = Zl[JK(my, k)];
+      ZnyR[k - 1] = Zr[JK(my, k)];
+    }
+    surf_mesh(mx, mz, XnyL, XnyR, XnyB, XnyT, ZnyL, ZnyR, ZnyB, ZnyT, Xbo, Zbo);
+  }
+  for (int c = 0; c < 3; ++c) B.X[c].assign(B.np, 0);
+  gen3_mesh(B, 0, Xl, Xr, Xt, Xbo, Xf, Xbk);
+  gen3_mesh(B, 1, Yl, Yr, Yt, Ybo, Yf, Ybk);
+  gen3_mesh(B, 2, Zl, Zr, Zt, Zbo, Zf, Zbk);
+  return true;
+}
+
+// Curve_Grid_3D3 without topography: src/grid.f90:471-1160, 1873-1875
 bool curve_grid(RBlock& B, const wql::BlockParams& bp, const std::string& base_dir, std::string& err) {
   int mx = B.nq, my = B.nr, mz = B.ns;
   wp ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1], az = bp.aqrs[2], bz = bp.bqrs[2];
@@ -860,41 +1089,12 @@ bool curve_grid(RBlock& B, const wql::BlockParams& bp, const std::string& base_d
     }
     surf_mesh(mx, mz, XnyL, XnyR, XnyB, XnyT, ZnyL, ZnyR, ZnyB, ZnyT, Xbo, Zbo);
   }
-  // Gen3_Curve_Mesh for x, y, z components
-  auto gen3 = [&](int comp, const vector<wp>& Lf, const vector<wp>& Rf, const vector<wp>& Tf,
-                  const vector<wp>& Bf, const vector<wp>& Ff, const vector<wp>& Kf) {
-    // Lf,Rf: (j,k); Tf,Bf: (i,k); Ff,Kf: (i,j)
-    int nq = mx, nr = my, ns = mz;
-    wp hq = 1.0 / (wp)(nq - 1), hr = 1.0 / (wp)(nr - 1), hs = 1.0 / (wp)(ns - 1);
-    auto LK = [&](const vector<wp>& a, int j, int k) { return a[(size_t)(j - 1) + (size_t)my * (k - 1)]; };
-    auto IK = [&](const vector<wp>& a, int i, int k) { return a[(size_t)(i - 1) + (size_t)mx * (k - 1)]; };
-    auto IJ = [&](const vector<wp>& a, int i, int j) { return a[(size_t)(i - 1) + (size_t)mx * (j - 1)]; };
-    for (int k = 1; k <= mz; ++k)
-      for (int j = 1; j <= my; ++j)
-        for (int i = 1; i <= mx; ++i) {
-          wp q = (wp)(i - 1) * hq, r = (wp)(j - 1) * hr, s = (wp)(k - 1) * hs;
-          wp U = (1.0 - q) * LK(Lf, j, k) + q * LK(Rf, j, k);
-          wp V = (1.0 - r) * IK(Tf, i, k) + r * IK(Bf, i, k);
-          wp W = (1.0 - s) * IJ(Ff, i, j) + s * IJ(Kf, i, j);
-          wp UW = (1.0 - q) * ((1.0 - r) * LK(Lf, 1, k) + r * LK(Lf, nr, k)) +
-                  q * ((1.0 - r) * LK(Rf, 1, k) + r * LK(Rf, nr, k));
-          wp UV = (1.0 - r) * ((1.0 - s) * IK(Tf, i, 1) + s * IK(Tf, i, ns)) +
-                  r * ((1.0 - s) * IK(Bf, i, 1) + s * IK(Bf, i, ns));
-          wp VW = (1.0 - s) * ((1.0 - q) * IJ(Ff, 1, j) + q * IJ(Ff, nq, j)) +
-                  s * ((1.0 - q) * IJ(Kf, 1, j) + q * IJ(Kf, nq, j));
-          wp UVW1 = (1.0 - q) * ((1.0 - r) * ((1.0 - s) * IK(Tf, 1, 1) + s * IK(Tf, 1, ns)) +
-                                 r * ((1.0 - s) * IK(Bf, 1, 1) + s * IK(Bf, 1, ns)));
-          wp UVW2 = q * ((1.0 - r) * ((1.0 - s) * IK(Tf, nq, 1) + s * IK(Tf, nq, ns)) +
-                         r * ((1.0 - s) * IK(Bf, nq, 1) + s * IK(Bf, nq, ns)));
-          B.X[comp][B.id(i, j, k)] = U + V + W - UV - UW - VW + UVW1 + UVW2;
-        }
-  };
   vector<wp> Yt((size_t)mx * mz, ay), Ybo((size_t)mx * mz, by), Zf((size_t)mx * my, az),
       Zbk((size_t)mx * my, bz);
   for (int c = 0; c < 3; ++c) B.X[c].assign(B.np, 0);
-  gen3(0, Xl, Xr, Xt, Xbo, Xf, Xbk);
-  gen3(1, Yl, Yr, Yt, Ybo, Yf, Ybk);
-  gen3(2, Zl, Zr, Zt, Zbo, Zf, Zbk);
+  gen3_mesh(B, 0, Xl, Xr, Xt, Xbo, Xf, Xbk);
+  gen3_mesh(B, 1, Yl, Yr, Yt, Ybo, Yf, Ybk);
+  gen3_mesh(B, 2, Zl, Zr, Zt, Zbo, Zf, Zbk);
   return true;
 }
 
@@ -1202,10 +1402,10 @@ int init_block(Domain& D, int b, const Media& md) {
         }
   } else if (D.P.type_of_mesh == "curvilinear") {
     if (D.P.use_topography) {
-      D.err = "topography grids are not supported by the oracle";
+      if (!curve_grid_topo(B, D.P, bp, D.err)) return 1;
+    } else if (!curve_grid(B, bp, D.P.base_dir, D.err)) {
       return 1;
     }
-    if (!curve_grid(B, bp, D.P.base_dir, D.err)) return 1;
   } else {
     D.err = "unknown type_of_mesh " + D.P.type_of_mesh;
     return 1;

@@ -196,3 +196,40 @@ def mms_relative_error(sim):
         e2 += e.sum()
         r2 += r.sum()
     return (e2 / r2) ** 0.5
+
+
+def topography_case(dirpath, n=21, amp=0.12, fault_amp=0.08, fault_file=True, seed=5):
+    """truth/1's geometry (2 x n^3, x in [-3, 3], y in [6, 9], z in [-1.5, 1.5])
+    with use_topography = T: a seeded smooth free surface read from
+    topo_<b>.dat ('read_topo_from_memory', src/grid.f90:1394-1425: nq*ns rows
+    of x y z, s fastest, y offset from ay) and, with fault_file, the fault
+    surface from fault.dat ('read_from_memomry_fractal' under topography,
+    src/grid.f90:1538-1676: nr*ns rows of x offset, y, z, r fastest), whose
+    y runs from the topography's fault edge down to by.  Writes the files
+    into dirpath and returns the .in text."""
+    import numpy as np
+    surf = _smooth_surface(seed, amp)
+    bump = _smooth_surface(seed + 1, fault_amp)
+    ay, by, az, bz = 6.0, 9.0, -1.5, 1.5
+    z = az + (bz - az) * np.arange(n) / (n - 1)
+    for b, (ax, bx) in enumerate(((-3.0, 0.0), (0.0, 3.0))):
+        x = ax + (bx - ax) * np.arange(n) / (n - 1)
+        with open(os.path.join(str(dirpath), f"topo_{b + 1}.dat"), "w") as f:
+            for i in range(n):
+                for k in range(n):
+                    f.write(f"{float(x[i])!r} {float(surf(x[i], z[k]))!r} {float(z[k])!r}\n")
+    if fault_file:
+        with open(os.path.join(str(dirpath), "fault.dat"), "w") as f:
+            for k in range(n):
+                ytop = ay + surf(0.0, z[k])
+                for j in range(n):
+                    r = j / (n - 1)
+                    y = ytop + (by - ytop) * r
+                    f.write(f"{float(bump(y, z[k]) * r * (1 - r) * 4.0)!r} {float(y)!r} {float(z[k])!r}\n")
+    prof = ("'read_from_memomry_fractal'", "'fault.dat'") if fault_file else ("'no_path'", "'none'")
+    extra = {b: (f"btp({b})%lc = {1 if b == 1 else 0}d0,\nbtp({b})%rc = {0 if b == 1 else 1}d0,\n"
+                 f"btp({b})%profile_type = {prof[0]},\nbtp({b})%profile_path = {prof[1]},\n"
+                 f"btp({b})%topography_type = 'read_topo_from_memory',\n"
+                 f"btp({b})%topography_path = 'topo_{b}.dat',") for b in (1, 2)}
+    return (problem(mesh="curvilinear", extra=",\n use_topography = T") +
+            block_list(n, extra1=extra[1], extra2=extra[2]))

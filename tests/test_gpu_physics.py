@@ -79,6 +79,22 @@ def test_rate_state_fp64_parity_converged(ctx, wqlmod, oracle_lib, tmp_path, cas
         assert rel_l2(s.iface(copy, 4), o.iface(copy, 4)) < TOL  # state variable
 
 
+def test_topography_from_files(ctx, wqlmod, oracle_lib, tmp_path):
+    """use_topography = T with the free surface and the fault surface read
+    from files (read_topo_from_memory, read_from_memomry_fractal; src/grid.f90:
+    1349-1875), slip weakening: FP64 against the oracle to 1e-11, FP32C
+    against FP64 to 1e-5."""
+    from inputs import topography_case
+    p = write(tmp_path, "topo.in", topography_case(tmp_path))
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, 30)
+    assert max(field_errors(s, o)) < TOL
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    f.step(30)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), s.fields(b)) < 1e-5
+
+
 def test_plasticity_is_active(ctx, wqlmod, tmp_path):
     """The plastic run departs from the elastic run of the same problem."""
     pl = write(tmp_path, "pl.in", case_text("plastic"))

@@ -113,6 +113,170 @@ int read_fault_profile(const std::string& path, size_t n, std::vector<double>& x
   return 0;
 }
 
+// A list-directed text file of `n` rows of three numbers (read_2darray,
+// src/grid.f90:2457-2481); Fortran exponent letters and commas accepted,
+// lines that do not hold three numbers skipped.  Output column-major: the
+// c-th column is out[c*n .. (c+1)*n).
+int read_xyz_rows(const std::string& path, size_t n, std::vector<double>& out, std::string& err) {
+  std::FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) {
+    err = "cannot open " + path;
+    return 1;
+  }
+  out.assign(3 * n, 0.0);
+  char line[4096];
+  size_t row = 0;
+  while (row < n && std::fgets(line, sizeof(line), f)) {
+    for (char* c = line; *c; ++c)
+      if (*c == 'd' || *c == 'D') *c = 'e';
+      else if (*c == ',') *c = ' ';
+    double v[3];
+    if (std::sscanf(line, "%lf %lf %lf", &v[0], &v[1], &v[2]) != 3) continue;
+    for (int c = 0; c < 3; ++c) out[(size_t)c * n + row] = v[c];
+    ++row;
+  }
+  std::fclose(f);
+  if (row != n) {
+    err = path + " holds " + std::to_string(row) + " rows of x y z, not " + std::to_string(n);
+    return 1;
+  }
+  return 0;
+}
+
+// Curvilinear block with a free-surface topography on the r-min face
+// (use_topography = T, src/grid.f90:1349-1875).  The top face comes from
+// 'read_topo_from_memory' (a file of nq*ns rows x y z, s fastest, with
+// y = ay + topo * the file's y; :1394-1425) or 'analytical_topography'
+// (:1364-1392).  The x faces: (y, z) meshed from edges that run from the
+// topography down to by (:1440-1518), x = ax / bx, or, with
+// 'read_from_memomry_fractal', the fault file's rows taken whole on the
+// interface face: x = ax (bx) + the file's x, y and z the file's (:1538-1676).
+// The s faces join the x faces, the topography's edge and y = by
+// (:1695-1805); the bottom face joins the others (:1826-1858).
+int curvilinear_topo(const Problem& P, const BlockParams& bp, BlockGrid& G, std::string& err) {
+  const int mx = G.nq, my = G.nr, mz = G.ns;
+  const double ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1];
+  const double az = bp.aqrs[2], bz = bp.bqrs[2];
+  Faces X, Y, Z;
+  const size_t ntop = (size_t)mx * mz;
+  X.top.resize(ntop);
+  Y.top.resize(ntop);
+  Z.top.resize(ntop);
+  if (bp.topography_type == "read_topo_from_memory") {
+    std::vector<double> t;
+    if (read_xyz_rows(resolve_path(P.base_dir, bp.topography_path), ntop, t, err)) return 1;
+    for (int k = 0; k < mz; ++k)
+      for (int i = 0; i < mx; ++i) {
+        const size_t row = (size_t)k + (size_t)mz * i, o = (size_t)i + (size_t)mx * k;
+        X.top[o] = t[row];
+        Y.top[o] = ay + P.topo * t[ntop + row];
+        Z.top[o] = t[2 * ntop + row];
+      }
+  } else if (bp.topography_type == "analytical_topography") {
+    const double hx = (bx - ax) / (double)(mx - 1), hz = (bz - az) / (double)(mz - 1);
+    for (int k = 0; k < mz; ++k)
+      for (int i = 0; i < mx; ++i) {
+        const size_t o = (size_t)i + (size_t)mx * k;
+        X.top[o] = ax + (double)i * hx;
+        Z.top[o] = az + (double)k * hz;
+        const double r1 = std::sqrt((X.top[o] - 10.0) * (X.top[o] - 10.0) + (Z.top[o] - 10.0) * (Z.top[o] - 10.0));
+        const double f = r1 <= 3.0 ? -0.3 * (1.0 + std::cos(kPi * r1 / 3.0)) : 0.0;
+        Y.top[o] = ay - P.topo * 1.5 * f;
+      }
+  } else {
+    err = "topography_type '" + bp.topography_type + "' is not supported ('read_topo_from_memory' or "
+          "'analytical_topography')";
+    return 1;
+  }
+  auto top = [&](const std::vector<double>& a, int i, int k) { return a[(size_t)i + (size_t)mx * k]; };
+  // x faces: y from the topography's edge down to by, z uniform
+  const size_t nx = (size_t)my * mz;
+  const double hr = 1.0 / (double)(my - 1), hs = 1.0 / (double)(mz - 1);
+  for (int side = 0; side < 2; ++side) {
+    const int i = side == 0 ? 0 : mx - 1;
+    std::vector<double> yL(mz), yR(mz, by), yB(my), yT(my), zL(mz), zR(mz), zB(my, az), zT(my, bz);
+    for (int j = 0; j < my; ++j) {
+      const double r = (double)j * hr;
+      yT[j] = top(Y.top, i, mz - 1) + (by - top(Y.top, i, mz - 1)) * r;
+      yB[j] = top(Y.top, i, 0) + (by - top(Y.top, i, 0)) * r;
+    }
+    for (int k = 0; k < mz; ++k) {
+      zL[k] = zR[k] = az + (bz - az) * ((double)k * hs);
+      yL[k] = top(Y.top, i, k);
+    }
+    face_tfi(my, mz, yL, yR, yB, yT, side == 0 ? Y.left : Y.right);
+    face_tfi(my, mz, zL, zR, zB, zT, side == 0 ? Z.left : Z.right);
+  }
+  X.left.assign(nx, ax);
+  X.right.assign(nx, bx);
+  const std::string& pt = bp.profile_type;
+  if (pt == "read_from_memomry_fractal") {
+    std::vector<double> f;
+    if (read_xyz_rows(resolve_path(P.base_dir, bp.profile_path), nx, f, err)) return 1;
+    for (size_t p = 0; p < nx; ++p) {
+      if (bp.rc != 0.0) {
+        X.left[p] = ax + f[p];
+        Y.left[p] = f[nx + p];
+        Z.left[p] = f[2 * nx + p];
+      }
+      if (bp.lc != 0.0) {
+        X.right[p] = bx + f[p];
+        Y.right[p] = f[nx + p];
+        Z.right[p] = f[2 * nx + p];
+      }
+    }
+  } else if (pt != "no_path") {
+    err = "with use_topography, profile_type must be 'no_path' or 'read_from_memomry_fractal'";
+    return 1;
+  }
+  auto lr = [&](const std::vector<double>& a, int j, int k) { return a[(size_t)j + (size_t)my * k]; };
+  // s faces (front k = 0, back k = mz - 1)
+  for (int side = 0; side < 2; ++side) {
+    const int k = side == 0 ? 0 : mz - 1;
+    std::vector<double> xL(my), xR(my), xB(mx), xT(mx), yL(my), yR(my), yB(mx), yT(mx, by);
+    const double hq = 1.0 / (double)(mx - 1);
+    for (int i = 0; i < mx; ++i) {
+      const double q = (double)i * hq;
+      xT[i] = lr(X.left, my - 1, k) + (lr(X.right, my - 1, k) - lr(X.left, my - 1, k)) * q;
+      xB[i] = top(X.top, i, k);
+      yB[i] = top(Y.top, i, k);
+    }
+    for (int j = 0; j < my; ++j) {
+      xL[j] = lr(X.left, j, k);
+      xR[j] = lr(X.right, j, k);
+      yL[j] = lr(Y.left, j, k);
+      yR[j] = lr(Y.right, j, k);
+    }
+    face_tfi(mx, my, xL, xR, xB, xT, side == 0 ? X.front : X.back);
+    face_tfi(mx, my, yL, yR, yB, yT, side == 0 ? Y.front : Y.back);
+  }
+  Z.front.assign((size_t)mx * my, az);
+  Z.back.assign((size_t)mx * my, bz);
+  // bottom face (j = my - 1): y = by, x and z from the edges of the others
+  {
+    std::vector<double> xL(mz), xR(mz), xB(mx), xT(mx), zL(mz), zR(mz), zB(mx), zT(mx);
+    for (int i = 0; i < mx; ++i) {
+      xT[i] = X.back[(size_t)i + (size_t)mx * (my - 1)];
+      xB[i] = X.front[(size_t)i + (size_t)mx * (my - 1)];
+      zT[i] = Z.back[(size_t)i + (size_t)mx * (my - 1)];
+      zB[i] = Z.front[(size_t)i + (size_t)mx * (my - 1)];
+    }
+    for (int k = 0; k < mz; ++k) {
+      xL[k] = lr(X.left, my - 1, k);
+      xR[k] = lr(X.right, my - 1, k);
+      zL[k] = lr(Z.left, my - 1, k);
+      zR[k] = lr(Z.right, my - 1, k);
+    }
+    face_tfi(mx, mz, xL, xR, xB, xT, X.bottom);
+    face_tfi(mx, mz, zL, zR, zB, zT, Z.bottom);
+  }
+  Y.bottom.assign(ntop, by);
+  block_tfi(mx, my, mz, X, G.x[0]);
+  block_tfi(mx, my, mz, Y, G.x[1]);
+  block_tfi(mx, my, mz, Z, G.x[2]);
+  return 0;
+}
+
 int curvilinear(const BlockParams& bp, const std::string& base_dir, BlockGrid& G, std::string& err) {
   const int mx = G.nq, my = G.nr, mz = G.ns;
   const double ax = bp.aqrs[0], bx = bp.bqrs[0], ay = bp.aqrs[1], by = bp.bqrs[1];
@@ -331,10 +495,10 @@ int make_block_grid(const Problem& P, int block, const SurfaceMods& mods, BlockG
     });
   } else if (P.type_of_mesh == "curvilinear") {
     if (P.use_topography) {
-      err = "use_topography reads topography files; pass a seeded surface through the API instead";
+      if (curvilinear_topo(P, bp, G, err)) return 1;
+    } else if (curvilinear(bp, P.base_dir, G, err)) {
       return 1;
     }
-    if (curvilinear(bp, P.base_dir, G, err)) return 1;
   } else {
     err = "unknown type_of_mesh '" + P.type_of_mesh + "'";
     return 1;

@@ -1,13 +1,16 @@
 // Host-side block geometry: grid point coordinates for one block.
 //
 // Cartesian blocks follow cartesian_grid_3d (src/grid.f90:213-240).
-// Curvilinear blocks follow the flat-topography branch of Curve_Grid_3D3
-// (src/grid.f90:471-1160, 1873-1875): six boundary surfaces, each face meshed
-// by 2D transfinite interpolation (Gen_Surf_Mesh, src/grid.f90:2418-2455),
-// then 3D transfinite interpolation (Gen3_Curve_Mesh, src/grid.f90:2290-2416).
-// Supported fault profiles: flat (default / 'No-path' / 'no_path'),
-// 'analytical_tpv28' (src/grid.f90:650-683) and 'analytical_test_problem'
-// (src/grid.f90:790-841).  Two extensions feed the seeded rough-fault and
+// Curvilinear blocks follow Curve_Grid_3D3 (src/grid.f90:471-1875): six
+// boundary surfaces, each face meshed by 2D transfinite interpolation
+// (Gen_Surf_Mesh, src/grid.f90:2418-2455), then 3D transfinite interpolation
+// (Gen3_Curve_Mesh, src/grid.f90:2290-2416).  Without topography (:592-1160)
+// the supported fault profiles are flat (default / 'No-path' / 'no_path'),
+// 'analytical_tpv28' (:650-683), 'analytical_test_problem' (:790-841) and
+// 'read_from_memomry_fractal' (:832-924); with use_topography = T
+// (:1349-1875) the top face comes from 'read_topo_from_memory' or
+// 'analytical_topography', and the fault is 'no_path' or
+// 'read_from_memomry_fractal'.  Two extensions feed the seeded rough-fault and
 // topography generators: `fault_offset` displaces the interface face along x
 // and `topo_offset` displaces the r-min face along y (both given on the
 // face's own (r,s) / (q,s) grid, see wql_surfaces.h).
