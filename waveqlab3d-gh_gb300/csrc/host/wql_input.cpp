@@ -385,6 +385,7 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
     else if (it.key == "tpv28_prestress") P.tpv28_prestress = s;
     else if (it.key == "rs_tol") P.rs_tol = to_double(s);
     else if (it.key == "rs_maxit") P.rs_maxit = (int)to_double(s);
+    else if (it.key == "fp32c_fault") P.fp32c_fault = s;
   }
   if (P.bc_penalty != "characteristic" && P.bc_penalty != "weighted") {
     err = "bc_penalty must be 'characteristic' or 'weighted'";
@@ -392,6 +393,10 @@ int parse_in_text(const std::string& text, const std::string& base_dir,
   }
   if (P.tpv28_prestress != "source" && P.tpv28_prestress != "benchmark") {
     err = "tpv28_prestress must be 'source' or 'benchmark'";
+    return 1;
+  }
+  if (P.fp32c_fault != "compensated" && P.fp32c_fault != "fp32") {
+    err = "fp32c_fault must be 'compensated' or 'fp32'";
     return 1;
   }
   if (!(P.rs_tol > 0.0) || P.rs_maxit < 1 || P.rs_maxit > 1000000) {

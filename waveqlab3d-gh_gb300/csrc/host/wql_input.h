@@ -135,6 +135,10 @@ struct Problem {
   // be compared to rounding.
   double rs_tol = 1.0e-12;
   int rs_maxit = 5000;
+  // &gb300_list fp32c_fault: in the FP32-compensated mode the fault's
+  // characteristic algebra reads the compensated face values (F - C) and
+  // runs in FP64 ('compensated'), or works on the FP32 fields in FP32 ('fp32')
+  std::string fp32c_fault = "compensated";
   FrictionExt fric;
   PlasticExt plast;
   // raw groups for anything not mapped above

@@ -145,6 +145,7 @@ struct wql_scn {
   int bc_form = BC_CHARACTERISTIC;
   double rs_tol = 1.0e-12;  // FP64 regula falsi tolerance and iteration cap
   int rs_maxit = 5000;
+  bool fault_comp = true;   // FP32C: fault algebra on the compensated face values in FP64
   // manufactured solution (&mms_list use_mms): T(t) = cos(kt t) and T'(t)
   // at the current stage's time, and an 18-double accumulator for the norms
   bool mms = false;
@@ -760,6 +761,7 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   S->bc_form = Pr.bc_penalty == "weighted" ? BC_WEIGHTED : BC_CHARACTERISTIC;
   S->rs_tol = Pr.rs_tol;
   S->rs_maxit = Pr.rs_maxit;
+  S->fault_comp = Pr.fp32c_fault == "compensated";
   S->mms = Pr.use_mms;
   if (S->mms) {
     // the manufactured solution is smooth across the fault: a locked
@@ -1056,6 +1058,9 @@ void stage_head(wql_scn* S, StepCtx& c, int stage) {
   }
   ia.rs_tol = S->rs_tol;
   ia.rs_maxit = S->rs_maxit;
+  ia.C0 = S->B[0].C;
+  ia.C1 = S->B[1].C;
+  ia.fault_comp = S->fault_comp && S->B[0].C && S->B[1].C;
   if (S->mms) {
     // T(t) and T'(t) of the manufactured solution at this stage's time, for
     // the interface here and the block phases of the same stage

@@ -130,22 +130,27 @@ __device__ bool newton_mixed(double& V, double Phi, double eta, double sn, doubl
   return fabs(du) <= 1.0e-9 * fmax(1.0, fabs(ud));
 }
 
-template <typename T>
-__device__ __forceinline__ void load_face(const void* F, long long np, long long p, T out[9]) {
+// The nine fields of one face point in the algebra type R.  With C (the
+// Kahan compensation of FP32 fields) the value is the compensated one,
+// F - C in FP64: the field to about twice the FP32 precision.
+template <typename T, typename R>
+__device__ __forceinline__ void load_face(const void* F, const void* C, long long np, long long p, R out[9]) {
   const T* f = (const T*)F;
+  const T* k = (const T*)C;
 #pragma unroll
-  for (int c = 0; c < 9; ++c) out[c] = f[c * np + p];
+  for (int c = 0; c < 9; ++c) out[c] = k ? (R)f[c * np + p] - (R)k[c * np + p] : (R)f[c * np + p];
 }
 
-// R is the arithmetic type of the characteristic algebra: the field type
-// (FP64 fields keep every operation of the FP64 restatement; FP32 fields do
-// the algebra in FP32 with the slip, state and their rates kept in FP64).
-// FP32 fields: capped at 96 registers so that five 128-thread CTAs share an
-// SM and a 201^2 fault (2 x 40401 threads) runs in about one round (measured
-// 0.092 -> 0.078 ms per launch on config 1 despite some spilling).
-template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(const __grid_constant__ InterfaceArgs a) {
-  using R = T;
+// T is the field type, R the arithmetic type of the characteristic algebra.
+// FP64 fields (R = T = double) keep every operation of the FP64 restatement.
+// FP32 fields either do the algebra in FP32 (R = float) or read the
+// compensated face values and do it in FP64 (R = double); the slip, state,
+// their rates and the friction law are FP64 in every case.  FP32 algebra:
+// capped at 96 registers so that five 128-thread CTAs share an SM and a 201^2
+// fault (2 x 40401 threads) runs in about one round (measured 0.092 -> 0.078
+// ms per launch on config 1 despite some spilling).
+template <typename T, typename R>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 5 : 3) interface_kernel(const __grid_constant__ InterfaceArgs a) {
   constexpr bool F64 = sizeof(T) == 8;
   const long long nf = (long long)a.nr * a.ns;
   const long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -156,8 +161,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(
   R u[9], v[9];
   const long long pu = (a.nq0 - 1) + (long long)a.pq0 * (j + (long long)a.nr * k);
   const long long pv = (long long)a.pq1 * (j + (long long)a.nr * k);
-  load_face<T>(a.F0, a.np0, pu, u);
-  load_face<T>(a.F1, a.np1, pv, v);
+  const bool comp = sizeof(R) > sizeof(T);
+  load_face<T, R>(a.F0, comp ? a.C0 : nullptr, a.np0, pu, u);
+  load_face<T, R>(a.F1, comp ? a.C1 : nullptr, a.np1, pv, v);
   if (a.ms0) {
     // manufactured solution: both sides' velocities and tractions less the
     // exact solution at their own fault points (src/CouplingForcing.f90:147-185)
@@ -431,8 +437,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 3) interface_kernel(
 void launch_interface(const InterfaceArgs& a, void* stream) {
   const long long nf = (long long)a.nr * a.ns;
   dim3 blk(128), grd((unsigned)((nf + 127) / 128), 2);
-  if (a.fp64) interface_kernel<double><<<grd, blk, 0, (cudaStream_t)stream>>>(a);
-  else interface_kernel<float><<<grd, blk, 0, (cudaStream_t)stream>>>(a);
+  if (a.fp64) interface_kernel<double, double><<<grd, blk, 0, (cudaStream_t)stream>>>(a);
+  else if (a.fault_comp) interface_kernel<float, double><<<grd, blk, 0, (cudaStream_t)stream>>>(a);
+  else interface_kernel<float, float><<<grd, blk, 0, (cudaStream_t)stream>>>(a);
 }
 
 }  // namespace wql

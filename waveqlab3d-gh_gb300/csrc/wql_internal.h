@@ -127,6 +127,12 @@ struct InterfaceArgs {
   FaultParams fp;
   float* frame;             // 39 x nf or nullptr
   unsigned int* solver_fail;  // count of non-converged rate-and-state solves
+  // FP32 fields: the Kahan compensation of both blocks, and whether the
+  // fault algebra reads the compensated face values in FP64 (1) or works
+  // on the FP32 fields in FP32 (0)
+  const void* C0;
+  const void* C1;
+  int fault_comp;
   // manufactured solution: the two blocks' shapes (2 x np, field type) or
   // nullptr, and T(t) at the stage's time
   const void* ms0;

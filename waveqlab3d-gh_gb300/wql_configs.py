@@ -148,8 +148,9 @@ def config2(nq=401, nrs=201, steps=3000, seed=2239, npml=20):
     """2 x nq x nrs x nrs blocks, (-20,0,-5)-(0,10,5) and (0,0,-5)-(20,10,5) km,
     20-point PML on the 5 non-free-surface outer sides, von Karman medium (a = 2 km,
     H = 0.2, 5 % on cp and cs, rho from cp), scec viscoplasticity (c = 1 MPa,
-    friction 0.75, Tv = 0.03 s), TPV26 depth-dependent stress, slip weakening as
-    config 0."""
+    friction 0.75, Tv = 0.03 s), TPV26 depth-dependent stress, linear slip weakening
+    (the config-0 law with the TPV26 preset's fs 0.18, fd 0.12, Dc 0.3 m) and a
+    20 MPa Gaussian overstress (R = 1.5 km) at 7.5 km depth."""
     ext = (20.0, 10.0, 10.0)
     h = ext[0] / (nq - 1)
     dt = dt_of((nq, nrs, nrs), ext)
@@ -159,7 +160,10 @@ def config2(nq=401, nrs=201, steps=3000, seed=2239, npml=20):
                                      (True, False, True), (False, True, True), npml)
     text += _block(2, (nq, nrs, nrs), (0.0, 0.0, -5.0), (20.0, 10.0, 5.0), (0, 2, 1), (1, 1, 1),
                    (False, False, True), (True, True, True), npml) + " /\n"
-    text += ("&fault_list\n fs = 0.677d0, fd = 0.525d0, Dc = 0.4d0, stress_profile = 'TPV26',\n"
+    # the linear slip-weakening law of config 0 with the TPV26 preset's own
+    # parameters (src/Interface_Condition.f90:1378-1380): under the TPV26
+    # stress (tau/sigma_n about 0.16) config 0's fs = 0.677, fd = 0.525 never slip
+    text += ("&fault_list\n fs = 0.18d0, fd = 0.12d0, Dc = 0.3d0, stress_profile = 'TPV26',\n"
              " nuc_amp = 20d0, nuc_radius = 1.5d0, nuc_y = 7.5d0, nuc_z = 0d0, nuc_rise = 0d0 /\n"
              "&plastic_list\n cohesion = 1d0, friction = 0.75d0, Tv = 0.03d0 /\n")
     r = von_karman((2 * nq - 1, nrs, nrs), (h, h, h), 2.0, 0.2, 0.05, seed, kmax=np.pi / h)
