@@ -21,7 +21,7 @@ SRCS = [os.path.join(HERE, "wql_ref.cpp"),
 def build(force=False, verbose=False):
     if not force and os.path.exists(OUT):
         newest = max(os.path.getmtime(s) for s in SRCS + [os.path.join(
-            ROOT, "waveqlab3d-gh_gb300", "csrc", "host", "wql_input.h")])
+            ROOT, "waveqlab3d-gh_gb300", "csrc", "host", "wql_input.h"), os.path.join(HERE, "upwind_tables.inc")])
         if os.path.getmtime(OUT) >= newest:
             return OUT
     os.makedirs(os.path.dirname(OUT), exist_ok=True)

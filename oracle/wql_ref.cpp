@@ -441,10 +441,57 @@ const wp UP5_CB[6] = {-1.0 / 30.0, 0.25, -1.0, 1.0 / 3.0, 0.5, -0.05};
 // Closure rows per end and interior-row limit of the upwind operator of an order.
 int up_rows(int order) { return order == 5 ? 4 : 6; }
 
+// The other upwind operators (orders 2, 3, 4, 7, 8, 9 of fd_type 'upwind' and
+// the 'upwind_drp' variants), as tables read from the reference's routines by
+// oracle/make_upwind_tables.py (src/JU_xJU_yJU_z6.f90:815-2048, 3707-16122 near
+// the boundaries, :16451-20922 inside; tau0 src/block.f90:195-252).
+#include "upwind_tables.inc"
+
+const UpTable* find_uptable(const std::string& fd, int order) {
+  if (fd == "upwind" && (order == 5 || order == 6)) return nullptr;  // the rows above
+  for (int k = 0; k < kUpTableCount; ++k)
+    if (fd == kUpTable[k].fd_type && order == kUpTable[k].order) return &kUpTable[k];
+  return nullptr;
+}
+
+// Row of D+ (plus) or D- of a table operator at 1-based index i of n points
+// along axis ax, as the near-boundary routine JJU_x<order>_upwind(_drp)
+// forms it: its interior case (bp/bm) on rows R+1..n-R, its closure rows
+// elsewhere; terms in increasing point index.  pt and c hold 13 entries.
+int stencil_upg(const UpTable& T, bool plus, int i, int n, int* pt, wp* c, int ax) {
+  int m = 0;
+  if (i >= T.R + 1 && i <= n - T.R) {
+    const int lo = plus ? T.plo : T.mlo, cnt = plus ? T.pn : T.mn;
+    const double* w = plus ? T.bp : T.bm;
+    for (int k = 0; k < cnt; ++k)
+      if (w[k] != 0.0) {
+        pt[m] = i + lo + k;
+        c[m++] = w[k];
+      }
+    return m;
+  }
+  if (i <= T.R) {
+    const double* w = plus ? T.lp[ax][i - 1] : T.lm[ax][i - 1];
+    for (int t = 0; t < 13; ++t)
+      if (w[t] != 0.0) {
+        pt[m] = t + 1;
+        c[m++] = w[t];
+      }
+    return m;
+  }
+  const double* w = plus ? T.rp[ax][n - i] : T.rm[ax][n - i];
+  for (int t = 12; t >= 0; --t)
+    if (w[t] != 0.0) {
+      pt[m] = n - t;
+      c[m++] = w[t];
+    }
+  return m;
+}
+
 // Row of D+ (plus = true) or D- of the given order (5 or 6) at 1-based
-// index i of n points along axis ax (0..2).  Reference quirk, kept: on the
-// s axis the order-5 D+ row 4 weights point 7 with a default-real (single
-// precision) literal (src/JU_xJU_yJU_z6.f90:2558).
+// index i of n points along axis ax (0..2).  The unsuffixed literal of the
+// order-5 s-axis D+ row 4 (src/JU_xJU_yJU_z6.f90:2558) is a double: the
+// reference compiles with -fdefault-real-8 / -r8 (src/CMakeLists.txt:24, 28).
 int stencil_up(int order, bool plus, int i, int n, int* pt, wp* c, int ax = 0) {
   const int R = up_rows(order);
   if (i >= R + 1 && i <= n - R) {
@@ -465,7 +512,6 @@ int stencil_up(int order, bool plus, int i, int n, int* pt, wp* c, int ax = 0) {
       pt[k] = r.pt[k];
       c[k] = r.c[k];
     }
-    if (order == 5 && plus && ax == 2 && i == 4) c[0] = (wp)(float)0.032476319350474;
     return r.n;
   }
   const URow& r = (plus ? MR : PR)[n - i];
@@ -496,7 +542,8 @@ struct RBlock {
   int npml = 0;
   vector<wp> Q[7][9], DQ[7][9];    // full-size per active side
   wp tau0 = 0;
-  bool upwind = false;  // fd_type 'upwind', order 5 or 6
+  bool upwind = false;  // fd_type 'upwind' or 'upwind_drp'
+  const UpTable* ug = nullptr;  // the operator's table (nullptr: upwind order 5 or 6)
   int up_order = 0;
   // response = 'anelastic' (src/datatypes.f90:38-50): four relaxation
   // mechanisms per stress component 4..9
@@ -1458,9 +1505,11 @@ int init_block(Domain& D, int b, const Media& md) {
         B.DQ[s][c].assign(B.np, 0.0);
       }
   // src/block.f90:189-214
-  B.upwind = D.P.fd_type == "upwind";
+  B.upwind = D.P.fd_type == "upwind" || D.P.fd_type == "upwind_drp";
   B.up_order = B.upwind ? D.P.order : 0;
-  B.tau0 = !B.upwind ? 1.0 / (0.315949074074074) : (B.up_order == 5 ? 720.0 / 251.0 : 42300.0 / 13613.0);
+  B.ug = B.upwind ? find_uptable(D.P.fd_type, D.P.order) : nullptr;
+  B.tau0 = !B.upwind ? 1.0 / (0.315949074074074)
+                     : (B.ug ? B.ug->tau0 : (B.up_order == 5 ? 720.0 / 251.0 : 42300.0 / 13613.0));
   return 0;
 }
 
@@ -1498,14 +1547,16 @@ void jju_x6(const RBlock& B, int x, int y, int z, const vector<wp>* Xm, wp Ju[9]
 // metric times the D+ row; stresses: the D- row of c*metric*J*sigma.
 void jju_x6_upwind(const RBlock& B, int x, int y, int z, const vector<wp>* Xm, wp Ju[9]) {
   wp Jq[9], Jr[9], Js[9];
-  int ptp[10], ptm[10];
-  wp cp[10], cm[10];
+  int ptp[13], ptm[13];
+  wp cp[13], cm[13];
   const int dims[3] = {B.nq, B.nr, B.ns};
   const int pos[3] = {x, y, z};
   wp* out[3] = {Jq, Jr, Js};
   for (int ax = 0; ax < 3; ++ax) {
-    const int mp = stencil_up(B.up_order, true, pos[ax], dims[ax], ptp, cp, ax);
-    const int mm = stencil_up(B.up_order, false, pos[ax], dims[ax], ptm, cm, ax);
+    const int mp = B.ug ? stencil_upg(*B.ug, true, pos[ax], dims[ax], ptp, cp, ax)
+                        : stencil_up(B.up_order, true, pos[ax], dims[ax], ptp, cp, ax);
+    const int mm = B.ug ? stencil_upg(*B.ug, false, pos[ax], dims[ax], ptm, cm, ax)
+                        : stencil_up(B.up_order, false, pos[ax], dims[ax], ptm, cm, ax);
     const vector<wp>& Xa = Xm[ax];
     const wp centre = Xa[B.id(x, y, z)];
     for (int comp = 0; comp < 9; ++comp) {
@@ -1653,7 +1704,7 @@ void anelastic_point(RBlock& B, size_t p, int x, int y, int z, const wp Ux[9], c
 void interior_limits(const RBlock& B, int& ix, int& iy, int& iz, int& fx, int& fy, int& fz) {
   // JU:16211-16226; 4 for the order-5 upwind operators (JU:17434-17446,
   // src/RHS_Interior.f90:517-530)
-  const int L = B.up_order == 5 ? 4 : 6;
+  const int L = B.ug ? B.ug->R : (B.up_order == 5 ? 4 : 6);
   ix = iy = iz = fx = fy = fz = L;
   if (B.pml[5]) iz = std::max(B.npml, L);
   if (B.pml[6]) fz = std::max(B.npml, L);
@@ -1753,16 +1804,22 @@ void rhs_interior_upwind(RBlock& B, bool cart) {
   int ix, iy, iz, fx, fy, fz;
   interior_limits(B, ix, iy, iz, fx, fy, fz);
   // order 6: s = -2..4, stresses at s-2; order 5 (JU:17364-17671): s = -2..3,
-  // stresses at s-1
+  // stresses at s-1;
+  // table operators (the interior routines JJU_x<order>_interior_upwind(_drp),
+  // src/JU_xJU_yJU_z6.f90:16451-20922): D+ on offsets plo.., D- on mlo..
   const bool o5 = B.up_order == 5;
   const int shi = o5 ? 3 : 4, bsh = o5 ? 1 : 2;
-  const wp* CF = o5 ? UP5_CF : UP_CF;
-  const wp* CB = o5 ? UP5_CB : UP_CB;
-  wp cfx[7], cfy[7], cfz[7], cbx[7], cby[7], cbz[7];
-  for (int k = 0; k <= shi + 2; ++k) {
-    cfx[k] = CF[k] / B.hq; cfy[k] = CF[k] / B.hr; cfz[k] = CF[k] / B.hs;
-    cbx[k] = CB[k] / B.hq; cby[k] = CB[k] / B.hr; cbz[k] = CB[k] / B.hs;
+  const wp* CF = B.ug ? B.ug->ip : (o5 ? UP5_CF : UP_CF);
+  const wp* CB = B.ug ? B.ug->im : (o5 ? UP5_CB : UP_CB);
+  const int npf = B.ug ? B.ug->pn : shi + 3, npb = B.ug ? B.ug->mn : shi + 3;
+  const int vlo = B.ug ? B.ug->plo : -2, slo = B.ug ? B.ug->mlo : -2 - bsh;
+  wp cfx[13], cfy[13], cfz[13], cbx[13], cby[13], cbz[13];
+  for (int k = 0; k < 13; ++k) {
+    const wp f = k < npf ? CF[k] : 0.0, g = k < npb ? CB[k] : 0.0;
+    cfx[k] = f / B.hq; cfy[k] = f / B.hr; cfz[k] = f / B.hs;
+    cbx[k] = g / B.hq; cby[k] = g / B.hr; cbz[k] = g / B.hs;
   }
+  const int nk = std::max(npf, npb);
   const int nx = B.nq, ny = B.nr, nz = B.ns;
 #pragma omp parallel for schedule(static)
   for (int z = 1; z <= nz; ++z)
@@ -1772,10 +1829,12 @@ void rhs_interior_upwind(RBlock& B, bool cart) {
           continue;
         const size_t p = B.id(x, y, z);
         wp DFx[9] = {0}, DFy[9] = {0}, DFz[9] = {0};
-        for (int s = -2; s <= shi; ++s) {
-          const int k = s + 2;
-          const size_t xf = B.id(x + s, y, z), yf = B.id(x, y + s, z), zf = B.id(x, y, z + s);
-          const size_t xb = B.id(x + s - bsh, y, z), yb = B.id(x, y + s - bsh, z), zb = B.id(x, y, z + s - bsh);
+        for (int k = 0; k < nk; ++k) {
+          // velocity and stress points of entry k (clamped where its weight
+          // is zero, outside the operator's own span)
+          const int sf = std::min(vlo + k, vlo + npf - 1), sb = std::min(slo + k, slo + npb - 1);
+          const size_t xf = B.id(x + sf, y, z), yf = B.id(x, y + sf, z), zf = B.id(x, y, z + sf);
+          const size_t xb = B.id(x + sb, y, z), yb = B.id(x, y + sb, z), zb = B.id(x, y, z + sb);
           if (!cart) {
             const vector<wp>* Ms[3] = {B.mx, B.my, B.mz};
             wp* Ds[3] = {DFx, DFy, DFz};
@@ -2620,6 +2679,38 @@ int wqlref_fd_matrix(int fd, int plus, int n, double* D) {
   return 0;
 }
 
+// Table operator k (0 .. count-1 of oracle/upwind_tables.inc): its fd_type
+// (up to 15 characters), order, closure rows and tau0.  Returns the count of
+// table operators, or -1 for k out of range.
+int wqlref_up_table(int k, char* fd_type, int* order, int* R, double* tau0) {
+  if (k < 0 || k >= kUpTableCount) return -1;
+  if (fd_type) std::snprintf(fd_type, 16, "%s", kUpTable[k].fd_type);
+  if (order) *order = kUpTable[k].order;
+  if (R) *R = kUpTable[k].R;
+  if (tau0) *tau0 = kUpTable[k].tau0;
+  return kUpTableCount;
+}
+
+// Dense n x n matrix (row-major, times h) of table operator k along axis ax:
+// D+ (plus != 0) or D-, with the interior rows of the near-boundary routine
+// (interior_set 0) or of the interior routine (1).  Returns 0, or -1.
+int wqlref_up_matrix(int k, int plus, int ax, int interior_set, int n, double* D) {
+  if (k < 0 || k >= kUpTableCount || ax < 0 || ax > 2 || n < 2 * kUpTable[k].R + 13 || !D) return -1;
+  UpTable T = kUpTable[k];
+  if (interior_set) {
+    std::memcpy(T.bp, T.ip, sizeof(T.bp));
+    std::memcpy(T.bm, T.im, sizeof(T.bm));
+  }
+  int pt[13];
+  wp c[13];
+  for (size_t q = 0; q < (size_t)n * n; ++q) D[q] = 0.0;
+  for (int i = 1; i <= n; ++i) {
+    const int m = stencil_upg(T, plus != 0, i, n, pt, c, ax);
+    for (int t = 0; t < m; ++t) D[(size_t)(i - 1) * n + (pt[t] - 1)] += c[t];
+  }
+  return 0;
+}
+
 static void* create_domain(Domain* D, const Media& md);
 
 void* wqlref_create(const char* in_path) {
@@ -2666,10 +2757,11 @@ static void* create_domain(Domain* D, const Media& md) {
   D->rs = cp == "rate-and-state_friction";
   D->locked = cp == "locked";
   D->linear = cp == "linear_friction";
-  // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator, or the
-  // upwind operators of order 6 (the other orders and the DRP variants are
-  // not restated)
-  if (!(D->P.fd_type == "traditional" || (D->P.fd_type == "upwind" && (D->P.order == 5 || D->P.order == 6)))) {
+  // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator, the upwind
+  // operators of orders 2..9 or the upwind DRP operators of orders 3..7, 66
+  // and 679
+  if (!(D->P.fd_type == "traditional" || (D->P.fd_type == "upwind" && (D->P.order == 5 || D->P.order == 6)) ||
+        find_uptable(D->P.fd_type, D->P.order))) {
     std::snprintf(g_err, sizeof(g_err), "fd_type %s with order %d is not restated", D->P.fd_type.c_str(), D->P.order);
     delete D;
     return nullptr;

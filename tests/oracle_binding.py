@@ -36,6 +36,8 @@ def lib():
         L.wqlref_station_index.argtypes = [vp, ctypes.c_int, vp]
         L.wqlref_get_seismograms.argtypes = [vp, ctypes.c_int, vp]
         L.wqlref_fd_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+        L.wqlref_up_table.argtypes = [ctypes.c_int, ctypes.c_char_p, vp, vp, vp]
+        L.wqlref_up_matrix.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         _LIB = L
     return _LIB
 
@@ -138,6 +140,28 @@ class Oracle:
         out = np.empty(nf * NCOMP[name] * nr * ns, np.float32)
         lib().wqlref_get_frames(self.h, STREAMS.index(name), out.ctypes.data)
         return out.reshape(nf, NCOMP[name], ns, nr)
+
+
+def up_tables():
+    """[(fd_type, order, closure rows, tau0)] of the oracle's table operators."""
+    out = []
+    k = 0
+    while True:
+        fd = ctypes.create_string_buffer(16)
+        o, R, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        if lib().wqlref_up_table(k, fd, ctypes.byref(o), ctypes.byref(R), ctypes.byref(t)) < 0:
+            return out
+        out.append((fd.value.decode(), o.value, R.value, t.value))
+        k += 1
+
+
+def up_matrix(k, plus, n, axis=0, interior=False):
+    """Dense n x n D+ (plus) or D- (times h) of table operator k along an axis;
+    interior: the interior routine's rows inside instead of the near-boundary
+    routine's."""
+    D = np.zeros((n, n))
+    assert lib().wqlref_up_matrix(k, int(plus), axis, int(interior), n, D.ctypes.data) == 0
+    return D
 
 
 def fd_matrix(fd, plus, n):

@@ -1,6 +1,8 @@
-"""The upwind SBP operators of orders 6 and 5 (fd_type = 'upwind') on the
-GPU against the oracle: FP64 fields to 1e-11 relative L2 (rate and state to
-its solver tolerance), and the FP32-compensated mode against FP64 to 1e-5."""
+"""The upwind SBP operators on the GPU against the oracle: orders 6 and 5
+(fd_type = 'upwind'), and the table operators (upwind orders 2, 3, 4, 7, 8,
+9 and upwind_drp orders 3..7, 66, 679).  FP64 fields to 1e-11 relative L2
+(rate and state to its solver tolerance), and the FP32-compensated mode
+against FP64 to 1e-5."""
 import numpy as np
 import pytest
 
@@ -106,7 +108,45 @@ def test_upwind_in_batch_equals_alone(ctx, wqlmod, tmp_path):
     bt.close()
 
 
-def test_upwind_other_orders_rejected(ctx, wqlmod, tmp_path):
-    p = write(tmp_path, "u4.in", case_text("up_pml").replace("order = 6", "order = 4"))
-    with pytest.raises(Exception, match="order = 5 or 6"):
+def test_upwind_unknown_orders_rejected(ctx, wqlmod, tmp_path):
+    p = write(tmp_path, "u10.in", case_text("up_pml").replace("order = 6", "order = 10"))
+    with pytest.raises(Exception, match="not supported"):
         wqlmod.Scenario(ctx, p)
+
+
+# The table operators (orders 2, 3, 4, 7, 8, 9 and the DRP variants, read from
+# the reference's routines by oracle/make_upwind_tables.py), per point.
+TABLE_OPS = [("upwind", o) for o in (2, 3, 4, 7, 8, 9)] + [("upwind_drp", o) for o in (3, 4, 5, 6, 7, 66, 679)]
+
+
+def _op_text(fd, order, base):
+    return case_text(base).replace(" w_stride = 1,", f" w_stride = 1,\n fd_type = '{fd}',\n order = {order},", 1)
+
+
+@pytest.mark.parametrize("fd,order", TABLE_OPS)
+def test_table_operator_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, fd, order):
+    """A point source in a locked two-block domain (2 x 21^3): FP64 fields
+    against the oracle to 1e-11."""
+    p = write(tmp_path, "op.in", _op_text(fd, order, "mt4"))
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, 30)
+    assert max(field_errors(s, o)) < TOL
+
+
+@pytest.mark.parametrize("fd,order,base,steps", [("upwind", 2, "pml_curv", 20), ("upwind", 4, "pml", 30),
+                                                 ("upwind", 8, "pml_curv", 20), ("upwind_drp", 66, "pml_curv", 20),
+                                                 ("upwind_drp", 679, "pml", 30), ("upwind", 3, "an_pml", 20),
+                                                 ("upwind_drp", 66, "an_pml", 20)])
+def test_table_operator_pml_anelastic_parity(ctx, wqlmod, oracle_lib, tmp_path, fd, order, base, steps):
+    """PML slabs (7 points, inside and outside the closure rows) on Cartesian
+    and curvilinear grids, and the anelastic response: FP64 against the
+    oracle to 1e-11, FP32C against FP64 to 1e-5.  upwind_drp 66 uses the
+    interior routine's stencil inside the block and the near-boundary
+    routine's on the shell, as the reference does."""
+    p = write(tmp_path, "op.in", _op_text(fd, order, base))
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, steps)
+    assert max(field_errors(s, o)) < TOL
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    f.step(steps)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), s.fields(b)) < 1e-5

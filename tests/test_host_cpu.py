@@ -2,6 +2,8 @@
 files that mesh_source = 'file' reads (wql_write_block_grids, the role of
 the reference's preprocessor) and the device-footprint estimate used for
 admission."""
+import os
+
 import numpy as np
 import pytest
 
@@ -197,3 +199,19 @@ def test_library_upwind_tables_match_oracle(oracle_lib, tmp_path):
            oracle_lib.fd_matrix(0, True, 30)]
     for got, want in zip(mats, ref):
         assert np.abs(got - want).max() < 1e-15
+
+
+def test_upwind_table_copies_agree():
+    """The library's and the oracle's copies of the table upwind operators
+    (written by oracle/make_upwind_tables.py) hold the same numbers."""
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = open(os.path.join(root, "waveqlab3d-gh_gb300", "csrc", "wql_upwind_tables.h")).read()
+    orc = open(os.path.join(root, "oracle", "upwind_tables.inc")).read()
+
+    def data(text):
+        body = text[text.index("= {"):]
+        return re.findall(r'"[a-z_]+"|-?\d+\.?\d*(?:e[+-]?\d+)?', body)
+    a, b = data(lib), data(orc)
+    assert len(a) == len(b) > 15 * 1300
+    assert a == b

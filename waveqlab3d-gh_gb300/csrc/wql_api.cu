@@ -21,6 +21,7 @@
 #include "host/wql_input.h"
 #include "wql_internal.h"
 #include "wql_sbp.cuh"
+#include "wql_upwind_tables.h"
 
 using namespace wql;
 
@@ -158,7 +159,9 @@ struct wql_scn {
   double stage_t0 = 0.0;
   int stage_launches = 0;
   int kernel_variant = 0;  // stencil variant (0 default per precision)
-  int fd = 0;              // 0: traditional SBP-6; 1: upwind order 6; 2: upwind order 5
+  int fd = 0;              // 0: traditional SBP-6; 1: upwind order 6; 2: upwind order 5; 3: a table operator
+  const UpwindTable* ut = nullptr;  // fd 3: the operator's table
+  void* ug_dev = nullptr;           // fd 3: the table on the device, in the field type
   bool anel = false;       // response = 'anelastic'
   double an_tau[4] = {}, an_w[4] = {};
   int schunk = 0;          // planes per CTA along s (0: default)
@@ -548,7 +551,8 @@ int setup_block(wql_scn* S, int b) {
   // to the anelastic kernel
   if (S->prec == WQL_FP32C && S->anel && (rc = S->alloc(&B.G, 9 * B.np * S->esz))) return rc;
   // src/block.f90:189-214
-  const double tau0 = S->fd == 1 ? kTau0Upwind6 : (S->fd == 2 ? kTau0Upwind5 : 1.0 / (0.315949074074074));
+  const double tau0 = S->fd == 1 ? kTau0Upwind6
+                      : (S->fd == 2 ? kTau0Upwind5 : (S->fd == 3 ? S->ut->tau0 : 1.0 / (0.315949074074074)));
   const int dims[3] = {B.nq, B.nr, B.ns};
   for (int d = 0; d < 3; ++d) B.tau_h[d] = tau0 / (1.0 / (double)(dims[d] - 1));
   // manufactured solution: shapes, forcing shapes and the initial fields
@@ -719,13 +723,46 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
   const Problem& Pr = S->P;
-  // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator or the
-  // upwind operators of order 6
+  // src/RHS_Interior.f90:31-125: the traditional SBP-6 operator, the upwind
+  // operators of orders 2..9 or the upwind DRP operators of orders 3..7, 66
+  // and 679 (the ones other than upwind 5 and 6 from wql_upwind_tables.h)
   if (Pr.fd_type == "upwind" && Pr.order == 6) S->fd = 1;
   else if (Pr.fd_type == "upwind" && Pr.order == 5) S->fd = 2;
-  else if (Pr.fd_type != "traditional")
-    return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' with order " + std::to_string(Pr.order) +
-                                 " is not supported (traditional SBP-6, or upwind with order = 5 or 6)");
+  else if (Pr.fd_type != "traditional") {
+    for (int k = 0; k < kUpwindTableCount; ++k)
+      if (Pr.fd_type == kUpwindTable[k].fd_type && Pr.order == kUpwindTable[k].order) S->ut = &kUpwindTable[k];
+    if (!S->ut)
+      return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' with order " + std::to_string(Pr.order) +
+                                   " is not supported (traditional; upwind with order 2..9; upwind_drp with order "
+                                   "3..7, 66 or 679)");
+    S->fd = 3;
+    // every row must fit in the block: the closure rows reach at most point
+    // 13, the interior rows R points either side
+    int reach = 2 * S->ut->R + 1;
+    const double* rows[4] = {&S->ut->lp[0][0][0], &S->ut->lm[0][0][0], &S->ut->rp[0][0][0], &S->ut->rm[0][0][0]};
+    for (const double* r : rows)
+      for (int e = 0; e < kUgRowBlock; ++e)
+        if (r[e] != 0.0) reach = std::max(reach, e % kUgCol + 1);
+    for (int b = 0; b < 2; ++b)
+      for (int d = 0; d < 3; ++d)
+        if (Pr.btp[b].nqrs[d] < reach)
+          return fail(WQL_E_INPUT, "fd_type '" + Pr.fd_type + "' with order " + std::to_string(Pr.order) +
+                                       " needs at least " + std::to_string(reach) + " points per axis");
+    std::vector<double> w(kUgWords, 0.0);
+    std::copy(S->ut->ip, S->ut->ip + kUgCol, w.begin());
+    std::copy(S->ut->im, S->ut->im + kUgCol, w.begin() + kUgCol);
+    std::copy(S->ut->bp, S->ut->bp + kUgCol, w.begin() + 2 * kUgCol);
+    std::copy(S->ut->bm, S->ut->bm + kUgCol, w.begin() + 3 * kUgCol);
+    for (int q = 0; q < 4; ++q) std::copy(rows[q], rows[q] + kUgRowBlock, w.begin() + 4 * kUgCol + q * kUgRowBlock);
+    int rc;
+    if ((rc = S->alloc(&S->ug_dev, kUgWords * S->esz, false))) return rc;
+    if (precision == WQL_FP64) {
+      CK(cudaMemcpy(S->ug_dev, w.data(), kUgWords * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+      std::vector<float> wf(w.begin(), w.end());
+      CK(cudaMemcpy(S->ug_dev, wf.data(), kUgWords * sizeof(float), cudaMemcpyHostToDevice));
+    }
+  }
   if (Pr.response == "anelastic") {
     // init_anelastic_properties (src/material.f90:85-115): relaxation times
     // and weights exist for weight_exp 0 and 0.6 only
@@ -962,6 +999,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.bc_form = S->bc_form;
   a.kernel = S->kernel_variant;
   a.fd = S->fd;
+  if (S->ut) a.ug = UpG{S->ug_dev, S->ut->R, S->ut->plo, S->ut->pn, S->ut->mlo, S->ut->mn};
   a.schunk = S->schunk;
   a.fault_sat = (const T*)S->sat + (long long)b * 9 * B.nr * B.ns;
   a.npml = B.npml;

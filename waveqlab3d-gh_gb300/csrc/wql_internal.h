@@ -33,6 +33,19 @@ constexpr int kCartCoef = 3;
 // Boundary penalty selection for the outer faces.
 enum BcForm : int { BC_CHARACTERISTIC = 0, BC_WEIGHTED = 1 };
 
+// A table upwind operator (fd 3: the upwind operators of orders 2, 3, 4, 7,
+// 8, 9 and the DRP variants of src/JU_xJU_yJU_z6.f90, tabulated in
+// wql_upwind_tables.h) in device memory, in the field type: the interior
+// weights ip[13] im[13] (the interior routine) and bp[13] bm[13] (the
+// interior rows of the boundary shell), then the closure rows lp, lm, rp, rm,
+// each [axis 3][row 8][point 13].  R closure rows per end; interior D+ on
+// offsets plo .. plo+pn-1, D- on mlo .. mlo+mn-1.
+struct UpG {
+  const void* w;
+  int R, plo, pn, mlo, mn;
+};
+constexpr int kUgCol = 13, kUgRows = 8, kUgRowBlock = 3 * kUgRows * kUgCol, kUgWords = 4 * kUgCol + 4 * kUgRowBlock;
+
 template <typename T>
 struct VolumeArgs {
   int nq, nr, ns;
@@ -64,7 +77,9 @@ struct VolumeArgs {
   // kernel and read by the PML and anelastic kernels of the same stage;
   // nullptr where those kernels form it themselves
   T* G;
-  int fd;             // difference operator: 0 SBP-6 central; upwind pair (D+ on v, D- on fluxes) of order 6 (1) or 5 (2)
+  int fd;             // difference operator: 0 SBP-6 central; upwind pair (D+ on v, D- on fluxes) of order 6 (1),
+                      // of order 5 (2), or a table operator (3, ug)
+  UpG ug;
   int kernel;         // stencil variant: 0 default, 1 per-point, 2..4 tiled
   int schunk;         // planes per CTA along s for the tiled kernel (0: default)
   // RK

@@ -122,7 +122,6 @@ __device__ __forceinline__ void upx_entry(int kind, int t, int ax, T& wv, T& wf,
     wv = upw<T, FD>(0, i, t);
     wf = upw<T, FD>(1, i, t);
     off = t - i;
-    if (FD == 2 && ax == 2 && i == 3 && t == 6) wv = (T)WQL_UP5_S_ROW4_P7;
   } else {
     const int k = kind - 1;
     wv = -upw<T, FD>(1, k, t);

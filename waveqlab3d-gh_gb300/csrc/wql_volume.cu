@@ -259,6 +259,102 @@ __device__ void diff_pml_flux_up(const T* __restrict__ F, const T* __restrict__ 
   }
 }
 
+// ---- table upwind operators (fd 3), as the reference applies them: the
+// near-boundary routine JJU_x<order>_upwind(_drp) at points of the boundary
+// shell (its closure rows, and its interior case bp/bm on the axes where the
+// point is interior), the interior routine JJU_x<order>_interior_upwind(_drp)
+// (ip/im) at the other points (src/RHS_Interior.f90:40-125, 276-1512).
+template <typename T>
+__device__ __forceinline__ T ugw(const UpG& g, int idx) {
+  return ((const T*)g.w)[idx];
+}
+
+// Whether point idx lies in the boundary shell: outside [lo, n-1-hi] on some
+// axis, with lo and hi the closure rows R, or npml on a PML side if larger
+// (the interior limits of the interior routines).
+template <typename T>
+__device__ __forceinline__ bool ug_shell(const VolumeArgs<T>& a, const int idx[3], const int nn[3]) {
+  bool shell = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int lo = a.pml[2 * d] ? max(a.ug.R, a.npml) : a.ug.R;
+    const int hi = a.pml[2 * d + 1] ? max(a.ug.R, a.npml) : a.ug.R;
+    shell = shell || idx[d] < lo || idx[d] > nn[d] - 1 - hi;
+  }
+  return shell;
+}
+
+// Weights of the D+ (plus) or D- row at 0-based index i of n along axis d:
+// calls f(offset from the point, weight) for each nonzero weight.
+template <typename T, typename Fn>
+__device__ __forceinline__ void ug_row(const UpG& g, bool shell, bool plus, int i, int n, int d, Fn&& f) {
+  if (i >= g.R && i < n - g.R) {
+    const int base = (shell ? 2 * kUgCol : 0) + (plus ? 0 : kUgCol);
+    const int lo = plus ? g.plo : g.mlo, cnt = plus ? g.pn : g.mn;
+    for (int k = 0; k < cnt; ++k) {
+      const T w = ugw<T>(g, base + k);
+      if (w != T(0)) f(lo + k, w);
+    }
+  } else if (i < g.R) {  // left row i, points 0..12
+    const int base = 4 * kUgCol + (plus ? 0 : kUgRowBlock) + (d * kUgRows + i) * kUgCol;
+    for (int t = 0; t < kUgCol; ++t) {
+      const T w = ugw<T>(g, base + t);
+      if (w != T(0)) f(t - i, w);
+    }
+  } else {  // right row k = n-1-i, points n-1-t
+    const int k = n - 1 - i;
+    const int base = 4 * kUgCol + (plus ? 2 : 3) * kUgRowBlock + (d * kUgRows + k) * kUgCol;
+    for (int t = 0; t < kUgCol; ++t) {
+      const T w = ugw<T>(g, base + t);
+      if (w != T(0)) f(k - t, w);
+    }
+  }
+}
+
+// The six differenced quantities of load6 along axis d: D+ of the
+// velocities, D- of the d-face momentum fluxes.
+template <typename T, bool CURV>
+__device__ void diff6_ug(const T* __restrict__ F, const T* __restrict__ coef, long long np, long long p, int i,
+                         int n, long long st, int d, const UpG& g, bool shell, T r[6]) {
+#pragma unroll
+  for (int c = 0; c < 6; ++c) r[c] = T(0);
+  ug_row<T>(g, shell, true, i, n, d, [&](int off, T w) {
+    const long long q = p + off * st;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + q];
+  });
+  ug_row<T>(g, shell, false, i, n, d, [&](int off, T w) {
+    T t[6];
+    load6<T, CURV>(F, coef, np, p + off * st, d, t);
+#pragma unroll
+    for (int c = 3; c < 6; ++c) r[c] += w * t[c];
+  });
+}
+
+// D+ of the three velocities only, along axis d.
+template <typename T>
+__device__ void diff_v_ug(const T* __restrict__ F, long long np, long long p, int i, int n, long long st, int d,
+                          const UpG& g, bool shell, T r[3]) {
+  r[0] = r[1] = r[2] = T(0);
+  ug_row<T>(g, shell, true, i, n, d, [&](int off, T w) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c] += w * F[c * np + p + off * st];
+  });
+}
+
+// D- of the three fluxes J*metric_j(d)*sigma_{c,j} (the PML split).
+template <typename T>
+__device__ void diff_pml_flux_ug(const T* __restrict__ F, const T* __restrict__ coef, long long np, long long p,
+                                 int i, int n, long long st, int d, int j, const UpG& g, bool shell, T r[3]) {
+  r[0] = r[1] = r[2] = T(0);
+  ug_row<T>(g, shell, false, i, n, d, [&](int off, T w) {
+    const long long q = p + off * st;
+    const T a = coef[(d * 3 + j) * np + q];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c] += w * (a * F[sig(c, j) * np + q]);
+  });
+}
+
 // Operator dispatch on the compile-time fd of a kernel.
 template <typename T, bool CURV, int FD>
 __device__ __forceinline__ void diff6_op(const T* __restrict__ F, const T* __restrict__ coef, long long np,
@@ -511,9 +607,11 @@ __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_con
   const int idx[3] = {i, j, k}, nn[3] = {a.nq, a.nr, a.ns};
   const long long st[3] = {1, a.pq, (long long)a.pq * a.nr};
 #pragma unroll
+  const bool shell = FD == 3 && ug_shell(a, idx, nn);
   for (int d = 0; d < 3; ++d) {
     T o[6];
-    diff6_op<T, CURV, FD>(a.Fin, a.coef, np, p, idx[d], nn[d], st[d], d, o);
+    if (FD == 3) diff6_ug<T, CURV>(a.Fin, a.coef, np, p, idx[d], nn[d], st[d], d, a.ug, shell, o);
+    else diff6_op<T, CURV, FD == 3 ? 0 : FD>(a.Fin, a.coef, np, p, idx[d], nn[d], st[d], d, o);
     const T rh = a.rh[d];
     if (CURV) {
       T m[3];
@@ -636,6 +734,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
   const long long st[3] = {1, a.pq, (long long)a.pq * nr};
   const T* __restrict__ F = a.Fin;
   const T* __restrict__ coef = a.coef;
+  const bool shell = FD == 3 && ug_shell(a, idx, nn);
   // velocity gradient at the point: from the TMA stencil of this stage
   // (a.G), else formed here
   T g[3][3];
@@ -653,7 +752,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T o[3];
-      if (FD) diff_v_up<T, FD ? FD : 1>(F, np, p, idx[d], nn[d], st[d], d, o);
+      if (FD == 3) diff_v_ug<T>(F, np, p, idx[d], nn[d], st[d], d, a.ug, shell, o);
+      else if (FD) diff_v_up<T, FD == 3 ? 1 : (FD ? FD : 1)>(F, np, p, idx[d], nn[d], st[d], d, o);
       else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
       const T rh = a.rh[d];
       for (int c = 0; c < 3; ++c) {
@@ -707,14 +807,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         T r3[3];
-        if (FD) diff_pml_flux_up<T, FD ? FD : 1>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
+        if (FD == 3) diff_pml_flux_ug<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, a.ug, shell, r3);
+        else if (FD) diff_pml_flux_up<T, FD == 3 ? 1 : (FD ? FD : 1)>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
         else diff_pml_flux<T>(F, coef, np, p, idx[d], nn[d], st[d], d, axis, r3);
         for (int c = 0; c < 3; ++c) acc3[c] += a.rh[d] * r3[c];
       }
       for (int c = 0; c < 3; ++c) sd[c] = acc3[c] * Jinv;
     } else {
       T o[6];
-      diff6_op<T, false, FD>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, o);
+      if (FD == 3) diff6_ug<T, false>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, a.ug, shell, o);
+      else diff6_op<T, false, FD == 3 ? 0 : FD>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, o);
       for (int c = 0; c < 3; ++c) sd[c] = a.cart_metric[axis] * a.rh[axis] * o[3 + c];
     }
     corr[0] -= damp * qv[0] * rhoinv;
@@ -798,7 +900,8 @@ __global__ void __launch_bounds__(256, WQL_ANEL_MINB) anelastic_kernel(const __g
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T o[3];
-      if (FD) diff_v_up<T, FD ? FD : 1>(F, np, p, idx[d], nn[d], st[d], d, o);
+      if (FD == 3) diff_v_ug<T>(F, np, p, idx[d], nn[d], st[d], d, a.ug, ug_shell(a, idx, nn), o);
+      else if (FD) diff_v_up<T, FD == 3 ? 1 : (FD ? FD : 1)>(F, np, p, idx[d], nn[d], st[d], d, o);
       else diff_v<T>(F, np, p, idx[d], nn[d], st[d], o);
       const T rh = a.rh[d];
 #pragma unroll
@@ -1147,6 +1250,7 @@ void launch_stencil(const VolumeArgs<T>& a, cudaStream_t s) {
       dim3 blk(32, 8, 1), grd((a.nq + 31) / 32, (a.nr + 7) / 8, a.ns);
       if (a.fd == 1) stencil_kernel_pointwise<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a, 0);
       else if (a.fd == 2) stencil_kernel_pointwise<T, CURV, KAHAN, 2><<<grd, blk, 0, s>>>(a, 0);
+      else if (a.fd == 3) stencil_kernel_pointwise<T, CURV, KAHAN, 3><<<grd, blk, 0, s>>>(a, 0);
       else stencil_kernel_pointwise<T, CURV, KAHAN, 0><<<grd, blk, 0, s>>>(a, 0);
       return;
     }
@@ -1170,6 +1274,7 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
   if (a.anel) {  // before the PML kernel: it reads Q of the stage's input
     if (a.fd == 1) anelastic_kernel<T, CURV, KAHAN, 1><<<grd, blk, 0, s>>>(a);
     else if (a.fd == 2) anelastic_kernel<T, CURV, KAHAN, 2><<<grd, blk, 0, s>>>(a);
+    else if (a.fd == 3) anelastic_kernel<T, CURV, KAHAN, 3><<<grd, blk, 0, s>>>(a);
     else anelastic_kernel<T, CURV, KAHAN, 0><<<grd, blk, 0, s>>>(a);
     ++n;
   }
@@ -1179,6 +1284,7 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
     if (bx.start[bx.n] > 0) {
       if (a.fd == 1) pml_kernel<T, CURV, KAHAN, 1><<<nblk, 256, 0, s>>>(a, bx);
       else if (a.fd == 2) pml_kernel<T, CURV, KAHAN, 2><<<nblk, 256, 0, s>>>(a, bx);
+      else if (a.fd == 3) pml_kernel<T, CURV, KAHAN, 3><<<nblk, 256, 0, s>>>(a, bx);
       else pml_kernel<T, CURV, KAHAN, 0><<<nblk, 256, 0, s>>>(a, bx);
     }
     ++n;
