@@ -1,8 +1,9 @@
 """Build recipe for the oracle (test infrastructure only).
 
 Compiles oracle/wql_ref.cpp -- the FP64 CPU restatement of the reference's
-time step -- together with the product's `.in` text parser into
-oracle/_build/libwqlref.so.  FMA contraction is disabled so the restatement
+time step -- and oracle/ref_input.cpp, its own reader of the `.in` files,
+into oracle/_build/libwqlref.so (the library's header wql_input.h supplies
+only the layout of the parsed record).  FMA contraction is disabled so the restatement
 rounds like the reference's x86-64 gfortran build (no FMA at -O5 without
 -march).  OpenMP parallelises the stencil loops for the timed CPU baseline;
 each grid point is independent, so results do not depend on the thread count.
@@ -14,8 +15,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build", "libwqlref.so")
-SRCS = [os.path.join(HERE, "wql_ref.cpp"),
-        os.path.join(ROOT, "waveqlab3d-gh_gb300", "csrc", "host", "wql_input.cpp")]
+SRCS = [os.path.join(HERE, "wql_ref.cpp"), os.path.join(HERE, "ref_input.cpp")]
 
 
 def build(force=False, verbose=False):

@@ -50,6 +50,13 @@
 
 #include "wql_input.h"
 
+// The oracle's own reader of the .in files (oracle/ref_input.cpp); the
+// Problem record is the library's data layout, filled independently.
+namespace oref {
+int read_in_text(const std::string& text, const std::string& base_dir, wql::Problem& P, std::string& err);
+int read_in_file(const std::string& path, wql::Problem& P, std::string& err);
+}  // namespace oref
+
 namespace {
 
 using std::vector;
@@ -2716,7 +2723,7 @@ static void* create_domain(Domain* D, const Media& md);
 void* wqlref_create(const char* in_path) {
   Domain* D = new Domain();
   std::string err;
-  if (wql::parse_in_file(in_path, D->P, err) != 0) {
+  if (oref::read_in_file(in_path, D->P, err) != 0) {
     std::snprintf(g_err, sizeof(g_err), "%s", err.c_str());
     delete D;
     return nullptr;
@@ -2733,7 +2740,7 @@ void* wqlref_create_ex(const char* in_text, const double* fault_offset, const do
                        const double* rho1) {
   Domain* D = new Domain();
   std::string err;
-  if (wql::parse_in_text(in_text, "", D->P, err) != 0) {
+  if (oref::read_in_text(in_text, "", D->P, err) != 0) {
     std::snprintf(g_err, sizeof(g_err), "%s", err.c_str());
     delete D;
     return nullptr;
