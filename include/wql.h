@@ -112,7 +112,11 @@ int wql_sync(wql_scn* scn, int check_nan);
 int wql_get_info(wql_scn* scn, wql_info* info);
 
 /* Field component comp (0..8 = vx,vy,vz,sxx,syy,szz,sxy,sxz,syz,
- * src/JU_xJU_yJU_z6.f90:16304-16314) of block (0/1) to host, as double. */
+ * src/JU_xJU_yJU_z6.f90:16304-16314) of block (0/1) to host, as double.
+ * With the plastic_flow model (response = 'plastic', plastic_model other
+ * than 'scec'), comp 9 and 10 read the plastic strain rate lambda and the
+ * plastic strain gammap per point (P%P(:,:,:,1:2), src/plastic.f90:141,
+ * src/plastic_material.f90:38-44); otherwise they return WQL_E_STATE. */
 int wql_get_field(wql_scn* scn, int block, int comp, double* host_out);
 int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in);
 

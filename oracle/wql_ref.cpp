@@ -160,6 +160,17 @@ bool initial_stress_tensor(wp s0[6], const wp x[3], const std::string& problem,
     s0[5] = 0.0;
     return true;
   }
+  if (problem == "rate-weakening") {  // :184-193, with the routine's pi = 3.14159265359
+    const wp pi_isc = 3.14159265359;
+    wp psi = 50.0 / 180.0 * pi_isc;
+    s0[0] = -126.0;
+    s0[4] = 42.0;
+    s0[2] = (1.0 - 2.0 * s0[4] / (s0[0] * std::tan(2.0 * psi))) * s0[0];
+    s0[1] = 0.5 * (s0[0] + s0[2]);
+    s0[3] = 0.0;
+    s0[5] = 0.0;
+    return true;
+  }
   return false;
 }
 
@@ -219,6 +230,17 @@ void prestress(wp& T0n, wp& T0m, wp& T0l, const wp x[3], wp t, const Presets& P,
     if (t > 0.0 && t < 1.0) G = std::exp((t - 1.0) * (t - 1.0) / (t * (t - 2.0)));
     if (t >= 1.0) G = 1.0;
     T0l = T0l + 25.0 * F * G;
+  } else if (pb == "rate-weakening") {  // :2387-2423
+    initial_stress_tensor(s0, x, pb);
+    traction_nml(s0, n, m, l, T0n, T0m, T0l);
+    wp tau_pulse = -0.2429 * T0n;
+    wp r0 = 3.0 * 1.5 * 0.3;
+    wp y0 = 8.0, z0 = 0.0;
+    wp r = std::sqrt((x[1] - y0) * (x[1] - y0) + (x[2] + z0) * (x[2] + z0));
+    wp F = std::exp(-((r / r0) * (r / r0)) / 2.0);
+    wp G = 0.0;
+    if (t > 0.0) G = 1.0;
+    T0l = T0l + 2.0 * tau_pulse * F * G;
   } else if (pb == "TPV10") {
     T0n = -7.378 * x[1] * (2.0 / (std::sqrt(3.0)));
     T0m = -0.55 * T0n;
@@ -343,6 +365,11 @@ bool rs_params(const Presets& P, const wp x[3], RSPar& r) {  // IC:384-417
   if (pb == "rs_param") {
     const wql::FrictionExt& e = *P.fx;
     r.L0 = e.L; r.f0 = e.f0; r.b = e.b; r.V0 = e.V0; r.a = e.a;
+    return true;
+  }
+  if (pb == "rate-weakening") {  // :410-416
+    r.L0 = 2.0 * 0.2572; r.f0 = 0.7; r.b = 0.02; r.V0 = 1.0e-6;
+    r.a = 0.016 + 0.016 * (1.0 - smooth_boxcar(x[1], 20.0, 2.5) * smooth_boxcar(x[2], 20.0, 2.5));
     return true;
   }
   return false;
@@ -535,6 +562,7 @@ struct Face {
 };
 
 struct RBlock {
+  int index = 0;  // 0 or 1
   int nq = 0, nr = 0, ns = 0;
   size_t np = 0;
   wp hq = 0, hr = 0, hs = 0;
@@ -558,6 +586,7 @@ struct RBlock {
   vector<wp> Qs_inv, Qp_inv;
   vector<wp> eta[6][4], Deta[6][4];
   wp tau[4] = {0, 0, 0, 0}, weight[4] = {0, 0, 0, 0};
+  vector<wp> Pl[2];  // plastic_flow: P(1) plastic strain rate, P(2) plastic strain
   size_t id(int i, int j, int k) const {
     return (size_t)(i - 1) + (size_t)nq * ((size_t)(j - 1) + (size_t)nr * (size_t)(k - 1));
   }
@@ -1433,6 +1462,7 @@ void init_anelastic(RBlock& B, const wql::AnelasticParams& ap) {
 int init_block(Domain& D, int b, const Media& md) {
   RBlock& B = D.Bk[b];
   const wql::BlockParams& bp = D.P.btp[b];
+  B.index = b;
   B.nq = bp.nqrs[0];
   B.nr = bp.nqrs[1];
   B.ns = bp.nqrs[2];
@@ -1497,6 +1527,8 @@ int init_block(Domain& D, int b, const Media& md) {
     B.F[c].assign(B.np, 0.0);
     B.DF[c].assign(B.np, 0.0);  // 1e40 in the reference; A(1)=0 clears it
   }
+  if (D.P.response == "plastic")  // init_plastic_material: src/plastic_material.f90:27-44
+    for (int c = 0; c < 2; ++c) B.Pl[c].assign(B.np, 0.0);
   normals(B);
   // init_boundaries: src/BoundaryConditions.f90:15-48
   B.Lx = bp.lqrs[0]; B.Ly = bp.lqrs[1]; B.Lz = bp.lqrs[2];
@@ -2334,7 +2366,15 @@ void impose_interface(Domain& D, int b, int stage, bool write_frame) {
       Hat h;
       interface_point(D, ur, vr, Z1s, Z2s, Z1p, Z2p, I.S[3][f], D.rs ? I.W[f] : 0.0, xij, D.t,
                       l, m, n, h, have_rs ? &rsp : nullptr);
-      if (D.rs && have_rs) {
+      if (D.rs && have_rs && D.P.problem == "rate-weakening") {
+        // slip law with a steady state weakening above V_w (Interface_Condition.f90:438-443)
+        wp V_w = 0.17 + 5.0 * (1.0 - smooth_boxcar(xij[1], 20.0, 2.5) * smooth_boxcar(xij[2], 20.0, 2.5));
+        wp Fss = rsp.f0 - (rsp.b - rsp.a) * std::log(h.Vel / rsp.V0);
+        wp rv = h.Vel / V_w;
+        Fss = 0.13 + (Fss - 0.13) / std::pow(1.0 + rv * rv * rv * rv * rv * rv * rv * rv, 0.125);
+        I.DW[f] = I.DW[f] - h.Vel / rsp.L0 *
+                                (rsp.a * std::asinh(h.Vel / (2.0 * rsp.V0) * std::exp(I.W[f] / rsp.a)) - Fss);
+      } else if (D.rs && have_rs) {
         // aging law, TPV101/TPV102 (Interface_Condition.f90:431-436)
         I.DW[f] = I.DW[f] + rsp.b * rsp.V0 / rsp.L0 * std::exp(-(I.W[f] - rsp.f0) / rsp.b) -
                   h.Vel * rsp.b / rsp.L0;
@@ -2502,7 +2542,29 @@ void plasticity(Domain& D, RBlock& B) {
                  (sa[2] - sa[0]) * (sa[2] - sa[0])) / 6.0 +
                 sa[3] * sa[3] + sa[4] * sa[4] + sa[5] * sa[5];
         wp tau = std::sqrt(J2);
-        if (D.scec) {
+        if (!D.scec) {
+          // plastic_flow (src/plastic.f90:220-290), lambda = P(1), gammap = P(2)
+          const wp* mbe = D.P.btp[B.index].mu_beta_eta;
+          wp mu = mbe[0], beta = mbe[1], eta = mbe[2];
+          wp G = B.M[1][p];
+          wp K = B.M[0][p] + 2.0 / 3.0 * B.M[1][p];
+          wp Y = tau + mu * sigma;  // yield
+          if (Y <= 0.0) {
+            B.Pl[0][p] = 0.0;
+            continue;
+          }
+          const wp delta[6] = {1, 1, 1, 0, 0, 0};
+          wp sd[6];
+          for (int t = 0; t < 6; ++t) sd[t] = sa[t] - sigma * delta[t];
+          wp lambda = (tau + mu * sigma) / (eta + D.dt * (G + mu * beta * K));
+          B.Pl[0][p] = lambda;
+          B.Pl[1][p] = B.Pl[1][p] + D.dt * lambda;
+          tau = tau - D.dt * lambda * G;
+          sigma = sigma - D.dt * lambda * beta * K;
+          for (int t = 0; t < 6; ++t) sd[t] = sd[t] * tau / (tau + D.dt * lambda * G);
+          for (int t = 0; t < 6; ++t) sa[t] = sigma * delta[t] + sd[t];
+          for (int t = 0; t < 6; ++t) B.F[3 + t][p] = sa[t] - s0[t];
+        } else {
           wp Ys = std::max(0.0, c * std::cos(std::atan(nu)) - (sigma)*std::sin(std::atan(nu)));
           wp Yf = tau - Ys;
           if (Yf <= 0.0) continue;
@@ -2636,7 +2698,8 @@ void init_vel_state(Domain& D, int b) {
   wp aa = (b == 0) ? -1.0 : 1.0;
   int side = (b == 0) ? 2 : 1;
   int xend = (b == 0) ? B.nq : 1;
-  wp Vin = (D.P.problem == "rs_param") ? D.P.fric.Vini : 1.0e-12;
+  const bool rw = D.P.problem == "rate-weakening";  // :2819-2843: at rest, uniform state
+  wp Vin = (D.P.problem == "rs_param") ? D.P.fric.Vini : (rw ? 0.0 : 1.0e-12);
   for (size_t p = 0; p < B.np; ++p) B.F[2][p] = (aa >= 0 ? 1.0 : -1.0) * std::fabs(0.5 * Vin);
   for (int k = 1; k <= B.ns; ++k)
     for (int j = 1; j <= B.nr; ++j) {
@@ -2647,6 +2710,10 @@ void init_vel_state(Domain& D, int b) {
         n[c] = B.B[side].n_n[c][f];
         m[c] = B.B[side].n_m[c][f];
         l[c] = B.B[side].n_l[c][f];
+      }
+      if (rw) {
+        I.W[f] = 0.4367;
+        continue;
       }
       wp T0n, T0m, T0l;
       prestress(T0n, T0m, T0l, x, 0.0, D.pre, l, m, n);
@@ -2786,7 +2853,7 @@ static void* create_domain(Domain* D, const Media& md) {
     const std::string& pb = D->P.problem;
     bool sw_ok = pb == "TPV5" || pb == "TPV26" || pb == "TPV27" || pb == "TPV28" || pb == "TPV29" ||
                  pb == "TPV30" || pb == "TPV10" || pb == "sw_param";
-    bool rs_ok = pb == "TPV101" || pb == "TPV102" || pb == "rs_param";
+    bool rs_ok = pb == "TPV101" || pb == "TPV102" || pb == "rs_param" || pb == "rate-weakening";
     if ((D->sw && !sw_ok) || (D->rs && !rs_ok)) {
       std::snprintf(g_err, sizeof(g_err), "problem preset %s is not restated for coupling %s",
                     pb.c_str(), cp.c_str());
@@ -2813,8 +2880,10 @@ static void* create_domain(Domain* D, const Media& md) {
       return nullptr;
     }
   }
-  if (D->plastic && !D->scec) {
-    std::snprintf(g_err, sizeof(g_err), "only plastic_model='scec' is restated");
+  if (D->plastic && !D->scec && D->P.problem != "rate-weakening") {
+    // plastic_flow reads mu_beta_eta, set only for this problem
+    // (src/plastic_material.f90:38-42)
+    std::snprintf(g_err, sizeof(g_err), "plastic_flow needs problem='rate-weakening'");
     delete D;
     return nullptr;
   }
@@ -2917,11 +2986,14 @@ int wqlref_step(void* h, int nsteps) {
   return 0;
 }
 
+// comp 0..8: the fields; 9, 10: plastic_flow's P(1), P(2) (plastic strain
+// rate and plastic strain)
 int wqlref_get_field(void* h, int block, int comp, double* out) {
   Domain* D = (Domain*)h;
-  if (block < 0 || block > 1 || comp < 0 || comp > 8) return 1;
+  if (block < 0 || block > 1 || comp < 0 || comp > 10) return 1;
   RBlock& B = D->Bk[block];
-  std::memcpy(out, B.F[comp].data(), B.np * sizeof(double));
+  if (comp > 8 && B.Pl[comp - 9].size() != B.np) return 1;
+  std::memcpy(out, comp > 8 ? B.Pl[comp - 9].data() : B.F[comp].data(), B.np * sizeof(double));
   return 0;
 }
 

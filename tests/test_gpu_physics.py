@@ -79,6 +79,33 @@ def test_rate_state_fp64_parity_converged(ctx, wqlmod, oracle_lib, tmp_path, cas
         assert rel_l2(s.iface(copy, 4), o.iface(copy, 4)) < TOL  # state variable
 
 
+@pytest.mark.parametrize("case,steps", [("rw", 40), ("rw_curv", 20), ("rw_plastic", 40)])
+def test_rate_weakening_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, steps):
+    """Problem 'rate-weakening' (slip law with flash weakening, a stress
+    pulse switched on at t > 0) and, in rw_plastic, the default plastic
+    model plastic_flow with its per-point plastic strain rate and strain:
+    FP64 against the oracle at 1e-11 with the friction solve iterated to a
+    fixed point; FP32C against FP64."""
+    p = write(tmp_path, case + ".in", case_text(case) + RS_CONVERGED)
+    s, o = run_pair(wqlmod, oracle_lib, ctx, p, steps)
+    errs = field_errors(s, o)
+    assert max(errs) < TOL, errs
+    for copy in range(2):
+        assert rel_l2(s.iface(copy, 4), o.iface(copy, 4)) < TOL
+        assert rel_l2(s.iface(copy, 3), o.iface(copy, 3)) < TOL
+    if case == "rw_plastic":
+        for b in range(2):
+            lam_o = o.field(b, 9)
+            assert (lam_o > 0).sum() > 10  # points yield
+            for comp in (9, 10):
+                assert rel_l2(s.field(b, comp), o.field(b, comp)) < TOL, (b, comp)
+    f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)
+    f.step(steps)
+    f.sync(check_nan=True)
+    for b in range(2):
+        assert rel_l2(f.fields(b), s.fields(b)) < 1e-4
+
+
 def test_topography_from_files(ctx, wqlmod, oracle_lib, tmp_path):
     """use_topography = T with the free surface and the fault surface read
     from files (read_topo_from_memory, read_from_memomry_fractal; src/grid.f90:

@@ -63,6 +63,12 @@ struct RK {
   }
 };
 
+// Frames per fault-frame ring: as many as fit in 128 MiB, 4 to 64.
+int frame_ring_cap(long long nf) {
+  const long long frame_bytes = (long long)kFrameWords * nf * (long long)sizeof(float);
+  return (int)std::max(4LL, std::min(64LL, (128LL << 20) / std::max(frame_bytes, 1LL)));
+}
+
 int preset_of(const std::string& pb) {
   if (pb == "TPV5" || pb == "LOH1" || pb == "OKLAHOMA") return PRE_TPV5;
   if (pb == "TPV26") return PRE_TPV26;
@@ -75,6 +81,7 @@ int preset_of(const std::string& pb) {
   if (pb == "TPV102") return PRE_TPV102;
   if (pb == "sw_param") return PRE_SW_PARAM;
   if (pb == "rs_param") return PRE_RS_PARAM;
+  if (pb == "rate-weakening") return PRE_RATE_WEAKENING;
   return PRE_NONE;
 }
 
@@ -129,6 +136,8 @@ struct wql_scn {
     void* Deta = nullptr;  // and their rates
     void* qs = nullptr;    // 1/Qs per point
     void* y = nullptr;
+    void* pl_lambda = nullptr;  // plastic_flow: plastic strain rate and
+    void* pl_gammap = nullptr;  // plastic strain per point
     void* ms = nullptr;    // manufactured-solution shapes (2 x np) and
     void* mp = nullptr;    // forcing shapes (9 x np), use_mms only
     double cart_metric[3] = {1, 1, 1};
@@ -166,11 +175,20 @@ struct wql_scn {
   double an_tau[4] = {}, an_w[4] = {};
   int schunk = 0;          // planes per CTA along s (0: default)
   bool plastic = false;
+  bool pl_flow = false;  // plastic_flow (the reference's default model) instead of scec
   double pl_c = 1.36, pl_nu = 0.1934, pl_Tv = 0.03;
-  // fault frames
-  float* frame_dev = nullptr;
-  int frame_cap = 0, frame_fill = 0;
-  std::vector<float> frames_host;
+  // fault frames: two device rings of frame_cap frames.  When the ring
+  // being filled is full, its copy to pinned host memory is queued on the
+  // stream and the other ring takes the next frames, so stepping never
+  // waits on the copy; the pinned frames move to the host chunks when the
+  // next ring fills or the frames are read.
+  float* frame_ring[2] = {nullptr, nullptr};
+  float* frame_dev = nullptr;  // the ring being filled
+  int frame_cap = 0, frame_fill = 0, ring_cur = 0;
+  float* frame_pin = nullptr;  // pinned staging of one ring (null: synchronous copies)
+  int pin_frames = 0;          // frames in flight to frame_pin
+  cudaEvent_t pin_done = nullptr;
+  std::vector<std::vector<float>> frame_chunks;  // flushed frames, whole frames per chunk
   int nframes = 0;
   // seismogram stations per block (src/seismogram.f90): 1-based grid
   // indices, device point offsets, a device ring of velocity records
@@ -215,6 +233,9 @@ struct wql_scn {
   }
 
   ~wql_scn() {
+    if (stream) cudaStreamSynchronize(stream);  // no copy in flight to frame_pin
+    if (frame_pin) cudaFreeHost(frame_pin);
+    if (pin_done) cudaEventDestroy(pin_done);
     for (auto e : ev_pool) cudaEventDestroy(e);
     for (auto& a : allocs)
       if (a.p) cudaFree(a.p);
@@ -565,7 +586,13 @@ int setup_block(wql_scn* S, int b) {
                      B.F[S->cur], S->stream);
     CK(cudaGetLastError());
   }
-  // depth coordinate for the plastic update
+  // depth coordinate for the plastic update; plastic_flow's per-point
+  // plastic strain rate and strain, zero at the start
+  // (src/plastic_material.f90:38-44)
+  if (S->pl_flow) {
+    if ((rc = S->alloc(&B.pl_lambda, B.np * S->esz))) return rc;
+    if ((rc = S->alloc(&B.pl_gammap, B.np * S->esz))) return rc;
+  }
   if (S->plastic) {
     if ((rc = S->alloc(&B.y, B.np * S->esz))) return rc;
     if (S->prec == WQL_FP64)
@@ -659,7 +686,7 @@ int precompute_fault(wql_scn* S) {
         x[c] = xi[c * nf + f];
       }
       prestress_static(S->fp, x, l, m, n, P[f], P[nf + f], P[2 * nf + f]);
-      P[3 * nf + f] = nucleation_weight(S->fp, x);
+      P[3 * nf + f] = nucleation_weight(S->fp, x, P[f]);
       P[4 * nf + f] = S->fp.coupling == CPL_RS ? rs_direct_a(S->fp, x) : 0.0;
     }
   }
@@ -672,7 +699,10 @@ int precompute_fault(wql_scn* S) {
 // Init_Vel_State (src/Interface_Condition.f90:2722-2850) for each block copy.
 int init_rate_state(wql_scn* S) {
   const long long nf = (long long)S->B[0].nr * S->B[0].ns;
-  const double Vin = (S->fp.preset == PRE_RS_PARAM) ? S->fp.Vini : 1.0e-12;
+  // 'rate-weakening' starts at rest with a uniform state 0.4367
+  // (src/Interface_Condition.f90:2819-2843)
+  const bool rw = S->fp.preset == PRE_RATE_WEAKENING;
+  const double Vin = (S->fp.preset == PRE_RS_PARAM) ? S->fp.Vini : (rw ? 0.0 : 1.0e-12);
   std::vector<double> W(2 * nf);
   for (int b = 0; b < 2; ++b) {
     auto& B = S->B[b];
@@ -687,6 +717,10 @@ int init_rate_state(wql_scn* S) {
         m[c] = face[(3 + c) * nf + f];
         l[c] = face[(6 + c) * nf + f];
         x[c] = xi[c * nf + f];
+      }
+      if (rw) {
+        W[b * nf + f] = 0.4367;
+        continue;
       }
       double Tn, Tm, Tl;
       prestress(S->fp, x, 0.0, l, m, n, Tn, Tm, Tl);
@@ -811,8 +845,13 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
     S->mms_kt = Pr.mms_nt * 3.141592653589793;
   }
   S->plastic = Pr.response == "plastic";
-  if (S->plastic && Pr.plastic_model != "scec")
-    return fail(WQL_E_INPUT, "only plastic_model='scec' is supported");
+  S->pl_flow = S->plastic && Pr.plastic_model != "scec";
+  // plastic_flow reads mu_beta_eta, which init_plastic_material sets only for
+  // problem 'rate-weakening' (src/plastic_material.f90:38-42); elsewhere the
+  // reference leaves it undefined
+  if (S->pl_flow && Pr.problem != "rate-weakening")
+    return fail(WQL_E_INPUT, "plastic_model '" + Pr.plastic_model +
+                                 "' (plastic_flow) needs problem 'rate-weakening', the only one that sets mu_beta_eta");
   if (Pr.plast.set) {
     S->pl_c = Pr.plast.cohesion;
     S->pl_nu = Pr.plast.friction;
@@ -834,7 +873,8 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   const bool sw_ok = fp.preset == PRE_TPV5 || fp.preset == PRE_TPV26 || fp.preset == PRE_TPV27 ||
                      fp.preset == PRE_TPV28 || fp.preset == PRE_TPV28_BENCH || fp.preset == PRE_TPV29 || fp.preset == PRE_TPV30 ||
                      fp.preset == PRE_TPV10 || fp.preset == PRE_SW_PARAM;
-  const bool rs_ok = fp.preset == PRE_TPV101 || fp.preset == PRE_TPV102 || fp.preset == PRE_RS_PARAM;
+  const bool rs_ok = fp.preset == PRE_TPV101 || fp.preset == PRE_TPV102 || fp.preset == PRE_RS_PARAM ||
+                     fp.preset == PRE_RATE_WEAKENING;
   if ((fp.coupling == CPL_SW && !sw_ok) || (fp.coupling == CPL_RS && !rs_ok))
     return fail(WQL_E_INPUT, "problem '" + Pr.problem + "' has no preset for coupling '" + cp + "'");
   const FrictionExt& fe = Pr.fric;
@@ -917,8 +957,19 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
     if ((rc = init_rate_state(S.get()))) return rc;
   S->st_cap = 64;
   if (Pr.w_fault) {
-    S->frame_cap = 64;
-    if ((rc = S->alloc((void**)&S->frame_dev, (size_t)S->frame_cap * kFrameWords * nf * sizeof(float)))) return rc;
+    S->frame_cap = frame_ring_cap(nf);
+    const size_t ring_bytes = (size_t)S->frame_cap * kFrameWords * nf * sizeof(float);
+    for (int k = 0; k < 2; ++k)
+      if ((rc = S->alloc((void**)&S->frame_ring[k], ring_bytes))) return rc;
+    S->frame_dev = S->frame_ring[0];
+    // pinned staging for the overlapped copies; without it every full ring
+    // is copied synchronously
+    if (cudaMallocHost((void**)&S->frame_pin, ring_bytes) != cudaSuccess ||
+        cudaEventCreateWithFlags(&S->pin_done, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      if (S->frame_pin) cudaFreeHost(S->frame_pin);
+      S->frame_pin = nullptr;
+    }
   }
   // time step: src/domain.f90:222-235, src/block.f90:437-452
   double dtmin = 1e300;
@@ -956,17 +1007,46 @@ int flush_stations(wql_scn* S) {
   return WQL_OK;
 }
 
+// Appends the frames of the pinned staging buffer to the host chunks, after
+// their copy has completed.
+int drain_pinned(wql_scn* S) {
+  if (S->pin_frames == 0) return WQL_OK;
+  CK(cudaEventSynchronize(S->pin_done));
+  const size_t words = (size_t)S->pin_frames * kFrameWords * S->B[0].nr * S->B[0].ns;
+  S->frame_chunks.emplace_back(S->frame_pin, S->frame_pin + words);
+  S->pin_frames = 0;
+  return WQL_OK;
+}
+
+// Every frame to the host (before a read or the output files).
 int flush_frames(wql_scn* S) {
   int rc = flush_stations(S);
   if (rc) return rc;
+  if ((rc = drain_pinned(S))) return rc;
   if (S->frame_fill == 0) return WQL_OK;
   const long long nf = (long long)S->B[0].nr * S->B[0].ns;
   const size_t words = (size_t)S->frame_fill * kFrameWords * nf;
-  const size_t old = S->frames_host.size();
-  S->frames_host.resize(old + words);
-  CK(cudaMemcpyAsync(S->frames_host.data() + old, S->frame_dev, words * sizeof(float),
-                     cudaMemcpyDeviceToHost, S->stream));
+  S->frame_chunks.emplace_back(words);
+  CK(cudaMemcpyAsync(S->frame_chunks.back().data(), S->frame_dev, words * sizeof(float), cudaMemcpyDeviceToHost,
+                     S->stream));
   CK(cudaStreamSynchronize(S->stream));
+  S->frame_fill = 0;
+  return WQL_OK;
+}
+
+// The ring being filled is full: queue its copy to the pinned buffer (once
+// the previous copy has been taken out of it) and switch rings.  Kernels
+// that write the other ring later are queued after its own copy.
+int rotate_frames(wql_scn* S) {
+  if (!S->frame_pin) return flush_frames(S);
+  int rc = drain_pinned(S);
+  if (rc) return rc;
+  const size_t words = (size_t)S->frame_fill * kFrameWords * S->B[0].nr * S->B[0].ns;
+  CK(cudaMemcpyAsync(S->frame_pin, S->frame_dev, words * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+  CK(cudaEventRecord(S->pin_done, S->stream));
+  S->pin_frames = S->frame_fill;
+  S->ring_cur ^= 1;
+  S->frame_dev = S->frame_ring[S->ring_cur];
   S->frame_fill = 0;
   return WQL_OK;
 }
@@ -1014,6 +1094,12 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.pl_ccos = S->pl_c * std::cos(std::atan(S->pl_nu));
   a.pl_sin = std::sin(std::atan(S->pl_nu));
   a.pl_decay = std::exp(-S->dt / S->pl_Tv);
+  a.pl_flow = S->pl_flow ? 1 : 0;
+  a.pl_mu = S->P.btp[b].mu_beta_eta[0];
+  a.pl_beta = S->P.btp[b].mu_beta_eta[1];
+  a.pl_eta = S->P.btp[b].mu_beta_eta[2];
+  a.pl_lambda = (T*)B.pl_lambda;
+  a.pl_gammap = (T*)B.pl_gammap;
   a.err = S->err_dev;
   a.anel = S->anel ? 1 : 0;
   a.eta = (T*)B.eta;
@@ -1183,7 +1269,7 @@ int step_end(wql_scn* S, StepCtx& c) {
   if (c.want_frame) {
     S->frame_fill += 1;
     S->nframes += 1;
-    if (S->frame_fill == S->frame_cap) return flush_frames(S);
+    if (S->frame_fill == S->frame_cap) return rotate_frames(S);
   }
   return WQL_OK;
 }
@@ -1550,18 +1636,22 @@ int wql_get_info(wql_scn* scn, wql_info* info) {
 }
 
 int wql_get_field(wql_scn* scn, int block, int comp, double* host_out) {
-  if (!scn || !host_out || block < 0 || block > 1 || comp < 0 || comp > 8)
+  if (!scn || !host_out || block < 0 || block > 1 || comp < 0 || comp > 10)
     return fail(WQL_E_INPUT, "bad argument");
   auto& B = scn->B[block];
+  if (comp > 8 && !scn->pl_flow)
+    return fail(WQL_E_STATE, "components 9 and 10 (plastic strain rate and strain) need plastic_flow");
+  const void* src = comp == 9 ? B.pl_lambda : (comp == 10 ? B.pl_gammap : B.F[scn->cur]);
+  const long long off = comp > 8 ? 0 : comp * B.np;
   CK(cudaStreamSynchronize(scn->stream));
   const long long rows = (long long)B.nr * B.ns;
   double* tmp = nullptr;
   CK(cudaMalloc(&tmp, B.npd * sizeof(double)));
   const unsigned grid = (unsigned)std::min<long long>((B.npd + 255) / 256, 4096);
   if (scn->prec == WQL_FP64)
-    pitched_to_dense<double><<<grid, 256, 0, scn->stream>>>((const double*)B.F[scn->cur] + comp * B.np, B.pq, B.nq, rows, tmp);
+    pitched_to_dense<double><<<grid, 256, 0, scn->stream>>>((const double*)src + off, B.pq, B.nq, rows, tmp);
   else
-    pitched_to_dense<float><<<grid, 256, 0, scn->stream>>>((const float*)B.F[scn->cur] + comp * B.np, B.pq, B.nq, rows, tmp);
+    pitched_to_dense<float><<<grid, 256, 0, scn->stream>>>((const float*)src + off, B.pq, B.nq, rows, tmp);
   cudaError_t e = cudaStreamSynchronize(scn->stream);
   if (e == cudaSuccess) e = cudaMemcpy(host_out, tmp, B.npd * sizeof(double), cudaMemcpyDeviceToHost);
   cudaFree(tmp);
@@ -1718,10 +1808,11 @@ int wql_get_frames(wql_scn* scn, int what, float* host_out) {
   if (rc) return rc;
   const long long nf = (long long)scn->B[0].nr * scn->B[0].ns;
   const int off = kFrameOff[what], nc = kFrameOff[what + 1] - kFrameOff[what];
-  for (int fr = 0; fr < scn->nframes; ++fr) {
-    const float* src = scn->frames_host.data() + (size_t)fr * kFrameWords * nf + (size_t)off * nf;
-    std::memcpy(host_out + (size_t)fr * nc * nf, src, (size_t)nc * nf * sizeof(float));
-  }
+  int fr = 0;
+  for (const auto& chunk : scn->frame_chunks)
+    for (size_t k = 0; k < chunk.size(); k += (size_t)kFrameWords * nf, ++fr)
+      std::memcpy(host_out + (size_t)fr * nc * nf, chunk.data() + k + (size_t)off * nf,
+                  (size_t)nc * nf * sizeof(float));
   return WQL_OK;
 }
 
@@ -2001,6 +2092,7 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
     for (int s2 = 0; s2 < 3; ++s2) any_pml = any_pml || bp.pml_lqrs[s2] || bp.pml_rqrs[s2];
     if (any_pml && bp.npml > 0 && precision == WQL_FP32C) res += al(9 * np * esz);
     if (P.response == "plastic") res += al(np * esz);
+    if (P.response == "plastic" && P.plastic_model != "scec") res += 2 * al(np * esz);
     if (P.response == "anelastic") {
       res += 2 * al(24 * np * esz) + al(np * esz) + al(npd * 8);
       if (precision == WQL_FP32C && !(any_pml && bp.npml > 0)) res += al(9 * np * esz);
@@ -2009,7 +2101,7 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
     transient = std::max(transient, al(3 * npd * 8) + al(9 * npd * 8) + al(npd * 8) + al(3 * npd * 8));
   }
   res += al(6 * nf * 8) + 2 * al(8 * nf * 8) + 3 * al(2 * nf * 8) + al(18 * nf * esz) + al(10 * nf * 8) + 2 * 512;
-  if (P.w_fault) res += al(64LL * kFrameWords * nf * 4);
+  if (P.w_fault) res += 2 * al((long long)frame_ring_cap(nf) * kFrameWords * nf * 4);
   *resident = res;
   *peak = res + transient;
   return WQL_OK;

@@ -310,7 +310,10 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 5 : 3) interface_kernel(
       tau_l_hat = (phi_2 - es * vv_l) - T0l;
       // aging law (src/Interface_Condition.f90:431-436); the FP32-field mode
       // multiplies by the reciprocals (FP64 division is slow on this part)
-      if (F64) {
+      if (a.fp.preset == PRE_RATE_WEAKENING) {
+        DW[f] = a.A * DW[f] + rs_rate_weakening_state_rate(psi, V, rs.a, rs.b, rs.V0, rs.f0, rs.L0,
+                                                            rs_weakening_velocity(x));
+      } else if (F64) {
         DW[f] = a.A * DW[f] + (rs.b * rs.V0 / rs.L0 * exp(-(psi - rs.f0) / rs.b) - V * rs.b / rs.L0);
       } else {
         DW[f] = a.A * DW[f] + (a.rs_bL * rs.V0 * exp((rs.f0 - psi) * a.rs_binv) - V * a.rs_bL);

@@ -91,6 +91,13 @@ struct VolumeArgs {
   const T* __restrict__ ycoord;  // depth coordinate for the initial stress
   double pl_c, pl_nu, pl_Tv, dt;
   double pl_ccos, pl_sin, pl_decay;  // c*cos(atan nu), sin(atan nu), exp(-dt/Tv)
+  // plastic_flow (plastic_model other than 'scec', src/plastic.f90:220-290):
+  // the block's internal friction mu, dilatancy beta and viscosity eta, and
+  // per point the plastic strain rate lambda and plastic strain gammap
+  int pl_flow;
+  double pl_mu, pl_beta, pl_eta;
+  T* pl_lambda;
+  T* pl_gammap;
   // anelastic response (src/RHS_Interior.f90:2390-2509): memory variables
   // eta and their rates Deta (24 x np each, component c*4 + i for stress
   // component 4+c and mechanism i), 1/Qs per point (1/Qp = 1/(2 Qs)), the

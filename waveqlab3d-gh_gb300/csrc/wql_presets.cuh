@@ -29,6 +29,10 @@ enum Preset : int {
   // TPV28 with the SCEC benchmark's szz = -60 MPa in place of the +60 of
   // src/initial_stress_condition.f90:80 (&gb300_list tpv28_prestress = 'benchmark')
   PRE_TPV28_BENCH = 12,
+  // problem = 'rate-weakening': rate and state with strong velocity
+  // weakening (src/Interface_Condition.f90:410-416, 438-443, 2387-2423,
+  // 2819-2843; src/initial_stress_condition.f90:184-193)
+  PRE_RATE_WEAKENING = 13,
 };
 
 enum Coupling : int { CPL_LOCKED = 0, CPL_LINEAR = 1, CPL_SW = 2, CPL_RS = 3 };
@@ -55,6 +59,18 @@ WQL_HD double smooth_boxcar(double x, double w, double wr) {
   const double ax = fabs(x);
   if (ax > w && ax < w + wr) return 0.5 * (1.0 + tanh(wr / (ax - w - wr) + wr / (ax - w)));
   return 0.0;
+}
+
+// The uniform tensor of problem 'rate-weakening' (src/initial_stress_condition.f90:
+// 184-193), with that routine's pi = 3.14159265359.
+WQL_HD void rate_weakening_stress(double s0[6]) {
+  const double psi = 50.0 / 180.0 * 3.14159265359;
+  s0[0] = -126.0;
+  s0[4] = 42.0;
+  s0[2] = (1.0 - 2.0 * s0[4] / (s0[0] * tan(2.0 * psi))) * s0[0];
+  s0[1] = 0.5 * (s0[0] + s0[2]);
+  s0[3] = 0.0;
+  s0[5] = 0.0;
 }
 
 // initial_stress_tensor (src/initial_stress_condition.f90:8-254): s0 =
@@ -93,6 +109,9 @@ WQL_HD bool initial_stress(int preset, const double x[3], double s0[6]) {
     case PRE_TPV10:
       s0[0] = -7.378 * x[1]; s0[1] = 0.0; s0[2] = -7.378 * x[1]; s0[3] = 0.0;
       s0[4] = -0.55 * s0[0]; s0[5] = 0.0;
+      return true;
+    case PRE_RATE_WEAKENING:
+      rate_weakening_stress(s0);
       return true;
     case PRE_SW_PARAM:
     case PRE_RS_PARAM:
@@ -140,6 +159,12 @@ WQL_HD bool initial_stress_y(int preset, R y, R s0[6]) {
       s0[0] = R(-7.378) * y; s0[1] = R(0.0); s0[2] = R(-7.378) * y; s0[3] = R(0.0);
       s0[4] = R(-0.55) * s0[0]; s0[5] = R(0.0);
       return true;
+    case PRE_RATE_WEAKENING: {  // uniform: the FP64 values rounded to R
+      double d[6];
+      rate_weakening_stress(d);
+      for (int c = 0; c < 6; ++c) s0[c] = R(d[c]);
+      return true;
+    }
     default:
       return false;
   }
@@ -187,6 +212,7 @@ WQL_HD void prestress_static(const FaultParams& fp, const double x[3], const dou
     case PRE_TPV30:
     case PRE_TPV101:
     case PRE_TPV102:
+    case PRE_RATE_WEAKENING:
       initial_stress(fp.preset, x, s0);
       tensor_traction(s0, n, m, l, Tn, Tm, Tl);
       return;
@@ -221,9 +247,19 @@ WQL_HD void prestress_static(const FaultParams& fp, const double x[3], const dou
   }
 }
 
-// Amplitude of the time-ramped nucleation traction at x (MPa).
-WQL_HD double nucleation_weight(const FaultParams& fp, const double x[3]) {
+// Amplitude of the time-ramped nucleation traction at x (MPa); Tn is the
+// static normal traction there.
+WQL_HD double nucleation_weight(const FaultParams& fp, const double x[3], double Tn) {
   switch (fp.preset) {
+    case PRE_RATE_WEAKENING: {
+      // a Gaussian pulse of twice tau_pulse = -0.2429 Tn
+      const double tau_pulse = -0.2429 * Tn;
+      const double r0 = 3.0 * 1.5 * 0.3;
+      const double y0 = 8.0, z0 = 0.0;
+      const double r = sqrt((x[1] - y0) * (x[1] - y0) + (x[2] + z0) * (x[2] + z0));
+      const double F = exp(-((r / r0) * (r / r0)) / 2.0);
+      return 2.0 * tau_pulse * F;
+    }
     case PRE_TPV101:
     case PRE_TPV102: {
       const double r = sqrt((x[1] - 7.5) * (x[1] - 7.5) + x[2] * x[2]);
@@ -251,6 +287,8 @@ WQL_HD double nucleation_ramp(const FaultParams& fp, double t) {
     case PRE_SW_PARAM:
     case PRE_RS_PARAM:
       return fp.nuc_rise > 0.0 ? smooth_ramp(t / fp.nuc_rise) : 1.0;
+    case PRE_RATE_WEAKENING:
+      return t > 0.0 ? 1.0 : 0.0;
     default:
       return 0.0;
   }
@@ -259,7 +297,7 @@ WQL_HD double nucleation_ramp(const FaultParams& fp, double t) {
 WQL_HD void prestress(const FaultParams& fp, const double x[3], double t, const double l[3],
                       const double m[3], const double n[3], double& Tn, double& Tm, double& Tl) {
   prestress_static(fp, x, l, m, n, Tn, Tm, Tl);
-  const double w = nucleation_weight(fp, x);
+  const double w = nucleation_weight(fp, x, Tn);
   if (w != 0.0) Tl = Tl + w * nucleation_ramp(fp, t);
 }
 
@@ -334,7 +372,28 @@ struct RSParams {
 // only the direct-effect parameter a varies along the fault
 WQL_HD double rs_direct_a(const FaultParams& fp, const double x[3]) {
   if (fp.preset == PRE_RS_PARAM) return fp.a;
+  if (fp.preset == PRE_RATE_WEAKENING)
+    return 0.016 + 0.016 * (1.0 - smooth_boxcar(x[1], 20.0, 2.5) * smooth_boxcar(x[2], 20.0, 2.5));
   return 0.008 + 0.008 * (1.0 - smooth_boxcar(x[1], 15.0, 3.0) * smooth_boxcar(x[2], 15.0, 3.0));
+}
+
+// Weakening velocity V_w(x) of problem 'rate-weakening' (src/Interface_Condition.f90:439-440).
+WQL_HD double rs_weakening_velocity(const double x[3]) {
+  return 0.17 + 5.0 * (1.0 - smooth_boxcar(x[1], 20.0, 2.5) * smooth_boxcar(x[2], 20.0, 2.5));
+}
+
+// Rate of the state variable psi at slip rate V: the aging law of TPV101/102
+// and rs_param (src/Interface_Condition.f90:431-436), or for
+// 'rate-weakening' the slip law with a steady state that weakens above V_w
+// (:438-443):
+//   Fss = 0.13 + (f0 - (b-a) ln(V/V0) - 0.13) / (1 + (V/V_w)^8)^(1/8),
+//   dpsi/dt = -V/L0 (a asinh(V/(2 V0) e^{psi/a}) - Fss).
+WQL_HD double rs_rate_weakening_state_rate(double psi, double V, double a, double b, double V0, double f0,
+                                           double L0, double Vw) {
+  double Fss = f0 - (b - a) * log(V / V0);
+  const double r = V / Vw, r2 = r * r, r4 = r2 * r2;  // (V/V_w)**8 by squaring, as an integer power
+  Fss = 0.13 + (Fss - 0.13) / pow(1.0 + r4 * r4, 0.125);
+  return -V / L0 * (a * asinh(V / (2.0 * V0) * exp(psi / a)) - Fss);
 }
 
 WQL_HD RSParams rs_params(const FaultParams& fp, const double x[3], double a) {
@@ -342,6 +401,8 @@ WQL_HD RSParams rs_params(const FaultParams& fp, const double x[3], double a) {
   RSParams r;
   if (fp.preset == PRE_RS_PARAM) {
     r.L0 = fp.L; r.f0 = fp.f0; r.b = fp.b; r.V0 = fp.V0;
+  } else if (fp.preset == PRE_RATE_WEAKENING) {
+    r.L0 = 2.0 * 0.2572; r.f0 = 0.7; r.b = 0.02; r.V0 = 1.0e-6;
   } else {
     r.L0 = 0.02; r.f0 = 0.6; r.b = 0.012; r.V0 = 1.0e-6;
   }

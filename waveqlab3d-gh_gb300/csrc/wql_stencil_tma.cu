@@ -664,14 +664,51 @@ __global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
   ring.drain(tb);
 }
 
-// Planes per s chunk: the tuned value, else about 16 in equal chunks
-// (measured on 2 x 201^3 blocks with 32 x 12 tiles: 14-24 planes within 1 %,
-// longer chunks leave a longer tail of the last wave, shorter ones pay the
-// per-chunk start -- the first six planes of the s window -- more often).
+// Planes per s chunk: the tuned value, else about 32 in equal chunks.
+// Measured with 32 x 12 tiles on 2 x 201^3 blocks (ms per launch, planes per
+// chunk): 0.905 (16), 0.903 (24), 0.892 (32), 0.903 (40), 0.950 (51), 0.941
+// (67); on 2 x 401x201x201 blocks 1.829, 1.781, 1.763, 1.801, 1.833, 1.943.
+// Shorter chunks pay the chunk start (the first six planes of the s window)
+// more often; longer ones leave fewer, longer CTAs for the last wave.
 int chunk_planes(const VolumeArgs<float>& a) {
   if (a.schunk > 0) return a.schunk;
-  const int nc = std::max(1, (a.ns + 8) / 16);
+  const int nc = std::max(1, (a.ns + 16) / 32);
   return (a.ns + nc - 1) / nc;
+}
+
+int sm_count() {
+  static int n[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 152;
+  if (!n[dev] && cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) n[dev] = 152;
+  return n[dev];
+}
+
+// Common chunk length for a launch over both blocks with `tiles[b]` (q, r)
+// tiles each: the length c in 16..32 planes whose estimated time, (waves of
+// one CTA per SM) x (planes of the longest chunk + 8 for the chunk start),
+// is least.  On grids with few tiles per plane the wave count dominates:
+// 2 x 76x101x151 blocks have 54 tiles, and 9 chunks of 17 planes make 486
+// CTAs, 3.2 waves of 152, where 5 chunks of 31 make 270, 1.8 waves.
+int chunk_planes2(const VolumeArgs<float>* const a[2], const int tiles[2]) {
+  if (a[0]->schunk > 0) return a[0]->schunk;
+  const int sms = sm_count();
+  int best = chunk_planes(*a[0]);
+  long long best_cost = -1;
+  for (int c = 16; c <= 32; ++c) {
+    long long ncta = 0;
+    int longest = 0;
+    for (int b = 0; b < 2; ++b) {
+      const int nc = std::max(1, (a[b]->ns + c - 1) / c);
+      const int len = (a[b]->ns + nc - 1) / nc;
+      ncta += (long long)tiles[b] * nc;
+      longest = std::max(longest, len);
+    }
+    const long long cost = (ncta + sms - 1) / sms * (longest + 8);
+    if (best_cost < 0 || cost < best_cost) best_cost = cost, best = c;
+  }
+  return best;
 }
 
 MapArgs stage_maps(const StencilMaps& sm) {
@@ -729,13 +766,20 @@ void launch_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, cudaS
   TwoBlocks P;
   const VolumeArgs<float>* a[2] = {&a0, &a1};
   int ntile[2];
+  int tiles[2];
   for (int b = 0; b < 2; ++b) {
     P.a[b] = *a[b];
     P.m[b] = stage_maps(*static_cast<const StencilMaps*>(a[b]->tma));
-    P.schunk[b] = chunk_planes(*a[b]);
     P.tq[b] = (a[b]->nq + TL::TQ - 1) / TL::TQ;
     P.tr[b] = (a[b]->nr + TL::TR - 1) / TL::TR;
-    ntile[b] = P.tq[b] * P.tr[b] * ((a[b]->ns + P.schunk[b] - 1) / P.schunk[b]);
+    tiles[b] = P.tq[b] * P.tr[b];
+  }
+  const int c = chunk_planes2(a, tiles);
+  for (int b = 0; b < 2; ++b) {
+    // equal chunks of at most c planes in each block
+    const int nc = std::max(1, (a[b]->ns + c - 1) / c);
+    P.schunk[b] = a[b]->schunk > 0 ? a[b]->schunk : (a[b]->ns + nc - 1) / nc;
+    ntile[b] = tiles[b] * ((a[b]->ns + P.schunk[b] - 1) / P.schunk[b]);
   }
   P.ntile0 = ntile[0];
   kern<<<ntile[0] + ntile[1], TL::NC + 32, smem, s>>>(P);

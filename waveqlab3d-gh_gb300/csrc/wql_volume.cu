@@ -1146,9 +1146,10 @@ __global__ void __launch_bounds__(256) source_kernel(const __grid_constant__ Vol
 
 // ---------------------------------------------------------------------------
 // Plastic return map after the last stage (update_fields_plastic,
-// src/plastic.f90:11-151, plastic_flow2 :153-217), on points outside the PML
-// slabs, applied to the updated stresses.
-template <typename T, bool KAHAN>
+// src/plastic.f90:11-151: plastic_flow2 :153-217 for plastic_model 'scec',
+// plastic_flow :220-290 otherwise), on points outside the PML slabs,
+// applied to the updated stresses.
+template <typename T, bool CURV, bool KAHAN>
 __global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ VolumeArgs<T> a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -1171,6 +1172,33 @@ __global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ Vo
                 (sa[2] - sa[0]) * (sa[2] - sa[0])) / T(6) +
                sa[3] * sa[3] + sa[4] * sa[4] + sa[5] * sa[5];
   const T tau = sqrt(J2);
+  if (a.pl_flow) {
+    // plastic_flow (src/plastic.f90:220-290): yield function Y = tau + mu*sigma;
+    // above it the closed-form solution of eta*lambda = Y(s) for the plastic
+    // strain rate, with shear modulus G and bulk modulus K of the point
+    const T mu = (T)a.pl_mu, beta = (T)a.pl_beta, eta = (T)a.pl_eta, dt = (T)a.dt;
+    const T Y = tau + mu * sigma;
+    if (Y <= T(0)) {
+      a.pl_lambda[p] = T(0);
+      return;
+    }
+    const T* coef = a.coef;
+    const T G = CURV ? coef[11 * np + p] : coef[1 * np + p];
+    const T K = (CURV ? coef[10 * np + p] : coef[0 * np + p]) + T(2.0 / 3.0) * G;
+    T sd[6];
+    for (int c = 0; c < 6; ++c) sd[c] = sa[c] - sigma * (c < 3 ? T(1) : T(0));
+    const T lambda = (tau + mu * sigma) / (eta + dt * (G + mu * beta * K));
+    a.pl_lambda[p] = lambda;
+    a.pl_gammap[p] = a.pl_gammap[p] + dt * lambda;
+    const T tau1 = tau - dt * lambda * G;
+    const T sigma1 = sigma - dt * lambda * beta * K;
+    for (int c = 0; c < 6; ++c) {
+      const T sdc = sd[c] * tau1 / (tau1 + dt * lambda * G);
+      a.Fout[(3 + c) * np + p] = (sigma1 * (c < 3 ? T(1) : T(0)) + sdc) - s0[c];
+      if (KAHAN) a.C[(3 + c) * np + p] = T(0);
+    }
+    return;
+  }
   // c cos(atan nu), sin(atan nu) and exp(-dt/Tv) are uniform: set on the host
   const T Ys = fmax(T(0), (T)a.pl_ccos - sigma * (T)a.pl_sin);
   if (!(tau - Ys > T(0))) return;
@@ -1299,7 +1327,7 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
     ++n;
   }
   if (a.plastic) {
-    plastic_kernel<T, KAHAN><<<grd, blk, 0, s>>>(a);
+    plastic_kernel<T, CURV, KAHAN><<<grd, blk, 0, s>>>(a);
     ++n;
   }
   return n;
