@@ -270,43 +270,92 @@ def cpu_sample(text, media, steps, warmup=0):
     return t1 - t0, os.cpu_count()
 
 
-def accuracy(wql, ctx, text, media, steps, stride=20):
+def perturbed_prestress(text, rel=2.0 ** -24):
+    """The workload with its background shear traction s0(5) (the &fault_list
+    extension of the parametric presets) scaled by (1 + rel), or None."""
+    import re
+    m = re.search(r"(s0 = [^,]+, [^,]+, [^,]+, [^,]+, )([-0-9.eEdD+]+)", text)
+    if not m:
+        return None
+    v = float(m.group(2).replace("d", "e").replace("D", "e")) * (1.0 + rel)
+    return text[:m.start(2)] + repr(v) + text[m.end(2):]
+
+
+def accuracy(wql, ctx, text, media, steps, stride=20, checkpoints=8, sensitivity=False):
     """FP32C against FP64 on the same workload after `steps` steps: relative
     L2 of the velocity fields and of the slip, relative error of the peak
     slip rate (over fault frames every `stride` steps) and the largest
     rupture-time difference in time steps over points that ruptured in both,
     with the number of points at each difference; for workloads with
-    stations, the relative L2 of the seismograms."""
+    stations, the relative L2 of the seismograms.  The two runs advance side
+    by side, and the velocity error is also recorded at `checkpoints` times
+    with the FP64 velocity norm there (a field that has left the domain
+    through the PML has a small norm, which inflates the relative error).
+    sensitivity: a third run, FP64 with the background shear traction
+    scaled by 1 + 2^-24 (one FP32 rounding), recorded against FP64 at the
+    same times: how far the workload itself carries a perturbation of FP32
+    size."""
     import numpy as np
     text_f = text.replace("w_fault = F", "w_fault = T").replace("w_stride = 1", f"w_stride = {stride}")
-    out = {}
-    runs = {}
-    for name, prec in (("fp64", wql.FP64), ("fp32c", wql.FP32C)):
-        s = wql.Scenario(ctx, text=text_f, precision=prec, media=media)
-        for _ in range(0, steps, 100):
-            s.step(min(100, steps - _))
-        s.sync(check_nan=True)
-        seis = [s.stations(b)[1] for b in range(2)] if "output_seismograms = T" in text_f else None
-        runs[name] = dict(seis=seis, v=[np.concatenate([s.field(b, c).ravel() for c in range(3)]) for b in range(2)],
-                          slip=s.iface(0, 3), trup=s.iface(0, 5),
-                          peak=float(np.sqrt((s.frames("Svel")[:, 1:3].astype(np.float64) ** 2).sum(axis=1)).max()),
-                          dt=s.info().dt)
-        s.close()
-    d, f = runs["fp64"], runs["fp32c"]
     rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
+    runs = {name: wql.Scenario(ctx, text=text_f, precision=prec, media=media)
+            for name, prec in (("fp64", wql.FP64), ("fp32c", wql.FP32C))}
+    text_p = perturbed_prestress(text_f) if sensitivity else None
+    if text_p:
+        runs["fp64_perturbed"] = wql.Scenario(ctx, text=text_p, precision=wql.FP64, media=media)
+    vel = lambda s: [np.concatenate([s.field(b, c).ravel() for c in range(3)]) for b in range(2)]  # noqa: E731
+    history = []
+    done = 0
+    every = max(1, -(-steps // checkpoints))
+    while done < steps:
+        n = min(every, steps - done)
+        for s in runs.values():
+            for k in range(0, n, 100):
+                s.step(min(100, n - k))
+        for s in runs.values():
+            s.sync(check_nan=True)
+        done += n
+        vd, vf = vel(runs["fp64"]), vel(runs["fp32c"])
+        h = {"step": done, "velocity_rel_l2": max(rel(vf[b], vd[b]) for b in range(2)),
+             "fp64_velocity_l2": float(np.sqrt(sum(np.linalg.norm(v) ** 2 for v in vd)))}
+        if "fp64_perturbed" in runs:
+            vp = vel(runs["fp64_perturbed"])
+            h["fp64_perturbed_velocity_rel_l2"] = max(rel(vp[b], vd[b]) for b in range(2))
+            h["fp64_perturbed_slip_rel_l2"] = rel(runs["fp64_perturbed"].iface(0, 3), runs["fp64"].iface(0, 3))
+        history.append(h)
+    out = {"steps": steps}
+    res = {}
+    if "fp64_perturbed" in runs:
+        tp = runs["fp64_perturbed"].iface(0, 5)
+        runs.pop("fp64_perturbed").close()
+    else:
+        tp = None
+    for name, s in runs.items():
+        seis = [s.stations(b)[1] for b in range(2)] if "output_seismograms = T" in text_f else None
+        res[name] = dict(seis=seis, v=vel(s), slip=s.iface(0, 3), trup=s.iface(0, 5),
+                         peak=float(np.sqrt((s.frames("Svel")[:, 1:3].astype(np.float64) ** 2).sum(axis=1)).max()),
+                         dt=s.info().dt)
+        s.close()
+    d, f = res["fp64"], res["fp32c"]
     rup_d, rup_f = d["trup"] < 1e8, f["trup"] < 1e8
     both = rup_d & rup_f
-    out["steps"] = steps
     out["velocity_rel_l2"] = max(rel(f["v"][b], d["v"][b]) for b in range(2))
-    out["slip_rel_l2"] = rel(f["slip"], d["slip"])
-    out["peak_slip_rate_rel"] = abs(f["peak"] - d["peak"]) / max(abs(d["peak"]), 1e-300)
-    out["peak_slip_rate_fp64"] = d["peak"]
+    out["velocity_history"] = history
     out["ruptured_points_fp64"] = int(rup_d.sum())
     out["ruptured_points_fp32c"] = int(rup_f.sum())
+    if rup_d.any():  # slip and slip rate only where the fault slipped
+        out["slip_rel_l2"] = rel(f["slip"], d["slip"])
+        out["peak_slip_rate_rel"] = abs(f["peak"] - d["peak"]) / max(abs(d["peak"]), 1e-300)
+        out["peak_slip_rate_fp64"] = d["peak"]
     out["rupture_time_err_dt"] = float(np.abs(f["trup"][both] - d["trup"][both]).max() / d["dt"]) if both.any() else None
     if both.any():
         k = np.rint(np.abs(f["trup"][both] - d["trup"][both]) / d["dt"]).astype(int)
         out["rupture_time_err_points"] = {str(v): int((k == v).sum()) for v in np.unique(k)}
+    if tp is not None:
+        bp = rup_d & (tp < 1e8)
+        if bp.any():
+            k = np.rint(np.abs(tp[bp] - d["trup"][bp]) / d["dt"]).astype(int)
+            out["fp64_perturbed_rupture_time_err_points"] = {str(v): int((k == v).sum()) for v in np.unique(k)}
     if d["seis"] is not None:
         out["seismogram_rel_l2"] = max(rel(f["seis"][b][..., 1:], d["seis"][b][..., 1:])
                                        for b in range(2) if d["seis"][b].size)
@@ -340,10 +389,14 @@ def batch_mode(wql, device, args):
     st = torch.cuda.ExternalStream(batch.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(device) as clk:
+        # a profiler started with --profile-from-start off sees the timed
+        # steps only (no-ops otherwise)
+        torch.cuda.profiler.start()
         e0.record(st)
         batch.step(args.steps)
         e1.record(st)
         torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     ms = e0.elapsed_time(e1)
     batched = points * 5 * args.steps / (ms * 1e-3)
     for s, *_ in members:
@@ -456,6 +509,8 @@ def main():
     ap.add_argument("--requests", type=int, default=32, help="serve mode: number of requests")
     ap.add_argument("--rate", type=float, default=4.0, help="serve mode: Poisson arrival rate (requests/s)")
     ap.add_argument("--serve-steps", type=int, default=100, help="serve mode: time steps per request")
+    ap.add_argument("--sensitivity", action="store_true",
+                    help="with --accuracy-steps: also FP64 with the shear prestress scaled by 1 + 2^-24")
     ap.add_argument("--accuracy-steps", type=int, default=0,
                     help="instead of timing, run FP32C and FP64 this many steps and report their differences")
     args = ap.parse_args()
@@ -513,7 +568,7 @@ def main():
         return
     if args.accuracy_steps > 0:
         ctx = wql.Context(local)
-        res = accuracy(wql, ctx, text, media, args.accuracy_steps)
+        res = accuracy(wql, ctx, text, media, args.accuracy_steps, sensitivity=args.sensitivity)
         if rank == 0:
             print(json.dumps({"workload": wl, "fp32c_vs_fp64": res}))
         return

@@ -187,7 +187,8 @@ int wql_station_index(wql_scn* scn, int block, int* ijk);
 int wql_get_seismograms(wql_scn* scn, int block, double* host_out);
 
 /* Autotuner: times the stencil-kernel candidates (WQL_FP32C: the TMA
- * kernel with s chunks of 12..48 planes or automatic;
+ * kernel with s chunks of 12..48 planes or automatic, and on Cartesian
+ * blocks that fill 40-wide tiles better both tile widths, variants 5 and 6;
  * WQL_FP64: tiled and per-point) on the scenario's own blocks, reps
  * launches each, into scratch arrays (the scenario's state is not
  * changed), applies the fastest with wql_set_tuning and returns it.
@@ -265,9 +266,10 @@ int wql_kernel_times(wql_scn* scn, int kind, double* ms, int* launches);
  * in WQL_FP32C, tiled 32x8 in WQL_FP64), 1 = per-point form (every
  * neighbour read through the caches), 2 = tiled shared-memory kernel with
  * 32x8 tiles, 3 = the same at three blocks per SM (FP32), 4 = 64x8 tiles
- * (WQL_FP32C only), 5 = TMA-pipelined kernel (32x12 tiles, two-deep stage
- * ring; WQL_FP32C only), 6 = accepted as 5; schunk = planes per thread
- * block along s (0 = automatic). */
+ * (WQL_FP32C only), 5 = TMA-pipelined kernel (two-deep stage ring;
+ * WQL_FP32C only; 32x12 tiles, or 40x12 on Cartesian blocks whose q extent
+ * fills 40-wide tiles better), 6 = the TMA kernel on 32x12 tiles always;
+ * schunk = planes per thread block along s (0 = automatic). */
 int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk);
 
 /* Number of kernel launches the last wql_step issued per time step (for

@@ -248,7 +248,7 @@ void defaults(Problem& P) {
   P.tpv28_prestress = "source";
   P.rs_tol = 1.0e-12;  // the reference's tolerance, src/Interface_Condition.f90:1188
   P.rs_maxit = 5000;   // src/Interface_Condition.f90:1194
-  P.fp32c_fault = "compensated";
+  P.fp32c_fault = "fp32";
   P.fric = wql::FrictionExt();
   P.fric.set = false;
   P.fric.fs = 0.677; P.fric.fd = 0.525; P.fric.Dc = 0.4;   // IC:1283-1299

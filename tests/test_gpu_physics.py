@@ -133,16 +133,20 @@ def test_plasticity_is_active(ctx, wqlmod, tmp_path):
     assert rel_l2(a.fields(0), b.fields(0)) > 1e-6
 
 
-@pytest.mark.parametrize("case", ["slip_weakening", "rate_state"])
-def test_fp32c_error_vs_fp64(ctx, wqlmod, tmp_path, case):
+@pytest.mark.parametrize("case,fault", [("slip_weakening", "fp32"), ("rate_state", "fp32"),
+                                        ("slip_weakening", "compensated"), ("rate_state", "compensated")])
+def test_fp32c_error_vs_fp64(ctx, wqlmod, tmp_path, case, fault):
     """FP32 + Kahan RK vs FP64 on the truth/1 problem (slip weakening) and on
     its rate-and-state variant (FP32C solves the friction law by Newton's
     method, FP64 by the reference's regula falsi): velocity fields, slip,
-    peak slip rate and rupture time (at most one time step)."""
+    peak slip rate and rupture time (at most one time step); with the fault
+    algebra in FP32 (the default) and on the compensated face values in
+    FP64."""
     if case == "slip_weakening":
         text, steps = golden_in("test_rup_cart_fric"), 46
     else:  # ruptures from about step 60
         text, steps = problem("TPV101", "rate-and-state_friction", t_final="3.0d0") + block_list(), 100
+    text += f"&gb300_list\n fp32c_fault = '{fault}' /\n"
     p = write(tmp_path, "cart.in", text)
     d = wqlmod.Scenario(ctx, p, precision=wqlmod.FP64)
     f = wqlmod.Scenario(ctx, p, precision=wqlmod.FP32C)

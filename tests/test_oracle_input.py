@@ -96,7 +96,7 @@ def _decks(tmp_path):
     decks = {"truth1": golden_in("test_rup_cart_fric"), "truth2": golden_in("test_rup_curv_fric"),
              "truth2_bench": with_groups(golden_in("test_rup_curv_fric"),
                                          "&gb300_list\n bc_penalty = 'weighted', tpv28_prestress = 'benchmark',\n"
-                                         " rs_tol = 1d-300, rs_maxit = 200000, fp32c_fault = 'fp32' /"),
+                                         " rs_tol = 1d-300, rs_maxit = 200000, fp32c_fault = 'compensated' /"),
              "curv_flat": set_key(golden_in("test_rup_cart_fric"), "type_of_mesh", "'curvilinear'")}
     for c in ("pml", "pml_curv", "plastic", "rs", "rs_curv", "locked", "linear_mt4", "an_up_pml", "an0_pml",
               "up5_pml", *MT_CASES):

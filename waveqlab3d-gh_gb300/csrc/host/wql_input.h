@@ -136,9 +136,12 @@ struct Problem {
   double rs_tol = 1.0e-12;
   int rs_maxit = 5000;
   // &gb300_list fp32c_fault: in the FP32-compensated mode the fault's
-  // characteristic algebra reads the compensated face values (F - C) and
-  // runs in FP64 ('compensated'), or works on the FP32 fields in FP32 ('fp32')
-  std::string fp32c_fault = "compensated";
+  // characteristic algebra works on the FP32 fields in FP32 ('fp32'), or
+  // reads the compensated face values (F - C) and runs in FP64
+  // ('compensated').  Measured on 2 x 201^3 curvilinear rate and state over
+  // 2000 steps: velocity error against FP64 2.27e-5 ('fp32') and 2.25e-5
+  // ('compensated'), for 0.07 against 0.22 ms per interface launch.
+  std::string fp32c_fault = "fp32";
   FrictionExt fric;
   PlasticExt plast;
   // raw groups for anything not mapped above

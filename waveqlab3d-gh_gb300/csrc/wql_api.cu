@@ -544,7 +544,8 @@ int setup_block(wql_scn* S, int b) {
   if ((rc = S->alloc(&B.DF, 9 * B.np * S->esz))) return rc;
   if (S->prec == WQL_FP32C) {
     if ((rc = S->alloc(&B.C, 9 * B.np * S->esz))) return rc;
-    const int erc = make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, S->curv, S->fd);
+    const int erc = make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, S->curv, S->fd,
+                                      tma_tile_width(S->P.btp[0].nqrs[0], S->P.btp[1].nqrs[0], S->curv));
     if (erc) return fail(WQL_E_CUDA, "cuTensorMapEncodeTiled failed for the stencil maps (error " + std::to_string(erc) + ")");
   }
   // boundary codes (src/BoundaryConditions.f90:15-48) and PML slabs (src/block.f90:163-178)
@@ -1219,8 +1220,8 @@ void stage_head(wql_scn* S, StepCtx& c, int stage) {
 
 void stage_block_pre(wql_scn* S, StepCtx& c, int stage, int b) {
   mark_begin(S, 2);
-  if (S->prec == WQL_FP64) c.launches += launch_pre<double>(volume_args<double>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->stream);
-  else c.launches += launch_pre<float>(volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->stream);
+  if (S->prec == WQL_FP64) c.launches += launch_pre<double>(volume_args<double>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->curv, S->stream);
+  else c.launches += launch_pre<float>(volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->curv, S->stream);
   mark_end(S);
 }
 
@@ -1963,12 +1964,17 @@ int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
       return WQL_OK;
     }
   }
-  // candidates: the TMA kernel with several s chunk sizes (FP32C), the
-  // tiled and per-point kernels (FP64)
+  // candidates: the TMA kernel with several s chunk sizes (FP32C; on
+  // Cartesian blocks that fill 40-wide tiles better, with both tile
+  // widths), the tiled and per-point kernels (FP64)
   std::vector<std::pair<int, int>> cand;
   if (scn->prec == WQL_FP32C) {
+    const bool wide = tma_tile_width(scn->B[0].nq, scn->B[1].nq, scn->curv) != kTmaTQ;
     for (int c : {0, 12, 14, 16, 24, 32, 48})
-      if (c <= scn->B[0].ns) cand.push_back({5, c});
+      if (c <= scn->B[0].ns) {
+        cand.push_back({5, c});
+        if (wide) cand.push_back({6, c});
+      }
   } else {
     for (int c : {8, 16, 32}) cand.push_back({2, c});
     cand.push_back({1, 0});
@@ -2011,7 +2017,8 @@ int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
             StencilMaps m = scn->B[b].maps;
             void* Fs[2] = {scn->B[b].F[0], scn->B[b].F[1]};
             if (make_stencil_maps(m, Fs, scn->B[b].coef, scratch[b][0], scratch[b][1], scn->B[b].nq, scn->B[b].nr,
-                                  scn->B[b].ns, scn->B[b].pq, scn->curv, scn->fd)) {
+                                  scn->B[b].ns, scn->B[b].pq, scn->curv, scn->fd,
+                                  c.first == 6 ? kTmaTQ : tma_tile_width(scn->B[0].nq, scn->B[1].nq, scn->curv))) {
               rc = fail(WQL_E_CUDA, "autotune tensor maps");
               return;
             }
@@ -2132,6 +2139,16 @@ int wql_batch_add(wql_batch* b, wql_scn* scn) {
   for (auto* m : b->members)
     if (m == scn) return fail(WQL_E_STATE, "scenario is already in the batch");
   if (scn->next_stage != 1) return fail(WQL_E_STATE, "the scenario is in the middle of a step (wql_stage)");
+  // the packed launch runs 32-wide tiles: a member set up with the wide
+  // Cartesian tiles gets 32-wide tensor maps
+  if (scn->prec == WQL_FP32C)
+    for (int k = 0; k < 2; ++k) {
+      auto& B = scn->B[k];
+      if (B.maps.tq == kTmaTQ) continue;
+      const int erc =
+          make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, scn->curv, scn->fd, kTmaTQ);
+      if (erc) return fail(WQL_E_CUDA, "cuTensorMapEncodeTiled failed for the stencil maps (error " + std::to_string(erc) + ")");
+    }
   b->members.push_back(scn);
   return WQL_OK;
 }
@@ -2208,6 +2225,19 @@ int wql_set_tuning(wql_scn* scn, int kernel_variant, int schunk) {
   // 64x8 tiles of FP64 need 273 KiB of shared memory, more than a block may hold.
   if (kernel_variant == 4 && scn->prec == WQL_FP64)
     return fail(WQL_E_INPUT, "stencil variant 4 (64x8 tiles) is FP32-only");
+  // variant 6 runs the TMA kernel on 32-wide tiles; the others keep (or
+  // restore) the width chosen for the blocks at set-up
+  if (scn->prec == WQL_FP32C) {
+    CK(cudaStreamSynchronize(scn->stream));  // no launch in flight reads the old maps
+    const int want = kernel_variant == 6 ? kTmaTQ : tma_tile_width(scn->B[0].nq, scn->B[1].nq, scn->curv);
+    for (int k = 0; k < 2; ++k) {
+      auto& B = scn->B[k];
+      if (B.maps.tq == want) continue;
+      const int erc =
+          make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, scn->curv, scn->fd, want);
+      if (erc) return fail(WQL_E_CUDA, "cuTensorMapEncodeTiled failed for the stencil maps (error " + std::to_string(erc) + ")");
+    }
+  }
   scn->kernel_variant = kernel_variant;
   scn->schunk = schunk;
   return WQL_OK;

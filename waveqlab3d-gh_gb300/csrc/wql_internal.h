@@ -180,6 +180,10 @@ constexpr int kFrameOff[9] = {FR_UFACE, FR_VFACE, FR_S, FR_UHAT, FR_VHAT, FR_SVE
 // stages fill one SM's shared memory (measured faster than 32 x 8 tiles with
 // three stages, 32 x 10 and 64 x 6 on 2 x 201^3 blocks).
 constexpr int kTmaTQ = 32, kTmaTR = 12, kTmaStages = 2;
+// Cartesian blocks whose q extent fills 40-wide tiles better (76 points: 2
+// tiles of 40 use 95 % of their columns, 3 of 32 use 79 %) take this width;
+// 15 consumer warps, the same 128-register cap.
+constexpr int kTmaTQWide = 40;
 struct StencilMaps {
   CUtensorMap fbox[2], flead[2];  // per field buffer
   CUtensorMap ca, cb, cc, cl;     // coefficients: q-halo rows, r-halo columns, tile, lead plane
@@ -187,13 +191,17 @@ struct StencilMaps {
   CUtensorMap flead2[2];          // upwind pair: the stress lead tile (else = flead)
   int cur;                        // which field buffer is the stage input
   int fd;                         // operator the boxes are shaped for (0 central, 1 upwind)
+  int tq;                         // tile width along q the boxes are shaped for
   int ok;
 };
 // Fills m for a block (fd: 0 the central SBP-6 operator, 1 the upwind pair:
 // r halo of 4 rows, velocity and stress lead tiles from different planes);
 // returns 0 or a CUDA driver error code.
 int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
-                      bool curv, int fd);
+                      bool curv, int fd, int tq);
+// Tile width along q (kTmaTQ or kTmaTQWide) for a scenario whose blocks have
+// nq0 and nq1 points along q.
+int tma_tile_width(int nq0, int nq1, bool curv);
 // Launches the TMA stencil kernel (every plane of the block).
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream);
 // The same for both blocks of a scenario in one launch.
@@ -233,7 +241,7 @@ void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream);
 // boundary and fault penalties folded into DF of the face points.  Returns
 // the number of launches.
 template <typename T>
-int launch_pre(const VolumeArgs<T>& a, void* stream);
+int launch_pre(const VolumeArgs<T>& a, bool curv, void* stream);
 template <typename T>
 int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream);
 // One moment-tensor source: DF(4:9) -= am * delta on a box of points

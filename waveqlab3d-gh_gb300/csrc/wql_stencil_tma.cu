@@ -51,14 +51,15 @@
 namespace wql {
 namespace {
 
-template <bool CURV, bool KAHAN, int FD>
+template <bool CURV, bool KAHAN, int FD, int TQ_ = kTmaTQ>
 struct TmaTile {
-  static constexpr int TQ = kTmaTQ, TR = kTmaTR, NC = TQ * TR;
+  static constexpr int TQ = TQ_, TR = kTmaTR, NC = TQ * TR;
   // r halo: 3 rows for the central operator, 4 for the upwind pair
   static constexpr int HR = FD ? 4 : 3;
   static constexpr int BQ = TQ + 16, BR = TR + 2 * HR;  // field box: q from q0-8, r from r0-HR
   static constexpr int NCC = CURV ? 7 : 3;         // tile coefficients: 6..12 or lambda, mu, 1/rho
-  static constexpr int F_W = 9 * BR * BQ;
+  static constexpr int F_BOX = 9 * BR * BQ;          // words the field box copy delivers
+  static constexpr int F_W = (F_BOX + 31) / 32 * 32;  // its slot, padded to 128 bytes
   static constexpr int CA_W = CURV ? 3 * TR * BQ : 0;
   static constexpr int CB_W = CURV ? 3 * BR * TQ : 0;
   static constexpr int CC_W = NCC * NC;
@@ -75,7 +76,7 @@ struct TmaTile {
   static constexpr int OFF_DF = OFF_LC + LC_W;
   static constexpr int OFF_CK = OFF_DF + DF_W;
   static constexpr int STAGE_W = OFF_CK + CK_W;
-  static constexpr unsigned MAIN_BYTES = 4u * (F_W + CA_W + CB_W + CC_W + DF_W + CK_W);
+  static constexpr unsigned MAIN_BYTES = 4u * (F_BOX + CA_W + CB_W + CC_W + DF_W + CK_W);
   static constexpr unsigned LEAD_BYTES = 4u * (LF_W + LC_W);
   // every sub-buffer starts on a 128-byte boundary
   static_assert(F_W % 32 == 0 && CA_W % 32 == 0 && CB_W % 32 == 0 && CC_W % 32 == 0 && LF_W % 32 == 0 &&
@@ -179,10 +180,10 @@ struct MapArgs {
 // the CTA has used before this tile (the same count in every thread), so a
 // persistent CTA keeps its mbarriers and the producer runs ahead into the
 // next tile.  Returns false after a wait ran out (the error word is set).
-template <bool CURV, bool KAHAN, int NS, int FD>
+template <bool CURV, bool KAHAN, int NS, int FD, int TQW = kTmaTQ>
 __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapArgs& m, int schunk, int bx, int by,
                                          int bz, int& tb) {
-  using TL = TmaTile<CURV, KAHAN, FD>;
+  using TL = TmaTile<CURV, KAHAN, FD, TQW>;
   constexpr int TQ = TL::TQ, TR = TL::TR, NC = TL::NC, BQ = TL::BQ, BR = TL::BR, HR = TL::HR;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   // 128-byte aligned start, derived from the shared array itself so the
@@ -246,8 +247,9 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
   // PML points (every point with the anelastic response) hand their
   // velocity gradient to the correction kernels (a.G)
   const int npml = a.npml;
-  const bool pml_qr = a.G != nullptr && ((a.pml[0] && q < npml) || (a.pml[1] && q >= nq - npml) ||
-                                         (a.pml[2] && r < npml) || (a.pml[3] && r >= nr - npml));
+  const bool slab_qr = npml > 0 && ((a.pml[0] && q < npml) || (a.pml[1] && q >= nq - npml) ||
+                                    (a.pml[2] && r < npml) || (a.pml[3] && r >= nr - npml));
+  const bool pml_qr = a.G != nullptr && slab_qr;
   const long long np = a.np;
   const long long sts = (long long)a.pq * nr;
   const long long col = q + (long long)a.pq * r;
@@ -492,7 +494,7 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
           }
         }
       }
-      if (a.G != nullptr && (a.anel || pml_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))) {
+      if (a.G != nullptr && (a.anel || pml_qr || (npml > 0 && ((a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))))) {
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -516,12 +518,15 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       // the face pre-kernel has folded the boundary and fault penalties
       // into DF of the face points: DF - tot/A, or -tot on the first stage
       // (A = 0, where DF holds nothing else)
+      // and the PML pre-kernel the damping terms into DF of the slab points
+      // (corr/A, or corr itself on the first stage)
       const bool face = q == 0 || q == nq - 1 || r == 0 || r == nr - 1 || s == 0 || s == ns - 1;
+      const bool slab = slab_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml);
 #pragma unroll
       for (int c = 0; c < 9; ++c) {
         const float f0 = fb(c, lr, lq);
         const float dfs = S[TL::OFF_DF + c * NC + ty * TQ + tx];
-        const float df = a.A != 0.0f ? a.A * dfs + du[c] : (face ? dfs : 0.0f) + du[c];
+        const float df = a.A != 0.0f ? a.A * dfs + du[c] : ((face || slab) ? dfs : 0.0f) + du[c];
         a.DF[c * np + p] = df;
         if (KAHAN) {
           const float y = a.Bdt * df - S[TL::OFF_CK + c * NC + ty * TQ + tx];
@@ -551,12 +556,12 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
 }
 
 // Shared-memory ring of a persistent CTA: NS stages then the mbarriers.
-template <bool CURV, bool KAHAN, int NS, int FD>
+template <bool CURV, bool KAHAN, int NS, int FD, int TQW = kTmaTQ>
 struct Ring {
   float* sm;
   uint64_t *full, *empty, *fluxbar;
   __device__ Ring() {
-    using TL = TmaTile<CURV, KAHAN, FD>;
+    using TL = TmaTile<CURV, KAHAN, FD, TQW>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     sm = reinterpret_cast<float*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
     full = reinterpret_cast<uint64_t*>(sm + NS * TL::STAGE_W);
@@ -565,7 +570,7 @@ struct Ring {
   }
   // one thread initialises the barriers once per CTA
   __device__ void init() {
-    using TL = TmaTile<CURV, KAHAN, FD>;
+    using TL = TmaTile<CURV, KAHAN, FD, TQW>;
     if (threadIdx.x == 0) {
       for (int i = 0; i < NS; ++i) {
         mbar_init(&full[i], 1);
@@ -579,7 +584,7 @@ struct Ring {
   // the producer's copies of the last stages land before the CTA leaves
   // (tb = stages issued)
   __device__ void drain(int tb) {
-    if (threadIdx.x == TmaTile<CURV, KAHAN, FD>::NC)
+    if (threadIdx.x == TmaTile<CURV, KAHAN, FD, TQW>::NC)
       for (int T = max(0, tb - NS); T < tb; ++T) mbar_wait(&full[T % NS], (T / NS) & 1);
   }
 };
@@ -587,15 +592,15 @@ struct Ring {
 // Each CTA takes tiles w = blockIdx.x, blockIdx.x + gridDim.x, ... of the
 // tq x tr x nchunk tiles of the block (q fastest, so neighbouring CTAs share
 // halos in L2); with one CTA per tile that is one tile each.
-template <bool CURV, bool KAHAN, int NS, int FD>
-__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
+template <bool CURV, bool KAHAN, int NS, int FD, int TQW>
+__global__ void __launch_bounds__(TQW * kTmaTR + 32, 1)
     stencil_kernel_tma(const __grid_constant__ VolumeArgs<float> a, const __grid_constant__ MapArgs m, int schunk,
                        int tq, int tr, int ntile) {
-  Ring<CURV, KAHAN, NS, FD> ring;
+  Ring<CURV, KAHAN, NS, FD, TQW> ring;
   ring.init();
   int tb = 0;
   for (int w = blockIdx.x; w < ntile; w += gridDim.x)
-    if (!tma_body<CURV, KAHAN, NS, FD>(a, m, schunk, w % tq, (w / tq) % tr, w / (tq * tr), tb)) break;
+    if (!tma_body<CURV, KAHAN, NS, FD, TQW>(a, m, schunk, w % tq, (w / tq) % tr, w / (tq * tr), tb)) break;
   ring.drain(tb);
 }
 
@@ -646,34 +651,28 @@ struct TwoBlocks {
   int ntile0;
 };
 
-template <bool CURV, bool KAHAN, int NS, int FD>
-__global__ void __launch_bounds__(kTmaTQ * kTmaTR + 32, 1)
+template <bool CURV, bool KAHAN, int NS, int FD, int TQW>
+__global__ void __launch_bounds__(TQW * kTmaTR + 32, 1)
     stencil_kernel_tma2(const __grid_constant__ TwoBlocks P) {
-  Ring<CURV, KAHAN, NS, FD> ring;
+  Ring<CURV, KAHAN, NS, FD, TQW> ring;
   ring.init();
   int tb = 0;
   const int w = blockIdx.x;
   if (w < P.ntile0) {
-    tma_body<CURV, KAHAN, NS, FD>(P.a[0], P.m[0], P.schunk[0], w % P.tq[0], (w / P.tq[0]) % P.tr[0],
+    tma_body<CURV, KAHAN, NS, FD, TQW>(P.a[0], P.m[0], P.schunk[0], w % P.tq[0], (w / P.tq[0]) % P.tr[0],
                               w / (P.tq[0] * P.tr[0]), tb);
   } else {
     const int l = w - P.ntile0;
-    tma_body<CURV, KAHAN, NS, FD>(P.a[1], P.m[1], P.schunk[1], l % P.tq[1], (l / P.tq[1]) % P.tr[1],
+    tma_body<CURV, KAHAN, NS, FD, TQW>(P.a[1], P.m[1], P.schunk[1], l % P.tq[1], (l / P.tq[1]) % P.tr[1],
                               l / (P.tq[1] * P.tr[1]), tb);
   }
   ring.drain(tb);
 }
 
-// Planes per s chunk: the tuned value, else about 32 in equal chunks.
-// Measured with 32 x 12 tiles on 2 x 201^3 blocks (ms per launch, planes per
-// chunk): 0.905 (16), 0.903 (24), 0.892 (32), 0.903 (40), 0.950 (51), 0.941
-// (67); on 2 x 401x201x201 blocks 1.829, 1.781, 1.763, 1.801, 1.833, 1.943.
-// Shorter chunks pay the chunk start (the first six planes of the s window)
-// more often; longer ones leave fewer, longer CTAs for the last wave.
+// Planes per s chunk of a single-block launch: the tuned value, else 32.
 int chunk_planes(const VolumeArgs<float>& a) {
   if (a.schunk > 0) return a.schunk;
-  const int nc = std::max(1, (a.ns + 16) / 32);
-  return (a.ns + nc - 1) / nc;
+  return 32;
 }
 
 int sm_count() {
@@ -685,30 +684,24 @@ int sm_count() {
   return n[dev];
 }
 
-// Common chunk length for a launch over both blocks with `tiles[b]` (q, r)
-// tiles each: the length c in 16..32 planes whose estimated time, (waves of
-// one CTA per SM) x (planes of the longest chunk + 8 for the chunk start),
-// is least.  On grids with few tiles per plane the wave count dominates:
-// 2 x 76x101x151 blocks have 54 tiles, and 9 chunks of 17 planes make 486
-// CTAs, 3.2 waves of 152, where 5 chunks of 31 make 270, 1.8 waves.
+// Chunk length for a launch over both blocks with `tiles[b]` (q, r) tiles
+// each: 32 planes while that gives at least 8 waves of one CTA per SM, else
+// shorter chunks (down to 12 planes) for more CTAs.  Measured per launch
+// (planes per chunk: ms): 2 x 201^3 curvilinear, 1666 CTAs at 32 planes,
+// 16: 0.904, 24: 0.902, 32: 0.891; 2 x 401x201x201, 3094 CTAs at 32,
+// 16: 1.829, 24: 1.782, 32: 1.765; 2 x 76x101x151 Cartesian upwind, 270 CTAs
+// at 32, 12: 0.173, 16: 0.176, 24: 0.197, 32: 0.194.  Equal-length chunks
+// (29 planes on 201) measured slower than 32 with a short last chunk.
 int chunk_planes2(const VolumeArgs<float>* const a[2], const int tiles[2]) {
   if (a[0]->schunk > 0) return a[0]->schunk;
-  const int sms = sm_count();
-  int best = chunk_planes(*a[0]);
-  long long best_cost = -1;
-  for (int c = 16; c <= 32; ++c) {
+  const long long want = 8LL * sm_count();
+  int c = 32;
+  for (; c > 12; c -= 4) {
     long long ncta = 0;
-    int longest = 0;
-    for (int b = 0; b < 2; ++b) {
-      const int nc = std::max(1, (a[b]->ns + c - 1) / c);
-      const int len = (a[b]->ns + nc - 1) / nc;
-      ncta += (long long)tiles[b] * nc;
-      longest = std::max(longest, len);
-    }
-    const long long cost = (ncta + sms - 1) / sms * (longest + 8);
-    if (best_cost < 0 || cost < best_cost) best_cost = cost, best = c;
+    for (int b = 0; b < 2; ++b) ncta += (long long)tiles[b] * ((a[b]->ns + c - 1) / c);
+    if (ncta >= want) break;
   }
-  return best;
+  return c;
 }
 
 MapArgs stage_maps(const StencilMaps& sm) {
@@ -725,15 +718,18 @@ MapArgs stage_maps(const StencilMaps& sm) {
   return m;
 }
 
-template <bool CURV, bool KAHAN, int FD>
+template <bool CURV, bool KAHAN, int FD, int TQW = kTmaTQ>
 constexpr size_t tma_smem_bytes(int NS) {
-  return sizeof(float) * (size_t)NS * TmaTile<CURV, KAHAN, FD>::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
+  return sizeof(float) * (size_t)NS * TmaTile<CURV, KAHAN, FD, TQW>::STAGE_W + (2 * NS + 1) * sizeof(uint64_t) + 128;
 }
 static_assert(tma_smem_bytes<true, true, 0>(kTmaStages) <= 227 * 1024 &&
                   tma_smem_bytes<false, true, 0>(kTmaStages) <= 227 * 1024 &&
                   tma_smem_bytes<true, true, 1>(kTmaStages) <= 227 * 1024 &&
                   tma_smem_bytes<false, true, 1>(kTmaStages) <= 227 * 1024,
               "the stage ring must fit in the shared memory of one CTA");
+static_assert(tma_smem_bytes<false, true, 0, kTmaTQWide>(kTmaStages) <= 227 * 1024 &&
+                  tma_smem_bytes<false, true, 1, kTmaTQWide>(kTmaStages) <= 227 * 1024,
+              "the wide Cartesian stage ring must fit in the shared memory of one CTA");
 
 template <typename K>
 size_t prepare(K kern, int NS, int stage_words) {
@@ -747,10 +743,10 @@ size_t prepare(K kern, int NS, int stage_words) {
 // tiles statically interleaved that measured slower on 2 x 201^3 blocks
 // (0.54 ms against 0.50 ms per launch): the chunks holding the s closure
 // rows take longer, and the hardware's dynamic CTA scheduling balances them.
-template <bool CURV, bool KAHAN, int NS, int FD>
+template <bool CURV, bool KAHAN, int NS, int FD, int TQW = kTmaTQ>
 void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t s) {
-  using TL = TmaTile<CURV, KAHAN, FD>;
-  auto kern = stencil_kernel_tma<CURV, KAHAN, NS, FD>;
+  using TL = TmaTile<CURV, KAHAN, FD, TQW>;
+  auto kern = stencil_kernel_tma<CURV, KAHAN, NS, FD, TQW>;
   static const size_t smem = prepare(kern, NS, TL::STAGE_W);
   const int tq = (a.nq + TL::TQ - 1) / TL::TQ, tr = (a.nr + TL::TR - 1) / TL::TR;
   const int schunk = chunk_planes(a);
@@ -758,10 +754,10 @@ void launch_tma(const VolumeArgs<float>& a, const StencilMaps& sm, cudaStream_t 
   kern<<<ntile, TL::NC + 32, smem, s>>>(a, stage_maps(sm), schunk, tq, tr, ntile);
 }
 
-template <bool CURV, bool KAHAN, int NS, int FD>
+template <bool CURV, bool KAHAN, int NS, int FD, int TQW = kTmaTQ>
 void launch_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, cudaStream_t s) {
-  using TL = TmaTile<CURV, KAHAN, FD>;
-  auto kern = stencil_kernel_tma2<CURV, KAHAN, NS, FD>;
+  using TL = TmaTile<CURV, KAHAN, FD, TQW>;
+  auto kern = stencil_kernel_tma2<CURV, KAHAN, NS, FD, TQW>;
   static const size_t smem = prepare(kern, NS, TL::STAGE_W);
   TwoBlocks P;
   const VolumeArgs<float>* a[2] = {&a0, &a1};
@@ -776,9 +772,7 @@ void launch_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, cudaS
   }
   const int c = chunk_planes2(a, tiles);
   for (int b = 0; b < 2; ++b) {
-    // equal chunks of at most c planes in each block
-    const int nc = std::max(1, (a[b]->ns + c - 1) / c);
-    P.schunk[b] = a[b]->schunk > 0 ? a[b]->schunk : (a[b]->ns + nc - 1) / nc;
+    P.schunk[b] = a[b]->schunk > 0 ? a[b]->schunk : c;
     ntile[b] = tiles[b] * ((a[b]->ns + P.schunk[b] - 1) / P.schunk[b]);
   }
   P.ntile0 = ntile[0];
@@ -829,13 +823,14 @@ int encode4(CUtensorMap* map, void* base, int nq, int nr, int ns, int ncomp, int
 }  // namespace
 
 int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, void* C, int nq, int nr, int ns, int pq,
-                      bool curv, int fd) {
-  constexpr int TQ = kTmaTQ, TR = kTmaTR;
+                      bool curv, int fd, int tq) {
+  const int TQ = (tq == kTmaTQWide && !curv) ? kTmaTQWide : kTmaTQ, TR = kTmaTR;
   const int hr = fd ? 4 : 3;  // r halo rows
   int rc = 0;
   m.ok = 0;
   m.cur = 0;
   m.fd = fd;
+  m.tq = TQ;
   for (int i = 0; i < 2 && !rc; ++i) {
     rc = encode4(&m.fbox[i], F[i], nq, nr, ns, 9, pq, TQ + 16, TR + 2 * hr, 9);
     // lead tiles: all 9 components of one plane, or (upwind) the 3
@@ -874,10 +869,17 @@ long long fill_tma_desc(const VolumeArgs<float>& a, TmaBatchDesc& d) {
 }
 
 bool tma_eligible(const VolumeArgs<float>& a) {
-  // the packed launch runs the central operator; tile_span keeps every r
-  // closure row inside tile + halo unless the shifted last tile starts at 4
-  // or 5
-  return a.tma != nullptr && a.fd == 0 && (a.nr <= kTmaTR + 3 || a.nr >= kTmaTR + 6);
+  // the packed launch runs the central operator on 32-wide tiles; tile_span
+  // keeps every r closure row inside tile + halo unless the shifted last
+  // tile starts at 4 or 5
+  return a.tma != nullptr && a.fd == 0 && static_cast<const StencilMaps*>(a.tma)->tq == kTmaTQ &&
+         (a.nr <= kTmaTR + 3 || a.nr >= kTmaTR + 6);
+}
+
+int tma_tile_width(int nq0, int nq1, bool curv) {
+  if (curv) return kTmaTQ;
+  auto used = [&](int T) { return (double)(nq0 + nq1) / (double)(((nq0 + T - 1) / T + (nq1 + T - 1) / T) * T); };
+  return used(kTmaTQWide) > used(kTmaTQ) + 0.02 ? kTmaTQWide : kTmaTQ;
 }
 
 void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bool curv, bool kahan, void* stream) {
@@ -894,6 +896,11 @@ void launch_stencil_tma_batch(const TmaBatchDesc* d, int nd, long long total, bo
 void launch_stencil_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a1, bool curv, bool kahan,
                          void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  if (!curv && kahan && static_cast<const StencilMaps*>(a0.tma)->tq == kTmaTQWide) {
+    if (a0.fd) launch_tma2<false, true, kTmaStages, 1, kTmaTQWide>(a0, a1, s);
+    else launch_tma2<false, true, kTmaStages, 0, kTmaTQWide>(a0, a1, s);
+    return;
+  }
   if (a0.fd) {
     if (curv) launch_tma2<true, true, kTmaStages, 1>(a0, a1, s);
     else launch_tma2<false, true, kTmaStages, 1>(a0, a1, s);
@@ -906,6 +913,11 @@ void launch_stencil_tma2(const VolumeArgs<float>& a0, const VolumeArgs<float>& a
 void launch_stencil_tma(const VolumeArgs<float>& a, bool curv, bool kahan, void* stream) {
   const StencilMaps& sm = *static_cast<const StencilMaps*>(a.tma);
   cudaStream_t s = (cudaStream_t)stream;
+  if (!curv && kahan && sm.tq == kTmaTQWide) {
+    if (a.fd) launch_tma<false, true, kTmaStages, 1, kTmaTQWide>(a, sm, s);
+    else launch_tma<false, true, kTmaStages, 0, kTmaTQWide>(a, sm, s);
+    return;
+  }
   if (a.fd) {
     if (curv) launch_tma<true, true, kTmaStages, 1>(a, sm, s);
     else launch_tma<false, true, kTmaStages, 1>(a, sm, s);
