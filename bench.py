@@ -29,10 +29,12 @@ UNIT = "grid-point RK-stage updates/s"
 RUN_STEPS = {"config1": 2000, "config2": 3000, "config3_member": 1500, "config4_request": 100,
              "upwind": 2000, "upwind_anelastic": 2000}
 # Algorithmic bytes per grid-point RK stage of the fused volume kernel:
-# F read 9 + F write 9 + DF read 9 + DF write 9 (+ Kahan compensation read 9 +
-# write 9 in FP32C) + coefficients (J*metric 9, 1/J, lambda, mu, 1/(rho J)).
-BYTES_PER_UPDATE = {("curv", "fp32c"): (54 + 13) * 4, ("curv", "fp64"): (36 + 13) * 8,
-                    ("cart", "fp32c"): (54 + 3) * 4, ("cart", "fp64"): (36 + 3) * 8}
+# F read 9 + F write 9 + DF read 9 + DF write 9 words of the field type, in
+# FP32C plus the Kahan compensation read 9 + write 9 as bfloat16 (9 FP32
+# words), + coefficients (J*metric 9, 1/J, lambda, mu, 1/(rho J); Cartesian
+# lambda, mu, 1/rho).
+BYTES_PER_UPDATE = {("curv", "fp32c"): (45 + 13) * 4, ("curv", "fp64"): (36 + 13) * 8,
+                    ("cart", "fp32c"): (45 + 3) * 4, ("cart", "fp64"): (36 + 3) * 8}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -427,7 +429,7 @@ def batch_mode(wql, device, args):
     fp64 = fp64_pts / fp64_s
     return {"mode": "batch", "metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "dtype": "f32 fields, Kahan-compensated RK update, f64 fault solve",
+            "higher_is_better": True, "dtype": "f32 fields, Kahan-compensated RK update (bf16 compensation term), f64 fault solve",
             "data": "synthetic (seeded)",
             "config": {"workload": f"config3: {args.members} slip-weakening scenarios, blocks of 64^3..160^3 "
                                    f"points, planar/rough faults, homogeneous/von Karman media, 10-point PML, "
@@ -473,7 +475,7 @@ def serve_mode(wql, device, args):
     span = max(done) - arrivals[0]
     upd = sum(2 * (n // 2 + 1) * n * n for n in sizes) * 5 * args.serve_steps
     return {"mode": "serve", "metric": METRIC, "value": len(ids) / span, "unit": "solves/s", "n_gpus": 1,
-            "higher_is_better": True, "dtype": "f32 fields, Kahan-compensated RK update, f64 sources",
+            "higher_is_better": True, "dtype": "f32 fields, Kahan-compensated RK update (bf16 compensation term), f64 sources",
             "data": "synthetic (seeded)",
             "config": {"workload": f"config4: {args.requests} point-source requests, n^3 grids n in 96..256, "
                                    f"von Karman media, 32 stations, {args.serve_steps} steps each",
@@ -633,7 +635,7 @@ def main():
         "metric": METRIC, "value": out["fp32c"]["value"], "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["fp32c"]["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 fields, Kahan-compensated RK update, f64 fault solve",
+        "dtype": "f32 fields, Kahan-compensated RK update (bf16 compensation term), f64 fault solve",
         "data": {"config1": "synthetic (seeded topography, fault roughness)",
                  "config2": "synthetic (seeded von Karman medium)",
                  "upwind": "synthetic (uniform medium, one point source)",

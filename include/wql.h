@@ -125,7 +125,7 @@ int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in);
  * so a monitoring thread reading a scenario would stall other threads'
  * streams; a memory-capped host may have no room left).  FP32 fields are
  * widened one s plane at a time through a fixed 8 MiB device array; a block
- * whose pitched plane (pq*nr, pq = nq rounded up to a multiple of 4)
+ * whose pitched plane (pq*nr, pq = nq rounded up to a multiple of 8)
  * exceeds 1048576 points returns WQL_E_INPUT.  The first call on a device
  * resolves the array's address and must not happen during stream capture.
  * The array is shared by all calls on a device: calls that overlap in time

@@ -117,7 +117,7 @@ struct wql_scn {
   long long device_bytes = 0;
   struct Block {
     int nq = 0, nr = 0, ns = 0;
-    int pq = 0;         // row pitch along q: nq rounded up to a multiple of 16 bytes
+    int pq = 0;         // row pitch along q: nq rounded up to 8 (FP32) or 2 (FP64) points
     long long npd = 0;  // nq * nr * ns (dense, the precompute arrays)
     long long np = 0;
     void* F[2] = {nullptr, nullptr};
@@ -444,8 +444,10 @@ int setup_block(wql_scn* S, int b) {
   B.nr = G.nr;
   B.ns = G.ns;
   // resident arrays (fields, rates, coefficients) use a row pitch of a
-  // multiple of 16 bytes so that every row starts on a TMA-legal address
-  const int per16 = 16 / S->esz;
+  // multiple of 16 bytes so that every row starts on a TMA-legal address;
+  // FP32 rows round to 8 points (32 bytes) so that the bfloat16
+  // compensation rows (2 bytes a point) are 16-byte multiples too
+  const int per16 = S->esz == 4 ? 8 : 2;
   B.pq = (G.nq + per16 - 1) / per16 * per16;
   B.npd = (long long)G.nq * G.nr * G.ns;
   B.np = (long long)B.pq * G.nr * G.ns;
@@ -543,7 +545,7 @@ int setup_block(wql_scn* S, int b) {
     if ((rc = S->alloc(&B.F[i], 9 * B.np * S->esz))) return rc;
   if ((rc = S->alloc(&B.DF, 9 * B.np * S->esz))) return rc;
   if (S->prec == WQL_FP32C) {
-    if ((rc = S->alloc(&B.C, 9 * B.np * S->esz))) return rc;
+    if ((rc = S->alloc(&B.C, 9 * B.np * sizeof(comp_t)))) return rc;
     const int erc = make_stencil_maps(B.maps, B.F, B.coef, B.DF, B.C, B.nq, B.nr, B.ns, B.pq, S->curv, S->fd,
                                       tma_tile_width(S->P.btp[0].nqrs[0], S->P.btp[1].nqrs[0], S->curv));
     if (erc) return fail(WQL_E_CUDA, "cuTensorMapEncodeTiled failed for the stencil maps (error " + std::to_string(erc) + ")");
@@ -1062,7 +1064,7 @@ VolumeArgs<T> volume_args(wql_scn* S, int b, double A, double Bdt, bool last) {
   a.Fin = (const T*)B.F[S->cur];
   a.Fout = (T*)B.F[S->cur ^ 1];
   a.DF = (T*)B.DF;
-  a.C = (T*)B.C;
+  a.C = (comp_t*)B.C;
   a.coef = (const T*)B.coef;
   for (int d = 0; d < 3; ++d) {
     a.cart_metric[d] = (T)B.cart_metric[d];
@@ -1220,8 +1222,8 @@ void stage_head(wql_scn* S, StepCtx& c, int stage) {
 
 void stage_block_pre(wql_scn* S, StepCtx& c, int stage, int b) {
   mark_begin(S, 2);
-  if (S->prec == WQL_FP64) c.launches += launch_pre<double>(volume_args<double>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->curv, S->stream);
-  else c.launches += launch_pre<float>(volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->curv, S->stream);
+  if (S->prec == WQL_FP64) c.launches += launch_pre<double>(volume_args<double>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->stream);
+  else c.launches += launch_pre<float>(volume_args<float>(S, b, stage_A(S, stage), stage_Bdt(S, stage), stage == 5), S->stream);
   mark_end(S);
 }
 
@@ -1754,7 +1756,9 @@ int wql_set_field(wql_scn* scn, int block, int comp, const double* host_in) {
       dense_to_pitched<double><<<grid, 256, 0, scn->stream>>>(tmp, B.pq, B.nq, rows, (double*)B.F[scn->cur] + comp * B.np);
     else
       dense_to_pitched<float><<<grid, 256, 0, scn->stream>>>(tmp, B.pq, B.nq, rows, (float*)B.F[scn->cur] + comp * B.np);
-    e = cudaStreamSynchronize(scn->stream);
+    // the new values carry no rounding error yet: clear their compensation
+    if (B.C) e = cudaMemsetAsync((comp_t*)B.C + comp * B.np, 0, B.np * sizeof(comp_t), scn->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(scn->stream);
   }
   cudaFree(tmp);
   if (e != cudaSuccess) return fail(WQL_E_CUDA, cudaGetErrorString(e));
@@ -2009,7 +2013,7 @@ int wql_autotune(wql_scn* scn, int reps, int* variant, int* schunk) {
         } else {
           VolumeArgs<float> a = volume_args<float>(scn, b, 0.5, 1e-4, false);
           a.DF = (float*)scratch[b][0];
-          a.C = (float*)scratch[b][1];
+          a.C = (comp_t*)scratch[b][1];
           a.Fout = (float*)scratch[b][2];
           if (c.first == 5 || c.first == 6) {
             // the TMA kernel reads DF and C through the block's tensor maps:
@@ -2083,11 +2087,11 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
   for (int b = 0; b < 2; ++b) {
     const BlockParams& bp = P.btp[b];
     const long long nq = bp.nqrs[0], nr = bp.nqrs[1], ns = bp.nqrs[2];
-    const long long per16 = 16 / esz, pq = (nq + per16 - 1) / per16 * per16;
+    const long long per16 = esz == 4 ? 8 : 2, pq = (nq + per16 - 1) / per16 * per16;
     const long long npd = nq * nr * ns, np = pq * nr * ns;
     const bool curv = P.type_of_mesh == "curvilinear";
     res += 2 * al(9 * np * esz) + al(9 * np * esz) + al((curv ? kCurvCoef : kCartCoef) * np * esz);
-    if (precision == WQL_FP32C) res += al(9 * np * esz);
+    if (precision == WQL_FP32C) res += al(9 * np * (long long)sizeof(comp_t));
     const long long nfs[3] = {nr * ns, nq * ns, nq * nr};
     for (int s2 = 0; s2 < 6; ++s2) res += al(kFaceWords * nfs[s2 / 2] * 8);
     const int dims[3] = {(int)nq, (int)nr, (int)ns};

@@ -136,9 +136,9 @@ __device__ bool newton_mixed(double& V, double Phi, double eta, double sn, doubl
 template <typename T, typename R>
 __device__ __forceinline__ void load_face(const void* F, const void* C, long long np, long long p, R out[9]) {
   const T* f = (const T*)F;
-  const T* k = (const T*)C;
+  const comp_t* k = (const comp_t*)C;
 #pragma unroll
-  for (int c = 0; c < 9; ++c) out[c] = k ? (R)f[c * np + p] - (R)k[c * np + p] : (R)f[c * np + p];
+  for (int c = 0; c < 9; ++c) out[c] = k ? (R)f[c * np + p] - (R)comp_get(k, c * np + p) : (R)f[c * np + p];
 }
 
 // T is the field type, R the arithmetic type of the characteristic algebra.

@@ -235,16 +235,16 @@ __device__ __forceinline__ void add_correction(const VolumeArgs<T>& a, long long
   // for the previous component's stores
   T* __restrict__ DF = a.DF;
   T* __restrict__ Fo = a.Fout;
-  T* __restrict__ Ck = a.C;
+  comp_t* __restrict__ Ck = a.C;
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
     if (corr[c] == T(0)) continue;
     DF[c * np + p] += corr[c];
     const T f0 = Fo[c * np + p];
     if (KAHAN) {
-      const T y = a.Bdt * corr[c] - Ck[c * np + p];
+      const T y = a.Bdt * corr[c] - (T)comp_get(Ck, c * np + p);
       const T t = f0 + y;
-      Ck[c * np + p] = (t - f0) - y;
+      comp_put(Ck, c * np + p, (float)((t - f0) - y));
       Fo[c * np + p] = t;
     } else {
       Fo[c * np + p] = f0 + a.Bdt * corr[c];

@@ -66,7 +66,10 @@ struct TmaTile {
   static constexpr int LF_W = 9 * NC;  // lead fields (FD 1: velocities of s+4, then stresses of s+2)
   static constexpr int LC_W = CURV ? 3 * NC : 0;
   static constexpr int DF_W = 9 * NC;            // rates of the main plane
-  static constexpr int CK_W = KAHAN ? 9 * NC : 0;  // compensation of the main plane
+  // compensation of the main plane: 9 x NC bfloat16 in a slot of whole
+  // 128-byte lines
+  static constexpr int CK_BOX = KAHAN ? 9 * NC * 2 : 0;  // bytes the copy delivers
+  static constexpr int CK_W = (CK_BOX / 4 + 31) / 32 * 32;
   static constexpr int OFF_F = 0;
   static constexpr int OFF_CA = OFF_F + F_W;
   static constexpr int OFF_CB = OFF_CA + CA_W;
@@ -76,7 +79,7 @@ struct TmaTile {
   static constexpr int OFF_DF = OFF_LC + LC_W;
   static constexpr int OFF_CK = OFF_DF + DF_W;
   static constexpr int STAGE_W = OFF_CK + CK_W;
-  static constexpr unsigned MAIN_BYTES = 4u * (F_BOX + CA_W + CB_W + CC_W + DF_W + CK_W);
+  static constexpr unsigned MAIN_BYTES = 4u * (F_BOX + CA_W + CB_W + CC_W + DF_W) + CK_BOX;
   static constexpr unsigned LEAD_BYTES = 4u * (LF_W + LC_W);
   // every sub-buffer starts on a 128-byte boundary
   static_assert(F_W % 32 == 0 && CA_W % 32 == 0 && CB_W % 32 == 0 && CC_W % 32 == 0 && LF_W % 32 == 0 &&
@@ -247,9 +250,8 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
   // PML points (every point with the anelastic response) hand their
   // velocity gradient to the correction kernels (a.G)
   const int npml = a.npml;
-  const bool slab_qr = npml > 0 && ((a.pml[0] && q < npml) || (a.pml[1] && q >= nq - npml) ||
-                                    (a.pml[2] && r < npml) || (a.pml[3] && r >= nr - npml));
-  const bool pml_qr = a.G != nullptr && slab_qr;
+  const bool pml_qr = a.G != nullptr && ((a.pml[0] && q < npml) || (a.pml[1] && q >= nq - npml) ||
+                                         (a.pml[2] && r < npml) || (a.pml[3] && r >= nr - npml));
   const long long np = a.np;
   const long long sts = (long long)a.pq * nr;
   const long long col = q + (long long)a.pq * r;
@@ -494,7 +496,7 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
           }
         }
       }
-      if (a.G != nullptr && (a.anel || pml_qr || (npml > 0 && ((a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))))) {
+      if (a.G != nullptr && (a.anel || pml_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml))) {
 #pragma unroll
         for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -518,20 +520,18 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
       // the face pre-kernel has folded the boundary and fault penalties
       // into DF of the face points: DF - tot/A, or -tot on the first stage
       // (A = 0, where DF holds nothing else)
-      // and the PML pre-kernel the damping terms into DF of the slab points
-      // (corr/A, or corr itself on the first stage)
       const bool face = q == 0 || q == nq - 1 || r == 0 || r == nr - 1 || s == 0 || s == ns - 1;
-      const bool slab = slab_qr || (a.pml[4] && s < npml) || (a.pml[5] && s >= ns - npml);
 #pragma unroll
       for (int c = 0; c < 9; ++c) {
         const float f0 = fb(c, lr, lq);
         const float dfs = S[TL::OFF_DF + c * NC + ty * TQ + tx];
-        const float df = a.A != 0.0f ? a.A * dfs + du[c] : ((face || slab) ? dfs : 0.0f) + du[c];
+        const float df = a.A != 0.0f ? a.A * dfs + du[c] : (face ? dfs : 0.0f) + du[c];
         a.DF[c * np + p] = df;
         if (KAHAN) {
-          const float y = a.Bdt * df - S[TL::OFF_CK + c * NC + ty * TQ + tx];
+          const comp_t* CKs = reinterpret_cast<const comp_t*>(S + TL::OFF_CK);
+          const float y = a.Bdt * df - comp_get(CKs, c * NC + ty * TQ + tx);
           const float tt = f0 + y;
-          a.C[c * np + p] = (tt - f0) - y;
+          comp_put(a.C, c * np + p, (tt - f0) - y);
           a.Fout[c * np + p] = tt;
         } else {
           a.Fout[c * np + p] = f0 + a.Bdt * df;
@@ -805,16 +805,20 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 4-D map over (q, r, s, component) of an FP32 array with row pitch pq.
-int encode4(CUtensorMap* map, void* base, int nq, int nr, int ns, int ncomp, int pq, int bq, int br, int bc) {
+// 4-D map over (q, r, s, component) of an FP32 array (bf16: of a bfloat16
+// array) with row pitch pq.
+int encode4(CUtensorMap* map, void* base, int nq, int nr, int ns, int ncomp, int pq, int bq, int br, int bc,
+            bool bf16 = false) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return 1;
   const long long np = (long long)pq * nr * ns;
+  const cuuint64_t es = bf16 ? 2 : 4;
   cuuint64_t dims[4] = {(cuuint64_t)nq, (cuuint64_t)nr, (cuuint64_t)ns, (cuuint64_t)ncomp};
-  cuuint64_t strides[3] = {(cuuint64_t)pq * 4, (cuuint64_t)pq * nr * 4, (cuuint64_t)np * 4};
+  cuuint64_t strides[3] = {(cuuint64_t)pq * es, (cuuint64_t)pq * nr * es, (cuuint64_t)np * es};
   cuuint32_t box[4] = {(cuuint32_t)bq, (cuuint32_t)br, 1, (cuuint32_t)bc};
   cuuint32_t estr[4] = {1, 1, 1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr,
+  CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims,
+                  strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return (int)r;
@@ -840,7 +844,8 @@ int make_stencil_maps(StencilMaps& m, void* const F[2], void* coef, void* DF, vo
     if (!fd) m.flead2[i] = m.flead[i];
   }
   if (!rc) rc = encode4(&m.df, DF, nq, nr, ns, 9, pq, TQ, TR, 9);
-  if (!rc) rc = encode4(&m.ck, C ? C : DF, nq, nr, ns, 9, pq, TQ, TR, 9);
+  // the compensation is bfloat16 (without one the map is never read)
+  if (!rc) rc = encode4(&m.ck, C ? C : DF, nq, nr, ns, 9, pq, TQ, TR, 9, true);
   if (curv) {
     if (!rc) rc = encode4(&m.ca, coef, nq, nr, ns, kCurvCoef, pq, TQ + 16, TR, 3);
     if (!rc) rc = encode4(&m.cb, coef, nq, nr, ns, kCurvCoef, pq, TQ, TR + 2 * hr, 3);

@@ -579,9 +579,9 @@ __global__ void __launch_bounds__(TQ * TR, MINB) stencil_kernel_tiled(const __gr
       const T df = a.A * a.DF[c * np + p] + du[c];
       a.DF[c * np + p] = df;
       if (KAHAN) {
-        const T y = a.Bdt * df - a.C[c * np + p];
+        const T y = a.Bdt * df - (T)comp_get(a.C, c * np + p);
         const T t = f0 + y;
-        a.C[c * np + p] = (t - f0) - y;
+        comp_put(a.C, c * np + p, (float)((t - f0) - y));
         a.Fout[c * np + p] = t;
       } else {
         a.Fout[c * np + p] = f0 + a.Bdt * df;
@@ -653,9 +653,9 @@ __global__ void __launch_bounds__(256) stencil_kernel_pointwise(const __grid_con
     const T df = a.A * a.DF[c * np + p] + du[c];
     a.DF[c * np + p] = df;
     if (KAHAN) {
-      const T y = a.Bdt * df - a.C[c * np + p];
+      const T y = a.Bdt * df - (T)comp_get(a.C, c * np + p);
       const T t = f0 + y;
-      a.C[c * np + p] = (t - f0) - y;
+      comp_put(a.C, c * np + p, (float)((t - f0) - y));
       a.Fout[c * np + p] = t;
     } else {
       a.Fout[c * np + p] = f0 + a.Bdt * df;
@@ -704,116 +704,10 @@ PmlBoxes pml_boxes(const VolumeArgs<T>& a) {
   return B;
 }
 
-// Point t of the slab union (boxes enumerated in turn, q fastest), or
-// false past its end or outside every active slab.
-__device__ __forceinline__ bool pml_point(const PmlBoxes& bx, int npml, const int pml[6], int nq, int nr, int ns,
-                                          long long t, int& i, int& j, int& k) {
-  int b = 0;
-  while (b < bx.n && t >= bx.start[b + 1]) ++b;
-  if (b >= bx.n) return false;
-  const long long l = t - bx.start[b];
-  i = bx.lo[b][0] + (int)(l % bx.dim[b][0]);
-  j = bx.lo[b][1] + (int)((l / bx.dim[b][0]) % bx.dim[b][1]);
-  k = bx.lo[b][2] + (int)(l / ((long long)bx.dim[b][0] * bx.dim[b][1]));
-  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
-  bool any = false;
-#pragma unroll
-  for (int side = 0; side < 6; ++side) {
-    const int ax = side >> 1;
-    if (pml[side] && ((side & 1) ? idx[ax] >= nn[ax] - npml : idx[ax] < npml)) any = true;
-  }
-  return any;
-}
-
-// Slab `side` at point (i, j, k): whether the point lies in it, and if so its
-// index in the slab arrays and the damping profile there, in grid-index
-// units (src/RHS_Interior.f90:1855, 1973, 2092), in the field precision.
-template <typename T>
-__device__ __forceinline__ bool pml_slab(const VolumeArgs<T>& a, int side, int i, int j, int k, long long& sp,
-                                         T& damp) {
-  if (!a.pml[side]) return false;
-  const int axis = side >> 1, npml = a.npml;
-  const bool hi = side & 1;
-  const int idx[3] = {i, j, k}, nn[3] = {a.nq, a.nr, a.ns};
-  const int ii = idx[axis], n = nn[axis];
-  if (!(hi ? (ii >= n - npml) : (ii < npml))) return false;
-  const int off = hi ? ii + 1 - (n - npml) : (axis == 2 ? ii + 1 - npml : ii - npml);
-  damp = (T)a.pml_d0 * (fabs((T)off / (T)npml));
-  const int sl = hi ? ii - (n - npml) : ii;
-  if (axis == 0) sp = sl + (long long)npml * (j + (long long)a.nr * k);
-  else if (axis == 1) sp = i + (long long)a.nq * (sl + (long long)npml * k);
-  else sp = i + (long long)a.nq * (j + (long long)a.nr * sl);
-  return true;
-}
-
-// The damping terms of the field rates at a slab point (pml_damping_and_q,
-// src/RHS_Interior.f90:1857-1888 and the two other axes), summed over the
-// point's slabs in the reference's order: s-low, s-high, r-low, r-high,
-// q-low, q-high.
-template <typename T, bool CURV>
-__device__ __forceinline__ void pml_damping(const VolumeArgs<T>& a, int i, int j, int k, long long p, T corr[9]) {
-  const long long np = a.np;
-  const T* __restrict__ coef = a.coef;
-  const T Jinv = CURV ? coef[9 * np + p] : T(1);
-  const T lam = CURV ? coef[10 * np + p] : coef[0 * np + p];
-  const T mu = CURV ? coef[11 * np + p] : coef[1 * np + p];
-  const T rinv = CURV ? coef[12 * np + p] : coef[2 * np + p];
-  const T rhoinv = CURV ? rinv / Jinv : rinv;
-  const T l2m = lam + T(2) * mu;
-#pragma unroll
-  for (int c = 0; c < 9; ++c) corr[c] = T(0);
-#pragma unroll
-  for (int oi = 0; oi < 6; ++oi) {
-    const int side = oi < 2 ? 4 + oi : (oi < 4 ? oi : oi - 4);
-    long long sp;
-    T damp;
-    if (!pml_slab(a, side, i, j, k, sp, damp)) continue;
-    const long long snp = a.slab_np[side];
-    const T* __restrict__ Q = a.Q[side];
-    T qv[9];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) qv[c] = Q[c * snp + sp];
-    corr[0] -= damp * qv[0] * rhoinv;
-    corr[1] -= damp * qv[1] * rhoinv;
-    corr[2] -= damp * qv[2] * rhoinv;
-    corr[3] -= damp * (l2m * qv[3] + lam * qv[4] + lam * qv[5]);
-    corr[4] -= damp * (lam * qv[3] + l2m * qv[4] + lam * qv[5]);
-    corr[5] -= damp * (lam * qv[3] + lam * qv[4] + l2m * qv[5]);
-    corr[6] -= mu * damp * qv[6];
-    corr[7] -= mu * damp * qv[7];
-    corr[8] -= mu * damp * qv[8];
-  }
-}
-
-// Before the TMA stencil: the damping terms of every slab point folded into
-// its rates, DF <- DF + corr/A, or DF <- corr on a stage with A = 0, so that
-// the stencil's A*DF + du (DF + du on slab points when A = 0) carries them
-// into DF and, with the compensated update, into F_out.  The PML kernel
-// after the stencil then advances only Q.  Runs before the face pre-kernel,
-// which on an A = 0 stage subtracts its penalty from a slab point's DF
-// instead of overwriting it.
-template <typename T, bool CURV>
-__global__ void __launch_bounds__(256) pml_pre_kernel(const __grid_constant__ VolumeArgs<T> a,
-                                                      const __grid_constant__ PmlBoxes bx) {
-  int i, j, k;
-  if (!pml_point(bx, a.npml, a.pml, a.nq, a.nr, a.ns, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
-    return;
-  const long long np = a.np;
-  const long long p = i + (long long)a.pq * (j + (long long)a.nr * k);
-  T corr[9];
-  pml_damping<T, CURV>(a, i, j, k, p, corr);
-#pragma unroll
-  for (int c = 0; c < 9; ++c) {
-    T* df = a.DF + c * np + p;
-    *df = a.A != T(0) ? *df + corr[c] / a.A : corr[c];
-  }
-}
-
 // FP32 fields: capped at 80 registers for three CTAs per SM (24 warps to
 // hide the latency of its dependent loads; measured 0.39 -> 0.31 ms per
-// correction launch on config 2 despite some spilling).  FOLDED: the damping
-// terms went into DF before the stencil (pml_pre_kernel); only Q advances.
-template <typename T, bool CURV, bool KAHAN, int FD, bool FOLDED = false>
+// correction launch on config 2 despite some spilling).
+template <typename T, bool CURV, bool KAHAN, int FD>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const __grid_constant__ VolumeArgs<T> a,
                                                                            const __grid_constant__ PmlBoxes bx) {
   // one thread per point of the slab union, enumerated box by box (q
@@ -925,17 +819,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
       else diff6_op<T, false, FD == 3 ? 0 : FD>(F, coef, np, p, idx[axis], nn[axis], st[axis], axis, o);
       for (int c = 0; c < 3; ++c) sd[c] = a.cart_metric[axis] * a.rh[axis] * o[3 + c];
     }
-    if (!FOLDED) {
-      corr[0] -= damp * qv[0] * rhoinv;
-      corr[1] -= damp * qv[1] * rhoinv;
-      corr[2] -= damp * qv[2] * rhoinv;
-      corr[3] -= damp * (l2m * qv[3] + lam * qv[4] + lam * qv[5]);
-      corr[4] -= damp * (lam * qv[3] + l2m * qv[4] + lam * qv[5]);
-      corr[5] -= damp * (lam * qv[3] + lam * qv[4] + l2m * qv[5]);
-      corr[6] -= mu * damp * qv[6];
-      corr[7] -= mu * damp * qv[7];
-      corr[8] -= mu * damp * qv[8];
-    }
+    corr[0] -= damp * qv[0] * rhoinv;
+    corr[1] -= damp * qv[1] * rhoinv;
+    corr[2] -= damp * qv[2] * rhoinv;
+    corr[3] -= damp * (l2m * qv[3] + lam * qv[4] + lam * qv[5]);
+    corr[4] -= damp * (lam * qv[3] + l2m * qv[4] + lam * qv[5]);
+    corr[5] -= damp * (lam * qv[3] + lam * qv[4] + l2m * qv[5]);
+    corr[6] -= mu * damp * qv[6];
+    corr[7] -= mu * damp * qv[7];
+    corr[8] -= mu * damp * qv[8];
     T src[9];
     for (int c = 0; c < 9; ++c) src[c] = T(0);
     src[0] = sd[0];
@@ -962,7 +854,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) pml_kernel(const 
       Q[c * snp + sp] = qv[c] + a.Bdt * dq[c];
     }
   }
-  if (!FOLDED) add_correction<T, KAHAN>(a, p, corr);
+  add_correction<T, KAHAN>(a, p, corr);
 }
 
 // ---------------------------------------------------------------------------
@@ -1216,16 +1108,10 @@ __global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ V
   for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
   mms_deviation(a, p, u);
   if (!face_penalty(a, i, j, k, u, tot)) return;
-  // a slab point's DF already holds its PML damping (pml_pre_kernel)
-  bool slab = false;
-  for (int side = 0; side < 6; ++side) {
-    const int ax = side >> 1;
-    if (a.pml[side] && a.npml > 0 && ((side & 1) ? idx[ax] >= nn[ax] - a.npml : idx[ax] < a.npml)) slab = true;
-  }
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
     T* df = a.DF + c * np + p;
-    *df = a.A != T(0) ? *df - tot[c] / a.A : (slab ? *df - tot[c] : -tot[c]);
+    *df = a.A != T(0) ? *df - tot[c] / a.A : -tot[c];
   }
 }
 
@@ -1316,7 +1202,7 @@ __global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ Vo
     for (int c = 0; c < 6; ++c) {
       const T sdc = sd[c] * tau1 / (tau1 + dt * lambda * G);
       a.Fout[(3 + c) * np + p] = (sigma1 * (c < 3 ? T(1) : T(0)) + sdc) - s0[c];
-      if (KAHAN) a.C[(3 + c) * np + p] = T(0);
+      if (KAHAN) a.C[(3 + c) * np + p] = 0;  // bfloat16 zero
     }
     return;
   }
@@ -1329,7 +1215,7 @@ __global__ void __launch_bounds__(256) plastic_kernel(const __grid_constant__ Vo
     const T dlt = c < 3 ? T(1) : T(0);
     const T sd = sa[c] - sigma * dlt;
     a.Fout[(3 + c) * np + p] = (sigma * dlt + rr * sd) - s0[c];
-    if (KAHAN) a.C[(3 + c) * np + p] = T(0);
+    if (KAHAN) a.C[(3 + c) * np + p] = 0;  // bfloat16 zero
   }
 }
 
@@ -1431,12 +1317,7 @@ int launch_corr(const VolumeArgs<T>& a, cudaStream_t s) {
     const PmlBoxes bx = pml_boxes(a);
     const unsigned nblk = (unsigned)((bx.start[bx.n] + 255) / 256);
     if (bx.start[bx.n] > 0) {
-      if (stencil_is_tma(a)) {  // damping folded before the stencil (pml_pre_kernel)
-        if constexpr (sizeof(T) == 4) {
-          if (a.fd == 1) pml_kernel<T, CURV, KAHAN, 1, true><<<nblk, 256, 0, s>>>(a, bx);
-          else pml_kernel<T, CURV, KAHAN, 0, true><<<nblk, 256, 0, s>>>(a, bx);
-        }
-      } else if (a.fd == 1) pml_kernel<T, CURV, KAHAN, 1><<<nblk, 256, 0, s>>>(a, bx);
+      if (a.fd == 1) pml_kernel<T, CURV, KAHAN, 1><<<nblk, 256, 0, s>>>(a, bx);
       else if (a.fd == 2) pml_kernel<T, CURV, KAHAN, 2><<<nblk, 256, 0, s>>>(a, bx);
       else if (a.fd == 3) pml_kernel<T, CURV, KAHAN, 3><<<nblk, 256, 0, s>>>(a, bx);
       else pml_kernel<T, CURV, KAHAN, 0><<<nblk, 256, 0, s>>>(a, bx);
@@ -1482,22 +1363,11 @@ void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream) {
 }
 
 template <typename T>
-int launch_pre(const VolumeArgs<T>& a, bool curv, void* stream) {
+int launch_pre(const VolumeArgs<T>& a, void* stream) {
   if (!stencil_is_tma(a)) return 0;
-  cudaStream_t s = (cudaStream_t)stream;
-  int n = 0;
-  if (a.npml > 0) {
-    const PmlBoxes bx = pml_boxes(a);
-    if (bx.start[bx.n] > 0) {
-      const unsigned nblk = (unsigned)((bx.start[bx.n] + 255) / 256);
-      if (curv) pml_pre_kernel<T, true><<<nblk, 256, 0, s>>>(a, bx);
-      else pml_pre_kernel<T, false><<<nblk, 256, 0, s>>>(a, bx);
-      ++n;
-    }
-  }
   const long long nface = 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
-  face_pre_kernel<T><<<(unsigned)((nface + 255) / 256), 256, 0, s>>>(a);
-  return n + 1;
+  face_pre_kernel<T><<<(unsigned)((nface + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a);
+  return 1;
 }
 
 template <typename T>
@@ -1536,8 +1406,8 @@ template void launch_source<float>(const VolumeArgs<float>&, const int*, const i
 template void launch_volume<double>(const VolumeArgs<double>&, bool, void*);
 template void launch_volume<float>(const VolumeArgs<float>&, bool, void*);
 template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
-template int launch_pre<double>(const VolumeArgs<double>&, bool, void*);
-template int launch_pre<float>(const VolumeArgs<float>&, bool, void*);
+template int launch_pre<double>(const VolumeArgs<double>&, void*);
+template int launch_pre<float>(const VolumeArgs<float>&, void*);
 template int launch_corrections<float>(const VolumeArgs<float>&, bool, void*);
 template bool stencil_is_tma<float>(const VolumeArgs<float>&);
 template bool stencil_is_tma<double>(const VolumeArgs<double>&);
