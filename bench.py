@@ -367,7 +367,9 @@ def accuracy(wql, ctx, text, media, steps, stride=20, checkpoints=8, sensitivity
 def batch_mode(wql, device, args):
     """Config 3: an ensemble of uneven scenarios advanced as one batch (one
     packed stencil launch per stage, tile chunks from the autotuner), against
-    the same scenarios stepped one after another, and FP64 stepped alone."""
+    the same scenarios stepped one after another (each to the end before the
+    next), against all of them queued at once on their own streams, and FP64
+    stepped alone."""
     import numpy as np
     import torch
     import wql_configs
@@ -404,14 +406,23 @@ def batch_mode(wql, device, args):
     for s, *_ in members:
         s.sync(check_nan=True)
     batch.close()
-    # the same members stepped one after another
+    # the same members stepped one after another, each to the end of its
+    # steps before the next starts (a caller without batching)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s, *_ in members:
+        s.step(args.steps)
+        s.sync()
+    seq = points * 5 * args.steps / (time.perf_counter() - t0)
+    # and all of them queued at once, each on its own stream (the streams
+    # overlap on the device)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s, *_ in members:
         s.step(args.steps)
     for s, *_ in members:
         s.sync()
-    seq = points * 5 * args.steps / (time.perf_counter() - t0)
+    streams = points * 5 * args.steps / (time.perf_counter() - t0)
     for s, *_ in members:
         s.close()
     # FP64 on a few members, one after another
@@ -435,6 +446,7 @@ def batch_mode(wql, device, args):
                                    f"points, planar/rough faults, homogeneous/von Karman media, 10-point PML, "
                                    f"{points} grid points", "setup_s": setup_s},
             "sequential_fp32c": seq, "batched_over_sequential": batched / seq,
+            "own_streams_fp32c": streams, "batched_over_own_streams": batched / streams,
             "fp64_alone": fp64, "batched_fp32c_over_fp64": batched / fp64, "clocks": clk.summary()}
 
 
