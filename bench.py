@@ -198,19 +198,24 @@ def time_e2e(wql, ctx, text, media, prec, steps):
         text_f = re.sub(r"w_stride = \d+", f"w_stride = {stride}", text_f)
     t0 = time.perf_counter()
     s = wql.Scenario(ctx, text=text_f, precision=prec, media=media)
+    s.sync()
+    t_create = time.perf_counter()
     for _ in range(steps):
         s.step(1)
+    s.sync()
+    t_steps = time.perf_counter()
     frames = s.frames("Svel")
     v = [s.field(b, c) for b in range(2) for c in range(3)]
     s.sync()
     t1 = time.perf_counter()
+    parts = {"create_s": t_create - t0, "steps_s": t_steps - t_create, "read_s": t1 - t_steps}
     info = s.info()
     np_pts = sum(info.nq[b] * info.nr[b] * info.ns[b] for b in range(2))
     h2d = 3 * np_pts * 8 + sum(a.nbytes for k, a in _media_arrays(media))
     d2h = s.frame_count() * frame_bytes + sum(x.nbytes for x in v)
     s.close()
     del frames
-    return t1 - t0, h2d, d2h, stride
+    return t1 - t0, h2d, d2h, stride, parts
 
 
 def host_available_bytes():
@@ -622,16 +627,16 @@ def main():
     e2e = None
     if not args.no_e2e:
         e_steps = args.e2e_steps or RUN_STEPS[args.workload]
-        secs, h2d, d2h, stride = time_e2e(wql, ctx, text, media, wql.FP32C, e_steps)
+        secs, h2d, d2h, stride, parts = time_e2e(wql, ctx, text, media, wql.FP32C, e_steps)
         e2e = {"value": total_ups * e_steps / allmax(world, secs), "unit": UNIT, "steps": e_steps,
-               "seconds": secs, "fault_frame_every": stride,
+               "seconds": secs, "parts": parts, "fault_frame_every": stride,
                "h2d_bytes_per_step": int(h2d / e_steps), "d2h_bytes_per_step": int(d2h / e_steps),
                "includes": "scenario creation (host grid generation, upload), the fault frames to the host "
                            "(every step unless host memory is short), final velocity fields to the host"}
         # the FP64 mode through the same public API path (like for like with
         # the FP64 CPU baseline)
         f_steps = res["fp64"]["steps"]
-        secs64, h2d64, d2h64, _ = time_e2e(wql, ctx, text, media, wql.FP64, f_steps)
+        secs64, h2d64, d2h64, _, _ = time_e2e(wql, ctx, text, media, wql.FP64, f_steps)
         e2e["fp64"] = {"value": total_ups * f_steps / allmax(world, secs64), "unit": UNIT, "steps": f_steps,
                        "h2d_bytes_per_step": int(h2d64 / f_steps), "d2h_bytes_per_step": int(d2h64 / f_steps)}
     cpu = None

@@ -96,7 +96,10 @@ int wql_scenario_create_ex(wql_ctx* ctx, const char* in_text, const char* base_d
                            const wql_media* media, wql_scn** out);
 int wql_scenario_destroy(wql_scn* scn);
 
-/* Advance nsteps steps = nsteps calls of time_step_RK (src/time_step.f90:68). */
+/* Advance nsteps steps = nsteps calls of time_step_RK (src/time_step.f90:68).
+ * The work is queued on the scenario's stream and the call returns without
+ * waiting for it; fault frames and station records are taken to host memory
+ * as their device rings fill and by the calls that return them. */
 int wql_step(wql_scn* scn, int nsteps);
 /* One RK stage (1..5, in order) of the current step: the body of one pass
  * of the stage loop of time_step_RK (src/time_step.f90:109-147), for parity

@@ -1464,8 +1464,14 @@ void run_stage(wql_scn* S, StepCtx& c, int stage) {
   if (pair) {
     // both blocks' pre-kernels, the stencil launch, both blocks'
     // corrections (the blocks touch disjoint arrays)
-    for (int b = 0; b < 2; ++b) stage_block_pre(S, c, stage, b);
     const double A = stage_A(S, stage), Bdt = stage_Bdt(S, stage);
+    {
+      const VolumeArgs<float> a0 = volume_args<float>(S, 0, A, Bdt, stage == 5);
+      const VolumeArgs<float> a1 = volume_args<float>(S, 1, A, Bdt, stage == 5);
+      mark_begin(S, 2);
+      c.launches += launch_pre2<float>(a0, a1, S->stream);
+      mark_end(S);
+    }
     mark_begin(S, 1);
     launch_stencil_tma2(volume_args<float>(S, 0, A, Bdt, stage == 5), volume_args<float>(S, 1, A, Bdt, stage == 5),
                         S->curv, true, S->stream);
@@ -1588,7 +1594,11 @@ int wql_step(wql_scn* scn, int nsteps) {
     int rc = run_step(scn);
     if (rc) return rc;
   }
-  return flush_frames(scn);
+  // no flush here: the frame and station rings are read out by the calls
+  // that return them (wql_get_frames, wql_get_seismograms, the output
+  // writer), so a caller stepping one step at a time never waits on the
+  // device between steps
+  return WQL_OK;
 }
 
 int wql_sync(wql_scn* scn, int check_nan) {

@@ -256,6 +256,10 @@ void launch_volume(const VolumeArgs<T>& a, bool curv, void* stream);
 // the number of launches.
 template <typename T>
 int launch_pre(const VolumeArgs<T>& a, void* stream);
+// The same for both blocks of a scenario whose stencils both run as the TMA
+// kernel, in one launch.
+template <typename T>
+int launch_pre2(const VolumeArgs<T>& a0, const VolumeArgs<T>& a1, void* stream);
 template <typename T>
 int launch_corrections(const VolumeArgs<T>& a, bool curv, void* stream);
 // One moment-tensor source: DF(4:9) -= am * delta on a box of points

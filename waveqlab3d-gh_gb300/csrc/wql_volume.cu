@@ -1078,11 +1078,10 @@ __global__ void __launch_bounds__(256) face_kernel(const __grid_constant__ Volum
 // One thread per face point, a point on several faces taken by its lowest
 // side.
 template <typename T>
-__global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ VolumeArgs<T> a) {
+__device__ __forceinline__ void face_pre_point(const VolumeArgs<T>& a, long long t) {
   const int nq = a.nq, nr = a.nr, ns = a.ns;
   const long long nfs[6] = {(long long)nr * ns, (long long)nr * ns, (long long)nq * ns, (long long)nq * ns,
                             (long long)nq * nr, (long long)nq * nr};
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int side = 0;
   while (side < 6 && t >= nfs[side]) {
     t -= nfs[side];
@@ -1113,6 +1112,27 @@ __global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ V
     T* df = a.DF + c * np + p;
     *df = a.A != T(0) ? *df - tot[c] / a.A : -tot[c];
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) face_pre_kernel(const __grid_constant__ VolumeArgs<T> a) {
+  face_pre_point(a, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
+
+// Both blocks of a scenario in one launch: threads [0, n0) take block 0's
+// face points, the rest block 1's (one launch of about twice the threads
+// hides the latency of these sub-wave launches better than two).
+template <typename T>
+struct FacePair {
+  VolumeArgs<T> a[2];
+  long long n0;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) face_pre_kernel2(const __grid_constant__ FacePair<T> P) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < P.n0) face_pre_point(P.a[0], t);
+  else face_pre_point(P.a[1], t - P.n0);
 }
 
 // ---------------------------------------------------------------------------
@@ -1371,6 +1391,20 @@ int launch_pre(const VolumeArgs<T>& a, void* stream) {
 }
 
 template <typename T>
+int launch_pre2(const VolumeArgs<T>& a0, const VolumeArgs<T>& a1, void* stream) {
+  FacePair<T> P;
+  P.a[0] = a0;
+  P.a[1] = a1;
+  auto nface = [](const VolumeArgs<T>& a) {
+    return 2LL * ((long long)a.nr * a.ns + (long long)a.nq * a.ns + (long long)a.nq * a.nr);
+  };
+  P.n0 = nface(a0);
+  const long long n = P.n0 + nface(a1);
+  face_pre_kernel2<T><<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(P);
+  return 1;
+}
+
+template <typename T>
 int launch_corrections(const VolumeArgs<T>& a0, bool curv, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   // the PML velocity gradient comes from the stencil only when that was the
@@ -1408,6 +1442,7 @@ template void launch_volume<float>(const VolumeArgs<float>&, bool, void*);
 template int launch_corrections<double>(const VolumeArgs<double>&, bool, void*);
 template int launch_pre<double>(const VolumeArgs<double>&, void*);
 template int launch_pre<float>(const VolumeArgs<float>&, void*);
+template int launch_pre2<float>(const VolumeArgs<float>&, const VolumeArgs<float>&, void*);
 template int launch_corrections<float>(const VolumeArgs<float>&, bool, void*);
 template bool stencil_is_tma<float>(const VolumeArgs<float>&);
 template bool stencil_is_tma<double>(const VolumeArgs<double>&);
