@@ -78,7 +78,7 @@ class Clocks:
             self.lines = [l for l in out.splitlines() if l.strip()]
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, pw, mx, reasons = [], [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for l in getattr(self, "lines", []):
             f = [x.strip() for x in l.split(",")]
@@ -87,10 +87,15 @@ class Clocks:
                 mx = float(f[2])
             except (ValueError, IndexError):
                 continue
+            try:
+                pw.append(float(f[3]))
+            except (ValueError, IndexError):
+                pass
             for n, v in zip(names, f[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_min_mhz": min(sm) if sm else None,
+                "sm_max_mhz": mx, "power_w": statistics.median(pw) if pw else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -627,9 +632,10 @@ def main():
     e2e = None
     if not args.no_e2e:
         e_steps = args.e2e_steps or RUN_STEPS[args.workload]
-        secs, h2d, d2h, stride, parts = time_e2e(wql, ctx, text, media, wql.FP32C, e_steps)
+        with Clocks(local) as eclk:
+            secs, h2d, d2h, stride, parts = time_e2e(wql, ctx, text, media, wql.FP32C, e_steps)
         e2e = {"value": total_ups * e_steps / allmax(world, secs), "unit": UNIT, "steps": e_steps,
-               "seconds": secs, "parts": parts, "fault_frame_every": stride,
+               "seconds": secs, "parts": parts, "fault_frame_every": stride, "clocks": eclk.summary(),
                "h2d_bytes_per_step": int(h2d / e_steps), "d2h_bytes_per_step": int(d2h / e_steps),
                "includes": "scenario creation (host grid generation, upload), the fault frames to the host "
                            "(every step unless host memory is short), final velocity fields to the host"}
