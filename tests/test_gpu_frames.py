@@ -47,3 +47,20 @@ def test_frames_same_overlapped_and_synchronous(ctx, prec):
     assert np.abs(fa["Svel"][-1] - fa["Svel"][0]).max() > 0
     a.close()
     b.close()
+
+
+def test_destroy_with_frames_in_flight(ctx):
+    """wql_step returns with the last ring's copy to pinned memory possibly
+    still queued; destroying the scenario right away waits for it (no read
+    of freed memory), and a scenario created afterwards starts clean."""
+    import wql
+    text = problem(t_final="5d0") + block_list(17)
+    for _ in range(3):
+        s = wql.Scenario(ctx, text=text, precision=wql.FP32C)
+        s.step(130)
+        s.close()
+    s = wql.Scenario(ctx, text=text, precision=wql.FP32C)
+    s.step(3)
+    assert s.frame_count() == 3
+    assert s.frames("Svel").shape[0] == 3
+    s.close()
