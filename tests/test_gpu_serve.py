@@ -51,9 +51,10 @@ def test_footprint_estimate(ctx, wqlmod, medium):
 
 
 def test_served_equals_alone(ctx, wqlmod, medium):
-    """Requests submitted while another runs join the running batch: each is
-    admitted before the first one completes, so their work overlaps on the
-    device; each result equals the request run alone (bitwise)."""
+    """Requests submitted while another runs join the running batch once
+    their set-up (done beside the stepping) is ready, so each request is on
+    the device while another is; each result equals the request run alone
+    (bitwise)."""
     import wql_configs
     steps = 120
     reqs = [wql_configs.config4_request(i, n_lo=24, n_hi=44, steps=steps, medium=medium) for i in range(4)]
@@ -67,8 +68,11 @@ def test_served_equals_alone(ctx, wqlmod, medium):
     for rid in ids:
         assert srv.wait(rid, 300.0) == 1
     times = [srv.result(rid, 0)[1] for rid in ids]
-    for k in range(1, len(ids)):
-        assert times[k][1] < times[0][2], (k, times[k], times[0])  # admitted while request 0 ran
+    # every request is on the device (admitted, not yet done) while another
+    # one is: their work overlaps
+    for k in range(len(ids)):
+        assert any(times[j][1] < times[k][2] and times[k][1] < times[j][2] for j in range(len(ids)) if j != k), \
+            (k, times)
     for (text, media, _), rid in zip(reqs, ids):
         ref = _alone(wqlmod, ctx, text, media, steps)
         for b in range(2):

@@ -4,12 +4,17 @@
 // timings kept until released.  One worker thread owns the GPU work; it is
 // written against the public C ABI only.
 //
-// Worker loop: admit queued requests in arrival order while the head's peak
-// footprint (wql_estimate_device_bytes) fits next to the resident bytes of
-// the active scenarios (the head is always admitted when nothing is active),
-// step the batch by the smallest remaining step count of its members (at
-// most round_steps), retire finished members.  Requests that arrive while
-// others run join the batch at the next round.
+// Two threads own the GPU work.  The worker admits queued requests in
+// arrival order while the head's peak footprint (wql_estimate_device_bytes)
+// fits next to the bytes held or reserved by the admitted ones (the head is
+// always admitted when nothing is admitted), hands each to the preparer,
+// moves prepared scenarios into the batch, steps the batch by the smallest
+// remaining step count of its members (at most round_steps) and retires
+// finished members.  The preparer creates the admitted scenarios (host grid
+// generation, uploads, set-up kernels on the scenario's own stream) while the
+// batch steps, so the device does not wait for a new request's set-up.
+// Requests that arrive while others run join the batch at the next round
+// after their set-up.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -67,15 +72,21 @@ struct wql_server {
   std::condition_variable done_cv;  // a request finished
   bool stop = false;
   long long next_id = 1;
-  std::deque<Request*> queue;
+  std::deque<Request*> queue;     // submitted, waiting for admission
+  std::deque<Request*> prep;      // admitted, waiting for the preparer
+  std::vector<Request*> ready;    // created, waiting to join the batch
+  int preparing = 0;              // admitted requests not yet in the batch
+  bool worker_done = false;       // the worker has returned (the preparer may too)
   std::vector<Request*> active;
+  std::condition_variable prep_cv;  // work for the preparer
   std::map<long long, std::unique_ptr<Request>> all;
   long long in_use = 0;
   long long completed = 0, steps_done = 0;
   wql_batch* batch = nullptr;
-  std::thread worker;
+  std::thread worker, preparer;
 
   void run();
+  void prepare();
   void finish(Request* r, int status, const std::string& err);
 };
 
@@ -88,59 +99,91 @@ void wql_server::finish(Request* r, int status, const std::string& err) {
   done_cv.notify_all();
 }
 
+// Creates the admitted scenarios, one at a time, in admission order.
+void wql_server::prepare() {
+  for (;;) {
+    Request* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lock(mu);
+      prep_cv.wait(lock, [&] { return worker_done || !prep.empty(); });
+      if (prep.empty()) return;
+      r = prep.front();
+      prep.pop_front();
+    }
+    wql_media m;
+    std::memset(&m, 0, sizeof(m));
+    if (r->has_media) {
+      m.fault_offset = r->fault.empty() ? nullptr : r->fault.data();
+      for (int b = 0; b < 2; ++b) {
+        m.topo_offset[b] = r->topo[b].empty() ? nullptr : r->topo[b].data();
+        m.lam[b] = r->lam[b].empty() ? nullptr : r->lam[b].data();
+        m.mu[b] = r->mu[b].empty() ? nullptr : r->mu[b].data();
+        m.rho[b] = r->rho[b].empty() ? nullptr : r->rho[b].data();
+      }
+    }
+    wql_scn* scn = nullptr;
+    const int rc = wql_scenario_create_ex(ctx, r->text.c_str(), nullptr, r->precision, r->has_media ? &m : nullptr, &scn);
+    if (rc) {
+      const std::string e = last_error();
+      {
+        std::lock_guard<std::mutex> lock(mu);
+        preparing -= 1;
+        in_use -= r->peak;
+        cv.notify_all();
+      }
+      finish(r, -rc, e);
+      continue;
+    }
+    wql_info info;
+    wql_get_info(scn, &info);
+    std::lock_guard<std::mutex> lock(mu);
+    r->scn = scn;
+    in_use += info.device_bytes - r->peak;  // the reservation becomes the bytes held
+    r->resident = info.device_bytes;
+    ready.push_back(r);
+    cv.notify_all();
+  }
+}
+
 void wql_server::run() {
   for (;;) {
-    // admit
-    for (;;) {
-      Request* r = nullptr;
-      {
-        std::unique_lock<std::mutex> lock(mu);
-        if (queue.empty() && active.empty()) {
-          if (stop) return;
-          cv.wait(lock, [&] { return stop || !queue.empty(); });
-          if (queue.empty()) return;
+    std::vector<Request*> joining, act;
+    {
+      std::unique_lock<std::mutex> lock(mu);
+      for (;;) {
+        // admit: reserve the head's peak bytes and hand it to the preparer
+        while (!queue.empty()) {
+          Request* head = queue.front();
+          if ((!active.empty() || preparing > 0) && in_use + head->peak > budget) break;
+          queue.pop_front();
+          in_use += head->peak;
+          preparing += 1;
+          prep.push_back(head);
+          prep_cv.notify_one();
         }
-        if (queue.empty()) break;
-        Request* head = queue.front();
-        if (!active.empty() && in_use + head->peak > budget) break;
-        queue.pop_front();
-        r = head;
-      }
-      wql_media m;
-      std::memset(&m, 0, sizeof(m));
-      if (r->has_media) {
-        m.fault_offset = r->fault.empty() ? nullptr : r->fault.data();
-        for (int b = 0; b < 2; ++b) {
-          m.topo_offset[b] = r->topo[b].empty() ? nullptr : r->topo[b].data();
-          m.lam[b] = r->lam[b].empty() ? nullptr : r->lam[b].data();
-          m.mu[b] = r->mu[b].empty() ? nullptr : r->mu[b].data();
-          m.rho[b] = r->rho[b].empty() ? nullptr : r->rho[b].data();
+        joining.swap(ready);
+        if (!joining.empty() || !active.empty()) break;
+        if (stop && queue.empty() && preparing == 0) {
+          worker_done = true;
+          prep_cv.notify_all();
+          return;
         }
+        cv.wait(lock);
       }
-      wql_scn* scn = nullptr;
-      const int rc = wql_scenario_create_ex(ctx, r->text.c_str(), nullptr, r->precision, r->has_media ? &m : nullptr, &scn);
-      if (rc) {
-        finish(r, -rc, last_error());
-        continue;
-      }
-      wql_info info;
-      wql_get_info(scn, &info);
-      wql_batch_add(batch, scn);
+      preparing -= (int)joining.size();
+    }
+    for (auto* r : joining) {
+      wql_batch_add(batch, r->scn);
       std::lock_guard<std::mutex> lock(mu);
-      r->scn = scn;
-      r->resident = info.device_bytes;
       r->t_admit = now_s(t0);
-      in_use += r->resident;
       active.push_back(r);
     }
-    // step
-    int k = round_steps;
-    std::vector<Request*> act;
     {
       std::lock_guard<std::mutex> lock(mu);
       act = active;
     }
-    if (act.empty()) continue;
+    // step
+    int k = round_steps;
     for (auto* r : act) {
       wql_info info;
       wql_get_info(r->scn, &info);
@@ -154,11 +197,13 @@ void wql_server::run() {
           wql_batch_remove(batch, r->scn);
           wql_scenario_destroy(r->scn);
           r->scn = nullptr;
+          {
+            std::lock_guard<std::mutex> lock(mu);
+            in_use -= r->resident;
+            active.erase(std::find(active.begin(), active.end(), r));
+          }
           finish(r, -rc, e);
         }
-        std::lock_guard<std::mutex> lock(mu);
-        active.clear();
-        in_use = 0;
         continue;
       }
       std::lock_guard<std::mutex> lock(mu);
@@ -204,6 +249,7 @@ int wql_server_create(wql_ctx* ctx, long long hbm_budget_bytes, int round_steps,
   if (rc) return rc;
   wql_server* p = s.release();
   p->worker = std::thread([p] { p->run(); });
+  p->preparer = std::thread([p] { p->prepare(); });
   *out = p;
   return WQL_OK;
 }
@@ -300,8 +346,10 @@ int wql_server_destroy(wql_server* s) {
     std::lock_guard<std::mutex> lock(s->mu);
     s->stop = true;
     s->cv.notify_all();
+    s->prep_cv.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
+  if (s->preparer.joinable()) s->preparer.join();
   wql_batch_destroy(s->batch);
   delete s;
   return WQL_OK;

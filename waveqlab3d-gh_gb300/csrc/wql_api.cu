@@ -63,6 +63,15 @@ struct RK {
   }
 };
 
+// Records per station ring: as many as fit in 16 MiB for the largest
+// requested station list, 64 to 1024 (a ring that fills is copied out
+// synchronously, so a short served request should not fill it).
+int station_ring_cap(const Problem& P) {
+  const size_t n = std::max({P.stations.size(), P.stationsU.size(), P.stationsV.size()}) / 3;
+  const long long per = std::max<long long>(1, (long long)n * 3 * (long long)sizeof(double));
+  return (int)std::max(64LL, std::min(1024LL, (16LL << 20) / per));
+}
+
 // Frames per fault-frame ring: as many as fit in 128 MiB, 4 to 64.
 int frame_ring_cap(long long nf) {
   const long long frame_bytes = (long long)kFrameWords * nf * (long long)sizeof(float);
@@ -617,7 +626,7 @@ int setup_block(wql_scn* S, int b) {
         off[i] = (T.ijk[3 * i] - 1) + (long long)B.pq * ((T.ijk[3 * i + 1] - 1) + (long long)B.nr * (T.ijk[3 * i + 2] - 1));
       if ((rc = S->alloc((void**)&T.idx_dev, n * sizeof(long long), false))) return rc;
       CK(cudaMemcpy(T.idx_dev, off.data(), n * sizeof(long long), cudaMemcpyHostToDevice));
-      if ((rc = S->alloc((void**)&T.ring, (size_t)64 * n * 3 * sizeof(double)))) return rc;
+      if ((rc = S->alloc((void**)&T.ring, (size_t)S->st_cap * n * 3 * sizeof(double)))) return rc;
     }
   }
   // interface coordinates of this block's fault face
@@ -900,6 +909,7 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
   const long long nf = (long long)Pr.btp[0].nqrs[1] * Pr.btp[0].nqrs[2];
   int rc;
   if ((rc = S->alloc((void**)&S->xij, 2 * 3 * nf * sizeof(double)))) return rc;
+  S->st_cap = station_ring_cap(Pr);
   for (int b = 0; b < 2; ++b)
     if ((rc = setup_block(S.get(), b))) return rc;
   // moment-tensor sources: the unified list goes to the preferred block when
@@ -958,7 +968,6 @@ int create(wql_ctx* ctx, Problem&& P, int precision, const wql_media* media, wql
     if ((rc = precompute_fault(S.get()))) return rc;
   if (fp.coupling == CPL_RS)
     if ((rc = init_rate_state(S.get()))) return rc;
-  S->st_cap = 64;
   if (Pr.w_fault) {
     S->frame_cap = frame_ring_cap(nf);
     const size_t ring_bytes = (size_t)S->frame_cap * kFrameWords * nf * sizeof(float);
@@ -2123,6 +2132,13 @@ int wql_estimate_device_bytes(const char* in_text, const char* base_dir, int pre
   }
   res += al(6 * nf * 8) + 2 * al(8 * nf * 8) + 3 * al(2 * nf * 8) + al(18 * nf * esz) + al(10 * nf * 8) + 2 * 512;
   if (P.w_fault) res += 2 * al((long long)frame_ring_cap(nf) * kFrameWords * nf * 4);
+  if (P.output_seismograms) {
+    // station rings: each requested station is found in at most one block
+    // (within half a cell of a grid point)
+    const long long n = !P.stations.empty() ? (long long)P.stations.size() / 3
+                                            : (long long)(P.stationsU.size() + P.stationsV.size()) / 3;
+    res += al((long long)station_ring_cap(P) * n * 3 * 8) + al(n * 8);
+  }
   *resident = res;
   *peak = res + transient;
   return WQL_OK;
@@ -2186,10 +2202,8 @@ int wql_batch_step(wql_batch* b, int nsteps) {
     const int rc = batch_step(b);
     if (rc) return rc;
   }
-  for (auto* m : b->members) {
-    const int rc = flush_frames(m);
-    if (rc) return rc;
-  }
+  // as wql_step: the members' frames and station records are read out by
+  // the calls that return them, so the call does not wait for the device
   return WQL_OK;
 }
 
