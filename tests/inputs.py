@@ -90,11 +90,12 @@ def case_text(name):
         # Gaussian stress pulse at (y, z) = (8, 0) switched on at t > 0
         return problem("rate-weakening", "rate-and-state_friction",
                        "curvilinear" if name == "rw_curv" else "cartesian") + block_list()
-    if name == "rw_plastic":
+    if name in ("rw_plastic", "rw_plastic_curv"):
         # the reference's default plastic model (plastic_flow) with the
         # mu_beta_eta of its plasticity.in deck
         mbe = "btp({})%mu_beta_eta = 0.5735d0, 0.2867d0, 0.2775d0,"
-        return (problem("rate-weakening", "rate-and-state_friction", extra=",\n response = 'plastic'") +
+        mesh = "curvilinear" if name.endswith("_curv") else "cartesian"
+        return (problem("rate-weakening", "rate-and-state_friction", mesh, extra=",\n response = 'plastic'") +
                 block_list(extra1=mbe.format(1), extra2=mbe.format(2)))
     if name.startswith(("an_", "an0_")):
         # anelastic response (GSLS memory variables, src/material.f90:11-142)

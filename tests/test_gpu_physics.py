@@ -79,7 +79,7 @@ def test_rate_state_fp64_parity_converged(ctx, wqlmod, oracle_lib, tmp_path, cas
         assert rel_l2(s.iface(copy, 4), o.iface(copy, 4)) < TOL  # state variable
 
 
-@pytest.mark.parametrize("case,steps", [("rw", 40), ("rw_curv", 20), ("rw_plastic", 40)])
+@pytest.mark.parametrize("case,steps", [("rw", 40), ("rw_curv", 20), ("rw_plastic", 40), ("rw_plastic_curv", 30)])
 def test_rate_weakening_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, steps):
     """Problem 'rate-weakening' (slip law with flash weakening, a stress
     pulse switched on at t > 0) and, in rw_plastic, the default plastic
@@ -93,7 +93,7 @@ def test_rate_weakening_fp64_parity(ctx, wqlmod, oracle_lib, tmp_path, case, ste
     for copy in range(2):
         assert rel_l2(s.iface(copy, 4), o.iface(copy, 4)) < TOL
         assert rel_l2(s.iface(copy, 3), o.iface(copy, 3)) < TOL
-    if case == "rw_plastic":
+    if case.startswith("rw_plastic"):
         for b in range(2):
             lam_o = o.field(b, 9)
             assert (lam_o > 0).sum() > 10  # points yield
