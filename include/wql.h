@@ -228,19 +228,22 @@ int wql_batch_stream(wql_batch* b, uintptr_t* stream);
 /* Request server (continuous batching with admission by device memory).
  * A worker thread admits submitted scenarios in arrival order while the
  * head request's peak footprint (wql_estimate_device_bytes) fits within
- * hbm_budget_bytes next to the resident bytes of the running scenarios
- * (the head is always admitted when nothing runs), advances all running
- * scenarios together with wql_batch_step (at most round_steps steps per
- * round, never past a member's step count), and retires each scenario when
- * it reaches its step count, keeping its station seismograms.  Requests that
- * arrive while others run join the batch at the next round.  submit copies
+ * hbm_budget_bytes next to the bytes held or reserved by the admitted ones
+ * (the head is always admitted when nothing is admitted); a second thread
+ * creates each admitted scenario while the batch steps; the worker moves
+ * created scenarios into the batch, advances all running scenarios together
+ * with wql_batch_step (at most round_steps steps per round, never past a
+ * member's step count), and retires each scenario when it reaches its step
+ * count, keeping its station seismograms.  Requests that arrive while others
+ * run join the batch at the first round after their set-up.  submit copies
  * the text and media arrays and returns at once; wait blocks until the
  * request is done (status 1) or failed (status < 0: minus its WQL_E_* code)
  * or the timeout passes (status 0); result gives one block's seismograms
  * (as wql_get_seismograms, may be NULL) and the request's arrival,
- * admission and completion times in seconds since the server started;
- * release frees a finished request's record; destroy finishes all submitted
- * work and stops the worker.  No counterpart in the reference. */
+ * admission (joining the batch) and completion times in seconds since the
+ * server started; stats counts admitted requests still being created as
+ * queued; release frees a finished request's record; destroy finishes all
+ * submitted work and stops both threads.  No counterpart in the reference. */
 typedef struct wql_server wql_server;
 int wql_server_create(wql_ctx* ctx, long long hbm_budget_bytes, int round_steps, wql_server** out);
 int wql_server_submit(wql_server* s, const char* in_text, int precision, const wql_media* media, int nsteps,

@@ -334,7 +334,7 @@ int wql_server_stats(wql_server* s, long long* completed, long long* queued, lon
   if (!s) return WQL_E_INPUT;
   std::lock_guard<std::mutex> lock(s->mu);
   if (completed) *completed = s->completed;
-  if (queued) *queued = (long long)s->queue.size();
+  if (queued) *queued = (long long)s->queue.size() + s->preparing;  // admitted ones in set-up too
   if (active) *active = (long long)s->active.size();
   if (bytes_in_use) *bytes_in_use = s->in_use;
   return WQL_OK;
