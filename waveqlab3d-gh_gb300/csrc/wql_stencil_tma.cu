@@ -29,7 +29,8 @@
 // the start of a chunk, then one pushed per step from the lead tile), so
 // the s derivative of a central row needs no shared memory (lead planes
 // outside 0..ns-1 load as zeros and are never used: the 12 s closure rows
-// read their 9 planes from global memory); the q and r derivatives read the
+// take the planes of their stencil that the window holds from it and read
+// the at most three others from global memory); the q and r derivatives read the
 // main box, the curvilinear q and r fluxes formed once per box point into
 // the stage (one mbarrier phase among the consumer threads per step).  The r
 // tiles follow the ownership rule of tile_span (the last
@@ -44,6 +45,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <utility>
 
 #include "wql_internal.h"
 #include "wql_stencil.cuh"
@@ -134,44 +136,94 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 }
 
 // s derivative of the six differenced quantities on a closure row (planes
-// 0..5 and ns-6..ns-1), read from global memory: the s window in registers
-// holds only the 7 planes of a central row.  Inlined: as a call, its
-// argument passing put values on the stack and made the caller spill.
-template <bool CURV, int FD>
-__device__ __forceinline__ void s_closure(const VolumeArgs<float>& a, long long p, int s, int ks, float o[6]) {
-  const long long np = a.np, st = (long long)a.pq * a.nr;
-  float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // in registers; o is written once
-#pragma unroll 3
-  for (int e = 0; e < (FD ? 10 : 9); ++e) {
-    float w, wf;
-    int off;
-    if (FD) {
-      up_entry<float>(ks, e, w, wf, off);
-    } else {
-      row_entry<float>(ks, e, w, off);
-      wf = w;
-    }
-    const long long pp = p + off * st;
-    float x[6];
-    const float* F = a.Fin;
+// 0..5 and ns-6..ns-1).  The s window already holds most of the planes a
+// closure row reads (planes s-3..s+3 for the central operator; velocities of
+// s-2..s+4 and fluxes of s-4..s+2 for the upwind pair); the at most three
+// planes of a row outside it are read from global memory.  Each row is a
+// separate instantiation (the weights, offsets and window positions are
+// compile-time constants, so the window stays in registers); the columns are
+// summed in the order of the operator table, zero weights skipped.
+//
+// Weight of column t in closure row `row`: the central SBP-6 operator (the
+// same weight for velocities and fluxes), or the upwind pair (left rows: D+
+// on the velocities, D- on the fluxes; right rows: the negated mirror, D-
+// on the velocities and D+ on the fluxes).
+constexpr double s_close_w(int fd, bool right, bool flux, int row, int t) {
+  constexpr double L[6][9] = WQL_SBP_TABLE;
+  constexpr double U[2][6][10] = WQL_UP_TABLE;
+  if (fd == 0) return t < 9 ? (right ? -L[row][t] : L[row][t]) : 0.0;
+  const int op = right ? (flux ? 0 : 1) : (flux ? 1 : 0);
+  return right ? -U[op][row][t] : U[op][row][t];
+}
+
+template <bool CURV, int FD, int ROW, bool RIGHT, int T>
+__device__ __forceinline__ void s_close_col(const VolumeArgs<float>& a, long long p, const float (&qv)[7][6],
+                                            float acc[6]) {
+  constexpr float wv = (float)s_close_w(FD, RIGHT, false, ROW, T);
+  constexpr float wf = (float)s_close_w(FD, RIGHT, true, ROW, T);
+  constexpr int off = RIGHT ? ROW - T : T - ROW;  // plane offset from s
+  constexpr int iv = off + (FD ? 2 : 3), iflux = off + (FD ? 4 : 3);  // window positions
+  const long long np = a.np, pp = p + off * ((long long)a.pq * a.nr);
+  const float* F = a.Fin;
+  if constexpr (wv != 0.0f) {
+    float x[3];
+    if constexpr (iv >= 0 && iv <= 6) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) x[c] = F[c * np + pp];
-    if (CURV) {
+      for (int c = 0; c < 3; ++c) x[c] = qv[iv][c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c] = F[c * np + pp];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] += wv * x[c];
+  }
+  if constexpr (wf != 0.0f) {
+    float x[3];
+    if constexpr (iflux >= 0 && iflux <= 6) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c] = qv[iflux][3 + c];
+    } else if constexpr (CURV) {
       const float a0 = a.coef[6 * np + pp], a1 = a.coef[7 * np + pp], a2 = a.coef[8 * np + pp];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
-        x[3 + c] = a0 * F[sig(c, 0) * np + pp] + a1 * F[sig(c, 1) * np + pp] + a2 * F[sig(c, 2) * np + pp];
+        x[c] = a0 * F[sig(c, 0) * np + pp] + a1 * F[sig(c, 1) * np + pp] + a2 * F[sig(c, 2) * np + pp];
     } else {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) x[3 + c] = F[sig(c, 2) * np + pp];
+      for (int c = 0; c < 3; ++c) x[c] = F[sig(c, 2) * np + pp];
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) acc[c] += w * x[c];
-#pragma unroll
-    for (int c = 3; c < 6; ++c) acc[c] += wf * x[c];
+    for (int c = 0; c < 3; ++c) acc[3 + c] += wf * x[c];
   }
+}
+
+template <bool CURV, int FD, int ROW, bool RIGHT, int... T>
+__device__ __forceinline__ void s_close_row(const VolumeArgs<float>& a, long long p, const float (&qv)[7][6],
+                                            float o[6], std::integer_sequence<int, T...>) {
+  float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  (s_close_col<CURV, FD, ROW, RIGHT, T>(a, p, qv, acc), ...);
 #pragma unroll
   for (int c = 0; c < 6; ++c) o[c] = acc[c];
+}
+
+// ks = sbp_kind(s, ns), nonzero: -1..-6 left rows 0..5, 1..6 right rows 0..5.
+template <bool CURV, int FD>
+__device__ __forceinline__ void s_closure(const VolumeArgs<float>& a, long long p, int ks, const float (&qv)[7][6],
+                                          float o[6]) {
+  using Cols = std::make_integer_sequence<int, FD ? 10 : 9>;
+  switch (ks) {
+    case -1: s_close_row<CURV, FD, 0, false>(a, p, qv, o, Cols{}); break;
+    case -2: s_close_row<CURV, FD, 1, false>(a, p, qv, o, Cols{}); break;
+    case -3: s_close_row<CURV, FD, 2, false>(a, p, qv, o, Cols{}); break;
+    case -4: s_close_row<CURV, FD, 3, false>(a, p, qv, o, Cols{}); break;
+    case -5: s_close_row<CURV, FD, 4, false>(a, p, qv, o, Cols{}); break;
+    case -6: s_close_row<CURV, FD, 5, false>(a, p, qv, o, Cols{}); break;
+    case 1: s_close_row<CURV, FD, 0, true>(a, p, qv, o, Cols{}); break;
+    case 2: s_close_row<CURV, FD, 1, true>(a, p, qv, o, Cols{}); break;
+    case 3: s_close_row<CURV, FD, 2, true>(a, p, qv, o, Cols{}); break;
+    case 4: s_close_row<CURV, FD, 3, true>(a, p, qv, o, Cols{}); break;
+    case 5: s_close_row<CURV, FD, 4, true>(a, p, qv, o, Cols{}); break;
+    default: s_close_row<CURV, FD, 5, true>(a, p, qv, o, Cols{}); break;
+  }
 }
 
 struct MapArgs {
@@ -408,10 +460,8 @@ __device__ __forceinline__ bool tma_body(const VolumeArgs<float>& a, const MapAr
             for (int c = 0; c < 6; ++c)
               o[c] = c1 * (qv[4][c] - qv[2][c]) + c2 * (qv[5][c] - qv[1][c]) + c3 * (qv[6][c] - qv[0][c]);
           } else {
-            // a separate array: only it goes through memory for the call,
-            // o stays in registers
             float os[6];
-            s_closure<CURV, FD>(a, p, s, ks, os);
+            s_closure<CURV, FD>(a, p, ks, qv, os);
 #pragma unroll
             for (int c = 0; c < 6; ++c) o[c] = os[c];
           }
