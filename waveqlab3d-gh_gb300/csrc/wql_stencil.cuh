@@ -262,7 +262,6 @@ __device__ __forceinline__ void add_correction(const VolumeArgs<T>& a, long long
 template <typename T>
 __device__ __forceinline__ bool face_penalty(const VolumeArgs<T>& a, int i, int j, int k, const T* u, T* tot) {
   const int nq = a.nq, nr = a.nr, ns = a.ns;
-  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
   bool any = false;
   for (int c = 0; c < 9; ++c) tot[c] = T(0);
   for (int s2 = 0; s2 < 6; ++s2) {
@@ -270,7 +269,9 @@ __device__ __forceinline__ bool face_penalty(const VolumeArgs<T>& a, int i, int 
     if (code < 1 || code > 3) continue;
     const int ax2 = s2 >> 1;
     const bool hi = s2 & 1;
-    if (idx[ax2] != (hi ? nn[ax2] - 1 : 0)) continue;
+    // selects, not arrays indexed by ax2 (those went to local memory)
+    const int ii = ax2 == 0 ? i : (ax2 == 1 ? j : k), n2 = ax2 == 0 ? nq : (ax2 == 1 ? nr : ns);
+    if (ii != (hi ? n2 - 1 : 0)) continue;
     const int na = ax2 == 0 ? nr : nq;
     const long long nf = (long long)na * (ax2 == 2 ? nr : ns);
     const long long f = ax2 == 0 ? (j + (long long)nr * k) : (ax2 == 1 ? (i + (long long)nq * k) : (i + (long long)nq * j));

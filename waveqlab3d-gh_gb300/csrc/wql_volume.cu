@@ -1095,23 +1095,27 @@ __device__ __forceinline__ void face_pre_point(const VolumeArgs<T>& a, long long
   if (axis == 0) { i = (side & 1) ? nq - 1 : 0; j = c1; k = c2; }
   else if (axis == 1) { i = c1; j = (side & 1) ? nr - 1 : 0; k = c2; }
   else { i = c1; j = c2; k = (side & 1) ? ns - 1 : 0; }
-  const int idx[3] = {i, j, k}, nn[3] = {nq, nr, ns};
   for (int s2 = 0; s2 < side; ++s2) {
     const int ax2 = s2 >> 1;
-    if (idx[ax2] == ((s2 & 1) ? nn[ax2] - 1 : 0)) return;
+    const int ii = ax2 == 0 ? i : (ax2 == 1 ? j : k), n2 = ax2 == 0 ? nq : (ax2 == 1 ? nr : ns);
+    if (ii == ((s2 & 1) ? n2 - 1 : 0)) return;
   }
   const long long np = a.np;
   const long long p = i + (long long)a.pq * (j + (long long)nr * k);
-  T u[9], tot[9];
+  T u[9], tot[9], df[9];
+  // the rates are read together with the fields (not after the penalty is
+  // formed), so the two loads' latencies overlap; a stage with A = 0
+  // overwrites them without reading
+  const bool keep = a.A != T(0);
 #pragma unroll
-  for (int c = 0; c < 9; ++c) u[c] = a.Fin[c * np + p];
+  for (int c = 0; c < 9; ++c) {
+    u[c] = a.Fin[c * np + p];
+    df[c] = keep ? a.DF[c * np + p] : T(0);
+  }
   mms_deviation(a, p, u);
   if (!face_penalty(a, i, j, k, u, tot)) return;
 #pragma unroll
-  for (int c = 0; c < 9; ++c) {
-    T* df = a.DF + c * np + p;
-    *df = a.A != T(0) ? *df - tot[c] / a.A : -tot[c];
-  }
+  for (int c = 0; c < 9; ++c) a.DF[c * np + p] = keep ? df[c] - tot[c] / a.A : -tot[c];
 }
 
 template <typename T>
