@@ -215,3 +215,85 @@ def test_upwind_table_copies_agree():
     a, b = data(lib), data(orc)
     assert len(a) == len(b) > 15 * 1300
     assert a == b
+
+
+_SCLOSE_PROBE = r"""
+#include <cmath>
+#include <cstdio>
+#include "wql_sbp.cuh"
+using namespace wql;
+// The s-closure rows as the TMA stencil forms them: columns whose window
+// position (s_close_vpos / s_close_fpos) lies in 0..6 come from the register
+// window, the others from memory.  The window holds planes s-3..s+3 for the
+// central operator; velocities of s-2..s+4 and fluxes of s-4..s+2 for the
+// upwind pair (zeros outside the block).
+int main() {
+  const int n = 30;
+  double v[n], g[n];
+  for (int s = 0; s < n; ++s) {
+    v[s] = std::sin(0.37 * s + 0.1) + 0.01 * s * s;
+    g[s] = std::cos(0.23 * s) - 0.02 * s;
+  }
+  for (int fd = 0; fd < 2; ++fd) {
+    const int ov = fd ? 2 : 3, of = fd ? 4 : 3;  // window position of plane s
+    for (int right = 0; right < 2; ++right)
+      for (int row = 0; row < 6; ++row) {
+        const int s = right ? n - 1 - row : row;
+        double dv = 0.0, df = 0.0;
+        int from_memory = 0;
+        for (int t = 0; t < (fd ? 10 : 9); ++t) {
+          const double wv = s_close_w(fd, right, false, row, t), wf = s_close_w(fd, right, true, row, t);
+          const int plane = s + s_close_off(right, row, t);
+          const int pv = s_close_vpos(fd, right, row, t), pf = s_close_fpos(fd, right, row, t);
+          auto win = [&](const double* a, int pos, int o) {
+            const int q = s + pos - o;
+            return q >= 0 && q < n ? a[q] : 0.0;
+          };
+          if (wv != 0.0) {
+            const bool w = pv >= 0 && pv <= 6;
+            dv += wv * (w ? win(v, pv, ov) : v[plane]);
+            from_memory += !w;
+          }
+          if (wf != 0.0) {
+            const bool w = pf >= 0 && pf <= 6;
+            df += wf * (w ? win(g, pf, of) : g[plane]);
+            from_memory += !w;
+          }
+        }
+        std::printf("%d %d %d %.17g %.17g %d\n", fd, right, s, dv, df, from_memory);
+      }
+  }
+  return 0;
+}
+"""
+
+
+def test_s_closure_rows_from_window(oracle_lib, tmp_path):
+    """The TMA stencil's s-closure rows (wql_sbp.cuh s_close_*: weights,
+    plane offsets and register-window positions) give the rows of the
+    oracle's operators: the central SBP-6 operator on velocities and fluxes,
+    and the order-6 upwind pair (D+ on velocities, D- on fluxes), at both
+    ends; at most four (quantity, plane) pairs of a row are read from
+    memory."""
+    import subprocess
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "waveqlab3d-gh_gb300", "csrc")
+    src = tmp_path / "sclose.cpp"
+    src.write_text(_SCLOSE_PROBE)
+    exe = tmp_path / "sclose"
+    subprocess.run(["g++", "-std=c++17", "-O0", "-I" + csrc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    n = 30
+    sv = np.arange(n)
+    v = np.sin(0.37 * sv + 0.1) + 0.01 * sv * sv
+    g = np.cos(0.23 * sv) - 0.02 * sv
+    D = oracle_lib.fd_matrix(0, True, n)
+    Dp, Dm = oracle_lib.fd_matrix(1, True, n), oracle_lib.fd_matrix(1, False, n)
+    rows = [line.split() for line in out if line.strip()]
+    assert len(rows) == 24
+    for fd, right, s, dv, df, nmem in rows:
+        fd, s = int(fd), int(s)
+        want_v = (Dp if fd else D)[s] @ v
+        want_f = (Dm if fd else D)[s] @ g
+        assert abs(float(dv) - want_v) <= 1e-13 * max(1.0, abs(want_v))
+        assert abs(float(df) - want_f) <= 1e-13 * max(1.0, abs(want_f))
+        assert int(nmem) <= 4

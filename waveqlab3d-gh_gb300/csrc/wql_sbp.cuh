@@ -96,6 +96,28 @@ constexpr double kTau0Upwind5 = 720.0 / 251.0;  // src/block.f90:208-210
 // operators' diagonal norm (h11 = 13613/43200).
 constexpr double kTau0Upwind6 = 42300.0 / 13613.0;
 
+// Closure rows of the s derivative in the TMA stencil, which keeps the
+// velocities and s fluxes of nearby planes in a register window (central
+// operator: planes s-3..s+3 for both; order-6 upwind pair: velocities of
+// s-2..s+4, fluxes of s-4..s+2).  Closure row `row` (0..5) at the left end
+// (plane s = row) or the right end (plane s = ns-1-row), column t:
+// its weight on the velocities (flux = false) or fluxes (flux = true) --
+// the central SBP-6 row, or for the upwind pair D+ on the velocities and D-
+// on the fluxes (right rows: the negated mirror images, D- on the velocities
+// and D+ on the fluxes) -- its plane offset from s, and its positions in
+// the velocity and flux windows (outside 0..6: the plane is read from
+// memory).
+constexpr double s_close_w(int fd, bool right, bool flux, int row, int t) {
+  constexpr double L[6][9] = WQL_SBP_TABLE;
+  constexpr double U[2][6][10] = WQL_UP_TABLE;
+  if (fd == 0) return t < 9 ? (right ? -L[row][t] : L[row][t]) : 0.0;
+  const int op = right ? (flux ? 0 : 1) : (flux ? 1 : 0);
+  return right ? -U[op][row][t] : U[op][row][t];
+}
+constexpr int s_close_off(bool right, int row, int t) { return right ? row - t : t - row; }
+constexpr int s_close_vpos(int fd, bool right, int row, int t) { return s_close_off(right, row, t) + (fd ? 2 : 3); }
+constexpr int s_close_fpos(int fd, bool right, int row, int t) { return s_close_off(right, row, t) + (fd ? 4 : 3); }
+
 // Row kind of 0-based index i on an axis of n points: -1..-6 left closure
 // rows (row = -kind-1), +1..+6 right closure rows (row = kind-1), 0 central.
 WQL_HD int sbp_kind(int i, int n) {

@@ -143,26 +143,13 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
 // separate instantiation (the weights, offsets and window positions are
 // compile-time constants, so the window stays in registers); the columns are
 // summed in the order of the operator table, zero weights skipped.
-//
-// Weight of column t in closure row `row`: the central SBP-6 operator (the
-// same weight for velocities and fluxes), or the upwind pair (left rows: D+
-// on the velocities, D- on the fluxes; right rows: the negated mirror, D-
-// on the velocities and D+ on the fluxes).
-constexpr double s_close_w(int fd, bool right, bool flux, int row, int t) {
-  constexpr double L[6][9] = WQL_SBP_TABLE;
-  constexpr double U[2][6][10] = WQL_UP_TABLE;
-  if (fd == 0) return t < 9 ? (right ? -L[row][t] : L[row][t]) : 0.0;
-  const int op = right ? (flux ? 0 : 1) : (flux ? 1 : 0);
-  return right ? -U[op][row][t] : U[op][row][t];
-}
-
 template <bool CURV, int FD, int ROW, bool RIGHT, int T>
 __device__ __forceinline__ void s_close_col(const VolumeArgs<float>& a, long long p, const float (&qv)[7][6],
                                             float acc[6]) {
   constexpr float wv = (float)s_close_w(FD, RIGHT, false, ROW, T);
   constexpr float wf = (float)s_close_w(FD, RIGHT, true, ROW, T);
-  constexpr int off = RIGHT ? ROW - T : T - ROW;  // plane offset from s
-  constexpr int iv = off + (FD ? 2 : 3), iflux = off + (FD ? 4 : 3);  // window positions
+  constexpr int off = s_close_off(RIGHT, ROW, T);  // plane offset from s
+  constexpr int iv = s_close_vpos(FD, RIGHT, ROW, T), iflux = s_close_fpos(FD, RIGHT, ROW, T);
   const long long np = a.np, pp = p + off * ((long long)a.pq * a.nr);
   const float* F = a.Fin;
   if constexpr (wv != 0.0f) {
